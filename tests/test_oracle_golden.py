@@ -1,0 +1,51 @@
+"""The CPU oracle against the reference's own outputs (golden vectors).
+
+The golden vectors were produced by the reference's CUDA sources and MEX
+gateways compiled for the CPU (tests/golden/make_golden.py).  On the host
+that made them (same libm) the oracle must agree bit for bit; elsewhere
+to 1e-13 relative (libm last-bit differences).
+"""
+import platform
+
+import numpy as np
+import pytest
+
+from golden_io import load, names
+from oracle.oracle import Problem
+
+EXACT = platform.machine() == "x86_64"
+
+
+def _close(a, b, rtol):
+    if EXACT:
+        np.testing.assert_array_equal(a, b)
+    else:
+        np.testing.assert_allclose(a, b, rtol=rtol, atol=rtol * max(1.0, float(np.abs(b).max())))
+
+
+@pytest.mark.parametrize("name", names())
+def test_oracle_matches_reference(name):
+    spec, ref = load(name)
+    P = Problem(spec)
+    tv = ref["tauVarMat"]
+    # the reference overwrites its trajectory per column: the last column survives
+    for col in range(tv.shape[0]):
+        r = P.forward(tv[col], with_obj=True)
+        if ref["objfcn"][col] == np.finfo(np.float64).max:
+            assert r["status"] == 1 and r["obj"] == np.finfo(np.float64).max
+        else:
+            _close(np.array([r["obj"]]), ref["objfcn"][col:col + 1], 1e-12)
+    if r["status"] == 0:
+        _close(r["lmkStk"], ref["lmkStk"], 1e-13)
+        _close(r["tauMat"], ref["tauMat"], 1e-13)
+
+
+def test_reference_runs_here_when_available():
+    """Re-run one case through the reference itself (development container only)."""
+    from oracle import ref as refmod
+    if not refmod.available():
+        pytest.skip("reference tree not present on this host")
+    spec, ref = load("frame2d_matern2")
+    lmk, tau, _ = refmod.deformation(spec, ref["tauVarMat"])
+    np.testing.assert_array_equal(lmk, ref["lmkStk"])
+    np.testing.assert_array_equal(tau, ref["tauMat"])
