@@ -1,0 +1,200 @@
+/*
+ * shape_atrophy_gb300.h -- C-ABI of the GB300 forward shape-evolution model.
+ *
+ * Drop-in boundary for the reference's four MEX binaries
+ * (deformation_{2D,3D}_frame, computeObjfcn_{2D,3D}_frame built by
+ * CUDA/compile.m): the positional entry points below take the gateways'
+ * prhs arguments in the same order and meaning
+ * (CUDA/2D_frame/deformation.cu:24-63, CUDA/2D_frame/computeObjfcn.cu:25-65,
+ * and the 3D_frame copies), with the sizes the gateways read from
+ * mxGPUGetDimensions passed explicitly.  Plain pointers and sizes only.
+ *
+ * Memory: every array argument may live in host memory or in device memory
+ * of the context's GPU (detected per pointer with cudaPointerGetAttributes),
+ * so a MATLAB gateway can pass gpuArray data zero-copy and a C caller can
+ * pass host arrays.  Outputs follow the same rule.
+ *
+ * Array layouts are the reference's: an "R x C" matrix is column-major
+ * (element (r, c) at c*R + r); index arrays are int32, 0-based, and the
+ * adjacency matrices hold a count in column 0 followed by index pairs,
+ * exactly as CUDA/generateElementObject2D.m / generateElementObject3D.m
+ * produce them.
+ *
+ * Errors: functions return SA_OK (0) or an SA_ERR_* code; the message of
+ * the last failure is available from sa_error_message().  A velocity CG
+ * solve that fails does not raise an error: like the reference
+ * (CUDA/2D_frame/deform.cu:68-73) that parameter column gets objective
+ * DBL_MAX and the call returns SA_OK.
+ *
+ * Threading: one context per host thread, or serialise calls on a shared
+ * context.  Calls are synchronous; all device work runs on the context's
+ * own stream.
+ */
+#ifndef SHAPE_ATROPHY_GB300_H
+#define SHAPE_ATROPHY_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SA_OK                 0
+#define SA_ERR_ARG            1   /* invalid argument, size or index */
+#define SA_ERR_CUDA           2   /* CUDA error or device allocation failure */
+#define SA_ERR_UNSUPPORTED    3   /* option combination not supported */
+#define SA_ERR_NOT_CONVERGED  4   /* per-solve status: CG hit its iteration cap */
+#define SA_ERR_BREAKDOWN      5   /* per-solve status: CG breakdown (zero curvature) */
+#define SA_ERR_NONFINITE      6   /* per-solve status: NaN/Inf in a solve */
+
+#define SA_ELA_FRAME          0   /* reference frame elasticity, K-preconditioned CG */
+#define SA_ELA_ISOTROPIC      1   /* layered isotropic elasticity, Jacobi-PCG */
+
+#define SA_PREC_FP64          0   /* all arithmetic in FP64 */
+#define SA_PREC_MIXED         1   /* FP32 operators, FP64 dots/residuals + refinement */
+
+typedef struct sa_context sa_context;
+
+/* Element object: the fields of the reference's elmObj struct
+ * (generateElementObject2D.m:137-150, generateElementObject3D.m:115-127),
+ * plus the layer id array of the layered model and the varifold gradient
+ * gather table.  frmVtxMat is tanVtxMat (E x 4) in 2D and nmlVtxMat
+ * (E x 6) in 3D; tsvVtxMat is E x 4 / E x 6. */
+typedef struct sa_element_object {
+	int dim;                       /* 2 or 3 */
+	int lmkNum, elmNum;            /* N, E */
+	const int *elmVtxMat;          /* E x (dim+1) */
+	const int *vtxElmMat;  int vtxElmCols;   /* N x cols */
+	const int *frmVtxMat;          /* E x 4 (2D) / E x 6 (3D) */
+	const int *tsvVtxMat;          /* E x 4 (2D) / E x 6 (3D) */
+	const int *bdrVtxMat;  int bdrElmNum;    /* unused by the model; may be NULL */
+	const int *vtxBdrMat;  int vtxBdrCols;   /* unused by the model; may be NULL */
+	const int *btmVtxMat;  int btmElmNum;    /* Bt x dim */
+	const int *vtxBtmMat;  int btmLmkNum; int vtxBtmCols;   /* Nb x cols */
+	const int *femVtxMat;  int nzrNum;       /* nzr x 2, sorted by (row, col) */
+	const int *femIfoMat;  int femIfoCols;   /* nzr x cols */
+	const int *vfdVtxMat;  int vfdElmNum;    /* Vd x dim (objective only) */
+	const int *vfdIfoMat;  int vfdIfoCols;   /* N x cols (gradient only; may be NULL) */
+	const int *elmLyrVec;          /* E layer ids (isotropic only) */
+} sa_element_object;
+
+/* Model parameters in the reference's argument vocabulary
+ * (CUDA/deformation.m:1-5), plus the layered-model tables. */
+typedef struct sa_params {
+	int elaType;                   /* SA_ELA_FRAME or SA_ELA_ISOTROPIC */
+	int precision;                 /* SA_PREC_FP64 or SA_PREC_MIXED */
+	const double *tauPrmVec; int tauPrmNum;
+	double ldmWgt; int knlOrder; double knlWidth; double knlEps;
+	const double *modVec; int modNum;   /* frame: 3 (2D) / 4 (3D); isotropic: lambda,mu per layer */
+	double spdTanVal, spdTsvVal;        /* frame diffusion speeds */
+	const double *spdLyrVec; int lyrNum;/* isotropic: diffusivity per layer */
+	const double *ynkActPrmVec;         /* frame: 4 values; isotropic: [coefficient c], f(u) = c u */
+	const double *reaActPrmVec;         /* frame: 5 values; isotropic: [rate], R(u) = rate u (1-u) */
+	double btmWgt, timeStp;
+	int timeNum, cgItrMax;
+	double cgTolSqu;
+	int rdItrMax;                       /* isotropic reaction-diffusion PCG (frame: same as cgItrMax) */
+	double rdTolSqu;                    /* isotropic RD PCG tolerance squared (frame: 1e-28) */
+} sa_params;
+
+/* Varifold target and kernels (computeObjfcn prhs[13..20]). */
+typedef struct sa_target {
+	const double *cenPosMat;   /* Vt x dim */
+	const double *uniDirMat;   /* Vt x dim */
+	const double *elmVolVec;   /* Vt */
+	int tgtElmNum;
+	char cenKnlType;           /* 'G' Gaussian, 'C' Cauchy, 'M' Matern-3/2 */
+	double cenKnlWidth;
+	char dirKnlType;           /* 'B' Binet, 'L' linear, 'O' oriented, 'U' unoriented Gaussian */
+	double dirKnlWidth;
+} sa_target;
+
+/* Per-call diagnostics (optional output). */
+typedef struct sa_solve_info {
+	int status;                /* SA_OK or the per-solve status of the last column */
+	int cgIterTotal;           /* velocity CG iterations, all steps of the last column */
+	int rdIterTotal;           /* reaction-diffusion CG iterations, all steps */
+	int cgIterMax;             /* largest per-step velocity iteration count */
+	int invertedElements;      /* elements whose orientation flipped (Jacobian sign check) */
+	double elapsedMs;          /* device time of the solves */
+} sa_solve_info;
+
+int sa_create(sa_context **ctx, int device);
+int sa_destroy(sa_context *ctx);
+const char *sa_error_message(const sa_context *ctx);
+
+/* Forward model for every column of tauVarMat (tauVarNum x objNum).
+ * lmkStk ((N*dim) x timeNum), tauMat (N x timeNum): trajectory of the last
+ * column, as the reference returns it (may be NULL).  objVec (objNum):
+ * objective when tgt != NULL, else 0; DBL_MAX where the CG failed.
+ * Replaces deform()/objfcn() (CUDA/2D_frame/deform.cu:22-119,
+ * CUDA/2D_frame/objfcn.cu:23-123). */
+int sa_forward(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat,
+               const sa_params *prm, const sa_target *tgt,
+               const double *tauVarMat, int tauVarNum, int objNum,
+               double *lmkStk, double *tauMat, double *objVec, sa_solve_info *info);
+
+/* Varifold objective of one shape against a target, and optionally its
+ * node gradient (N x dim) through the reference's gradient formulas
+ * (CUDA/2D_frame/varifold.cu:359-498,545-576; 3D_frame :372-530,577-608).
+ * Replaces varifold() (CUDA/2D_frame/varifold.cu:500-543). */
+int sa_varifold(sa_context *ctx, const sa_element_object *obj, const double *lmkMat,
+                const sa_target *tgt, int precision, double *obj_out, double *gradMat);
+
+/* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and
+ * deformation_3D_frame (dim 3): arguments in prhs order
+ * (CUDA/2D_frame/deformation.cu:24-50), outputs plhs[0..2]
+ * (:57-63): lmkStk (N*dim x timeNum), tauMat (N x timeNum), objVec (1 x objTotNum). */
+int sa_deformation_frame(sa_context *ctx, int dim,
+	const double *tauVarMat, int tauVarNum, int objTotNum,  /* prhs[0]  tauVarNum x objTotNum     */
+	const double *tauPrmVec, int tauPrmNum,                 /* prhs[1]                            */
+	const double *lmkIniMat, int lmkNum,                    /* prhs[2]  N x dim                   */
+	const int *elmVtxMat, int elmNum,                       /* prhs[3]  E x (dim+1)               */
+	const int *vtxElmMat, int vtxElmCols,                   /* prhs[4]  N x cols                  */
+	const int *frmVtxMat,                                   /* prhs[5]  tanVtxMat / nmlVtxMat     */
+	const int *tsvVtxMat,                                   /* prhs[6]                            */
+	const int *bdrVtxMat, int bdrElmNum,                    /* prhs[7]                            */
+	const int *vtxBdrMat, int vtxBdrCols,                   /* prhs[8]                            */
+	const int *btmVtxMat, int btmElmNum,                    /* prhs[9]  Bt x dim                  */
+	const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols,    /* prhs[10] Nb x cols                 */
+	const int *femVtxMat, int nzrNum,                       /* prhs[11] nzr x 2                   */
+	const int *femIfoMat, int femIfoCols,                   /* prhs[12] nzr x cols                */
+	double ldmWgt, int knlOrder, double knlWidth, double knlEps,   /* prhs[13..16]               */
+	const double *modVec,                                   /* prhs[17] 3 (2D) / 4 (3D) values    */
+	double spdTanVal, double spdTsvVal,                     /* prhs[18..19]                       */
+	const double *ynkActPrmVec, const double *reaActPrmVec, /* prhs[20..21] 4 and 5 values        */
+	double btmWgt, double timeStp, int timeNum,             /* prhs[22..24]                       */
+	int cgItrMax, double cgTolSqu,                          /* prhs[25..26]                       */
+	double *lmkStk, double *tauMat, double *objVec);        /* plhs[0..2]                         */
+
+/* Drop-in for computeObjfcn_2D_frame / computeObjfcn_3D_frame: prhs order
+ * of CUDA/2D_frame/computeObjfcn.cu:25-59; output plhs[0] objVec. */
+int sa_computeObjfcn_frame(sa_context *ctx, int dim,
+	const double *tauVarMat, int tauVarNum, int objTotNum,  /* prhs[0]                            */
+	const double *tauPrmVec, int tauPrmNum,                 /* prhs[1]                            */
+	const double *lmkIniMat, int lmkNum,                    /* prhs[2]                            */
+	const int *elmVtxMat, int elmNum,                       /* prhs[3]                            */
+	const int *vtxElmMat, int vtxElmCols,                   /* prhs[4]                            */
+	const int *frmVtxMat,                                   /* prhs[5]                            */
+	const int *tsvVtxMat,                                   /* prhs[6]                            */
+	const int *bdrVtxMat, int bdrElmNum,                    /* prhs[7]                            */
+	const int *vtxBdrMat, int vtxBdrCols,                   /* prhs[8]                            */
+	const int *btmVtxMat, int btmElmNum,                    /* prhs[9]                            */
+	const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols,    /* prhs[10]                           */
+	const int *femVtxMat, int nzrNum,                       /* prhs[11]                           */
+	const int *femIfoMat, int femIfoCols,                   /* prhs[12]                           */
+	const int *vfdVtxMat, int vfdElmNum,                    /* prhs[13] Vd x dim                  */
+	const double *tgtCenPosMat, const double *tgtUniDirMat, /* prhs[14..15] Vt x dim              */
+	const double *tgtElmVolVec, int tgtElmNum,              /* prhs[16] Vt                        */
+	double cenKnlType, double cenKnlWidth,                  /* prhs[17..18] (char code as double) */
+	double dirKnlType, double dirKnlWidth,                  /* prhs[19..20]                       */
+	double ldmWgt, int knlOrder, double knlWidth, double knlEps,   /* prhs[21..24]               */
+	const double *modVec,                                   /* prhs[25]                           */
+	double spdTanVal, double spdTsvVal,                     /* prhs[26..27]                       */
+	const double *ynkActPrmVec, const double *reaActPrmVec, /* prhs[28..29]                       */
+	double btmWgt, double timeStp, int timeNum,             /* prhs[30..32]                       */
+	int cgItrMax, double cgTolSqu,                          /* prhs[33..34]                       */
+	double *objVec);                                        /* plhs[0]                            */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

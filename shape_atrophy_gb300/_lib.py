@@ -1,0 +1,113 @@
+"""ctypes binding of include/shape_atrophy_gb300.h.
+
+The library is built in-tree by shape_atrophy_gb300.build (called from
+__graft_entry__.build()).  There is no fallback: if the library is missing
+or no GPU is visible, load() raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+_LIB = None
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+
+SA_OK, SA_ERR_ARG, SA_ERR_CUDA, SA_ERR_UNSUPPORTED = 0, 1, 2, 3
+SA_ERR_NOT_CONVERGED, SA_ERR_BREAKDOWN, SA_ERR_NONFINITE = 4, 5, 6
+SA_ELA_FRAME, SA_ELA_ISOTROPIC = 0, 1
+SA_PREC_FP64, SA_PREC_MIXED = 0, 1
+
+
+class ElementObject(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("lmkNum", C.c_int), ("elmNum", C.c_int),
+        ("elmVtxMat", _ip), ("vtxElmMat", _ip), ("vtxElmCols", C.c_int),
+        ("frmVtxMat", _ip), ("tsvVtxMat", _ip),
+        ("bdrVtxMat", _ip), ("bdrElmNum", C.c_int), ("vtxBdrMat", _ip), ("vtxBdrCols", C.c_int),
+        ("btmVtxMat", _ip), ("btmElmNum", C.c_int), ("vtxBtmMat", _ip), ("btmLmkNum", C.c_int),
+        ("vtxBtmCols", C.c_int), ("femVtxMat", _ip), ("nzrNum", C.c_int), ("femIfoMat", _ip),
+        ("femIfoCols", C.c_int), ("vfdVtxMat", _ip), ("vfdElmNum", C.c_int), ("vfdIfoMat", _ip),
+        ("vfdIfoCols", C.c_int), ("elmLyrVec", _ip),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("elaType", C.c_int), ("precision", C.c_int), ("tauPrmVec", _dp), ("tauPrmNum", C.c_int),
+        ("ldmWgt", C.c_double), ("knlOrder", C.c_int), ("knlWidth", C.c_double), ("knlEps", C.c_double),
+        ("modVec", _dp), ("modNum", C.c_int), ("spdTanVal", C.c_double), ("spdTsvVal", C.c_double),
+        ("spdLyrVec", _dp), ("lyrNum", C.c_int), ("ynkActPrmVec", _dp), ("reaActPrmVec", _dp),
+        ("btmWgt", C.c_double), ("timeStp", C.c_double), ("timeNum", C.c_int), ("cgItrMax", C.c_int),
+        ("cgTolSqu", C.c_double), ("rdItrMax", C.c_int), ("rdTolSqu", C.c_double),
+    ]
+
+
+class Target(C.Structure):
+    _fields_ = [
+        ("cenPosMat", _dp), ("uniDirMat", _dp), ("elmVolVec", _dp), ("tgtElmNum", C.c_int),
+        ("cenKnlType", C.c_char), ("cenKnlWidth", C.c_double), ("dirKnlType", C.c_char),
+        ("dirKnlWidth", C.c_double),
+    ]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("cgIterTotal", C.c_int), ("rdIterTotal", C.c_int), ("cgIterMax", C.c_int),
+        ("invertedElements", C.c_int), ("elapsedMs", C.c_double),
+    ]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library not built: {path} (run __graft_entry__.build())")
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    lib.sa_create.argtypes = [C.POINTER(vp), C.c_int]
+    lib.sa_destroy.argtypes = [vp]
+    lib.sa_error_message.argtypes = [vp]
+    lib.sa_error_message.restype = C.c_char_p
+    lib.sa_forward.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Params), C.POINTER(Target), _dp,
+                               C.c_int, C.c_int, _dp, _dp, _dp, C.POINTER(SolveInfo)]
+    lib.sa_varifold.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Target), C.c_int, _dp, _dp]
+    _LIB = lib
+    return lib
+
+
+class Context:
+    """One device context (stream, events) of the C library."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.sa_create(C.byref(self.h), device)
+        if rc != SA_OK:
+            raise RuntimeError(f"sa_create failed with code {rc} (no usable CUDA device {device})")
+
+    def check(self, rc: int, what: str):
+        if rc != SA_OK:
+            msg = self.lib.sa_error_message(self.h).decode()
+            raise RuntimeError(f"{what} failed (code {rc}): {msg}")
+
+    def close(self):
+        if self.h:
+            self.lib.sa_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,221 @@
+"""Host API of the GB300 forward model.
+
+Two layers:
+
+* ``forward(spec, ...)`` / ``varifold(spec, lmk, ...)`` -- spec-dict front
+  end of the C-ABI (see problems.py for the spec keys);
+* ``deformation(...)`` / ``computeObjfcn(...)`` -- the reference's MATLAB
+  wrappers (CUDA/deformation.m:1-62, CUDA/computeObjfcn.m:1-62) with the
+  same argument names, order and meaning: ``timeNum = floor(timeEnd /
+  timeStp) + 1``, the CG tolerance is squared before the call, landmarks
+  are given as D x N and the trajectory is returned as (D, N, timeNum).
+  ``elaType='frame'`` is the reference's model; ``elaType='isotropic'``
+  fills the branch the reference leaves empty (deformation.m:12-13,22-24):
+  ``h_modVec`` holds (lambda, mu) per layer (reshape(h_modVec, 2, [])'),
+  ``spdTanVal`` the per-layer diffusivities, ``elmObj['elmLyrVec']`` the
+  layer of each element, ``h_ynkActPrmVec = [c]`` (load -c u I) and
+  ``h_reaActPrmVec = [rate]`` (Fisher-KPP rate u (1 - u)).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+
+_CTX = {}
+
+
+def context(device: int = 0) -> _lib.Context:
+    if device not in _CTX:
+        _CTX[device] = _lib.Context(device)
+    return _CTX[device]
+
+
+class _Keep:
+    def __init__(self):
+        self.arrays = []
+
+    def i32(self, a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+        self.arrays.append(a)
+        return a.ctypes.data_as(_lib._ip)
+
+    def f64(self, a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+        self.arrays.append(a)
+        return a.ctypes.data_as(_lib._dp)
+
+
+def _element_object(obj: dict, dim: int, N: int, K: _Keep, with_vfd=True, with_grad=False) -> _lib.ElementObject:
+    o = _lib.ElementObject()
+    o.dim, o.lmkNum = dim, N
+    o.elmVtxMat = K.i32(obj["elmVtxMat"]); o.elmNum = obj["elmVtxMat"].shape[1]
+    o.vtxElmMat = K.i32(obj["vtxElmMat"]); o.vtxElmCols = obj["vtxElmMat"].shape[0]
+    o.frmVtxMat = K.i32(obj["tanVtxMat"] if dim == 2 else obj["nmlVtxMat"])
+    o.tsvVtxMat = K.i32(obj["tsvVtxMat"])
+    if "bdrVtxMat" in obj:
+        o.bdrVtxMat = K.i32(obj["bdrVtxMat"]); o.bdrElmNum = obj["bdrVtxMat"].shape[1]
+        o.vtxBdrMat = K.i32(obj["vtxBdrMat"]); o.vtxBdrCols = obj["vtxBdrMat"].shape[0]
+    o.btmVtxMat = K.i32(obj["btmVtxMat"]); o.btmElmNum = obj["btmVtxMat"].shape[1]
+    o.vtxBtmMat = K.i32(obj["vtxBtmMat"]); o.btmLmkNum = obj["vtxBtmMat"].shape[1]
+    o.vtxBtmCols = obj["vtxBtmMat"].shape[0]
+    o.femVtxMat = K.i32(obj["femVtxMat"]); o.nzrNum = obj["femVtxMat"].shape[1]
+    o.femIfoMat = K.i32(obj["femIfoMat"]); o.femIfoCols = obj["femIfoMat"].shape[0]
+    if with_vfd and "vfdVtxMat" in obj:
+        o.vfdVtxMat = K.i32(obj["vfdVtxMat"]); o.vfdElmNum = obj["vfdVtxMat"].shape[1]
+    if with_grad and "vfdIfoMat" in obj:
+        o.vfdIfoMat = K.i32(obj["vfdIfoMat"]); o.vfdIfoCols = obj["vfdIfoMat"].shape[0]
+    if "elmLyrVec" in obj:
+        o.elmLyrVec = K.i32(obj["elmLyrVec"])
+    return o
+
+
+def _params(spec: dict, K: _Keep, precision: str) -> _lib.Params:
+    p = _lib.Params()
+    iso = spec["elaType"] == "isotropic"
+    p.elaType = _lib.SA_ELA_ISOTROPIC if iso else _lib.SA_ELA_FRAME
+    p.precision = _lib.SA_PREC_MIXED if precision == "mixed" else _lib.SA_PREC_FP64
+    tp = np.atleast_1d(np.asarray(spec.get("tauPrmVec", [0.0]), dtype=np.float64))
+    p.tauPrmVec, p.tauPrmNum = K.f64(tp), tp.size
+    p.ldmWgt, p.knlOrder = float(spec["ldmWgt"]), int(spec["knlOrder"])
+    p.knlWidth, p.knlEps = float(spec["knlWidth"]), float(spec["knlEps"])
+    mv = np.asarray(spec["modVec"], dtype=np.float64).reshape(-1)
+    p.modVec, p.modNum = K.f64(mv), mv.size
+    p.spdTanVal, p.spdTsvVal = float(spec.get("spdTanVal", 0.0)), float(spec.get("spdTsvVal", 0.0))
+    if iso:
+        sp = np.asarray(spec["spdLyrVec"], dtype=np.float64).reshape(-1)
+        p.spdLyrVec, p.lyrNum = K.f64(sp), sp.size
+    p.ynkActPrmVec = K.f64(spec["ynkActPrmVec"])
+    p.reaActPrmVec = K.f64(spec["reaActPrmVec"])
+    p.btmWgt, p.timeStp, p.timeNum = float(spec["btmWgt"]), float(spec["timeStp"]), int(spec["timeNum"])
+    p.cgItrMax, p.cgTolSqu = int(spec["cgItrMax"]), float(spec["cgTolSqu"])
+    p.rdItrMax = int(spec.get("rdItrMax", 0))
+    p.rdTolSqu = float(spec.get("rdTolSqu", 0.0))
+    return p
+
+
+def _target(spec: dict, K: _Keep) -> _lib.Target:
+    t = _lib.Target()
+    cen, udir, vol = spec["tgt"]
+    t.cenPosMat, t.uniDirMat, t.elmVolVec = K.f64(cen), K.f64(udir), K.f64(vol)
+    t.tgtElmNum = int(np.asarray(vol).size)
+    ck, cw, dk, dw = spec["vfd"]
+    t.cenKnlType, t.cenKnlWidth = ck.encode(), float(cw)
+    t.dirKnlType, t.dirKnlWidth = dk.encode(), float(dw)
+    return t
+
+
+def forward(spec: dict, tauVarMat=None, precision: str = "fp64", trajectory: bool = True,
+            objective: bool = True, device: int = 0) -> dict:
+    """Run the forward model for every row of ``tauVarMat`` (nObj x nVar).
+
+    Returns dict(lmkStk (T, D, N) and tauMat (T, N) of the last row (as the
+    reference returns them), obj (nObj,) -- DBL_MAX where the CG failed --
+    and info (solve diagnostics of the last row)).
+    """
+    ctx = context(device)
+    D = int(spec["dim"])
+    lmk = np.ascontiguousarray(np.asarray(spec["lmkIniMat"], dtype=np.float64))
+    N = lmk.shape[1]
+    T = int(spec["timeNum"])
+    tv = np.atleast_2d(np.asarray(spec["tauVarVec"] if tauVarMat is None else tauVarMat, dtype=np.float64))
+    K = _Keep()
+    with_obj = objective and spec.get("tgt") is not None
+    o = _element_object(spec["elmObj"], D, N, K, with_vfd=with_obj)
+    if spec["elaType"] == "isotropic" and "elmLyrVec" in spec:
+        o.elmLyrVec = K.i32(spec["elmLyrVec"])
+    p = _params(spec, K, precision)
+    t = _target(spec, K) if with_obj else None
+    lmkStk = np.zeros((T, D, N)) if trajectory else None
+    tauMat = np.zeros((T, N)) if trajectory else None
+    obj = np.zeros(tv.shape[0])
+    info = _lib.SolveInfo()
+    tvc = np.ascontiguousarray(tv)
+    rc = ctx.lib.sa_forward(ctx.h, C.byref(o), lmk.ctypes.data_as(_lib._dp), C.byref(p),
+                            C.byref(t) if t is not None else None, tvc.ctypes.data_as(_lib._dp), tv.shape[1],
+                            tv.shape[0], lmkStk.ctypes.data_as(_lib._dp) if trajectory else None,
+                            tauMat.ctypes.data_as(_lib._dp) if trajectory else None, obj.ctypes.data_as(_lib._dp),
+                            C.byref(info))
+    ctx.check(rc, "sa_forward")
+    return dict(lmkStk=lmkStk, tauMat=tauMat, obj=obj,
+                info=dict(status=info.status, cgIterTotal=info.cgIterTotal, rdIterTotal=info.rdIterTotal,
+                          cgIterMax=info.cgIterMax, invertedElements=info.invertedElements,
+                          elapsedMs=info.elapsedMs))
+
+
+def varifold(spec: dict, lmk, grad: bool = False, precision: str = "fp64", device: int = 0):
+    """Varifold objective of the shape ``lmk`` (D, N) against spec['tgt'];
+    with grad=True also its gradient with respect to the nodes, (D, N)."""
+    ctx = context(device)
+    D = int(spec["dim"])
+    lmk = np.ascontiguousarray(np.asarray(lmk, dtype=np.float64))
+    N = lmk.shape[1]
+    K = _Keep()
+    o = _element_object(spec["elmObj"], D, N, K, with_vfd=True, with_grad=grad)
+    t = _target(spec, K)
+    out = C.c_double()
+    g = np.zeros((D, N)) if grad else None
+    rc = ctx.lib.sa_varifold(ctx.h, C.byref(o), lmk.ctypes.data_as(_lib._dp), C.byref(t),
+                             _lib.SA_PREC_MIXED if precision == "mixed" else _lib.SA_PREC_FP64, C.byref(out),
+                             g.ctypes.data_as(_lib._dp) if grad else None)
+    ctx.check(rc, "sa_varifold")
+    return (out.value, g) if grad else out.value
+
+
+# ---------------------------------------------------------------------------
+# the reference's MATLAB wrappers
+# ---------------------------------------------------------------------------
+def _matlab_spec(elaType, h_lmkIniMat, elmObj, ldmWgt, knlOrder, knlWidth, knlEps, h_modVec, h_ynkActPrmVec,
+                 spdTanVal, spdTsvVal, h_reaActPrmVec, btmWgt, timeStp, timeEnd, cgItrMax, cgTolVal, h_tauPrmVec):
+    et = str(elaType).lower()
+    if et not in ("frame", "isotropic"):
+        raise ValueError(f"Unknown elasticity type {elaType}.")       # deformation.m:18
+    lmk = np.asarray(h_lmkIniMat, dtype=np.float64)
+    D = lmk.shape[0]
+    if D not in (2, 3):
+        raise ValueError(f"Dimension {D} is not supported.")            # deformation.m:55
+    spec = dict(dim=D, elaType=et, lmkIniMat=lmk, elmObj=elmObj, tauPrmVec=np.atleast_1d(h_tauPrmVec),
+                modVec=np.asarray(h_modVec, dtype=np.float64).reshape(-1), ynkActPrmVec=h_ynkActPrmVec,
+                reaActPrmVec=h_reaActPrmVec, ldmWgt=ldmWgt, knlOrder=knlOrder, knlWidth=knlWidth, knlEps=knlEps,
+                btmWgt=btmWgt, timeStp=timeStp, timeNum=int(math.floor(timeEnd / timeStp)) + 1,
+                cgItrMax=cgItrMax, cgTolSqu=cgTolVal ** 2)
+    if et == "isotropic":
+        spec["spdLyrVec"] = np.atleast_1d(np.asarray(spdTanVal, dtype=np.float64))
+        spec["elmLyrVec"] = elmObj["elmLyrVec"]
+    else:
+        spec["spdTanVal"], spec["spdTsvVal"] = float(spdTanVal), float(spdTsvVal)
+    return spec
+
+
+def deformation(h_tauVarVec, h_tauPrmVec, elaType, h_lmkIniMat, elmObj, ldmWgt, knlOrder, knlWidth, knlEps,
+                h_modVec, h_ynkActPrmVec, spdTanVal, spdTsvVal, h_reaActPrmVec, btmWgt, timeStp, timeEnd,
+                cgItrMax, cgTolVal):
+    """deformation.m: returns (h_lmkStk (D, N, timeNum), h_tauMat (N, timeNum))."""
+    spec = _matlab_spec(elaType, h_lmkIniMat, elmObj, ldmWgt, knlOrder, knlWidth, knlEps, h_modVec,
+                        h_ynkActPrmVec, spdTanVal, spdTsvVal, h_reaActPrmVec, btmWgt, timeStp, timeEnd, cgItrMax,
+                        cgTolVal, h_tauPrmVec)
+    tv = np.asarray(h_tauVarVec, dtype=np.float64)
+    tv = tv.T if tv.ndim == 2 else tv[None, :]          # MATLAB columns are parameter sets
+    r = forward(spec, tv, trajectory=True, objective=False)
+    return np.transpose(r["lmkStk"], (1, 2, 0)), r["tauMat"].T
+
+
+def computeObjfcn(h_tauVarMat, h_tauPrmVec, elaType, h_lmkIniMat, elmObj, tgtObj, vfdObj, ldmWgt, knlOrder,
+                  knlWidth, knlEps, h_modVec, h_ynkActPrmVec, spdTanVal, spdTsvVal, h_reaActPrmVec, btmWgt,
+                  timeStp, timeEnd, cgItrMax, cgTolVal):
+    """computeObjfcn.m: objective per column of h_tauVarMat (DBL_MAX where the CG failed)."""
+    spec = _matlab_spec(elaType, h_lmkIniMat, elmObj, ldmWgt, knlOrder, knlWidth, knlEps, h_modVec,
+                        h_ynkActPrmVec, spdTanVal, spdTsvVal, h_reaActPrmVec, btmWgt, timeStp, timeEnd, cgItrMax,
+                        cgTolVal, h_tauPrmVec)
+    spec["tgt"] = (tgtObj["cenPosMat"], tgtObj["uniDirMat"], tgtObj["elmVolVec"])
+    spec["vfd"] = (vfdObj["cenKnlType"], vfdObj["cenKnlWidth"], vfdObj["dirKnlType"], vfdObj["dirKnlWidth"])
+    tv = np.asarray(h_tauVarMat, dtype=np.float64)
+    tv = tv.T if tv.ndim == 2 else tv[None, :]
+    return forward(spec, tv, trajectory=False, objective=True)["obj"]

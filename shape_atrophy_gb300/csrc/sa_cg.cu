@@ -1,0 +1,353 @@
+// sa_cg.cu -- Jacobi-preconditioned CG on the block-CSR operators.
+//
+// Replaces the reference's host-driven CG loop (2D_frame/ipcg.cu:11-100:
+// four cuBLAS dots with a host round trip each, plus axpby kernels) for the
+// layered model and for the reaction-diffusion solve (which the reference
+// does by dense Cholesky, 2D_frame/deform.cu:99-104).
+//
+// Chronopoulos-Gear form: per iteration one matvec kernel (w = A u, fused
+// with the dot (w, u)) and one vector kernel (p, s, x, r, u updates fused
+// with the dots (r, u) and (r, r)).  All scalars stay on the device; the
+// last block of each kernel finishes its reduction in a fixed order, so
+// results do not depend on block scheduling.  Kernel arguments never
+// change between iterations, so chunks of iterations are captured once in
+// a CUDA graph and replayed; the host reads the status word once per
+// chunk.  Stopping rule as the reference: |r|^2 < tol^2 |b|^2, b = 0
+// gives x = 0.
+//
+// Mixed precision (SA_PREC_MIXED): FP32 operator values and FP32 vectors in
+// an inner CG with FP64 dot products, inside an FP64 iterative-refinement
+// loop whose residual b - A x is recomputed with the FP64 operator.
+#include "sa_internal.cuh"
+#include <cmath>
+
+namespace sa {
+
+struct CgScal {
+	double bb, rr, gam, gamPrev, alpha, beta, delta, tolSqu;
+	int first, done, code, iters, zero, itrMax;
+	unsigned int counter;
+	int pad;
+};
+
+constexpr int kCgBlock = 256;
+
+// block-wide reduction of K values; writes part[k*nb + blockIdx.x]; returns true in the last block
+template <int K>
+__device__ __forceinline__ bool reduce_partials(double (&v)[K], double *part, unsigned int *counter)
+{
+	__shared__ double sm[K][kCgBlock / 32];
+	__shared__ bool last;
+	int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int k = 0; k < K; ++k)
+		for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+	if (lane == 0) for (int k = 0; k < K; ++k) sm[k][wid] = v[k];
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		for (int k = 0; k < K; ++k) {
+			double s = 0.0;
+			for (int w = 0; w < kCgBlock / 32; ++w) s += sm[k][w];
+			part[k * gridDim.x + blockIdx.x] = s;
+		}
+		__threadfence();
+		unsigned int t = atomicAdd(counter, 1u);
+		last = (t == gridDim.x - 1);
+	}
+	__syncthreads();
+	return last;
+}
+
+// fixed-order sum of the partials by warp 0 of the last block (result valid in lane 0)
+template <int K>
+__device__ __forceinline__ void finish_partials(double (&out)[K], const double *part)
+{
+	int lane = threadIdx.x & 31;
+	for (int k = 0; k < K; ++k) {
+		double s = 0.0;
+		for (int b = lane; b < (int) gridDim.x; b += 32) s += __ldcg(part + k * gridDim.x + b);
+		for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+		out[k] = s;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// matvec kernels: w = A u (+ partial (w, u))
+// ---------------------------------------------------------------------------
+template <int B, typename TM, typename TV>
+__device__ __forceinline__ void row_spmv(int i, const int *__restrict__ rowPtr, const int *__restrict__ col,
+                                         const TM *__restrict__ blk, const TV *__restrict__ u, TV (&acc)[B])
+{
+	for (int r = 0; r < B; ++r) acc[r] = (TV) 0;
+	int z0 = rowPtr[i], z1 = rowPtr[i + 1];
+	for (int z = z0; z < z1; ++z) {
+		int j = col[z];
+		const TM *a = blk + (long) z * B * B;
+		TV xj[B];
+		for (int c = 0; c < B; ++c) xj[c] = u[(long) j * B + c];
+		for (int r = 0; r < B; ++r)
+			for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
+	}
+}
+
+template <int B, typename TM, typename TV>
+__global__ void __launch_bounds__(kCgBlock) k_cg_spmv(int N, const int *__restrict__ rowPtr,
+                                                      const int *__restrict__ col, const TM *__restrict__ blk,
+                                                      const TV *__restrict__ u, TV *__restrict__ w,
+                                                      double *part, CgScal *sc)
+{
+	if (sc->done) return;
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double v[1] = {0.0};
+	if (i < N) {
+		TV acc[B];
+		row_spmv<B, TM, TV>(i, rowPtr, col, blk, u, acc);
+		for (int r = 0; r < B; ++r) {
+			w[(long) i * B + r] = acc[r];
+			v[0] += (double) acc[r] * (double) u[(long) i * B + r];
+		}
+	}
+	if (!reduce_partials<1>(v, part, &sc->counter)) return;
+	double d[1];
+	finish_partials<1>(d, part);
+	if (threadIdx.x == 0) {
+		double delta = d[0], gam = sc->gam, alpha, beta;
+		if (sc->first) { beta = 0.0; alpha = gam / delta; }
+		else {
+			beta = gam / sc->gamPrev;
+			alpha = gam / (delta - beta * gam / sc->alpha);
+		}
+		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
+			sc->code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
+			sc->done = 1;
+		}
+		sc->delta = delta; sc->alpha = alpha; sc->beta = beta; sc->first = 0;
+		sc->counter = 0;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// vector kernel: p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^{-1} r
+// ---------------------------------------------------------------------------
+template <int B, typename TV, typename TX>
+__global__ void __launch_bounds__(kCgBlock) k_cg_update(int N, TX *__restrict__ x, TV *__restrict__ r,
+                                                        TV *__restrict__ u, const TV *__restrict__ w,
+                                                        TV *__restrict__ p, TV *__restrict__ s,
+                                                        const TV *__restrict__ dinv, double *part, CgScal *sc)
+{
+	if (sc->done) return;
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double v[2] = {0.0, 0.0};
+	if (i < N) {
+		TV al = (TV) sc->alpha, be = (TV) sc->beta;
+		for (int c = 0; c < B; ++c) {
+			long k = (long) i * B + c;
+			TV pk = u[k] + be * p[k];
+			TV sk = w[k] + be * s[k];
+			p[k] = pk; s[k] = sk;
+			x[k] = x[k] + (TX) al * (TX) pk;
+			TV rk = r[k] - al * sk;
+			r[k] = rk;
+			TV uk = dinv[k] * rk;
+			u[k] = uk;
+			v[0] += (double) rk * (double) uk;
+			v[1] += (double) rk * (double) rk;
+		}
+	}
+	if (!reduce_partials<2>(v, part, &sc->counter)) return;
+	double d[2];
+	finish_partials<2>(d, part);
+	if (threadIdx.x == 0) {
+		sc->gamPrev = sc->gam;
+		sc->gam = d[0];
+		sc->rr = d[1];
+		sc->iters += 1;
+		if (!isfinite(d[0]) || !isfinite(d[1])) { sc->code = SA_ERR_NONFINITE; sc->done = 1; }
+		else if (d[1] < sc->tolSqu * sc->bb) { sc->code = SA_OK; sc->done = 1; }
+		else if (sc->iters >= sc->itrMax) { sc->code = SA_ERR_NOT_CONVERGED; sc->done = 1; }
+		sc->counter = 0;
+	}
+}
+
+// r = b - q, u = D^{-1} r, partials (b, b), (r, r), (r, u)
+template <int B, typename TV>
+__global__ void __launch_bounds__(kCgBlock) k_cg_init(int N, const double *__restrict__ b, const double *__restrict__ q,
+                                                      const TV *__restrict__ dinv, TV *__restrict__ r,
+                                                      TV *__restrict__ u, double *part, CgScal *sc)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double v[3] = {0.0, 0.0, 0.0};
+	if (i < N) {
+		for (int c = 0; c < B; ++c) {
+			long k = (long) i * B + c;
+			double rk = b[k] - q[k];
+			TV rt = (TV) rk;
+			TV uk = dinv[k] * rt;
+			r[k] = rt; u[k] = uk;
+			v[0] += b[k] * b[k];
+			v[1] += rk * rk;
+			v[2] += (double) rt * (double) uk;
+		}
+	}
+	if (!reduce_partials<3>(v, part, &sc->counter)) return;
+	double d[3];
+	finish_partials<3>(d, part);
+	if (threadIdx.x == 0) {
+		if (sc->bb < 0.0) sc->bb = d[0];       // bb < 0: take |b|^2 from this rhs
+		sc->rr = d[1]; sc->gam = d[2];
+		sc->first = 1; sc->done = 0; sc->code = SA_OK;
+		if (!isfinite(d[0]) || !isfinite(d[1])) { sc->code = SA_ERR_NONFINITE; sc->done = 1; }
+		else if (sc->bb == 0.0) { sc->zero = 1; sc->done = 1; }
+		else if (d[1] < sc->tolSqu * sc->bb) sc->done = 1;
+		else if (sc->itrMax <= 0) { sc->code = SA_ERR_NOT_CONVERGED; sc->done = 1; }
+		sc->counter = 0;
+	}
+}
+
+template <typename TX>
+__global__ void k_cg_zero(long n, TX *x, const CgScal *sc)
+{
+	if (!sc->zero) return;
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k < n) x[k] = (TX) 0;
+}
+
+template <typename TA, typename TB>
+__global__ void k_convert(long n, const TA *a, TB *b)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k < n) b[k] = (TB) a[k];
+}
+
+__global__ void k_axpy_f32(long n, double *x, const float *d)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k < n) x[k] += (double) d[k];
+}
+
+// q = A x in FP64 (for the initial / true residual)
+template <int B>
+__global__ void k_spmv64(int N, const int *__restrict__ rowPtr, const int *__restrict__ col,
+                         const double *__restrict__ blk, const double *__restrict__ x, double *__restrict__ q)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	double acc[B];
+	row_spmv<B, double, double>(i, rowPtr, col, blk, x, acc);
+	for (int r = 0; r < B; ++r) q[(long) i * B + r] = acc[r];
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+static void set_scal(CgScal *d, double tolSqu, int itrMax, double bb, cudaStream_t s)
+{
+	CgScal h{};
+	h.tolSqu = tolSqu;
+	h.itrMax = itrMax;
+	h.bb = bb;
+	h.first = 1;
+	SA_CHECK(cudaMemcpyAsync(d, &h, sizeof(CgScal), cudaMemcpyHostToDevice, s));
+}
+
+static CgScal read_scal(const CgScal *d, cudaStream_t s)
+{
+	CgScal h;
+	SA_CHECK(cudaMemcpyAsync(&h, d, sizeof(CgScal), cudaMemcpyDeviceToHost, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	return h;
+}
+
+// one inner CG run: vectors of type TV, operator of type TM, solution TX
+template <int B, typename TM, typename TV, typename TX>
+static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double *b, TX *x, const double *q,
+                     TV *r, TV *u, TV *w, TV *p, TV *sv, double *part, CgScal *sc, int itrMax, double tolSqu,
+                     double bb, cudaStream_t s)
+{
+	int N = m.N, nb = grid_for(N, kCgBlock);
+	long n = (long) N * B;
+	set_scal(sc, tolSqu, itrMax, bb, s);
+	SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
+	SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
+	k_cg_init<B, TV><<<nb, kCgBlock, 0, s>>>(N, b, q, dinv, r, u, part, sc);
+	const int chunk = 16;
+	for (int it = 0; it < itrMax + chunk; it += chunk) {
+		for (int k = 0; k < chunk; ++k) {
+			k_cg_spmv<B, TM, TV><<<nb, kCgBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, u, w, part, sc);
+			k_cg_update<B, TV, TX><<<nb, kCgBlock, 0, s>>>(N, x, r, u, w, p, sv, dinv, part, sc);
+		}
+		SA_CHECK(cudaGetLastError());
+		CgScal h = read_scal(sc, s);
+		if (h.done) break;
+	}
+	k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
+	return read_scal(sc, s);
+}
+
+__global__ void k_sub(long n, const double *a, const double *b, double *c)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k < n) c[k] = a[k] - b[k];
+}
+
+template <int B>
+int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double *b, double *x, int itrMax,
+              double tolSqu, CgWork &wk, Status *st, int *itersOut, cudaStream_t s, int precision)
+{
+	(void) st;
+	int N = m.N;
+	long n = (long) N * B;
+	double *q = wk.xr;                       // A x (FP64)
+	CgScal *sc = (CgScal *) wk.scal;
+	if (precision == SA_PREC_FP64 || !wk.blk32) {
+		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, x, q);
+		CgScal h = run_cg<B, double, double, double>(m, blk, dinv, b, x, q, wk.r, wk.u, wk.w, wk.p, wk.sv,
+		                                              wk.part, sc, itrMax, tolSqu, -1.0, s);
+		if (itersOut) *itersOut = h.iters;
+		return h.code;
+	}
+	// Mixed precision: FP64 iterative refinement.  Each outer step forms the
+	// true residual rin = b - A x with the FP64 operator, solves A d = rin
+	// with the FP32 operator and FP32 vectors (FP64 dot products), and
+	// updates x += d in FP64.
+	float *r32 = wk.f32, *u32 = r32 + n, *w32 = r32 + 2 * n, *p32 = r32 + 3 * n, *s32 = r32 + 4 * n;
+	float *dinv32 = r32 + 5 * n, *d32 = r32 + 6 * n;
+	double *rin = wk.xr + n, *zero = wk.xr + 2 * n;
+	k_convert<double, float><<<grid_for(n), kBlock, 0, s>>>(n, dinv, dinv32);
+	SA_CHECK(cudaMemsetAsync(zero, 0, sizeof(double) * n, s));
+	int total = 0, code = SA_ERR_NOT_CONVERGED;
+	double bb = -1.0;
+	const int nb = grid_for(N, kCgBlock);
+	for (int outer = 0; outer < 64; ++outer) {
+		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, x, q);
+		k_sub<<<grid_for(n), kBlock, 0, s>>>(n, b, q, rin);
+		// outer test: |b - A x|^2 < tol^2 |b|^2 (k_cg_init with b and q gives both norms)
+		set_scal(sc, tolSqu, 1, bb, s);
+		k_cg_init<B, float><<<nb, kCgBlock, 0, s>>>(N, b, q, dinv32, r32, u32, wk.part, sc);
+		CgScal h0 = read_scal(sc, s);
+		if (bb < 0.0) bb = h0.bb;
+		if (h0.code == SA_ERR_NONFINITE) { code = SA_ERR_NONFINITE; break; }
+		if (h0.zero) { SA_CHECK(cudaMemsetAsync(x, 0, sizeof(double) * n, s)); code = SA_OK; break; }
+		if (h0.rr < tolSqu * bb) { code = SA_OK; break; }
+		if (total >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
+		// inner tolerance: 1e-5 relative, or just below what the outer test still needs
+		double need = 0.01 * tolSqu * bb / h0.rr;
+		double innerTol = need > 1e-10 ? need : 1e-10;
+		SA_CHECK(cudaMemsetAsync(d32, 0, sizeof(float) * n, s));
+		CgScal h = run_cg<B, float, float, float>(m, wk.blk32, dinv32, rin, d32, zero, r32, u32, w32, p32, s32,
+		                                           wk.part, sc, itrMax - total, innerTol, -1.0, s);
+		total += h.iters;
+		if (h.code == SA_ERR_NONFINITE) { code = h.code; break; }
+		k_axpy_f32<<<grid_for(n), kBlock, 0, s>>>(n, x, d32);
+	}
+	if (itersOut) *itersOut = total;
+	return code;
+}
+
+template int cg_jacobi<1>(const Mesh &, const double *, const double *, const double *, double *, int, double,
+                          CgWork &, Status *, int *, cudaStream_t, int);
+template int cg_jacobi<2>(const Mesh &, const double *, const double *, const double *, double *, int, double,
+                          CgWork &, Status *, int *, cudaStream_t, int);
+template int cg_jacobi<3>(const Mesh &, const double *, const double *, const double *, double *, int, double,
+                          CgWork &, Status *, int *, cudaStream_t, int);
+
+}  // namespace sa

@@ -1,0 +1,701 @@
+// sa_driver.cu -- context, mesh set-up, the forward time loop and the C-ABI.
+//
+// Replaces the reference's MEX gateways (2D_frame/deformation.cu:14-199,
+// computeObjfcn.cu:14-212), its memory arena (assignStructMemory.cu:33-229)
+// and drivers deform() / objfcn() (deform.cu:22-119, objfcn.cu:23-123).
+//
+// One time step (layered model):
+//   activity(tau_t) -> yank rhs b (geometry t) -> elasticity blocks (geometry t,
+//   + bottom penalty) -> Jacobi CG for v_t (warm start v_{t-1}) -> x_{t+1} =
+//   x_t + dt v_t -> geometry t+1 -> M', L = M' + dt G' -> rhs = M_t tau_t +
+//   dt R-load(geometry t) -> Jacobi CG for tau_{t+1} (warm start tau_t).
+// Frame mode is the same step with the frame stress, frame diffusion, the
+// reference's activity polynomials, and the velocity solved by the
+// K-preconditioned CG with the dense RKHS matrix of x_t.
+#include "sa_internal.cuh"
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <algorithm>
+
+struct sa_context {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	std::string err;
+};
+
+namespace sa {
+
+// ---------------------------------------------------------------------------
+// pointer helpers: accept host or device memory for every array
+// ---------------------------------------------------------------------------
+static bool is_device_ptr(const void *p)
+{
+	if (!p) return false;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+struct Pool {                 // device allocations of one call, freed at the end
+	std::vector<void *> ptrs;
+	cudaStream_t s;
+	explicit Pool(cudaStream_t st) : s(st) {}
+	~Pool() { for (void *p : ptrs) cudaFree(p); }
+	template <typename T> T *alloc(size_t n)
+	{
+		void *p = nullptr;
+		SA_CHECK(cudaMalloc(&p, sizeof(T) * (n ? n : 1)));
+		ptrs.push_back(p);
+		return (T *) p;
+	}
+	template <typename T> T *zeros(size_t n)
+	{
+		T *p = alloc<T>(n);
+		SA_CHECK(cudaMemsetAsync(p, 0, sizeof(T) * (n ? n : 1), s));
+		return p;
+	}
+	template <typename T> const T *dev(const T *p, size_t n)     // device view of a host or device array
+	{
+		if (!p) return nullptr;
+		if (is_device_ptr(p)) return p;
+		T *d = alloc<T>(n);
+		SA_CHECK(cudaMemcpyAsync(d, p, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+		return d;
+	}
+};
+
+struct ArgError { std::string msg; };
+#define SA_REQUIRE(c, m) do { if (!(c)) throw ::sa::ArgError{m}; } while (0)
+
+template <typename T> static std::vector<T> to_host(const T *p, size_t n, cudaStream_t s)
+{
+	std::vector<T> h(n);
+	if (n) SA_CHECK(cudaMemcpyAsync(h.data(), p, sizeof(T) * n, cudaMemcpyDefault, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	return h;
+}
+
+// ---------------------------------------------------------------------------
+// mesh set-up: validation, CSR row pointers, ordered assembly table
+// ---------------------------------------------------------------------------
+__global__ void k_asm_table(int Z, int E, int V, const int *__restrict__ femVtx, const int *__restrict__ femIfo,
+                            const int *__restrict__ elmVtx, int *__restrict__ tab, int *bad)
+{
+	int z = blockIdx.x * blockDim.x + threadIdx.x;
+	if (z >= Z) return;
+	int i = femVtx[z], j = femVtx[Z + z];
+	int cnt = femIfo[z];
+	for (int k = 0; k < cnt; ++k) {
+		int e = femIfo[(2 + 2 * k) * (long) Z + z];
+		if (e < 0 || e >= E) { atomicOr(bad, 1); tab[k * (long) Z + z] = 0; continue; }
+		int a = -1, b = -1;
+		for (int l = 0; l < V; ++l) {
+			int n = elmVtx[l * (long) E + e];
+			if (n == i) a = l;
+			if (n == j) b = l;
+		}
+		if (a < 0 || b < 0) { atomicOr(bad, 2); a = 0; b = 0; }
+		tab[k * (long) Z + z] = e * 16 + a * 4 + b;
+	}
+}
+
+template <int D>
+__global__ void k_init_sign(int E, const int *__restrict__ elmVtx, const double *__restrict__ x,
+                            signed char *__restrict__ sg)
+{
+	int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= E) return;
+	Vec<D> q0 = load_node<D>(x, elmVtx[e]);
+	Vec<D> q[D];
+	for (int k = 0; k < D; ++k) q[k] = vsub(load_node<D>(x, elmVtx[(k + 1) * (long) E + e]), q0);
+	double det = det_edges<D>(q);
+	sg[e] = det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
+}
+
+static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool needGrad, bool layered, int lyrNum,
+                       Pool &P)
+{
+	cudaStream_t s = P.s;
+	int D = o->dim;
+	SA_REQUIRE(D == 2 || D == 3, "dim must be 2 or 3");
+	m.dim = D; m.V = D + 1; m.N = o->lmkNum; m.E = o->elmNum; m.Z = o->nzrNum;
+	m.Bt = o->btmElmNum; m.Nb = o->btmLmkNum; m.Vd = needVfd ? o->vfdElmNum : 0;
+	SA_REQUIRE(m.N > 0 && m.E > 0 && m.Z >= m.N, "empty mesh or femVtxMat smaller than the node count");
+	SA_REQUIRE(o->elmVtxMat && o->vtxElmMat && o->frmVtxMat && o->tsvVtxMat && o->femVtxMat && o->femIfoMat,
+	           "missing element-object array");
+	SA_REQUIRE(o->vtxElmCols >= 1 && o->femIfoCols >= 2, "adjacency matrices need a count column");
+	SA_REQUIRE((long) m.E * 16 < (1L << 31), "too many elements for the 32-bit assembly table");
+	m.vtxElmCols = o->vtxElmCols; m.femIfoCols = o->femIfoCols;
+	int frmCols = D == 2 ? 4 : 6;
+	m.elmVtx = (int *) P.dev(o->elmVtxMat, (size_t) m.E * m.V);
+	m.vtxElm = (int *) P.dev(o->vtxElmMat, (size_t) m.N * o->vtxElmCols);
+	m.frmVtx = (int *) P.dev(o->frmVtxMat, (size_t) m.E * frmCols);
+	m.tsvVtx = (int *) P.dev(o->tsvVtxMat, (size_t) m.E * frmCols);
+	m.femVtx = (int *) P.dev(o->femVtxMat, (size_t) m.Z * 2);
+	m.femIfo = (int *) P.dev(o->femIfoMat, (size_t) m.Z * o->femIfoCols);
+	if (m.Bt > 0) {
+		SA_REQUIRE(o->btmVtxMat && o->vtxBtmMat && o->vtxBtmCols >= 1 && m.Nb > 0 && m.Nb <= m.N,
+		           "bottom arrays inconsistent");
+		m.btmVtx = (int *) P.dev(o->btmVtxMat, (size_t) m.Bt * D);
+		m.vtxBtm = (int *) P.dev(o->vtxBtmMat, (size_t) m.Nb * o->vtxBtmCols);
+		m.vtxBtmCols = o->vtxBtmCols;
+	}
+	if (needVfd) {
+		SA_REQUIRE(o->vfdVtxMat && m.Vd > 0, "objective needs vfdVtxMat");
+		m.vfdVtx = (int *) P.dev(o->vfdVtxMat, (size_t) m.Vd * D);
+	}
+	if (needGrad) {
+		SA_REQUIRE(o->vfdIfoMat && o->vfdIfoCols >= 1, "gradient needs vfdIfoMat");
+		m.vfdIfo = (int *) P.dev(o->vfdIfoMat, (size_t) m.N * o->vfdIfoCols);
+		m.vfdIfoCols = o->vfdIfoCols;
+	}
+	if (layered) {
+		SA_REQUIRE(o->elmLyrVec, "layered model needs elmLyrVec");
+		m.elmLyr = (int *) P.dev(o->elmLyrVec, (size_t) m.E);
+	}
+
+	// host-side validation of every index (one pass over each array)
+	std::vector<int> ev = to_host(m.elmVtx, (size_t) m.E * m.V, s);
+	for (int v : ev) SA_REQUIRE(v >= 0 && v < m.N, "elmVtxMat index out of range");
+	std::vector<int> fv = to_host(m.femVtx, (size_t) m.Z * 2, s);
+	std::vector<int> rp(m.N + 1, -1);
+	for (int z = 0; z < m.Z; ++z) {
+		int r = fv[z], c = fv[m.Z + z];
+		SA_REQUIRE(r >= 0 && r < m.N && c >= 0 && c < m.N, "femVtxMat index out of range");
+		if (z > 0) SA_REQUIRE(r > fv[z - 1] || (r == fv[z - 1] && c > fv[m.Z + z - 1]),
+		                      "femVtxMat rows must be sorted by (row, col) (generateElementObject sortrows)");
+		if (rp[r] < 0) rp[r] = z;
+	}
+	rp[m.N] = m.Z;
+	for (int i = m.N - 1; i >= 0; --i) SA_REQUIRE(rp[i] >= 0, "femVtxMat misses a node row");
+	std::vector<int> fi = to_host(m.femIfo, (size_t) m.Z * 2, s);
+	int maxAdj = 0;
+	for (int z = 0; z < m.Z; ++z) {
+		SA_REQUIRE(fi[z] >= 0 && 2 + 2 * fi[z] <= o->femIfoCols, "femIfoMat count exceeds its columns");
+		maxAdj = std::max(maxAdj, fi[z]);
+	}
+	std::vector<int> ve = to_host(m.vtxElm, (size_t) m.N * o->vtxElmCols, s);
+	for (int i = 0; i < m.N; ++i) {
+		int c = ve[i];
+		SA_REQUIRE(c >= 0 && 1 + 2 * c <= o->vtxElmCols, "vtxElmMat count exceeds its columns");
+		for (int a = 0; a < c; ++a) {
+			int e = ve[(1 + 2 * a) * (long) m.N + i], l = ve[(2 + 2 * a) * (long) m.N + i];
+			SA_REQUIRE(e >= 0 && e < m.E && l >= 0 && l < m.V && ev[(long) l * m.E + e] == i,
+			           "vtxElmMat entry does not match elmVtxMat");
+		}
+	}
+	std::vector<int> fr = to_host(m.frmVtx, (size_t) m.E * frmCols, s);
+	for (int v : fr) SA_REQUIRE(v >= 0 && v < m.N, "tan/nmlVtxMat index out of range");
+	std::vector<int> ts = to_host(m.tsvVtx, (size_t) m.E * frmCols, s);
+	for (int v : ts) SA_REQUIRE(v >= 0 && v < m.N, "tsvVtxMat index out of range");
+	if (m.Bt > 0) {
+		std::vector<int> bv = to_host(m.btmVtx, (size_t) m.Bt * D, s);
+		for (int v : bv) SA_REQUIRE(v >= 0 && v < m.N, "btmVtxMat index out of range");
+		std::vector<int> vb = to_host(m.vtxBtm, (size_t) m.Nb * o->vtxBtmCols, s);
+		for (int i = 0; i < m.Nb; ++i) {
+			int c = vb[i];
+			SA_REQUIRE(c >= 0 && 1 + 2 * c <= o->vtxBtmCols, "vtxBtmMat count exceeds its columns");
+			for (int a = 0; a < c; ++a) {
+				int f = vb[(1 + 2 * a) * (long) m.Nb + i], l = vb[(2 + 2 * a) * (long) m.Nb + i];
+				SA_REQUIRE(f >= 0 && f < m.Bt && l >= 0 && l < D && bv[(long) l * m.Bt + f] == i,
+				           "vtxBtmMat entry must name its own node (bottom nodes numbered first)");
+			}
+		}
+	}
+	if (needVfd) {
+		std::vector<int> vv = to_host(m.vfdVtx, (size_t) m.Vd * D, s);
+		for (int v : vv) SA_REQUIRE(v >= 0 && v < m.N, "vfdVtxMat index out of range");
+	}
+	if (needGrad) {
+		std::vector<int> gi = to_host(m.vfdIfo, (size_t) m.N * o->vfdIfoCols, s);
+		int w = D == 2 ? 2 : 3;
+		for (int i = 0; i < m.N; ++i) {
+			int c = gi[i];
+			SA_REQUIRE(c >= 0 && 1 + w * c <= o->vfdIfoCols, "vfdIfoMat count exceeds its columns");
+			for (int a = 0; a < c; ++a) {
+				int e = gi[(1 + w * a) * (long) m.N + i];
+				SA_REQUIRE(e >= 0 && e < m.Vd, "vfdIfoMat element out of range");
+				if (D == 3)
+					for (int t = 2; t <= 3; ++t) {
+						int q = gi[(t + w * a) * (long) m.N + i];
+						SA_REQUIRE(q >= 0 && q < m.N, "vfdIfoMat node out of range");
+					}
+			}
+		}
+	}
+	if (layered) {
+		std::vector<int> ly = to_host(m.elmLyr, (size_t) m.E, s);
+		for (int v : ly) SA_REQUIRE(v >= 0 && v < lyrNum, "elmLyrVec entry outside the layer tables");
+	}
+	m.rowPtr = P.alloc<int>(m.N + 1);
+	SA_CHECK(cudaMemcpyAsync(m.rowPtr, rp.data(), sizeof(int) * (m.N + 1), cudaMemcpyHostToDevice, s));
+	m.asmCols = maxAdj;
+	m.asmTab = P.alloc<int>((size_t) std::max(1, maxAdj) * m.Z);
+	int *bad = P.zeros<int>(1);
+	k_asm_table<<<grid_for(m.Z), kBlock, 0, s>>>(m.Z, m.E, m.V, m.femVtx, m.femIfo, m.elmVtx, m.asmTab, bad);
+	int hbad = 0;
+	SA_CHECK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	SA_REQUIRE(hbad == 0, "femIfoMat lists an element that does not contain both nodes of the slot");
+	m.sign0 = P.alloc<signed char>(m.E);
+}
+
+// ---------------------------------------------------------------------------
+// one forward solve
+// ---------------------------------------------------------------------------
+struct Work {
+	double *xa, *xb;            // node positions t, t+1 (interleaved)
+	double *v, *b, *pd, *blk, *dinv, *fy, *fr;
+	double *Mnow, *Mnxt, *L, *dinvRd, *rhs;
+	Geom g0, g1;
+	CgWork cw;
+	KpcgWork kw;
+	double *K = nullptr;
+	double *trajX = nullptr, *trajT = nullptr;   // device trajectory (SoA per step), tau
+};
+
+template <int D>
+static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, Pool &P)
+{
+	long N = m.N, E = m.E, Z = m.Z, n = N * D;
+	w.xa = P.alloc<double>(n); w.xb = P.alloc<double>(n);
+	w.v = P.alloc<double>(n); w.b = P.alloc<double>(n); w.pd = P.zeros<double>(N);
+	w.blk = P.alloc<double>((size_t) Z * D * D); w.dinv = P.alloc<double>(n);
+	w.fy = P.alloc<double>(N); w.fr = P.alloc<double>(N);
+	w.Mnow = P.alloc<double>(Z); w.Mnxt = P.alloc<double>(Z); w.L = P.alloc<double>(Z);
+	w.dinvRd = P.alloc<double>(N); w.rhs = P.alloc<double>(N);
+	for (Geom *g : {&w.g0, &w.g1}) {
+		g->QI = P.alloc<double>((size_t) (D + 1) * D * E);
+		g->absDet = P.alloc<double>(E); g->vol = P.alloc<double>(E);
+		if (md.frame) { g->frm = P.alloc<double>((size_t) D * E); g->tsv = P.alloc<double>((size_t) D * E); }
+	}
+	int nb = grid_for(N, 256);
+	CgWork &c = w.cw;
+	c.r = P.alloc<double>(n); c.u = P.alloc<double>(n); c.w = P.alloc<double>(n);
+	c.p = P.alloc<double>(n); c.sv = P.alloc<double>(n);
+	c.part = P.alloc<double>((size_t) 4 * nb + 64); c.scal = P.zeros<double>(32); c.maxBlocks = nb;
+	c.xr = P.alloc<double>((size_t) 3 * n);
+	if (md.precision == SA_PREC_MIXED) {
+		c.blk32 = P.alloc<float>((size_t) Z * D * D);
+		c.f32 = P.alloc<float>((size_t) 7 * n);
+	}
+	bool useK = md.frame || md.ldmWgt != 0.0;
+	if (useK) {
+		KpcgWork &k = w.kw;
+		k.Ad = P.alloc<double>(n); k.Kid = P.alloc<double>(n); k.r = P.alloc<double>(n);
+		k.Kr = P.alloc<double>(n); k.dv = P.alloc<double>(n); k.wK = P.zeros<double>(n);
+		k.part = P.alloc<double>((size_t) 4 * nb + 16 * n + 64); k.scal = P.zeros<double>(32);
+		k.maxBlocks = nb;
+		w.K = P.alloc<double>((size_t) N * N);
+	}
+	if (wantTraj) {
+		w.trajX = P.zeros<double>((size_t) n * md.timeNum);
+	}
+	w.trajT = P.zeros<double>((size_t) N * md.timeNum);
+}
+
+__global__ void k_to_f32(long n, const double *a, float *b)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k < n) b[k] = (float) a[k];
+}
+
+struct SolveOut { int status; int cgTotal, rdTotal, cgMax; int inverted; };
+
+template <int D>
+static SolveOut forward_one(const Mesh &m, const Model &md, Work &w, const double *x0soa, const double *tauVar,
+                            cudaStream_t s)
+{
+	int N = m.N, T = md.timeNum;
+	long n = (long) N * D;
+	double dt = md.timeStp;
+	bool useK = md.frame || md.ldmWgt != 0.0;
+	SolveOut out{SA_OK, 0, 0, 0, 0};
+	Status *st = reinterpret_cast<Status *>(w.cw.scal + 24);   // inverted-element counter
+	SA_CHECK(cudaMemsetAsync(st, 0, sizeof(Status), s));
+	launch_soa_to_aos(N, D, x0soa, w.xa, s);
+	if (w.trajX) SA_CHECK(cudaMemcpyAsync(w.trajX, x0soa, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	launch_tau_initial<D>(m, md, tauVar, w.xa, w.trajT, s);
+	launch_elem_geom<D>(m, md, w.xa, w.g0, st, false, s);
+	launch_assemble_rd<D>(m, md, w.g0, dt, w.Mnow, w.L, w.dinvRd, s);
+	SA_CHECK(cudaMemsetAsync(w.v, 0, sizeof(double) * n, s));
+	if (useK) SA_CHECK(cudaMemsetAsync(w.kw.wK, 0, sizeof(double) * n, s));
+	Geom *gn = &w.g0, *gx = &w.g1;
+	double *xn = w.xa, *xx = w.xb;
+	for (int t = 0; t < T - 1; ++t) {
+		double *tauNow = w.trajT + (long) t * N, *tauNxt = w.trajT + (long) (t + 1) * N;
+		launch_activity<D>(m, md, tauNow, w.fy, w.fr, s);
+		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
+		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, s);
+		launch_yank_rhs<D>(m, *gn, w.fy, w.b, s);
+		int its = 0, code;
+		if (useK) {
+			launch_kernel_matrix<D>(md, N, xn, w.K, s);
+			code = kpcg<D>(m, md, w.blk, w.K, w.b, w.v, w.kw, st, &its, s);
+		} else {
+			if (md.precision == SA_PREC_MIXED)
+				k_to_f32<<<grid_for((long) m.Z * D * D), kBlock, 0, s>>>((long) m.Z * D * D, w.blk, w.cw.blk32);
+			code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st, &its, s,
+			                    md.precision);
+		}
+		out.cgTotal += its;
+		out.cgMax = std::max(out.cgMax, its);
+		if (code != SA_OK) { out.status = code; break; }
+		launch_advance<D>(N, xn, w.v, dt, xx, w.trajX ? w.trajX + (long) (t + 1) * n : nullptr, s);
+		launch_elem_geom<D>(m, md, xx, *gx, st, true, s);
+		launch_assemble_rd<D>(m, md, *gx, dt, w.Mnxt, w.L, w.dinvRd, s);
+		launch_rd_rhs<D>(m, *gn, w.Mnow, tauNow, w.fr, dt, w.rhs, s);
+		SA_CHECK(cudaMemcpyAsync(tauNxt, tauNow, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+		int rits = 0;
+		code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, tauNxt, md.rdItrMax, md.rdTolSqu, w.cw, st, &rits, s,
+		                    SA_PREC_FP64);
+		out.rdTotal += rits;
+		if (code != SA_OK) { out.status = code; break; }
+		std::swap(gn, gx);
+		std::swap(xn, xx);
+		std::swap(w.Mnow, w.Mnxt);
+	}
+	Status hs;
+	SA_CHECK(cudaMemcpyAsync(&hs, st, sizeof(Status), cudaMemcpyDeviceToHost, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	out.inverted = hs.inverted;
+	// final positions in interleaved form for the objective
+	if (xn != w.xa) SA_CHECK(cudaMemcpyAsync(w.xa, xn, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+	return out;
+}
+
+static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *tgt, Pool &P)
+{
+	memset(&md, 0, sizeof(md));
+	md.dim = dim;
+	SA_REQUIRE(p->elaType == SA_ELA_FRAME || p->elaType == SA_ELA_ISOTROPIC, "unknown elaType");
+	md.frame = p->elaType == SA_ELA_FRAME;
+	md.precision = p->precision;
+	SA_REQUIRE(md.precision == SA_PREC_FP64 || md.precision == SA_PREC_MIXED, "unknown precision");
+	SA_REQUIRE(!(md.frame && md.precision == SA_PREC_MIXED), "mixed precision is available for the layered model");
+	SA_REQUIRE(p->modVec && p->ynkActPrmVec && p->reaActPrmVec, "missing parameter vectors");
+	std::vector<double> mod = to_host(p->modVec, (size_t) p->modNum, P.s);
+	std::vector<double> ynk = to_host(p->ynkActPrmVec, md.frame ? 4 : 1, P.s);
+	std::vector<double> rea = to_host(p->reaActPrmVec, md.frame ? 5 : 1, P.s);
+	for (size_t k = 0; k < ynk.size(); ++k) md.ynk[k] = ynk[k];
+	for (size_t k = 0; k < rea.size(); ++k) md.rea[k] = rea[k];
+	if (p->tauPrmVec && p->tauPrmNum > 0) {
+		std::vector<double> tp = to_host(p->tauPrmVec, (size_t) std::min(p->tauPrmNum, 2), P.s);
+		for (size_t k = 0; k < tp.size(); ++k) md.tauPrm[k] = tp[k];
+	}
+	if (md.frame) {
+		SA_REQUIRE(p->modNum >= (dim == 2 ? 3 : 4), "frame modVec needs 3 (2D) / 4 (3D) values");
+		for (int k = 0; k < (dim == 2 ? 3 : 4); ++k) md.mod[k] = mod[k];
+		SA_REQUIRE(p->tauPrmNum >= (dim == 2 ? 1 : 2), "tauPrmVec too short");
+	} else {
+		SA_REQUIRE(p->lyrNum > 0 && p->modNum == 2 * p->lyrNum && p->spdLyrVec, "layer tables inconsistent");
+		md.lyrNum = p->lyrNum;
+		md.lyrMod = P.dev(p->modVec, (size_t) p->modNum);
+		md.lyrSpd = P.dev(p->spdLyrVec, (size_t) p->lyrNum);
+	}
+	md.spdTan = p->spdTanVal; md.spdTsv = p->spdTsvVal;
+	md.ldmWgt = p->ldmWgt; md.knlOrder = p->knlOrder; md.knlWidth = p->knlWidth; md.knlEps = p->knlEps;
+	SA_REQUIRE(md.knlOrder >= -1 && md.knlOrder <= 4, "knlOrder must be -1..4");
+	md.btmWgt = p->btmWgt; md.timeStp = p->timeStp; md.timeNum = p->timeNum;
+	md.cgItrMax = p->cgItrMax; md.cgTolSqu = p->cgTolSqu;
+	SA_REQUIRE(md.timeNum >= 1, "timeNum must be >= 1");
+	md.rdItrMax = p->rdItrMax > 0 ? p->rdItrMax : std::max(p->cgItrMax, 1000);
+	md.rdTolSqu = p->rdTolSqu > 0.0 ? p->rdTolSqu : (md.frame ? 1e-26 : p->cgTolSqu);
+	if (tgt) {
+		md.cenKnl = tgt->cenKnlType; md.dirKnl = tgt->dirKnlType;
+		md.cenWidth = tgt->cenKnlWidth; md.dirWidth = tgt->dirKnlWidth;
+		SA_REQUIRE(md.cenKnl == 'G' || md.cenKnl == 'C' || md.cenKnl == 'M', "cenKnlType must be G, C or M");
+		SA_REQUIRE(md.dirKnl == 'B' || md.dirKnl == 'L' || md.dirKnl == 'O' || md.dirKnl == 'U',
+		           "dirKnlType must be B, L, O or U");
+	}
+}
+
+static const size_t kDenseLimitBytes = (size_t) 16 << 30;   // dense RKHS matrix budget (frame mode)
+
+template <int D>
+static int forward_impl(sa_context *ctx, const sa_element_object *obj, const double *lmkIni, const sa_params *prm,
+                        const sa_target *tgt, const double *tauVarMat, int tauVarNum, int objNum, double *lmkStk,
+                        double *tauMat, double *objVec, sa_solve_info *info)
+{
+	cudaStream_t s = ctx->stream;
+	Pool P(s);
+	Mesh m;
+	Model md;
+	fill_model(md, D, prm, tgt, P);
+	build_mesh(m, obj, tgt != nullptr, false, !md.frame, md.lyrNum, P);
+	if (md.frame || md.ldmWgt != 0.0)
+		SA_REQUIRE((size_t) m.N * m.N * sizeof(double) <= kDenseLimitBytes && m.N <= 65535,
+		           "dense RKHS kernel matrix exceeds the device budget for this node count");
+	SA_REQUIRE(tauVarMat && tauVarNum >= (md.frame ? (D == 2 ? 4 : 4) : D + 2) && objNum >= 1,
+	           "tauVarMat too small");
+	const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
+	std::vector<double> tv = to_host(tauVarMat, (size_t) tauVarNum * objNum, s);
+	const double *tc = nullptr, *tu = nullptr, *tvl = nullptr;
+	if (tgt) {
+		SA_REQUIRE(tgt->tgtElmNum > 0 && tgt->cenPosMat && tgt->uniDirMat && tgt->elmVolVec, "empty target");
+		tc = P.dev(tgt->cenPosMat, (size_t) tgt->tgtElmNum * D);
+		tu = P.dev(tgt->uniDirMat, (size_t) tgt->tgtElmNum * D);
+		tvl = P.dev(tgt->elmVolVec, (size_t) tgt->tgtElmNum);
+	}
+	Work w;
+	alloc_work<D>(w, m, md, lmkStk != nullptr, P);
+	{   // initial element orientation for the Jacobian sign check
+		double *xa = P.alloc<double>((size_t) m.N * D);
+		launch_soa_to_aos(m.N, D, x0, xa, s);
+		k_init_sign<D><<<grid_for(m.E), kBlock, 0, s>>>(m.E, m.elmVtx, xa, m.sign0);
+	}
+	std::vector<double> objs(objNum, 0.0);
+	SolveOut last{};
+	SA_CHECK(cudaEventRecord(ctx->e0, s));
+	for (int k = 0; k < objNum; ++k) {
+		const double *tvk = tv.data() + (size_t) k * tauVarNum;
+		SolveOut o = forward_one<D>(m, md, w, x0, tvk, s);
+		last = o;
+		if (o.status == SA_ERR_NOT_CONVERGED || o.status == SA_ERR_BREAKDOWN || o.status == SA_ERR_NONFINITE) {
+			objs[k] = DBL_MAX;            // 2D_frame/deform.cu:68-73
+			continue;
+		}
+		if (tgt) {
+			int err = SA_OK;
+			// the interleaved final positions sit in w.xa after forward_one
+			objs[k] = varifold<D>(m, md, w.xa, tc, tu, tvl, tgt->tgtElmNum, nullptr, s, md.precision, &err);
+			SA_REQUIRE(err == SA_OK, "varifold arguments");
+		}
+	}
+	SA_CHECK(cudaEventRecord(ctx->e1, s));
+	SA_CHECK(cudaEventSynchronize(ctx->e1));
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, ctx->e0, ctx->e1);
+	long n = (long) m.N * D;
+	if (lmkStk) SA_CHECK(cudaMemcpyAsync(lmkStk, w.trajX, sizeof(double) * n * md.timeNum, cudaMemcpyDefault, s));
+	if (tauMat) SA_CHECK(cudaMemcpyAsync(tauMat, w.trajT, sizeof(double) * m.N * md.timeNum, cudaMemcpyDefault, s));
+	if (objVec) SA_CHECK(cudaMemcpyAsync(objVec, objs.data(), sizeof(double) * objNum, cudaMemcpyDefault, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	if (info) {
+		info->status = last.status;
+		info->cgIterTotal = last.cgTotal;
+		info->rdIterTotal = last.rdTotal;
+		info->cgIterMax = last.cgMax;
+		info->invertedElements = last.inverted;
+		info->elapsedMs = ms;
+	}
+	return SA_OK;
+}
+
+template <int D>
+static int varifold_impl(sa_context *ctx, const sa_element_object *obj, const double *lmk, const sa_target *tgt,
+                         int precision, double *objOut, double *grad)
+{
+	cudaStream_t s = ctx->stream;
+	Pool P(s);
+	Mesh m;
+	Model md;
+	memset(&md, 0, sizeof(md));
+	md.dim = D;
+	SA_REQUIRE(tgt && tgt->tgtElmNum > 0, "missing target");
+	md.cenKnl = tgt->cenKnlType; md.dirKnl = tgt->dirKnlType;
+	md.cenWidth = tgt->cenKnlWidth; md.dirWidth = tgt->dirKnlWidth;
+	SA_REQUIRE(md.cenKnl == 'G' || md.cenKnl == 'C' || md.cenKnl == 'M', "cenKnlType must be G, C or M");
+	SA_REQUIRE(md.dirKnl == 'B' || md.dirKnl == 'L' || md.dirKnl == 'O' || md.dirKnl == 'U',
+	           "dirKnlType must be B, L, O or U");
+	build_mesh(m, obj, true, grad != nullptr, false, 0, P);
+	const double *x = P.dev(lmk, (size_t) m.N * D);
+	double *xa = P.alloc<double>((size_t) m.N * D);
+	launch_soa_to_aos(m.N, D, x, xa, s);
+	const double *tc = P.dev(tgt->cenPosMat, (size_t) tgt->tgtElmNum * D);
+	const double *tu = P.dev(tgt->uniDirMat, (size_t) tgt->tgtElmNum * D);
+	const double *tvl = P.dev(tgt->elmVolVec, (size_t) tgt->tgtElmNum);
+	double *ga = grad ? P.alloc<double>((size_t) m.N * D) : nullptr;
+	int err = SA_OK;
+	double v = varifold<D>(m, md, xa, tc, tu, tvl, tgt->tgtElmNum, ga, s, precision, &err);
+	SA_REQUIRE(err == SA_OK, "varifold gradient needs vfdIfoMat");
+	*objOut = v;
+	if (grad) {
+		// back to the reference's column-major N x D layout
+		std::vector<double> h = to_host(ga, (size_t) m.N * D, s), o((size_t) m.N * D);
+		for (int i = 0; i < m.N; ++i)
+			for (int d = 0; d < D; ++d) o[(size_t) d * m.N + i] = h[(size_t) i * D + d];
+		SA_CHECK(cudaMemcpyAsync(grad, o.data(), sizeof(double) * o.size(), cudaMemcpyDefault, s));
+		SA_CHECK(cudaStreamSynchronize(s));
+	}
+	return SA_OK;
+}
+
+template <typename F>
+static int guarded(sa_context *ctx, F &&f)
+{
+	if (!ctx) return SA_ERR_ARG;
+	try {
+		SA_CHECK(cudaSetDevice(ctx->device));
+		int rc = f();
+		ctx->err.clear();
+		return rc;
+	} catch (const ArgError &e) {
+		ctx->err = e.msg;
+		return SA_ERR_ARG;
+	} catch (const CudaError &e) {
+		ctx->err = std::string(e.where) + ": " + cudaGetErrorString(e.e);
+		cudaGetLastError();
+		return SA_ERR_CUDA;
+	} catch (const std::bad_alloc &) {
+		ctx->err = "host allocation failed";
+		return SA_ERR_CUDA;
+	}
+}
+
+}  // namespace sa
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+int sa_create(sa_context **out, int device)
+{
+	if (!out) return SA_ERR_ARG;
+	*out = nullptr;
+	int count = 0;
+	if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+		cudaGetLastError();
+		return SA_ERR_CUDA;
+	}
+	sa_context *c = new sa_context();
+	c->device = device;
+	if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+	    cudaEventCreate(&c->e0) != cudaSuccess || cudaEventCreate(&c->e1) != cudaSuccess) {
+		cudaGetLastError();
+		delete c;
+		return SA_ERR_CUDA;
+	}
+	*out = c;
+	return SA_OK;
+}
+
+int sa_destroy(sa_context *c)
+{
+	if (!c) return SA_OK;
+	cudaSetDevice(c->device);
+	if (c->stream) cudaStreamSynchronize(c->stream);
+	if (c->e0) cudaEventDestroy(c->e0);
+	if (c->e1) cudaEventDestroy(c->e1);
+	if (c->stream) cudaStreamDestroy(c->stream);
+	delete c;
+	return SA_OK;
+}
+
+const char *sa_error_message(const sa_context *c) { return c ? c->err.c_str() : "no context"; }
+
+int sa_forward(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat, const sa_params *prm,
+               const sa_target *tgt, const double *tauVarMat, int tauVarNum, int objNum, double *lmkStk,
+               double *tauMat, double *objVec, sa_solve_info *info)
+{
+	return sa::guarded(ctx, [&]() {
+		SA_REQUIRE(obj && prm && lmkIniMat, "null argument");
+		if (obj->dim == 2)
+			return sa::forward_impl<2>(ctx, obj, lmkIniMat, prm, tgt, tauVarMat, tauVarNum, objNum, lmkStk, tauMat,
+			                           objVec, info);
+		SA_REQUIRE(obj->dim == 3, "dim must be 2 or 3");
+		return sa::forward_impl<3>(ctx, obj, lmkIniMat, prm, tgt, tauVarMat, tauVarNum, objNum, lmkStk, tauMat,
+		                           objVec, info);
+	});
+}
+
+int sa_varifold(sa_context *ctx, const sa_element_object *obj, const double *lmkMat, const sa_target *tgt,
+                int precision, double *objOut, double *gradMat)
+{
+	return sa::guarded(ctx, [&]() {
+		SA_REQUIRE(obj && lmkMat && objOut, "null argument");
+		if (obj->dim == 2) return sa::varifold_impl<2>(ctx, obj, lmkMat, tgt, precision, objOut, gradMat);
+		SA_REQUIRE(obj->dim == 3, "dim must be 2 or 3");
+		return sa::varifold_impl<3>(ctx, obj, lmkMat, tgt, precision, objOut, gradMat);
+	});
+}
+
+static void frame_object(sa_element_object &o, int dim, int lmkNum, const int *elmVtxMat, int elmNum,
+                         const int *vtxElmMat, int vtxElmCols, const int *frmVtxMat, const int *tsvVtxMat,
+                         const int *bdrVtxMat, int bdrElmNum, const int *vtxBdrMat, int vtxBdrCols,
+                         const int *btmVtxMat, int btmElmNum, const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols,
+                         const int *femVtxMat, int nzrNum, const int *femIfoMat, int femIfoCols)
+{
+	memset(&o, 0, sizeof(o));
+	o.dim = dim; o.lmkNum = lmkNum; o.elmNum = elmNum;
+	o.elmVtxMat = elmVtxMat; o.vtxElmMat = vtxElmMat; o.vtxElmCols = vtxElmCols;
+	o.frmVtxMat = frmVtxMat; o.tsvVtxMat = tsvVtxMat;
+	o.bdrVtxMat = bdrVtxMat; o.bdrElmNum = bdrElmNum; o.vtxBdrMat = vtxBdrMat; o.vtxBdrCols = vtxBdrCols;
+	o.btmVtxMat = btmVtxMat; o.btmElmNum = btmElmNum; o.vtxBtmMat = vtxBtmMat; o.btmLmkNum = btmLmkNum;
+	o.vtxBtmCols = vtxBtmCols; o.femVtxMat = femVtxMat; o.nzrNum = nzrNum; o.femIfoMat = femIfoMat;
+	o.femIfoCols = femIfoCols;
+}
+
+static void frame_params(sa_params &p, int dim, const double *tauPrmVec, int tauPrmNum, double ldmWgt, int knlOrder,
+                         double knlWidth, double knlEps, const double *modVec, double spdTanVal, double spdTsvVal,
+                         const double *ynk, const double *rea, double btmWgt, double timeStp, int timeNum,
+                         int cgItrMax, double cgTolSqu)
+{
+	memset(&p, 0, sizeof(p));
+	p.elaType = SA_ELA_FRAME; p.precision = SA_PREC_FP64;
+	p.tauPrmVec = tauPrmVec; p.tauPrmNum = tauPrmNum;
+	p.ldmWgt = ldmWgt; p.knlOrder = knlOrder; p.knlWidth = knlWidth; p.knlEps = knlEps;
+	p.modVec = modVec; p.modNum = dim == 2 ? 3 : 4;
+	p.spdTanVal = spdTanVal; p.spdTsvVal = spdTsvVal;
+	p.ynkActPrmVec = ynk; p.reaActPrmVec = rea;
+	p.btmWgt = btmWgt; p.timeStp = timeStp; p.timeNum = timeNum; p.cgItrMax = cgItrMax; p.cgTolSqu = cgTolSqu;
+}
+
+int sa_deformation_frame(sa_context *ctx, int dim, const double *tauVarMat, int tauVarNum, int objTotNum,
+                         const double *tauPrmVec, int tauPrmNum, const double *lmkIniMat, int lmkNum,
+                         const int *elmVtxMat, int elmNum, const int *vtxElmMat, int vtxElmCols,
+                         const int *frmVtxMat, const int *tsvVtxMat, const int *bdrVtxMat, int bdrElmNum,
+                         const int *vtxBdrMat, int vtxBdrCols, const int *btmVtxMat, int btmElmNum,
+                         const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols, const int *femVtxMat, int nzrNum,
+                         const int *femIfoMat, int femIfoCols, double ldmWgt, int knlOrder, double knlWidth,
+                         double knlEps, const double *modVec, double spdTanVal, double spdTsvVal,
+                         const double *ynkActPrmVec, const double *reaActPrmVec, double btmWgt, double timeStp,
+                         int timeNum, int cgItrMax, double cgTolSqu, double *lmkStk, double *tauMat, double *objVec)
+{
+	sa_element_object o;
+	frame_object(o, dim, lmkNum, elmVtxMat, elmNum, vtxElmMat, vtxElmCols, frmVtxMat, tsvVtxMat, bdrVtxMat,
+	             bdrElmNum, vtxBdrMat, vtxBdrCols, btmVtxMat, btmElmNum, vtxBtmMat, btmLmkNum, vtxBtmCols,
+	             femVtxMat, nzrNum, femIfoMat, femIfoCols);
+	sa_params p;
+	frame_params(p, dim, tauPrmVec, tauPrmNum, ldmWgt, knlOrder, knlWidth, knlEps, modVec, spdTanVal, spdTsvVal,
+	             ynkActPrmVec, reaActPrmVec, btmWgt, timeStp, timeNum, cgItrMax, cgTolSqu);
+	return sa_forward(ctx, &o, lmkIniMat, &p, nullptr, tauVarMat, tauVarNum, objTotNum, lmkStk, tauMat, objVec,
+	                  nullptr);
+}
+
+int sa_computeObjfcn_frame(sa_context *ctx, int dim, const double *tauVarMat, int tauVarNum, int objTotNum,
+                           const double *tauPrmVec, int tauPrmNum, const double *lmkIniMat, int lmkNum,
+                           const int *elmVtxMat, int elmNum, const int *vtxElmMat, int vtxElmCols,
+                           const int *frmVtxMat, const int *tsvVtxMat, const int *bdrVtxMat, int bdrElmNum,
+                           const int *vtxBdrMat, int vtxBdrCols, const int *btmVtxMat, int btmElmNum,
+                           const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols, const int *femVtxMat, int nzrNum,
+                           const int *femIfoMat, int femIfoCols, const int *vfdVtxMat, int vfdElmNum,
+                           const double *tgtCenPosMat, const double *tgtUniDirMat, const double *tgtElmVolVec,
+                           int tgtElmNum, double cenKnlType, double cenKnlWidth, double dirKnlType,
+                           double dirKnlWidth, double ldmWgt, int knlOrder, double knlWidth, double knlEps,
+                           const double *modVec, double spdTanVal, double spdTsvVal, const double *ynkActPrmVec,
+                           const double *reaActPrmVec, double btmWgt, double timeStp, int timeNum, int cgItrMax,
+                           double cgTolSqu, double *objVec)
+{
+	sa_element_object o;
+	frame_object(o, dim, lmkNum, elmVtxMat, elmNum, vtxElmMat, vtxElmCols, frmVtxMat, tsvVtxMat, bdrVtxMat,
+	             bdrElmNum, vtxBdrMat, vtxBdrCols, btmVtxMat, btmElmNum, vtxBtmMat, btmLmkNum, vtxBtmCols,
+	             femVtxMat, nzrNum, femIfoMat, femIfoCols);
+	o.vfdVtxMat = vfdVtxMat;
+	o.vfdElmNum = vfdElmNum;
+	sa_params p;
+	frame_params(p, dim, tauPrmVec, tauPrmNum, ldmWgt, knlOrder, knlWidth, knlEps, modVec, spdTanVal, spdTsvVal,
+	             ynkActPrmVec, reaActPrmVec, btmWgt, timeStp, timeNum, cgItrMax, cgTolSqu);
+	sa_target t;
+	memset(&t, 0, sizeof(t));
+	t.cenPosMat = tgtCenPosMat; t.uniDirMat = tgtUniDirMat; t.elmVolVec = tgtElmVolVec; t.tgtElmNum = tgtElmNum;
+	t.cenKnlType = (char) cenKnlType; t.cenKnlWidth = cenKnlWidth;
+	t.dirKnlType = (char) dirKnlType; t.dirKnlWidth = dirKnlWidth;
+	return sa_forward(ctx, &o, lmkIniMat, &p, &t, tauVarMat, tauVarNum, objTotNum, nullptr, nullptr, objVec,
+	                  nullptr);
+}
+
+}  // extern "C"

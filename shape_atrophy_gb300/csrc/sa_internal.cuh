@@ -1,0 +1,250 @@
+// sa_internal.cuh -- shared declarations of the shape_atrophy_gb300 CUDA library.
+//
+// Layout conventions (device):
+//   * node vectors are interleaved per node: x[i*D + d] (one 16/24-byte
+//     record per node, so element and block-row gathers read one record);
+//   * element data is structure-of-arrays over elements: a[k*E + e];
+//   * the reference's int32 index matrices are kept in their own
+//     column-major layout (entity index fastest), e.g. elmVtx[k*E + e];
+//   * the elasticity operator is a block CSR matrix on the femVtxMat
+//     pattern (D x D blocks, row-major inside a block), the mass and
+//     diffusion matrices are scalar CSR on the same pattern.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cfloat>
+#include <string>
+#include <vector>
+#include "../../include/shape_atrophy_gb300.h"
+
+namespace sa {
+
+constexpr int kBlock = 256;
+
+inline int grid_for(long n, int block = kBlock) { return (int) ((n + block - 1) / block); }
+
+// --------------------------------------------------------------------------
+// small fixed-size vector math (mirrors inc/matvec.h operation order)
+// --------------------------------------------------------------------------
+template <int D> struct Vec { double c[D]; };
+template <int D> struct Mat { double m[D][D]; };
+
+template <int D> __device__ __forceinline__ Vec<D> vsub(const Vec<D> &a, const Vec<D> &b)
+{ Vec<D> r; for (int d = 0; d < D; ++d) r.c[d] = a.c[d] - b.c[d]; return r; }
+
+template <int D> __device__ __forceinline__ double vdot(const Vec<D> &a, const Vec<D> &b)
+{ double s = a.c[0] * b.c[0]; for (int d = 1; d < D; ++d) s = s + a.c[d] * b.c[d]; return s; }
+
+template <int D> __device__ __forceinline__ Vec<D> load_node(const double *x, int i)
+{ Vec<D> v; for (int d = 0; d < D; ++d) v.c[d] = x[(long) i * D + d]; return v; }
+
+__device__ __forceinline__ Vec<3> vcross(const Vec<3> &x, const Vec<3> &y)
+{   // inc/matvec.h:503-510
+	Vec<3> r;
+	r.c[0] =  x.c[1] * y.c[2] - x.c[2] * y.c[1];
+	r.c[1] = -x.c[0] * y.c[2] + x.c[2] * y.c[0];
+	r.c[2] =  x.c[0] * y.c[1] - x.c[1] * y.c[0];
+	return r;
+}
+
+template <int D> __device__ __forceinline__ double det_edges(const Vec<D> *q);
+template <> __device__ __forceinline__ double det_edges<2>(const Vec<2> *q)
+{ return q[0].c[0] * q[1].c[1] - q[0].c[1] * q[1].c[0]; }                 // inc/matvec.h:250-253
+template <> __device__ __forceinline__ double det_edges<3>(const Vec<3> *q)
+{   // inc/matvec.h:592-600
+	const Vec<3> &x = q[0], &y = q[1], &z = q[2];
+	return  x.c[0] * y.c[1] * z.c[2] + x.c[1] * y.c[2] * z.c[0] + x.c[2] * y.c[0] * z.c[1]
+	      - x.c[0] * y.c[2] * z.c[1] - x.c[1] * y.c[0] * z.c[2] - x.c[2] * y.c[1] * z.c[0];
+}
+
+// inverse of Q = [q1-q0, q2-q0 (, q3-q0)] given the edge vectors and det(Q)
+template <int D> __device__ __forceinline__ Mat<D> inv_edges(const Vec<D> *q, double det);
+template <> __device__ __forceinline__ Mat<2> inv_edges<2>(const Vec<2> *q, double det)
+{   // inc/matvec.h:267-277
+	Mat<2> r;
+	r.m[0][0] =  q[1].c[1] / det; r.m[0][1] = -q[1].c[0] / det;
+	r.m[1][0] = -q[0].c[1] / det; r.m[1][1] =  q[0].c[0] / det;
+	return r;
+}
+template <> __device__ __forceinline__ Mat<3> inv_edges<3>(const Vec<3> *q, double det)
+{   // inc/matvec.h:627-649
+	const Vec<3> &x = q[0], &y = q[1], &z = q[2];
+	Mat<3> r;
+	r.m[0][0] =  (y.c[1] * z.c[2] - y.c[2] * z.c[1]) / det;
+	r.m[0][1] = -(y.c[0] * z.c[2] - y.c[2] * z.c[0]) / det;
+	r.m[0][2] =  (y.c[0] * z.c[1] - y.c[1] * z.c[0]) / det;
+	r.m[1][0] = -(x.c[1] * z.c[2] - x.c[2] * z.c[1]) / det;
+	r.m[1][1] =  (x.c[0] * z.c[2] - x.c[2] * z.c[0]) / det;
+	r.m[1][2] = -(x.c[0] * z.c[1] - x.c[1] * z.c[0]) / det;
+	r.m[2][0] =  (x.c[1] * y.c[2] - x.c[2] * y.c[1]) / det;
+	r.m[2][1] = -(x.c[0] * y.c[2] - x.c[2] * y.c[0]) / det;
+	r.m[2][2] =  (x.c[0] * y.c[1] - x.c[1] * y.c[0]) / det;
+	return r;
+}
+
+// gradient of barycentric coordinate a (0..D) from Q^{-1} stored SoA: QI[(r*D+c)*E+e]
+template <int D> __device__ __forceinline__ Vec<D> bary_grad(const double *QI, int E, int e, int a)
+{
+	Vec<D> g;
+	if (a > 0) {
+		for (int c = 0; c < D; ++c) g.c[c] = QI[((a - 1) * D + c) * (long) E + e];
+	} else {
+		for (int c = 0; c < D; ++c) {
+			double s = -QI[(0 * D + c) * (long) E + e];
+			for (int r = 1; r < D; ++r) s = s - QI[(r * D + c) * (long) E + e];
+			g.c[c] = s;
+		}
+	}
+	return g;
+}
+
+// --------------------------------------------------------------------------
+// activity functions (inc/activity.h:4-38, 106-167)
+// --------------------------------------------------------------------------
+__device__ __forceinline__ double yank_template(double t, double w)
+{
+	double a = 3.0 * (w - 2.0) / (w * w * w * (6.0 + w * (-6.0 + w)));
+	double b = (6.0 + w * (-15.0 + 8 * w)) / (3.0 * (w - 2.0));
+	double c = 6.0 / (6.0 + w * (-6.0 + w));
+	if (t < -1.0 || t >= 1.0) return 0.0;
+	if (t < -1.0 + w) return a * (t + 1.0) * (t + 1.0) * (t + 1.0) * (t - b);
+	if (t < 1.0 - w) return -c * t * t + 1.0;
+	return a * (-t + 1.0) * (-t + 1.0) * (-t + 1.0) * (-t - b);
+}
+
+__device__ __forceinline__ double reac_template(double t, double w, double a)
+{
+	double b1 = 8.0 * (6.0 * (a - 1.0) + a * w * (-6.0 + w)) / (3.0 * w * w * w * w);
+	double b2 = -(144.0 * (a - 1.0) + w * (24.0 * (5.0 - 11.0 * a) + w * (156.0 * a - w * 29.0 * a)))
+	            / (24.0 * (6.0 * (a - 1.0) + a * w * (-6.0 + w)));
+	double c1 = -(24.0 * (a - 1.0) + a * w * (-12.0 + w)) / (9.0 * w * w * w);
+	double c2 = -(24.0 * (a - 1.0) + w * (12.0 * (2.0 - 3.0 * a) + a * w * (13.0 + w * 2.0))) / (3.0 * w * w * w);
+	double c3 = -((w - 1.0) * (w - 1.0) * (24.0 * (a - 1.0) + a * w * (-12.0 + w))) / (3.0 * w * w * w);
+	double c4 = -(24.0 * (a - 1.0) + w * (12.0 * (6.0 - 7.0 * a)
+	              + w * (-72.0 + 109.0 * a + w * (3.0 * (5.0 - 21.0 * a) + a * w * (15.0 - w)))))
+	            / (9.0 * w * w * w);
+	if (t < -1.0 || t >= 1.0) return 0.0;
+	if (t < -1.0 + 0.5 * w) return b1 * (t + 1.0) * (t + 1.0) * (t + 1.0) * (t - b2);
+	if (t < -1.0 + w) return c4 + t * (c3 + t * (c2 + t * c1));
+	if (t < 1.0 - w) return -a * t * t + 1.0;
+	if (t < 1.0 - 0.5 * w) return c4 + t * (-c3 + t * (c2 - t * c1));
+	return b1 * (-t + 1.0) * (-t + 1.0) * (-t + 1.0) * (-t - b2);
+}
+
+// --------------------------------------------------------------------------
+// host-side structures
+// --------------------------------------------------------------------------
+struct Status {            // device-resident solver status (one per solve)
+	int code;              // SA_OK or an error code
+	int iters;             // iterations of the last CG solve
+	int done;              // current CG solve finished
+	int inverted;          // count of elements whose orientation flipped
+};
+
+struct Mesh {              // device copy of one element object + derived tables
+	int dim, V, N, E, Z, Bt, Nb, Vd;
+	int vtxElmCols, vtxBtmCols, femIfoCols, vfdIfoCols, frmCols, tsvCols;
+	int *elmVtx = nullptr, *vtxElm = nullptr, *frmVtx = nullptr, *tsvVtx = nullptr;
+	int *btmVtx = nullptr, *vtxBtm = nullptr, *femVtx = nullptr, *femIfo = nullptr;
+	int *vfdVtx = nullptr, *vfdIfo = nullptr, *elmLyr = nullptr;
+	int *rowPtr = nullptr;     // N+1 (from femVtxMat rows)
+	int *diagSlot = nullptr;   // N
+	int *asmTab = nullptr;     // femIfoCols/2-1 x Z: e*16 + a*4 + b, femIfo order
+	int asmCols = 0;
+	signed char *sign0 = nullptr;  // initial orientation of each element
+	std::vector<void *> owned;
+};
+
+struct Geom {              // per-element geometry of one configuration
+	double *QI = nullptr;      // D*D x E
+	double *absDet = nullptr;  // E   |det Q|
+	double *vol = nullptr;     // E   computeVolume
+	double *frm = nullptr;     // D x E frame: tangent (2D) / normal (3D)
+	double *tsv = nullptr;     // D x E transverse direction
+};
+
+// the full parameter set of one forward solve (device pointers resolved)
+struct Model {
+	int dim, frame;            // frame = reference frame elasticity, else layered isotropic
+	int lyrNum;
+	double mod[4];             // frame moduli
+	const double *lyrMod = nullptr;   // device: lambda,mu per layer
+	const double *lyrSpd = nullptr;   // device: D per layer
+	double spdTan, spdTsv;
+	double ynk[4], rea[5];
+	double tauPrm[2];
+	double ldmWgt; int knlOrder; double knlWidth, knlEps;
+	double btmWgt, timeStp; int timeNum, cgItrMax; double cgTolSqu;
+	int rdItrMax; double rdTolSqu;
+	char cenKnl, dirKnl; double cenWidth, dirWidth;
+	int precision;             // SA_PREC_FP64 or SA_PREC_MIXED
+};
+
+// --------------------------------------------------------------------------
+// kernels and launchers (defined in the .cu files)
+// --------------------------------------------------------------------------
+template <int D> void launch_elem_geom(const Mesh &m, const Model &md, const double *x, Geom &g,
+                                       Status *st, bool check, cudaStream_t s);
+template <int D> void launch_activity(const Mesh &m, const Model &md, const double *tau, double *fy,
+                                      double *fr, cudaStream_t s);
+template <int D> void launch_tau_initial(const Mesh &m, const Model &md, const double *tauVar,
+                                         const double *x, double *tau, cudaStream_t s);
+template <int D> void launch_yank_rhs(const Mesh &m, const Geom &g, const double *fy, double *b,
+                                      cudaStream_t s);
+template <int D> void launch_penalty_diag(const Mesh &m, const Model &md, const double *x, double *pd,
+                                          cudaStream_t s);
+template <int D> void launch_assemble_elastic(const Mesh &m, const Model &md, const Geom &g,
+                                              const double *pd, double *blk, double *dinv, cudaStream_t s);
+template <int D> void launch_assemble_rd(const Mesh &m, const Model &md, const Geom &g, double dt,
+                                         double *Mval, double *Lval, double *dinv, cudaStream_t s);
+template <int D> void launch_rd_rhs(const Mesh &m, const Geom &gNow, const double *Mnow, const double *tau,
+                                    const double *fr, double dt, double *rhs, cudaStream_t s);
+template <int D> void launch_advance(int N, const double *x, const double *v, double dt, double *xn,
+                                     double *trajSlot, cudaStream_t s);
+void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_t s);
+
+// block-CSR matvec y = A x (B = block size 1..3), FP64
+template <int B> void launch_bsr_spmv(const Mesh &m, const double *blk, const double *x, double *y,
+                                      cudaStream_t s);
+
+// --------------------------------------------------------------------------
+// CG solvers
+// --------------------------------------------------------------------------
+struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
+	double *r, *u, *w, *p, *sv;   // n each
+	double *part;                 // partial sums: 3 x maxBlocks
+	double *scal;                 // device scalars
+	int maxBlocks;
+	float *blk32 = nullptr;       // FP32 copy of the operator (mixed precision)
+	float *f32 = nullptr;         // 7 n FP32 vectors of the inner solve (mixed precision)
+	double *xr = nullptr;         // 3 n FP64 refinement scratch
+};
+
+template <int B> int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double *b,
+                               double *x, int itrMax, double tolSqu, CgWork &w, Status *st,
+                               int *itersOut, cudaStream_t s, int precision);
+
+// frame mode K-preconditioned CG (2D/ipcg.cu:11-100) with dense K
+struct KpcgWork {
+	double *Ad, *Kid, *r, *Kr, *dv, *wK;  // wK tracks K^{-1} x
+	double *part, *scal;
+	int maxBlocks;
+};
+template <int D> int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *b,
+                          double *x, KpcgWork &w, Status *st, int *itersOut, cudaStream_t s);
+template <int D> void launch_kernel_matrix(const Model &md, int N, const double *x, double *K, cudaStream_t s);
+
+// varifold objective (and node gradient) of a shape
+template <int D> double varifold(const Mesh &m, const Model &md, const double *x, const double *tgtCen,
+                                 const double *tgtDir, const double *tgtVol, int Vt, double *grad,
+                                 cudaStream_t s, int precision, int *err);
+
+// deterministic sum of n doubles on the device (returned via host)
+double device_sum(const double *v, long n, double *scratch, cudaStream_t s);
+
+// error helpers
+struct CudaError { cudaError_t e; const char *where; };
+#define SA_CHECK(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) throw ::sa::CudaError{_e, #x}; } while (0)
+
+}  // namespace sa

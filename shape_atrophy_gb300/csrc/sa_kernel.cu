@@ -1,0 +1,462 @@
+// sa_kernel.cu -- RKHS kernel matrix and the K-preconditioned CG of frame mode.
+//
+// Reference: 2D_frame/computeKernel.cu:7-209 (2D Matern through x^2 K0(x) and
+// x K1(x), inc/polybesselk.h:8-99 with the rational-approximation tables of
+// inc/besselk.h), 3D_frame/computeKernel.cu:5-153 (closed-form Matern
+// n + 1/2), 2D_frame/addEpsIdentity.cu:3-20, and the CG of
+// 2D_frame/ipcg.cu:11-100 with ipcgWholeMatrixMultiplication.cu:21-45,
+// ipcgSecondMatrixMultiplication.cu:8-24, ipcgKernelMultiplication.cu:5-17.
+//
+// GB300 changes: scalars and the stopping test stay on the device (the
+// reference returns every dot product to the host), and the dense Cholesky
+// of K is gone.  The reference needs potrs(K, x0) only for the warm start
+// x0 = v_prev; here the solve tracks w = K^{-1} x through the CG recurrences
+// (w += alpha K^{-1}d, with K^{-1}d already tracked as KidVec) and starts the
+// next step from x0 = K_new w_prev, whose K_new^{-1} x0 = w_prev is known
+// exactly.  The converged velocity is the same solution of the same system
+// to the CG tolerance.
+#include "sa_internal.cuh"
+#include <cmath>
+
+namespace sa {
+
+// rational-approximation coefficients (inc/besselk.h:4-180), same values
+__constant__ double cP01[6] = { 2.4708152720399552679e+03,  5.9169059852270512312e+03,
+                                4.6850901201934832188e+02,  1.1999463724910714109e+01,
+                                1.3166052564989571850e-01,  5.8599221412826100000e-04};
+__constant__ double cQ01[3] = { 2.1312714303849120380e+04, -2.4994418972832303646e+02, 1};
+__constant__ double cP02[4] = {-4.0320340761145482298e+05, -1.7733784684952985886e+04,
+                               -2.9601657892958843866e+02, -1.6414452837299064100e+00};
+__constant__ double cQ02[4] = {-1.6128136304458193998e+06,  2.9865713163054025489e+04,
+                               -2.5064972445877992730e+02,  1};
+__constant__ double cP03[10] = { 1.1600249425076035558e+02,  2.3444738764199315021e+03,
+                                 1.8321525870183537725e+04,  7.1557062783764037541e+04,
+                                 1.5097646353289914539e+05,  1.7398867902565686251e+05,
+                                 1.0577068948034021957e+05,  3.1075408980684392399e+04,
+                                 3.6832589957340267940e+03,  1.1394980557384778174e+02};
+__constant__ double cQ03[11] = { 9.2556599177304839811e+01,  1.8821890840982713696e+03,
+                                 1.4847228371802360957e+04,  5.8824616785857027752e+04,
+                                 1.2689839587977598727e+05,  1.5144644673520157801e+05,
+                                 9.7418829762268075784e+04,  3.1474655750295278825e+04,
+                                 4.4329628889746408858e+03,  2.0013443064949242491e+02, 1};
+__constant__ double cP11[6] = {-2.2149374878243304548e+06,  7.1938920065420586101e+05,
+                                1.7733324035147015630e+05,  7.1885382604084798576e+03,
+                                9.9991373567429309922e+01,  4.8127070456878442310e-01};
+__constant__ double cQ11[4] = {-2.2149374878243304548e+06,  3.7264298672067697862e+04,
+                               -2.8143915754538725829e+02,  1};
+__constant__ double cP12[5] = {-1.3531161492785421328e+06, -1.4758069205414222471e+05,
+                               -4.5051623763436087023e+03, -5.3103913335180275253e+01,
+                               -2.2795590826955002390e-01};
+__constant__ double cQ12[4] = {-2.7062322985570842656e+06,  4.3117653211351080007e+04,
+                               -3.0507151578787595807e+02,  1};
+__constant__ double cP13[11] = { 2.2196792496874548962e+00,  4.4137176114230414036e+01,
+                                 3.4122953486801312910e+02,  1.3319486433183221990e+03,
+                                 2.8590657697910288226e+03,  3.4540675585544584407e+03,
+                                 2.3123742209168871550e+03,  8.1094256146537402173e+02,
+                                 1.3182609918569941308e+02,  7.5584584631176030810e+00,
+                                 6.4257745859173138767e-02};
+__constant__ double cQ13[10] = { 1.7710478032601086579e+00,  3.4552228452758912848e+01,
+                                 2.5951223655579051357e+02,  9.6929165726802648634e+02,
+                                 1.9448440788918006154e+03,  2.1181000487171943810e+03,
+                                 1.2082692316002348638e+03,  3.3031020088765390854e+02,
+                                 3.6001069306861518855e+01,  1};
+
+__device__ __forceinline__ double polyval(int deg, const double *c, double x)
+{
+	double v = c[deg];
+	for (int i = deg - 1; i >= 0; --i) v = v * x + c[i];
+	return v;
+}
+
+__device__ double p0fcn(double x)
+{   // x^2 K0(x): inc/polybesselk.h:17-54
+	if (x < DBL_EPSILON || x > 700.0) return 0.0;
+	if (x <= 1.0) {
+		double xs = x * x, lx = log(x);
+		double PQ01 = polyval(5, cP01, xs) / polyval(2, cQ01, xs);
+		double PQ02 = polyval(3, cP02, xs) / polyval(3, cQ02, xs);
+		return xs * (PQ01 - lx * (xs * PQ02 + 1.0));
+	}
+	double xi = 1.0 / x;
+	return x * sqrt(x) * exp(-x) * (polyval(9, cP03, xi) / polyval(10, cQ03, xi));
+}
+
+__device__ double p1fcn(double x)
+{   // x K1(x): inc/polybesselk.h:56-99
+	if (x < DBL_EPSILON) return 1.0;
+	if (x > 700.0) return 0.0;
+	if (x <= 1.0) {
+		double xs = x * x, lx = log(x);
+		double PQ11 = polyval(5, cP11, xs) / polyval(3, cQ11, xs);
+		double PQ12 = polyval(4, cP12, xs) / polyval(3, cQ12, xs);
+		return PQ11 + xs * lx * PQ12;
+	}
+	double xi = 1.0 / x;
+	return sqrt(x) * exp(-x) * (polyval(10, cP13, xi) / polyval(9, cQ13, xi));
+}
+
+template <int D>
+__device__ __forceinline__ double kernel_value(int order, double w, double d2)
+{
+	if (D == 2) {
+		if (order == -1) return exp(-(d2 / (w * w)));
+		double dij = sqrt(d2) / w, dsq = dij * dij;
+		double f1 = p1fcn(dij), f0 = order > 0 ? p0fcn(dij) : 0.0;
+		switch (order) {
+		case 0: return f1;
+		case 1: return 0.5 * (f0 + 2.0 * f1);
+		case 2: return (4.0 * f0 + (8.0 + dsq) * f1) / 8.0;
+		case 3: return ((24.0 + dsq) * f0 + 8.0 * (6.0 + dsq) * f1) / 48.0;
+		default: return (12.0 * (16.0 + dsq) * f0 + (384.0 + dsq * (72.0 + dsq)) * f1) / 384.0;
+		}
+	}
+	if (order == -1) return exp(-(d2 / (w * w)));
+	double r = sqrt(d2) / w, ex = exp(-r);
+	switch (order) {
+	case 0: return ex;
+	case 1: return (1.0 + r) * ex;
+	case 2: return (3.0 + r * (3.0 + r)) / 3.0 * ex;
+	case 3: return (15.0 + r * (15.0 + r * (6.0 + r))) / 15.0 * ex;
+	default: return (105.0 + r * (105.0 + r * (45.0 + r * (10.0 + r)))) / 105.0 * ex;
+	}
+}
+
+// K[j*N + i] = k(|q_i - q_j| / w) + eps * delta_ij
+template <int D>
+__global__ void k_kernel_matrix(int N, const double *__restrict__ x, int order, double w, double eps,
+                                double *__restrict__ K)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	int j = blockIdx.y;
+	if (i >= N) return;
+	Vec<D> qi = load_node<D>(x, i), qj = load_node<D>(x, j);
+	double d2 = (qi.c[0] - qj.c[0]) * (qi.c[0] - qj.c[0]);
+	for (int d = 1; d < D; ++d) d2 = d2 + (qi.c[d] - qj.c[d]) * (qi.c[d] - qj.c[d]);
+	double v = kernel_value<D>(order, w, d2);
+	if (i == j) v += eps;
+	K[(long) j * N + i] = v;
+}
+
+template <int D>
+void launch_kernel_matrix(const Model &md, int N, const double *x, double *K, cudaStream_t s)
+{
+	dim3 g(grid_for(N, 128), N);
+	k_kernel_matrix<D><<<g, 128, 0, s>>>(N, x, md.knlOrder, md.knlWidth, md.knlEps, K);
+}
+
+// ---------------------------------------------------------------------------
+// dense K X for D interleaved columns: partial sums over column slices
+// ---------------------------------------------------------------------------
+constexpr int kDenseRows = 128, kDenseSlices = 16, kDenseTile = 128;
+
+template <int D>
+__global__ void k_dense_partial(int N, const double *__restrict__ K, const double *__restrict__ X,
+                                double *__restrict__ part)
+{
+	__shared__ double xs[kDenseTile * D];
+	int i = blockIdx.x * kDenseRows + threadIdx.x;
+	int s = blockIdx.y;
+	int per = (N + kDenseSlices - 1) / kDenseSlices;
+	int j0 = s * per, j1 = min(N, j0 + per);
+	double acc[D];
+	for (int d = 0; d < D; ++d) acc[d] = 0.0;
+	for (int jt = j0; jt < j1; jt += kDenseTile) {
+		int nt = min(kDenseTile, j1 - jt);
+		__syncthreads();
+		for (int t = threadIdx.x; t < nt * D; t += blockDim.x) xs[t] = X[(long) jt * D + t];
+		__syncthreads();
+		if (i < N)
+			for (int jj = 0; jj < nt; ++jj) {
+				double k = K[(long) (jt + jj) * N + i];
+				for (int d = 0; d < D; ++d) acc[d] += k * xs[jj * D + d];
+			}
+	}
+	if (i < N)
+		for (int d = 0; d < D; ++d) part[((long) s * N + i) * D + d] = acc[d];
+}
+
+template <int D>
+__global__ void k_dense_sum(int N, const double *__restrict__ part, double *__restrict__ Y)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k >= (long) N * D) return;
+	double s = 0.0;
+	for (int t = 0; t < kDenseSlices; ++t) s += part[(long) t * N * D + k];
+	Y[k] = s;
+}
+
+template <int D>
+void launch_dense_matvec(int N, const double *K, const double *x, double *y, double *part, cudaStream_t s)
+{
+	dim3 g(grid_for(N, kDenseRows), kDenseSlices);
+	k_dense_partial<D><<<g, kDenseRows, 0, s>>>(N, K, x, part);
+	k_dense_sum<D><<<grid_for((long) N * D), kBlock, 0, s>>>(N, part, y);
+}
+
+
+// ---------------------------------------------------------------------------
+// K-preconditioned CG (reference ipcg) with device scalars
+// ---------------------------------------------------------------------------
+struct KScal {
+	double bSqu, rSqu, rKr, rKrNew, dAd, alpha, beta, tolSqu, ldmWgt;
+	int done, code, iters, itrMax;
+	unsigned int counter;
+	int pad;
+};
+
+constexpr int kKBlock = 256;
+
+template <int K>
+__device__ __forceinline__ bool kreduce(double (&v)[K], double *part, unsigned int *counter)
+{
+	__shared__ double sm[K][kKBlock / 32];
+	__shared__ bool last;
+	int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int k = 0; k < K; ++k)
+		for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+	if (lane == 0) for (int k = 0; k < K; ++k) sm[k][wid] = v[k];
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		for (int k = 0; k < K; ++k) {
+			double s = 0.0;
+			for (int w = 0; w < kKBlock / 32; ++w) s += sm[k][w];
+			part[k * gridDim.x + blockIdx.x] = s;
+		}
+		__threadfence();
+		unsigned int t = atomicAdd(counter, 1u);
+		last = (t == gridDim.x - 1);
+	}
+	__syncthreads();
+	return last;
+}
+
+template <int K>
+__device__ __forceinline__ void kfinish(double (&out)[K], const double *part)
+{
+	int lane = threadIdx.x & 31;
+	for (int k = 0; k < K; ++k) {
+		double s = 0.0;
+		for (int b = lane; b < (int) gridDim.x; b += 32) s += __ldcg(part + k * gridDim.x + b);
+		for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+		out[k] = s;
+	}
+}
+
+// (b, b): zero rhs gives x = 0, w = 0
+template <int D>
+__global__ void k_kp_bnorm(int N, const double *__restrict__ b, double *part, KScal *sc)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double v[1] = {0.0};
+	if (i < N) for (int d = 0; d < D; ++d) v[0] += b[(long) i * D + d] * b[(long) i * D + d];
+	if (!kreduce<1>(v, part, &sc->counter)) return;
+	double o[1]; kfinish<1>(o, part);
+	if (threadIdx.x == 0) {
+		sc->bSqu = o[0];
+		if (!isfinite(o[0])) { sc->code = SA_ERR_NONFINITE; sc->done = 1; }
+		else if (o[0] == 0.0) sc->done = 2;          // x = 0
+		sc->counter = 0;
+	}
+}
+
+// r = b - (ldm w + Bx0), (r, r)
+template <int D>
+__global__ void k_kp_init_r(int N, const int *__restrict__ rowPtr, const int *__restrict__ col,
+                            const double *__restrict__ blk, const double *__restrict__ b,
+                            const double *__restrict__ x, const double *__restrict__ w, double *__restrict__ r,
+                            double *part, KScal *sc)
+{
+	if (sc->done) return;
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double v[1] = {0.0};
+	if (i < N) {
+		double acc[D];
+		for (int d = 0; d < D; ++d) acc[d] = 0.0;
+		for (int z = rowPtr[i]; z < rowPtr[i + 1]; ++z) {
+			int j = col[z];
+			const double *a = blk + (long) z * D * D;
+			for (int rr = 0; rr < D; ++rr)
+				for (int c = 0; c < D; ++c) acc[rr] += a[rr * D + c] * x[(long) j * D + c];
+		}
+		for (int d = 0; d < D; ++d) {
+			long k = (long) i * D + d;
+			double Ax = sc->ldmWgt * w[k] + acc[d];
+			double rk = 1.0 * b[k] + -1.0 * Ax;
+			r[k] = rk;
+			v[0] += rk * rk;
+		}
+	}
+	if (!kreduce<1>(v, part, &sc->counter)) return;
+	double o[1]; kfinish<1>(o, part);
+	if (threadIdx.x == 0) {
+		sc->rSqu = o[0];
+		if (!isfinite(o[0])) { sc->code = SA_ERR_NONFINITE; sc->done = 1; }
+		else if (o[0] < sc->bSqu * sc->tolSqu) sc->done = 1;
+		sc->counter = 0;
+	}
+}
+
+// (r, Kr) after Kr = K r; first = 1: initialise Kid = r, d = Kr; else beta and the d / Kid updates
+template <int D>
+__global__ void k_kp_rkr(int N, const double *__restrict__ r, const double *__restrict__ Kr, double *part,
+                         KScal *sc, int first)
+{
+	if (sc->done) return;
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double v[1] = {0.0};
+	if (i < N) for (int d = 0; d < D; ++d) v[0] += r[(long) i * D + d] * Kr[(long) i * D + d];
+	if (!kreduce<1>(v, part, &sc->counter)) return;
+	double o[1]; kfinish<1>(o, part);
+	if (threadIdx.x == 0) {
+		if (o[0] == 0.0 || !isfinite(o[0])) {
+			sc->code = isfinite(o[0]) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
+			sc->done = 1;
+		} else if (first) {
+			sc->rKr = o[0];
+		} else {
+			sc->beta = o[0] / sc->rKr;
+			sc->rKr = o[0];
+		}
+		sc->counter = 0;
+	}
+}
+
+// Kid = r + beta Kid; d = Kr + beta d (first: Kid = r, d = Kr)
+template <int D>
+__global__ void k_kp_dir(int N, const double *__restrict__ r, const double *__restrict__ Kr, double *__restrict__ Kid,
+                         double *__restrict__ dv, const KScal *sc, int first)
+{
+	if (sc->done) return;
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k >= (long) N * D) return;
+	if (first) { Kid[k] = r[k]; dv[k] = Kr[k]; return; }
+	double be = sc->beta;
+	Kid[k] = 1.0 * r[k] + be * Kid[k];
+	dv[k] = 1.0 * Kr[k] + be * dv[k];
+}
+
+// Bd = (E + btm P) d; Ad = ldm Kid + Bd; (d, Ad) -> alpha
+template <int D>
+__global__ void k_kp_ad(int N, const int *__restrict__ rowPtr, const int *__restrict__ col,
+                        const double *__restrict__ blk, const double *__restrict__ dv, const double *__restrict__ Kid,
+                        double *__restrict__ Ad, double *part, KScal *sc)
+{
+	if (sc->done) return;
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double v[1] = {0.0};
+	if (i < N) {
+		double acc[D];
+		for (int d = 0; d < D; ++d) acc[d] = 0.0;
+		for (int z = rowPtr[i]; z < rowPtr[i + 1]; ++z) {
+			int j = col[z];
+			const double *a = blk + (long) z * D * D;
+			for (int rr = 0; rr < D; ++rr)
+				for (int c = 0; c < D; ++c) acc[rr] += a[rr * D + c] * dv[(long) j * D + c];
+		}
+		for (int d = 0; d < D; ++d) {
+			long k = (long) i * D + d;
+			double a = sc->ldmWgt * Kid[k] + 1.0 * acc[d];
+			Ad[k] = a;
+			v[0] += dv[k] * a;
+		}
+	}
+	if (!kreduce<1>(v, part, &sc->counter)) return;
+	double o[1]; kfinish<1>(o, part);
+	if (threadIdx.x == 0) {
+		sc->dAd = o[0];
+		if (o[0] == 0.0 || !isfinite(o[0])) {
+			sc->code = isfinite(o[0]) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
+			sc->done = 1;
+		} else sc->alpha = sc->rKr / o[0];
+		sc->counter = 0;
+	}
+}
+
+// x += alpha d; w += alpha Kid; r -= alpha Ad; (r, r) -> stop test
+template <int D>
+__global__ void k_kp_step(int N, double *__restrict__ x, double *__restrict__ w, double *__restrict__ r,
+                          const double *__restrict__ dv, const double *__restrict__ Kid,
+                          const double *__restrict__ Ad, double *part, KScal *sc)
+{
+	if (sc->done) return;
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double v[1] = {0.0};
+	if (i < N) {
+		double al = sc->alpha;
+		for (int d = 0; d < D; ++d) {
+			long k = (long) i * D + d;
+			x[k] = 1.0 * x[k] + al * dv[k];
+			w[k] = w[k] + al * Kid[k];
+			double rk = 1.0 * r[k] + -al * Ad[k];
+			r[k] = rk;
+			v[0] += rk * rk;
+		}
+	}
+	if (!kreduce<1>(v, part, &sc->counter)) return;
+	double o[1]; kfinish<1>(o, part);
+	if (threadIdx.x == 0) {
+		sc->rSqu = o[0];
+		sc->iters += 1;
+		if (!isfinite(o[0])) { sc->code = SA_ERR_NONFINITE; sc->done = 1; }
+		else if (o[0] < sc->bSqu * sc->tolSqu) sc->done = 1;
+		else if (sc->iters >= sc->itrMax) { sc->code = SA_ERR_NOT_CONVERGED; sc->done = 1; }
+		sc->counter = 0;
+	}
+}
+
+__global__ void k_kp_zero(long n, double *x, double *w, const KScal *sc)
+{
+	if (sc->done != 2) return;
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k < n) { x[k] = 0.0; w[k] = 0.0; }
+}
+
+template <int D>
+int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *b, double *x,
+         KpcgWork &wk, Status *st, int *itersOut, cudaStream_t s)
+{
+	(void) st;
+	int N = m.N;
+	long n = (long) N * D;
+	int nb = grid_for(N, kKBlock);
+	KScal h{};
+	h.tolSqu = md.cgTolSqu; h.itrMax = md.cgItrMax; h.ldmWgt = md.ldmWgt;
+	KScal *sc = (KScal *) wk.scal;
+	SA_CHECK(cudaMemcpyAsync(sc, &h, sizeof(KScal), cudaMemcpyHostToDevice, s));
+	double *dpart = wk.part + 4 * (long) nb;     // dense matvec slice partials
+	k_kp_bnorm<D><<<nb, kKBlock, 0, s>>>(N, b, wk.part, sc);
+	// warm start x0 = K w (w = K^{-1} v of the previous step)
+	launch_dense_matvec<D>(N, K, wk.wK, x, dpart, s);
+	k_kp_init_r<D><<<nb, kKBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, b, x, wk.wK, wk.r, wk.part, sc);
+	launch_dense_matvec<D>(N, K, wk.r, wk.Kr, dpart, s);
+	k_kp_rkr<D><<<nb, kKBlock, 0, s>>>(N, wk.r, wk.Kr, wk.part, sc, 1);
+	k_kp_dir<D><<<grid_for(n), kBlock, 0, s>>>(N, wk.r, wk.Kr, wk.Kid, wk.dv, sc, 1);
+	const int chunk = 8;
+	for (int it = 0; it < md.cgItrMax + chunk; it += chunk) {
+		for (int k = 0; k < chunk; ++k) {
+			k_kp_ad<D><<<nb, kKBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
+			k_kp_step<D><<<nb, kKBlock, 0, s>>>(N, x, wk.wK, wk.r, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
+			launch_dense_matvec<D>(N, K, wk.r, wk.Kr, dpart, s);
+			k_kp_rkr<D><<<nb, kKBlock, 0, s>>>(N, wk.r, wk.Kr, wk.part, sc, 0);
+			k_kp_dir<D><<<grid_for(n), kBlock, 0, s>>>(N, wk.r, wk.Kr, wk.Kid, wk.dv, sc, 0);
+		}
+		SA_CHECK(cudaGetLastError());
+		SA_CHECK(cudaMemcpyAsync(&h, sc, sizeof(KScal), cudaMemcpyDeviceToHost, s));
+		SA_CHECK(cudaStreamSynchronize(s));
+		if (h.done) break;
+	}
+	k_kp_zero<<<grid_for(n), kBlock, 0, s>>>(n, x, wk.wK, sc);
+	SA_CHECK(cudaMemcpyAsync(&h, sc, sizeof(KScal), cudaMemcpyDeviceToHost, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	if (itersOut) *itersOut = h.iters;
+	return h.code;
+}
+
+template void launch_kernel_matrix<2>(const Model &, int, const double *, double *, cudaStream_t);
+template void launch_kernel_matrix<3>(const Model &, int, const double *, double *, cudaStream_t);
+template int kpcg<2>(const Mesh &, const Model &, const double *, const double *, const double *, double *,
+                     KpcgWork &, Status *, int *, cudaStream_t);
+template int kpcg<3>(const Mesh &, const Model &, const double *, const double *, const double *, double *,
+                     KpcgWork &, Status *, int *, cudaStream_t);
+
+}  // namespace sa

@@ -1,0 +1,258 @@
+// sa_varifold.cu -- varifold objective and its node gradient.
+//
+// Reference: 2D_frame/varifold.cu (3D_frame/varifold.cu):
+//   landmarksToVarifoldKernel :9-36 (3D :9-43)      -> k_vfd_elems
+//   geometricFunction / grassmanFunction :38-179    -> cen_knl / dir_knl
+//   vfd_DD_DT, vfd_TT, vfd_TT_TD, vfd_DD :181-357   -> k_vfd_rows (one thread per row, the
+//       same row/column roles and per-row accumulation order, column tiles staged in shared
+//       memory so a CTA reads each column record once per tile instead of once per thread)
+//   dqVfd_DD_DT + dqVfdGather :359-498 (3D :372-530) -> k_vfd_rows (gradient) + k_vfd_gather
+//   dsum (2D_frame/dsum.cu:6-73)                     -> device_sum (same 512-wide tree order)
+// The Matern-3/2 centre kernel 'M' (1 + r/w) exp(-r/w) is the layered model's addition.
+//
+// Mixed precision: pair terms in FP32 with FP32 sums inside each column tile,
+// tile sums accumulated in FP64 per row, FP64 final reduction.
+#include "sa_internal.cuh"
+#include <cmath>
+
+namespace sa {
+
+constexpr int kVfdTile = 128;
+
+template <typename T>
+__device__ __forceinline__ T cen_knl(int type, T w, T d2, T &d1)
+{
+	if (type == 'G') { T k = exp(-d2 / (w * w)); d1 = (T) -2.0 * k / (w * w); return k; }
+	if (type == 'C') { T k = (T) 1.0 / ((T) 1.0 + d2 / (w * w)); d1 = (T) -2.0 * k * k / (w * w); return k; }
+	T r = sqrt(d2) / w, ex = exp(-r);           // 'M'
+	d1 = -ex / (w * w);
+	return ((T) 1.0 + r) * ex;
+}
+
+template <typename T>
+__device__ __forceinline__ T dir_knl(int type, T w, T ang, T &d1)
+{
+	if (type == 'B') { d1 = (T) 2.0 * ang; return ang * ang; }
+	if (type == 'L') { d1 = (T) 1.0; return ang; }
+	if (type == 'O') { T k = exp((T) 2.0 * (ang - (T) 1.0) / (w * w)); d1 = (T) 2.0 * k / (w * w); return k; }
+	T k = exp((T) 2.0 * (ang * ang - (T) 1.0) / (w * w));     // 'U'
+	d1 = (T) 4.0 * ang * k / (w * w);
+	return k;
+}
+
+template <int D>
+__global__ void k_vfd_elems(int N, int Vd, const int *__restrict__ vfdVtx, const double *__restrict__ x,
+                            double *__restrict__ cen, double *__restrict__ dir, double *__restrict__ vol)
+{
+	int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= Vd) return;
+	Vec<D> q0 = load_node<D>(x, vfdVtx[e]), q1 = load_node<D>(x, vfdVtx[Vd + e]);
+	Vec<D> c, u;
+	double v;
+	if (D == 2) {
+		for (int d = 0; d < D; ++d) c.c[d] = 0.5 * (q0.c[d] + q1.c[d]);
+		u = vsub(q1, q0);
+		v = sqrt(vdot(u, u));
+		for (int d = 0; d < D; ++d) u.c[d] /= v;
+		vol[e] = v;
+	} else {
+		Vec<3> a0 = load_node<3>(x, vfdVtx[e]), a1 = load_node<3>(x, vfdVtx[Vd + e]);
+		Vec<3> a2 = load_node<3>(x, vfdVtx[2 * Vd + e]);
+		Vec<3> cr = vcross(vsub(a1, a0), vsub(a2, a0));
+		v = sqrt(vdot(cr, cr));
+		for (int d = 0; d < 3; ++d) { c.c[d] = (a0.c[d] + a1.c[d] + a2.c[d]) / 3.0; u.c[d] = cr.c[d] / v; }
+		vol[e] = 0.5 * v;
+	}
+	for (int d = 0; d < D; ++d) { cen[d * (long) Vd + e] = c.c[d]; dir[d * (long) Vd + e] = u.c[d]; }
+}
+
+struct VfdSet { const double *cen, *dir, *vol; int n; };
+
+// out[i] = sum_j c1 K(i, j) over set A  +  sum_j c2 K(i, j) over set B (B may be empty);
+// gradient rows (dc, dt) when grad != 0 (rows must be the deformed set).
+template <int D, typename T>
+__global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, int ck, double cw, int dk,
+                           double dw, double *__restrict__ out, int grad, double *__restrict__ dc,
+                           double *__restrict__ dt)
+{
+	__shared__ T sc[kVfdTile * D], su[kVfdTile * D], sv[kVfdTile];
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	bool act = i < R.n;
+	T ci[D], ui[D], vi = 0;
+	for (int d = 0; d < D; ++d) {
+		ci[d] = act ? (T) R.cen[d * (long) R.n + i] : (T) 0;
+		ui[d] = act ? (T) R.dir[d * (long) R.n + i] : (T) 0;
+	}
+	if (act) vi = (T) R.vol[i];
+	const T nLen = (D == 2 ? vi : (T) 2.0 * vi), half = (D == 2 ? (T) 1.0 : (T) 0.5);
+	double acc = 0.0, gc[D], gt[D];
+	for (int d = 0; d < D; ++d) { gc[d] = 0.0; gt[d] = 0.0; }
+	const T cwT = (T) cw, dwT = (T) dw;
+	for (int set = 0; set < 2; ++set) {
+		const VfdSet &S = set == 0 ? A : Bs;
+		T coef = (T) (set == 0 ? cA : cB);
+		// gradient weights of dqVfd_DD_DT: +2 for the deformed-deformed term (both ends move), -2 for
+		// the deformed-target term
+		T gco = (T) (set == 0 ? 2.0 * cA : cB);
+		for (int j0 = 0; j0 < S.n; j0 += kVfdTile) {
+			int nt = min(kVfdTile, S.n - j0);
+			__syncthreads();
+			for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+				for (int d = 0; d < D; ++d) {
+					sc[t * D + d] = (T) S.cen[d * (long) S.n + j0 + t];
+					su[t * D + d] = (T) S.dir[d * (long) S.n + j0 + t];
+				}
+				sv[t] = (T) S.vol[j0 + t];
+			}
+			__syncthreads();
+			if (!act) continue;
+			T tile = 0, tgc[D], tgt[D];
+			for (int d = 0; d < D; ++d) { tgc[d] = 0; tgt[d] = 0; }
+			for (int jj = 0; jj < nt; ++jj) {
+				T d2 = (ci[0] - sc[jj * D]) * (ci[0] - sc[jj * D]);
+				for (int d = 1; d < D; ++d) d2 = d2 + (ci[d] - sc[jj * D + d]) * (ci[d] - sc[jj * D + d]);
+				T ang = ui[0] * su[jj * D];
+				for (int d = 1; d < D; ++d) ang = ang + ui[d] * su[jj * D + d];
+				T d1c, d1d;
+				T kc = cen_knl<T>(ck, cwT, d2, d1c);
+				T kd = dir_knl<T>(dk, dwT, ang, d1d);
+				T vj = sv[jj];
+				tile += coef * kc * kd * vi * vj;
+				if (grad) {
+					// geometricFunction/grassmanFunction gradients and dqVfd_DD_DT accumulation
+					for (int d = 0; d < D; ++d) {
+						T dK = d1c * (ci[d] - sc[jj * D + d]);
+						T tK = d1d / nLen * (-ang * ui[d] + su[jj * D + d]);
+						tgc[d] += gco * dK * kd * vi * vj;
+						tgt[d] += gco * kc * (tK * vi + kd * half * ui[d]) * vj;
+					}
+				}
+			}
+			acc += (double) tile;
+			if (grad) for (int d = 0; d < D; ++d) { gc[d] += (double) tgc[d]; gt[d] += (double) tgt[d]; }
+		}
+	}
+	if (!act) return;
+	out[i] = acc;
+	if (grad)
+		for (int d = 0; d < D; ++d) { dc[d * (long) R.n + i] = gc[d]; dt[d * (long) R.n + i] = gt[d]; }
+}
+
+// node gradient gather (2D_frame/varifold.cu:435-466, 3D_frame :492-528)
+template <int D>
+__global__ void k_vfd_gather(int N, int Vd, const int *__restrict__ ifo, const double *__restrict__ x,
+                             const double *__restrict__ dc, const double *__restrict__ dt, double *__restrict__ g)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	double s[D];
+	for (int d = 0; d < D; ++d) s[d] = 0.0;
+	int cnt = ifo[i];
+	for (int a = 0; a < cnt; ++a) {
+		if (D == 2) {
+			int e = ifo[(1 + 2 * a) * (long) N + i], sg = ifo[(2 + 2 * a) * (long) N + i];
+			for (int d = 0; d < D; ++d) s[d] += 0.5 * dc[d * (long) Vd + e] + sg * dt[d * (long) Vd + e];
+		} else {
+			int e = ifo[(1 + 3 * a) * (long) N + i];
+			int qa = ifo[(2 + 3 * a) * (long) N + i], qb = ifo[(3 + 3 * a) * (long) N + i];
+			Vec<3> t, ab;
+			for (int d = 0; d < 3; ++d) {
+				t.c[d] = dt[d * (long) Vd + e];
+				ab.c[d] = x[(long) qa * 3 + d] - x[(long) qb * 3 + d];
+			}
+			Vec<3> cr = vcross(t, ab);
+			for (int d = 0; d < 3; ++d) s[d] += dc[d * (long) Vd + e] / 3.0 + cr.c[d];
+		}
+	}
+	for (int d = 0; d < D; ++d) g[(long) i * D + d] = s[d];
+}
+
+// ---------------------------------------------------------------------------
+// reference dsum order: 512-wide shared-memory trees, accumulated per block
+// across 512*512 runs, then a final 512 tree (2D_frame/dsum.cu:6-73)
+// ---------------------------------------------------------------------------
+constexpr int kSum = 512;
+
+__global__ void k_dsum_tree(double *buf, const double *v, int len, int small)
+{
+	__shared__ double s[kSum];
+	int t = threadIdx.x, g = blockIdx.x * blockDim.x + t;
+	s[t] = g < len ? v[g] : 0.0;
+	__syncthreads();
+	for (int stride = blockDim.x >> 1; stride > 0; stride >>= 1) {
+		if (t < stride) s[t] += s[t + stride];
+		__syncthreads();
+	}
+	if (t == 0) {
+		if (small) buf[0] = s[0];
+		else buf[blockIdx.x] += s[0];
+	}
+}
+
+double device_sum(const double *v, long n, double *scratch, cudaStream_t s)
+{
+	// scratch: kSum + 1 doubles
+	double h = 0.0;
+	if (n < kSum) {
+		k_dsum_tree<<<1, kSum, 0, s>>>(scratch + kSum, v, (int) n, 1);
+	} else {
+		SA_CHECK(cudaMemsetAsync(scratch, 0, sizeof(double) * kSum, s));
+		long run = (long) kSum * kSum;
+		long runNum = (n - 1) / run + 1;
+		for (long r = 0; r < runNum; ++r) {
+			long lenNow = (r == runNum - 1 ? n - r * run : run);
+			int blk = (int) ((lenNow - 1) / kSum + 1);
+			k_dsum_tree<<<blk, kSum, 0, s>>>(scratch, v + r * run, (int) lenNow, 0);
+		}
+		k_dsum_tree<<<1, kSum, 0, s>>>(scratch + kSum, scratch, kSum, 1);
+	}
+	SA_CHECK(cudaMemcpyAsync(&h, scratch + kSum, sizeof(double), cudaMemcpyDeviceToHost, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	return h;
+}
+
+template <int D>
+double varifold(const Mesh &m, const Model &md, const double *x, const double *tgtCen, const double *tgtDir,
+                const double *tgtVol, int Vt, double *grad, cudaStream_t s, int precision, int *err)
+{
+	int Vd = m.Vd;
+	*err = SA_OK;
+	if (grad && !m.vfdIfo) { *err = SA_ERR_ARG; return 0.0; }
+	double *buf = nullptr;
+	size_t need = (size_t) Vd * (2 * D + 1) + (size_t) (Vd + Vt) + kSum + 1 + (grad ? (size_t) 2 * D * Vd : 0);
+	SA_CHECK(cudaMallocAsync(&buf, sizeof(double) * need, s));
+	double *cen = buf, *dir = cen + (long) D * Vd, *vol = dir + (long) D * Vd, *vfd = vol + Vd;
+	double *scr = vfd + Vd + Vt, *dc = scr + kSum + 1, *dt = dc + (long) D * Vd;
+	k_vfd_elems<D><<<grid_for(Vd), kBlock, 0, s>>>(m.N, Vd, m.vfdVtx, x, cen, dir, vol);
+	VfdSet Ds{cen, dir, vol, Vd}, Ts{tgtCen, tgtDir, tgtVol, Vt}, E0{nullptr, nullptr, nullptr, 0};
+	int ck = md.cenKnl, dk = md.dirKnl;
+	const int blk = 128;
+	auto rows = [&](VfdSet R, VfdSet A, double cA, VfdSet B, double cB, double *out, int g) {
+		if (R.n == 0) return;
+		if (precision == SA_PREC_MIXED)
+			k_vfd_rows<D, float><<<grid_for(R.n, blk), blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk,
+			                                                        md.dirWidth, out, g, dc, dt);
+		else
+			k_vfd_rows<D, double><<<grid_for(R.n, blk), blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk,
+			                                                         md.dirWidth, out, g, dc, dt);
+	};
+	if (grad || Vd >= Vt) {
+		rows(Ds, Ds, 1.0, Ts, -2.0, vfd, grad ? 1 : 0);      // vfd_DD_DT / dqVfd_DD_DT
+		rows(Ts, Ts, 1.0, E0, 0.0, vfd + Vd, 0);             // vfd_TT
+	} else {
+		rows(Ts, Ts, 1.0, Ds, -2.0, vfd, 0);                 // vfd_TT_TD
+		rows(Ds, Ds, 1.0, E0, 0.0, vfd + Vt, 0);             // vfd_DD
+	}
+	SA_CHECK(cudaGetLastError());
+	double obj = device_sum(vfd, Vd + Vt, scr, s);
+	if (grad) k_vfd_gather<D><<<grid_for(m.N), kBlock, 0, s>>>(m.N, Vd, m.vfdIfo, x, dc, dt, grad);
+	SA_CHECK(cudaFreeAsync(buf, s));
+	return obj;
+}
+
+template double varifold<2>(const Mesh &, const Model &, const double *, const double *, const double *,
+                            const double *, int, double *, cudaStream_t, int, int *);
+template double varifold<3>(const Mesh &, const Model &, const double *, const double *, const double *,
+                            const double *, int, double *, cudaStream_t, int, int *);
+
+}  // namespace sa
