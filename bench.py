@@ -1,0 +1,273 @@
+"""Benchmark: 3D layered shell time steps per second on GB300.
+
+Workload (default): the 3D layered spherical shell -- icosphere level 5
+(10242 surface vertices) x 9 node layers (8 prism layers, 3 tets each) =
+92178 nodes, 491520 P1 tets, 3 material layers, Fisher-KPP + isotropic
+elasticity, Jacobi-PCG tolerance 1e-8, dt 0.01, plain FP64.  A "step" is
+one time step of the forward model (velocity solve, node update,
+reaction-diffusion solve).  Inputs are synthetic (seeded mesh + bump), the
+per-step working set (operator blocks, geometry, CG vectors, ~0.3 GB) is
+larger than the 129 MB L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py --impl reference ...   # CPU restatement on the host cores
+
+With N > 1 (torchrun) every rank runs its own replica of the workload (the
+model does not shard: independent solves only), value = sum over ranks of
+steps / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3D shell steps/s"
+WORKLOAD = ("3D layered spherical shell: icosphere level 5 x 8 prism layers, 92178 nodes, 491520 P1 tets, "
+            "3 material layers, Fisher-KPP + layered isotropic elasticity, Jacobi-PCG 1e-8, dt 0.01")
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return rank, local, ws, dist
+
+
+def reduce_max(x: float, dist, local: int) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = f"cuda:{local}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.proc, self.path = gpu, None, None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def spec_for(args, steps: int):
+    from shape_atrophy_gb300 import problems
+    if args.workload == "annulus":
+        return problems.annulus_layered(steps=steps)
+    return problems.shell_layered(steps=steps)
+
+
+def cpu_sample(spec_full, seconds: float = 25.0, max_steps: int = 3):
+    """Time the CPU oracle (all host cores, OpenMP) on the first steps of the same workload."""
+    from oracle.oracle import Problem
+
+    def run(k):
+        spec = dict(spec_full)
+        spec["timeNum"] = k + 1
+        P = Problem(spec)
+        t0 = time.perf_counter()
+        r = P.forward(spec["tauVarVec"], with_obj=False)
+        dt = time.perf_counter() - t0
+        if r["status"] != 0:
+            raise RuntimeError("oracle solve failed")
+        return dt
+
+    t_total, steps = run(1), 1                 # one step first, then as many as fit the time budget
+    k = int(min(max_steps, max(1, seconds // max(t_total, 1e-3))))
+    if k > 1:
+        t_total, steps = run(k), k
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return steps / t_total, cores, f"first {steps} time step(s) of the same shell workload, {t_total:.1f} s"
+
+
+def run_reference(args, rank, ws, dist):
+    """CPU restatement of the model on the host cores (the reference has no CPU path of its own)."""
+    if rank != 0:
+        return
+    spec = spec_for(args, 4)
+    value, cores, sample = cpu_sample(spec, seconds=min(90.0, 20.0 * max(1, args.steps)), max_steps=3)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="shell", choices=["shell", "annulus"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    args = ap.parse_args()
+    rank, local, ws, dist = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws, dist)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from shape_atrophy_gb300 import api
+
+    K, W = args.steps, max(3, args.warmup)
+    spec = spec_for(args, W + K)
+    sess = api.Session(spec, precision=args.precision, objective=False, device=local)
+    sess.step(W)                                       # untimed warm-up steps
+    sess.profile(1)                                    # CUDA-event timing of the velocity matvec
+    launches0 = sess.info()["kernelLaunches"]
+    clk = ClockSampler(local)
+    clk.start()
+    barrier(dist)
+    done = sess.step(K)                                # timed: device events around exactly K steps
+    info = sess.info()
+    clocks = clk.stop()
+    if done != K or info["status"] != 0:
+        raise RuntimeError(f"solve stopped after {done} of {K} steps, status {info['status']}")
+    ms_dev = info["lastStepMs"]
+    ms_max = reduce_max(ms_dev, dist, local)
+    barrier(dist)
+    spmv_ms, spmv_cnt, spmv_bytes = sess.profile(0)
+    launches = info["kernelLaunches"] - launches0
+    cg_iters = info["cgIterTotal"]
+    sess.close()
+
+    value = ws * K / (ms_max / 1000.0)
+    hbm, peak_kind = peaks()
+    avg_launch_s = (spmv_ms / spmv_cnt) / 1000.0 if spmv_cnt else float("nan")
+    achieved = spmv_bytes / avg_launch_s / 1e9 if spmv_cnt else None
+    D = 3
+    Z = spec["elmObj"]["femVtxMat"].shape[1]
+    fp64_flops = 2.0 * Z * D * D if args.precision == "fp64" else None
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "k_cg_spmv_shell_l5_traffic.txt")
+    if os.path.exists(tfile) and args.precision == "fp64" and args.workload == "shell":
+        for line in open(tfile):
+            if line.startswith("dram_bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                "kernel": "k_cg_spmv (velocity block-CSR matvec + dot)", "peak_source": peak_kind,
+                "bytes_per_launch": spmv_bytes, "avg_launch_us": avg_launch_s * 1e6, "launches": spmv_cnt}
+    if fp64_flops:
+        roofline["fp64_pipe"] = {"achieved_tflops": fp64_flops / avg_launch_s / 1e12, "peak_tflops": 1.19,
+                                 "frac": fp64_flops / avg_launch_s / 1e12 / 1.19,
+                                 "peak_source": "measured FP64 FMA loop on this pool's GB300"}
+
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        spec_e = spec_for(args, K)
+        t0 = time.perf_counter()
+        r = api.forward(spec_e, trajectory=True, objective=True, precision=args.precision, device=local)
+        wall = time.perf_counter() - t0
+        obj = spec_e["elmObj"]
+        h2d = spec_e["lmkIniMat"].nbytes + sum(v.nbytes for k, v in obj.items() if hasattr(v, "nbytes")) + \
+            sum(a.nbytes for a in spec_e["tgt"]) + 8 * len(spec_e["tauVarVec"])
+        d2h = r["lmkStk"].nbytes + r["tauMat"].nbytes + r["obj"].nbytes
+        e2e = {"value": K / wall, "unit": "steps/s", "h2d_bytes_per_step": h2d // K, "d2h_bytes_per_step": d2h // K,
+               "what": f"one sa_forward call ({K} steps + objective) with host buffers: mesh upload and set-up, "
+                       "solve, trajectory download"}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and ws == 1:
+        v, cores, sample = cpu_sample(spec_for(args, 4))
+        cpu = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": K, "warmup": W,
+                "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD if args.workload == "shell" else "2D layered annulus 4096 nodes",
+                           "precision": args.precision, "nodes": spec["lmkIniMat"].shape[1],
+                           "elements": spec["elmObj"]["elmVtxMat"].shape[1], "cg_iters_per_step": cg_iters / K,
+                           "l2": "per-step working set (~0.3 GB) larger than the 129 MB L2",
+                           "parallelism": f"replicas x{ws}"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "gpu_launches": launches}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -114,7 +114,8 @@ typedef struct sa_solve_info {
 	int rdIterTotal;           /* reaction-diffusion CG iterations, all steps */
 	int cgIterMax;             /* largest per-step velocity iteration count */
 	int invertedElements;      /* elements whose orientation flipped (Jacobian sign check) */
-	double elapsedMs;          /* device time of the solves */
+	double elapsedMs;          /* device time of the solves (sessions: of the last step call) */
+	long long kernelLaunches;  /* CUDA kernels launched by the solve (sessions: since creation) */
 } sa_solve_info;
 
 int sa_create(sa_context **ctx, int device);
@@ -138,6 +139,27 @@ int sa_forward(sa_context *ctx, const sa_element_object *obj, const double *lmkI
  * Replaces varifold() (CUDA/2D_frame/varifold.cu:500-543). */
 int sa_varifold(sa_context *ctx, const sa_element_object *obj, const double *lmkMat,
                 const sa_target *tgt, int precision, double *obj_out, double *gradMat);
+
+/* Stepwise solve of one parameter vector (no reference counterpart: the
+ * reference runs all timeNum-1 steps inside one call).  A session keeps
+ * mesh, state and solver work device-resident; sa_session_step advances up
+ * to nsteps time steps (never past timeNum-1, stopping early on a failed
+ * solve), sa_session_state copies the current nodes (N x dim) and
+ * concentration (N), sa_session_objective evaluates the varifold objective
+ * of the current shape (needs a target at creation).  sa_session_profile
+ * switches CUDA-event timing of the velocity matvec kernel on or off and
+ * returns its accumulated time, launch count and algorithmic bytes per
+ * launch. */
+typedef struct sa_session sa_session;
+int sa_session_create(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat,
+                      const sa_params *prm, const sa_target *tgt, const double *tauVarVec, int tauVarNum,
+                      sa_session **out);
+int sa_session_step(sa_session *s, int nsteps, int *stepsDone);
+int sa_session_state(sa_session *s, double *lmkMat, double *tauVec, int *step);
+int sa_session_objective(sa_session *s, double *obj);
+int sa_session_info(sa_session *s, sa_solve_info *info);
+int sa_session_profile(sa_session *s, int enable, double *spmvMs, long long *spmvCount, double *spmvBytes);
+int sa_session_destroy(sa_session *s);
 
 /* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and
  * deformation_3D_frame (dim 3): arguments in prhs order

@@ -57,7 +57,7 @@ class Target(C.Structure):
 class SolveInfo(C.Structure):
     _fields_ = [
         ("status", C.c_int), ("cgIterTotal", C.c_int), ("rdIterTotal", C.c_int), ("cgIterMax", C.c_int),
-        ("invertedElements", C.c_int), ("elapsedMs", C.c_double),
+        ("invertedElements", C.c_int), ("elapsedMs", C.c_double), ("kernelLaunches", C.c_longlong),
     ]
 
 
@@ -82,6 +82,14 @@ def load():
     lib.sa_forward.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Params), C.POINTER(Target), _dp,
                                C.c_int, C.c_int, _dp, _dp, _dp, C.POINTER(SolveInfo)]
     lib.sa_varifold.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Target), C.c_int, _dp, _dp]
+    lib.sa_session_create.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Params), C.POINTER(Target),
+                                      _dp, C.c_int, C.POINTER(vp)]
+    lib.sa_session_step.argtypes = [vp, C.c_int, _ip]
+    lib.sa_session_state.argtypes = [vp, _dp, _dp, _ip]
+    lib.sa_session_objective.argtypes = [vp, _dp]
+    lib.sa_session_info.argtypes = [vp, C.POINTER(SolveInfo)]
+    lib.sa_session_profile.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp]
+    lib.sa_session_destroy.argtypes = [vp]
     _LIB = lib
     return lib
 

@@ -169,6 +169,73 @@ def varifold(spec: dict, lmk, grad: bool = False, precision: str = "fp64", devic
     return (out.value, g) if grad else out.value
 
 
+class Session:
+    """Stepwise solve of one parameter vector with device-resident state."""
+
+    def __init__(self, spec: dict, tauVarVec=None, precision: str = "fp64", objective: bool = True,
+                 device: int = 0):
+        self.ctx = context(device)
+        self.D = int(spec["dim"])
+        self.K = _Keep()
+        lmk = np.ascontiguousarray(np.asarray(spec["lmkIniMat"], dtype=np.float64))
+        self.N = lmk.shape[1]
+        with_obj = objective and spec.get("tgt") is not None
+        o = _element_object(spec["elmObj"], self.D, self.N, self.K, with_vfd=with_obj)
+        if spec["elaType"] == "isotropic" and "elmLyrVec" in spec:
+            o.elmLyrVec = self.K.i32(spec["elmLyrVec"])
+        p = _params(spec, self.K, precision)
+        t = _target(spec, self.K) if with_obj else None
+        tv = np.ascontiguousarray(np.asarray(spec["tauVarVec"] if tauVarVec is None else tauVarVec,
+                                             dtype=np.float64).reshape(-1))
+        self.h = C.c_void_p()
+        rc = self.ctx.lib.sa_session_create(self.ctx.h, C.byref(o), lmk.ctypes.data_as(_lib._dp), C.byref(p),
+                                            C.byref(t) if t is not None else None, tv.ctypes.data_as(_lib._dp),
+                                            tv.size, C.byref(self.h))
+        self.ctx.check(rc, "sa_session_create")
+
+    def step(self, n: int = 1) -> int:
+        done = C.c_int()
+        self.ctx.check(self.ctx.lib.sa_session_step(self.h, int(n), C.byref(done)), "sa_session_step")
+        return done.value
+
+    def state(self):
+        lmk = np.zeros((self.D, self.N))
+        tau = np.zeros(self.N)
+        t = C.c_int()
+        self.ctx.check(self.ctx.lib.sa_session_state(self.h, lmk.ctypes.data_as(_lib._dp),
+                                                     tau.ctypes.data_as(_lib._dp), C.byref(t)), "sa_session_state")
+        return lmk, tau, t.value
+
+    def objective(self) -> float:
+        v = C.c_double()
+        self.ctx.check(self.ctx.lib.sa_session_objective(self.h, C.byref(v)), "sa_session_objective")
+        return v.value
+
+    def info(self) -> dict:
+        i = _lib.SolveInfo()
+        self.ctx.check(self.ctx.lib.sa_session_info(self.h, C.byref(i)), "sa_session_info")
+        return dict(status=i.status, cgIterTotal=i.cgIterTotal, rdIterTotal=i.rdIterTotal, cgIterMax=i.cgIterMax,
+                    invertedElements=i.invertedElements, lastStepMs=i.elapsedMs, kernelLaunches=i.kernelLaunches)
+
+    def profile(self, enable: int = -1):
+        """enable=1/0 switches matvec timing on/off (and resets it); returns (ms, launches, bytes/launch)."""
+        ms, cnt, by = C.c_double(), C.c_longlong(), C.c_double()
+        self.ctx.check(self.ctx.lib.sa_session_profile(self.h, int(enable), C.byref(ms), C.byref(cnt),
+                                                       C.byref(by)), "sa_session_profile")
+        return ms.value, cnt.value, by.value
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.sa_session_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ---------------------------------------------------------------------------
 # the reference's MATLAB wrappers
 # ---------------------------------------------------------------------------

@@ -19,6 +19,7 @@
 // an inner CG with FP64 dot products, inside an FP64 iterative-refinement
 // loop whose residual b - A x is recomputed with the FP64 operator.
 #include "sa_internal.cuh"
+#include <algorithm>
 #include <cmath>
 
 namespace sa {
@@ -261,7 +262,7 @@ static CgScal read_scal(const CgScal *d, cudaStream_t s)
 template <int B, typename TM, typename TV, typename TX>
 static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double *b, TX *x, const double *q,
                      TV *r, TV *u, TV *w, TV *p, TV *sv, double *part, CgScal *sc, int itrMax, double tolSqu,
-                     double bb, cudaStream_t s)
+                     double bb, cudaStream_t s, CgWork *prof = nullptr)
 {
 	int N = m.N, nb = grid_for(N, kCgBlock);
 	long n = (long) N * B;
@@ -270,16 +271,35 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
 	k_cg_init<B, TV><<<nb, kCgBlock, 0, s>>>(N, b, q, dinv, r, u, part, sc);
 	const int chunk = 16;
+	bool timing = prof && prof->profileEnabled && prof->profileOn;
+	if (timing && !prof->ev[0])
+		for (int k = 0; k < 2 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
+	int itersBefore = 0;
 	for (int it = 0; it < itrMax + chunk; it += chunk) {
 		for (int k = 0; k < chunk; ++k) {
+			if (timing) SA_CHECK(cudaEventRecord(prof->ev[2 * k], s));
 			k_cg_spmv<B, TM, TV><<<nb, kCgBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, u, w, part, sc);
+			if (timing) SA_CHECK(cudaEventRecord(prof->ev[2 * k + 1], s));
 			k_cg_update<B, TV, TX><<<nb, kCgBlock, 0, s>>>(N, x, r, u, w, p, sv, dinv, part, sc);
 		}
 		SA_CHECK(cudaGetLastError());
+		if (prof) prof->launches += 2 * chunk;
 		CgScal h = read_scal(sc, s);
+		if (timing) {
+			// matvec launches that did work in this chunk = iterations completed in it
+			int worked = std::min(chunk, h.iters - itersBefore);
+			for (int k = 0; k < worked; ++k) {
+				float ms = 0.f;
+				SA_CHECK(cudaEventElapsedTime(&ms, prof->ev[2 * k], prof->ev[2 * k + 1]));
+				prof->spmvMs += ms;
+			}
+			prof->spmvCount += worked;
+			itersBefore = h.iters;
+		}
 		if (h.done) break;
 	}
 	k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
+	if (prof) prof->launches += 2;          // k_cg_init + k_cg_zero
 	return read_scal(sc, s);
 }
 
@@ -300,8 +320,9 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 	CgScal *sc = (CgScal *) wk.scal;
 	if (precision == SA_PREC_FP64 || !wk.blk32) {
 		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, x, q);
+		wk.launches += 1;
 		CgScal h = run_cg<B, double, double, double>(m, blk, dinv, b, x, q, wk.r, wk.u, wk.w, wk.p, wk.sv,
-		                                              wk.part, sc, itrMax, tolSqu, -1.0, s);
+		                                              wk.part, sc, itrMax, tolSqu, -1.0, s, &wk);
 		if (itersOut) *itersOut = h.iters;
 		return h.code;
 	}
@@ -320,6 +341,7 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 	for (int outer = 0; outer < 64; ++outer) {
 		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, x, q);
 		k_sub<<<grid_for(n), kBlock, 0, s>>>(n, b, q, rin);
+		wk.launches += 4;                     // spmv64, sub, init, axpy of this outer step
 		// outer test: |b - A x|^2 < tol^2 |b|^2 (k_cg_init with b and q gives both norms)
 		set_scal(sc, tolSqu, 1, bb, s);
 		k_cg_init<B, float><<<nb, kCgBlock, 0, s>>>(N, b, q, dinv32, r32, u32, wk.part, sc);
@@ -334,7 +356,7 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 		double innerTol = need > 1e-10 ? need : 1e-10;
 		SA_CHECK(cudaMemsetAsync(d32, 0, sizeof(float) * n, s));
 		CgScal h = run_cg<B, float, float, float>(m, wk.blk32, dinv32, rin, d32, zero, r32, u32, w32, p32, s32,
-		                                           wk.part, sc, itrMax - total, innerTol, -1.0, s);
+		                                           wk.part, sc, itrMax - total, innerTol, -1.0, s, &wk);
 		total += h.iters;
 		if (h.code == SA_ERR_NONFINITE) { code = h.code; break; }
 		k_axpy_f32<<<grid_for(n), kBlock, 0, s>>>(n, x, d32);

@@ -304,66 +304,115 @@ __global__ void k_to_f32(long n, const double *a, float *b)
 
 struct SolveOut { int status; int cgTotal, rdTotal, cgMax; int inverted; };
 
+// time stepper of one parameter column: start() sets up t = 0, step(n)
+// advances up to n steps, finish() leaves the final positions in w.xa
+template <int D>
+struct Stepper {
+	const Mesh &m;
+	const Model &md;
+	Work &w;
+	cudaStream_t s;
+	Status *st = nullptr;
+	Geom *gn = nullptr, *gx = nullptr;
+	double *xn = nullptr, *xx = nullptr;
+	int t = 0;
+	bool useK = false;
+	SolveOut out{SA_OK, 0, 0, 0, 0};
+
+	Stepper(const Mesh &m_, const Model &md_, Work &w_, cudaStream_t s_) : m(m_), md(md_), w(w_), s(s_) {}
+
+	void start(const double *x0soa, const double *tauVar)
+	{
+		int N = m.N;
+		long n = (long) N * D;
+		useK = md.frame || md.ldmWgt != 0.0;
+		out = SolveOut{SA_OK, 0, 0, 0, 0};
+		t = 0;
+		st = reinterpret_cast<Status *>(w.cw.scal + 24);   // inverted-element counter
+		SA_CHECK(cudaMemsetAsync(st, 0, sizeof(Status), s));
+		launch_soa_to_aos(N, D, x0soa, w.xa, s);
+		if (w.trajX) SA_CHECK(cudaMemcpyAsync(w.trajX, x0soa, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+		launch_tau_initial<D>(m, md, tauVar, w.xa, w.trajT, s);
+		launch_elem_geom<D>(m, md, w.xa, w.g0, st, false, s);
+		launch_assemble_rd<D>(m, md, w.g0, md.timeStp, w.Mnow, w.L, w.dinvRd, s);
+		SA_CHECK(cudaMemsetAsync(w.v, 0, sizeof(double) * n, s));
+		if (useK) SA_CHECK(cudaMemsetAsync(w.kw.wK, 0, sizeof(double) * n, s));
+		gn = &w.g0; gx = &w.g1;
+		xn = w.xa; xx = w.xb;
+	}
+
+	// returns the number of steps taken; stops early at timeNum - 1 or on a failed solve
+	int step(int nsteps)
+	{
+		int N = m.N, T = md.timeNum, done = 0;
+		long n = (long) N * D;
+		double dt = md.timeStp;
+		while (done < nsteps && t < T - 1 && out.status == SA_OK) {
+			double *tauNow = w.trajT + (long) t * N, *tauNxt = w.trajT + (long) (t + 1) * N;
+			launch_activity<D>(m, md, tauNow, w.fy, w.fr, s);
+			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
+			launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, s);
+			launch_yank_rhs<D>(m, *gn, w.fy, w.b, s);
+			int its = 0, code;
+			if (useK) {
+				launch_kernel_matrix<D>(md, N, xn, w.K, s);
+				code = kpcg<D>(m, md, w.blk, w.K, w.b, w.v, w.kw, st, &its, s);
+			} else {
+				if (md.precision == SA_PREC_MIXED)
+					k_to_f32<<<grid_for((long) m.Z * D * D), kBlock, 0, s>>>((long) m.Z * D * D, w.blk, w.cw.blk32);
+				w.cw.profileOn = 1;
+				code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st, &its, s,
+				                    md.precision);
+				w.cw.profileOn = 0;
+			}
+			out.cgTotal += its;
+			out.cgMax = std::max(out.cgMax, its);
+			if (code != SA_OK) { out.status = code; break; }
+			launch_advance<D>(N, xn, w.v, dt, xx, w.trajX ? w.trajX + (long) (t + 1) * n : nullptr, s);
+			launch_elem_geom<D>(m, md, xx, *gx, st, true, s);
+			launch_assemble_rd<D>(m, md, *gx, dt, w.Mnxt, w.L, w.dinvRd, s);
+			launch_rd_rhs<D>(m, *gn, w.Mnow, tauNow, w.fr, dt, w.rhs, s);
+			SA_CHECK(cudaMemcpyAsync(tauNxt, tauNow, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+			int rits = 0;
+			code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, tauNxt, md.rdItrMax, md.rdTolSqu, w.cw, st, &rits, s,
+			                    SA_PREC_FP64);
+			out.rdTotal += rits;
+			if (code != SA_OK) { out.status = code; break; }
+			// activity, (penalty), elastic assembly, yank, (to_f32), advance, geometry, rd assembly, rd rhs
+			w.cw.launches += 8 + (m.Bt > 0 && md.btmWgt != 0.0) + (!useK && md.precision == SA_PREC_MIXED);
+			std::swap(gn, gx);
+			std::swap(xn, xx);
+			std::swap(w.Mnow, w.Mnxt);
+			++t;
+			++done;
+		}
+		return done;
+	}
+
+	void finish()
+	{
+		Status hs;
+		SA_CHECK(cudaMemcpyAsync(&hs, st, sizeof(Status), cudaMemcpyDeviceToHost, s));
+		SA_CHECK(cudaStreamSynchronize(s));
+		out.inverted = hs.inverted;
+		long n = (long) m.N * D;
+		if (xn != w.xa) {   // the objective reads the final positions from w.xa
+			SA_CHECK(cudaMemcpyAsync(w.xa, xn, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+			xx = w.xb;
+			xn = w.xa;
+		}
+	}
+};
+
 template <int D>
 static SolveOut forward_one(const Mesh &m, const Model &md, Work &w, const double *x0soa, const double *tauVar,
                             cudaStream_t s)
 {
-	int N = m.N, T = md.timeNum;
-	long n = (long) N * D;
-	double dt = md.timeStp;
-	bool useK = md.frame || md.ldmWgt != 0.0;
-	SolveOut out{SA_OK, 0, 0, 0, 0};
-	Status *st = reinterpret_cast<Status *>(w.cw.scal + 24);   // inverted-element counter
-	SA_CHECK(cudaMemsetAsync(st, 0, sizeof(Status), s));
-	launch_soa_to_aos(N, D, x0soa, w.xa, s);
-	if (w.trajX) SA_CHECK(cudaMemcpyAsync(w.trajX, x0soa, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-	launch_tau_initial<D>(m, md, tauVar, w.xa, w.trajT, s);
-	launch_elem_geom<D>(m, md, w.xa, w.g0, st, false, s);
-	launch_assemble_rd<D>(m, md, w.g0, dt, w.Mnow, w.L, w.dinvRd, s);
-	SA_CHECK(cudaMemsetAsync(w.v, 0, sizeof(double) * n, s));
-	if (useK) SA_CHECK(cudaMemsetAsync(w.kw.wK, 0, sizeof(double) * n, s));
-	Geom *gn = &w.g0, *gx = &w.g1;
-	double *xn = w.xa, *xx = w.xb;
-	for (int t = 0; t < T - 1; ++t) {
-		double *tauNow = w.trajT + (long) t * N, *tauNxt = w.trajT + (long) (t + 1) * N;
-		launch_activity<D>(m, md, tauNow, w.fy, w.fr, s);
-		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
-		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, s);
-		launch_yank_rhs<D>(m, *gn, w.fy, w.b, s);
-		int its = 0, code;
-		if (useK) {
-			launch_kernel_matrix<D>(md, N, xn, w.K, s);
-			code = kpcg<D>(m, md, w.blk, w.K, w.b, w.v, w.kw, st, &its, s);
-		} else {
-			if (md.precision == SA_PREC_MIXED)
-				k_to_f32<<<grid_for((long) m.Z * D * D), kBlock, 0, s>>>((long) m.Z * D * D, w.blk, w.cw.blk32);
-			code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st, &its, s,
-			                    md.precision);
-		}
-		out.cgTotal += its;
-		out.cgMax = std::max(out.cgMax, its);
-		if (code != SA_OK) { out.status = code; break; }
-		launch_advance<D>(N, xn, w.v, dt, xx, w.trajX ? w.trajX + (long) (t + 1) * n : nullptr, s);
-		launch_elem_geom<D>(m, md, xx, *gx, st, true, s);
-		launch_assemble_rd<D>(m, md, *gx, dt, w.Mnxt, w.L, w.dinvRd, s);
-		launch_rd_rhs<D>(m, *gn, w.Mnow, tauNow, w.fr, dt, w.rhs, s);
-		SA_CHECK(cudaMemcpyAsync(tauNxt, tauNow, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
-		int rits = 0;
-		code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, tauNxt, md.rdItrMax, md.rdTolSqu, w.cw, st, &rits, s,
-		                    SA_PREC_FP64);
-		out.rdTotal += rits;
-		if (code != SA_OK) { out.status = code; break; }
-		std::swap(gn, gx);
-		std::swap(xn, xx);
-		std::swap(w.Mnow, w.Mnxt);
-	}
-	Status hs;
-	SA_CHECK(cudaMemcpyAsync(&hs, st, sizeof(Status), cudaMemcpyDeviceToHost, s));
-	SA_CHECK(cudaStreamSynchronize(s));
-	out.inverted = hs.inverted;
-	// final positions in interleaved form for the objective
-	if (xn != w.xa) SA_CHECK(cudaMemcpyAsync(w.xa, xn, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-	return out;
+	Stepper<D> st(m, md, w, s);
+	st.start(x0soa, tauVar);
+	st.step(md.timeNum);
+	st.finish();
+	return st.out;
 }
 
 static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *tgt, Pool &P)
@@ -523,6 +572,131 @@ static int varifold_impl(sa_context *ctx, const sa_element_object *obj, const do
 	return SA_OK;
 }
 
+// ---------------------------------------------------------------------------
+// sessions: one parameter vector, stepped on demand, state device-resident
+// ---------------------------------------------------------------------------
+struct SessionBase {
+	sa_context *ctx;
+	explicit SessionBase(sa_context *c) : ctx(c) {}
+	virtual ~SessionBase() {}
+	virtual int step(int n) = 0;
+	virtual void state(double *lmk, double *tau, int *t) = 0;
+	virtual double objective() = 0;
+	virtual void info(sa_solve_info *i) = 0;
+	virtual void profile(int enable, double *ms, long long *cnt, double *bytes) = 0;
+};
+
+template <int D>
+struct Session : SessionBase {
+	Pool P;
+	Mesh m;
+	Model md;
+	Work w;
+	Stepper<D> st;
+	const double *tc = nullptr, *tu = nullptr, *tvl = nullptr;
+	int Vt = 0;
+	std::vector<double> tauVar;
+
+	Session(sa_context *c, const sa_element_object *obj, const double *lmkIni, const sa_params *prm,
+	        const sa_target *tgt, const double *tv, int tvNum)
+		: SessionBase(c), P(c->stream), st(m, md, w, c->stream)
+	{
+		cudaStream_t s = c->stream;
+		fill_model(md, D, prm, tgt, P);
+		build_mesh(m, obj, tgt != nullptr, false, !md.frame, md.lyrNum, P);
+		if (md.frame || md.ldmWgt != 0.0)
+			SA_REQUIRE((size_t) m.N * m.N * sizeof(double) <= kDenseLimitBytes && m.N <= 65535,
+			           "dense RKHS kernel matrix exceeds the device budget for this node count");
+		SA_REQUIRE(tv && tvNum >= (md.frame ? 4 : D + 2), "tauVarVec too small");
+		tauVar = to_host(tv, (size_t) tvNum, s);
+		const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
+		if (tgt) {
+			SA_REQUIRE(tgt->tgtElmNum > 0 && tgt->cenPosMat && tgt->uniDirMat && tgt->elmVolVec, "empty target");
+			Vt = tgt->tgtElmNum;
+			tc = P.dev(tgt->cenPosMat, (size_t) Vt * D);
+			tu = P.dev(tgt->uniDirMat, (size_t) Vt * D);
+			tvl = P.dev(tgt->elmVolVec, (size_t) Vt);
+		}
+		alloc_work<D>(w, m, md, false, P);
+		double *xa = P.alloc<double>((size_t) m.N * D);
+		launch_soa_to_aos(m.N, D, x0, xa, s);
+		k_init_sign<D><<<grid_for(m.E), kBlock, 0, s>>>(m.E, m.elmVtx, xa, m.sign0);
+		// the stepper keeps x0 in SoA for the trajectory; keep our own device copy alive
+		double *x0d = P.alloc<double>((size_t) m.N * D);
+		SA_CHECK(cudaMemcpyAsync(x0d, x0, sizeof(double) * m.N * D, cudaMemcpyDeviceToDevice, s));
+		st.start(x0d, tauVar.data());
+		SA_CHECK(cudaStreamSynchronize(s));
+	}
+	~Session() override
+	{
+		for (cudaEvent_t e : w.cw.ev) if (e) cudaEventDestroy(e);
+	}
+	double lastStepMs = 0.0;
+	int step(int n) override
+	{
+		SA_CHECK(cudaEventRecord(ctx->e0, ctx->stream));
+		int k = st.step(n);
+		SA_CHECK(cudaEventRecord(ctx->e1, ctx->stream));
+		SA_CHECK(cudaEventSynchronize(ctx->e1));
+		float ms = 0.f;
+		SA_CHECK(cudaEventElapsedTime(&ms, ctx->e0, ctx->e1));
+		lastStepMs = ms;
+		SA_CHECK(cudaGetLastError());
+		return k;
+	}
+	void state(double *lmk, double *tau, int *t) override
+	{
+		cudaStream_t s = ctx->stream;
+		if (t) *t = st.t;
+		if (lmk) {
+			std::vector<double> h = to_host(st.xn, (size_t) m.N * D, s), o((size_t) m.N * D);
+			for (int i = 0; i < m.N; ++i)
+				for (int d = 0; d < D; ++d) o[(size_t) d * m.N + i] = h[(size_t) i * D + d];
+			SA_CHECK(cudaMemcpyAsync(lmk, o.data(), sizeof(double) * o.size(), cudaMemcpyDefault, s));
+		}
+		if (tau) SA_CHECK(cudaMemcpyAsync(tau, w.trajT + (long) st.t * m.N, sizeof(double) * m.N,
+		                                  cudaMemcpyDefault, s));
+		SA_CHECK(cudaStreamSynchronize(s));
+	}
+	double objective() override
+	{
+		SA_REQUIRE(tc, "session has no target");
+		if (st.out.status != SA_OK) return DBL_MAX;
+		int err = SA_OK;
+		double v = varifold<D>(m, md, st.xn, tc, tu, tvl, Vt, nullptr, ctx->stream, md.precision, &err);
+		SA_REQUIRE(err == SA_OK, "varifold arguments");
+		return v;
+	}
+	void info(sa_solve_info *i) override
+	{
+		Status hs;
+		SA_CHECK(cudaMemcpyAsync(&hs, st.st, sizeof(Status), cudaMemcpyDeviceToHost, ctx->stream));
+		SA_CHECK(cudaStreamSynchronize(ctx->stream));
+		i->status = st.out.status;
+		i->cgIterTotal = st.out.cgTotal;
+		i->rdIterTotal = st.out.rdTotal;
+		i->cgIterMax = st.out.cgMax;
+		i->invertedElements = hs.inverted;
+		i->elapsedMs = lastStepMs;             // device time of the last sa_session_step call
+		i->kernelLaunches = w.cw.launches;
+	}
+	void profile(int enable, double *ms, long long *cnt, double *bytes) override
+	{
+		if (ms) *ms = w.cw.spmvMs;
+		if (cnt) *cnt = w.cw.spmvCount;
+		if (bytes) {
+			double val = md.precision == SA_PREC_MIXED ? 4.0 : 8.0;
+			// block values + column index per slot, row pointers, u read and w written once
+			*bytes = (double) m.Z * (D * D * val + 4.0) + 4.0 * (m.N + 1) + 2.0 * val * m.N * D;
+		}
+		if (enable >= 0) {
+			w.cw.profileEnabled = enable;
+			w.cw.spmvMs = 0.0;
+			w.cw.spmvCount = 0;
+		}
+	}
+};
+
 template <typename F>
 static int guarded(sa_context *ctx, F &&f)
 {
@@ -611,6 +785,72 @@ int sa_varifold(sa_context *ctx, const sa_element_object *obj, const double *lmk
 		SA_REQUIRE(obj->dim == 3, "dim must be 2 or 3");
 		return sa::varifold_impl<3>(ctx, obj, lmkMat, tgt, precision, objOut, gradMat);
 	});
+}
+
+struct sa_session {
+	sa::SessionBase *impl;
+};
+
+int sa_session_create(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat, const sa_params *prm,
+                      const sa_target *tgt, const double *tauVarVec, int tauVarNum, sa_session **out)
+{
+	if (!out) return SA_ERR_ARG;
+	*out = nullptr;
+	return sa::guarded(ctx, [&]() {
+		SA_REQUIRE(obj && prm && lmkIniMat, "null argument");
+		sa::SessionBase *impl;
+		if (obj->dim == 2) impl = new sa::Session<2>(ctx, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum);
+		else {
+			SA_REQUIRE(obj->dim == 3, "dim must be 2 or 3");
+			impl = new sa::Session<3>(ctx, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum);
+		}
+		*out = new sa_session{impl};
+		return SA_OK;
+	});
+}
+
+int sa_session_step(sa_session *s, int nsteps, int *stepsDone)
+{
+	if (!s) return SA_ERR_ARG;
+	return sa::guarded(s->impl->ctx, [&]() {
+		int k = s->impl->step(nsteps);
+		if (stepsDone) *stepsDone = k;
+		return SA_OK;
+	});
+}
+
+int sa_session_state(sa_session *s, double *lmkMat, double *tauVec, int *step)
+{
+	if (!s) return SA_ERR_ARG;
+	return sa::guarded(s->impl->ctx, [&]() { s->impl->state(lmkMat, tauVec, step); return SA_OK; });
+}
+
+int sa_session_objective(sa_session *s, double *obj)
+{
+	if (!s || !obj) return SA_ERR_ARG;
+	return sa::guarded(s->impl->ctx, [&]() { *obj = s->impl->objective(); return SA_OK; });
+}
+
+int sa_session_info(sa_session *s, sa_solve_info *info)
+{
+	if (!s || !info) return SA_ERR_ARG;
+	return sa::guarded(s->impl->ctx, [&]() { s->impl->info(info); return SA_OK; });
+}
+
+int sa_session_profile(sa_session *s, int enable, double *spmvMs, long long *spmvCount, double *spmvBytes)
+{
+	if (!s) return SA_ERR_ARG;
+	return sa::guarded(s->impl->ctx, [&]() { s->impl->profile(enable, spmvMs, spmvCount, spmvBytes); return SA_OK; });
+}
+
+int sa_session_destroy(sa_session *s)
+{
+	if (!s) return SA_OK;
+	cudaSetDevice(s->impl->ctx->device);
+	cudaStreamSynchronize(s->impl->ctx->stream);
+	delete s->impl;
+	delete s;
+	return SA_OK;
 }
 
 static void frame_object(sa_element_object &o, int dim, int lmkNum, const int *elmVtxMat, int elmNum,

@@ -219,6 +219,12 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	float *blk32 = nullptr;       // FP32 copy of the operator (mixed precision)
 	float *f32 = nullptr;         // 7 n FP32 vectors of the inner solve (mixed precision)
 	double *xr = nullptr;         // 3 n FP64 refinement scratch
+	// optional CUDA-event timing of the velocity matvec kernel (k_cg_spmv)
+	int profileEnabled = 0, profileOn = 0;
+	cudaEvent_t ev[64] = {};
+	double spmvMs = 0.0;
+	long spmvCount = 0;
+	long long launches = 0;       // kernel launches issued (CG loops and the time stepper)
 };
 
 template <int B> int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double *b,
