@@ -75,33 +75,17 @@ __device__ __forceinline__ void finish_partials(double (&out)[K], const double *
 // matvec kernels: w = A u (+ partial (w, u))
 // ---------------------------------------------------------------------------
 template <int B, typename TM, typename TV>
-__device__ __forceinline__ void row_spmv(int i, const int *__restrict__ rowPtr, const int *__restrict__ col,
-                                         const TM *__restrict__ blk, const TV *__restrict__ u, TV (&acc)[B])
-{
-	for (int r = 0; r < B; ++r) acc[r] = (TV) 0;
-	int z0 = rowPtr[i], z1 = rowPtr[i + 1];
-	for (int z = z0; z < z1; ++z) {
-		int j = col[z];
-		const TM *a = blk + (long) z * B * B;
-		TV xj[B];
-		for (int c = 0; c < B; ++c) xj[c] = u[(long) j * B + c];
-		for (int r = 0; r < B; ++r)
-			for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
-	}
-}
-
-template <int B, typename TM, typename TV>
-__global__ void __launch_bounds__(kCgBlock) k_cg_spmv(int N, const int *__restrict__ rowPtr,
-                                                      const int *__restrict__ col, const TM *__restrict__ blk,
+__global__ void __launch_bounds__(kCgBlock) k_cg_spmv(SellOp A, const TM *__restrict__ blk,
                                                       const TV *__restrict__ u, TV *__restrict__ w,
                                                       double *part, CgScal *sc)
 {
 	if (sc->done) return;
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int N = A.N;
 	double v[1] = {0.0};
 	if (i < N) {
 		TV acc[B];
-		row_spmv<B, TM, TV>(i, rowPtr, col, blk, u, acc);
+		sell_row<B, TM, TV>(A, blk, i, u, acc);
 		for (int r = 0; r < B; ++r) {
 			w[(long) i * B + r] = acc[r];
 			v[0] += (double) acc[r] * (double) u[(long) i * B + r];
@@ -227,13 +211,13 @@ __global__ void k_axpy_f32(long n, double *x, const float *d)
 
 // q = A x in FP64 (for the initial / true residual)
 template <int B>
-__global__ void k_spmv64(int N, const int *__restrict__ rowPtr, const int *__restrict__ col,
-                         const double *__restrict__ blk, const double *__restrict__ x, double *__restrict__ q)
+__global__ void k_spmv64(SellOp A, const double *__restrict__ blk, const double *__restrict__ x,
+                         double *__restrict__ q)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= N) return;
+	if (i >= A.N) return;
 	double acc[B];
-	row_spmv<B, double, double>(i, rowPtr, col, blk, x, acc);
+	sell_row<B, double, double>(A, blk, i, x, acc);
 	for (int r = 0; r < B; ++r) q[(long) i * B + r] = acc[r];
 }
 
@@ -278,7 +262,7 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	for (int it = 0; it < itrMax + chunk; it += chunk) {
 		for (int k = 0; k < chunk; ++k) {
 			if (timing) SA_CHECK(cudaEventRecord(prof->ev[2 * k], s));
-			k_cg_spmv<B, TM, TV><<<nb, kCgBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, u, w, part, sc);
+			k_cg_spmv<B, TM, TV><<<nb, kCgBlock, 0, s>>>(sell_of(m), blk, u, w, part, sc);
 			if (timing) SA_CHECK(cudaEventRecord(prof->ev[2 * k + 1], s));
 			k_cg_update<B, TV, TX><<<nb, kCgBlock, 0, s>>>(N, x, r, u, w, p, sv, dinv, part, sc);
 		}
@@ -319,7 +303,7 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 	double *q = wk.xr;                       // A x (FP64)
 	CgScal *sc = (CgScal *) wk.scal;
 	if (precision == SA_PREC_FP64 || !wk.blk32) {
-		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, x, q);
+		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(sell_of(m), blk, x, q);
 		wk.launches += 1;
 		CgScal h = run_cg<B, double, double, double>(m, blk, dinv, b, x, q, wk.r, wk.u, wk.w, wk.p, wk.sv,
 		                                              wk.part, sc, itrMax, tolSqu, -1.0, s, &wk);
@@ -339,7 +323,7 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 	double bb = -1.0;
 	const int nb = grid_for(N, kCgBlock);
 	for (int outer = 0; outer < 64; ++outer) {
-		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, x, q);
+		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(sell_of(m), blk, x, q);
 		k_sub<<<grid_for(n), kBlock, 0, s>>>(n, b, q, rin);
 		wk.launches += 4;                     // spmv64, sub, init, axpy of this outer step
 		// outer test: |b - A x|^2 < tol^2 |b|^2 (k_cg_init with b and q gives both norms)

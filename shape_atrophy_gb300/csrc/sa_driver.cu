@@ -231,6 +231,43 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 	}
 	m.rowPtr = P.alloc<int>(m.N + 1);
 	SA_CHECK(cudaMemcpyAsync(m.rowPtr, rp.data(), sizeof(int) * (m.N + 1), cudaMemcpyHostToDevice, s));
+	{   // sliced layout: 32-row slices, slot k of row 32 s + lane at off[s] + 32 k + lane
+		int nsl = (m.N + 31) / 32;
+		std::vector<int> wid(nsl), off(nsl);
+		long total = 0;
+		for (int sl = 0; sl < nsl; ++sl) {
+			int w = 0;
+			for (int i = sl * 32; i < std::min(m.N, sl * 32 + 32); ++i) w = std::max(w, rp[i + 1] - rp[i]);
+			wid[sl] = w;
+			off[sl] = (int) total;
+			total += 32L * w;
+		}
+		SA_REQUIRE(total < (1L << 31) / 8, "operator too large for 32-bit slot offsets");
+		std::vector<int> col(total), dest(m.Z);
+		for (int sl = 0; sl < nsl; ++sl)
+			for (int lane = 0; lane < 32; ++lane) {
+				int i = sl * 32 + lane;
+				int len = i < m.N ? rp[i + 1] - rp[i] : 0;
+				for (int k = 0; k < wid[sl]; ++k) {
+					long idx = off[sl] + 32L * k + lane;
+					if (k < len) {
+						col[idx] = fv[m.Z + rp[i] + k];
+						dest[rp[i] + k] = (int) idx;
+					} else col[idx] = i < m.N ? i : 0;     // padding: zero block on the row's own node
+				}
+			}
+		m.nslice = nsl;
+		m.slTotal = total;
+		m.slWidth = P.alloc<int>(nsl);
+		m.slOff = P.alloc<int>(nsl);
+		m.slCol = P.alloc<int>(total);
+		m.slDest = P.alloc<int>(m.Z);
+		SA_CHECK(cudaMemcpyAsync(m.slWidth, wid.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
+		SA_CHECK(cudaMemcpyAsync(m.slOff, off.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
+		SA_CHECK(cudaMemcpyAsync(m.slCol, col.data(), sizeof(int) * total, cudaMemcpyHostToDevice, s));
+		SA_CHECK(cudaMemcpyAsync(m.slDest, dest.data(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
+		SA_CHECK(cudaStreamSynchronize(s));      // host vectors go out of scope
+	}
 	m.asmCols = maxAdj;
 	m.asmTab = P.alloc<int>((size_t) std::max(1, maxAdj) * m.Z);
 	int *bad = P.zeros<int>(1);
@@ -262,9 +299,10 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	long N = m.N, E = m.E, Z = m.Z, n = N * D;
 	w.xa = P.alloc<double>(n); w.xb = P.alloc<double>(n);
 	w.v = P.alloc<double>(n); w.b = P.alloc<double>(n); w.pd = P.zeros<double>(N);
-	w.blk = P.alloc<double>((size_t) Z * D * D); w.dinv = P.alloc<double>(n);
+	long T = m.slTotal;                    // sliced slots, padding included (padding stays zero)
+	w.blk = P.zeros<double>((size_t) T * sell_vals<D>()); w.dinv = P.alloc<double>(n);
 	w.fy = P.alloc<double>(N); w.fr = P.alloc<double>(N);
-	w.Mnow = P.alloc<double>(Z); w.Mnxt = P.alloc<double>(Z); w.L = P.alloc<double>(Z);
+	w.Mnow = P.alloc<double>(Z); w.Mnxt = P.alloc<double>(Z); w.L = P.zeros<double>(T);
 	w.dinvRd = P.alloc<double>(N); w.rhs = P.alloc<double>(N);
 	for (Geom *g : {&w.g0, &w.g1}) {
 		g->QI = P.alloc<double>((size_t) (D + 1) * D * E);
@@ -278,7 +316,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	c.part = P.alloc<double>((size_t) 4 * nb + 64); c.scal = P.zeros<double>(32); c.maxBlocks = nb;
 	c.xr = P.alloc<double>((size_t) 3 * n);
 	if (md.precision == SA_PREC_MIXED) {
-		c.blk32 = P.alloc<float>((size_t) Z * D * D);
+		c.blk32 = P.alloc<float>((size_t) T * sell_vals<D>());
 		c.f32 = P.alloc<float>((size_t) 7 * n);
 	}
 	bool useK = md.frame || md.ldmWgt != 0.0;
@@ -359,7 +397,8 @@ struct Stepper {
 				code = kpcg<D>(m, md, w.blk, w.K, w.b, w.v, w.kw, st, &its, s);
 			} else {
 				if (md.precision == SA_PREC_MIXED)
-					k_to_f32<<<grid_for((long) m.Z * D * D), kBlock, 0, s>>>((long) m.Z * D * D, w.blk, w.cw.blk32);
+					k_to_f32<<<grid_for(m.slTotal * sell_vals<D>()), kBlock, 0, s>>>(m.slTotal * sell_vals<D>(), w.blk,
+					                                                                  w.cw.blk32);
 				w.cw.profileOn = 1;
 				code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st, &its, s,
 				                    md.precision);
@@ -686,8 +725,9 @@ struct Session : SessionBase {
 		if (cnt) *cnt = w.cw.spmvCount;
 		if (bytes) {
 			double val = md.precision == SA_PREC_MIXED ? 4.0 : 8.0;
-			// block values + column index per slot, row pointers, u read and w written once
-			*bytes = (double) m.Z * (D * D * val + 4.0) + 4.0 * (m.N + 1) + 2.0 * val * m.N * D;
+			// block values + column index per sliced slot (padding included), slice table, u read and w
+			// written once
+			*bytes = (double) m.slTotal * (sell_vals<D>() * val + 4.0) + 8.0 * m.nslice + 2.0 * val * m.N * D;
 		}
 		if (enable >= 0) {
 			w.cw.profileEnabled = enable;

@@ -150,6 +150,14 @@ struct Mesh {              // device copy of one element object + derived tables
 	int *vfdVtx = nullptr, *vfdIfo = nullptr, *elmLyr = nullptr;
 	int *rowPtr = nullptr;     // N+1 (from femVtxMat rows)
 	int *diagSlot = nullptr;   // N
+	// sliced layout of the operators: slices of 32 consecutive rows; inside a
+	// slice, block slot k of row (32 s + lane) sits at off[s] + 32 k + lane
+	int nslice = 0;
+	long slTotal = 0;          // slots including padding
+	int *slWidth = nullptr;    // nslice: longest row of the slice
+	int *slOff = nullptr;      // nslice: first slot of the slice
+	int *slCol = nullptr;      // slTotal: column (node) of each slot; padding points at the row itself
+	int *slDest = nullptr;     // Z: sliced slot of each femVtxMat slot
 	int *asmTab = nullptr;     // femIfoCols/2-1 x Z: e*16 + a*4 + b, femIfo order
 	int asmCols = 0;
 	signed char *sign0 = nullptr;  // initial orientation of each element
@@ -182,6 +190,96 @@ struct Model {
 };
 
 // --------------------------------------------------------------------------
+// sliced block-row matvec.  Values of a B x B block (row-major) are stored
+// in two regions so that every thread issues aligned vector loads: B = 3
+// puts entries 0..7 at val[8 slot + e] and entry 8 at val[8 total + slot];
+// B = 2 puts the 4 entries at val[4 slot + e]; B = 1 at val[slot].  A warp
+// covers one slice, so each load instruction reads one contiguous span.
+// --------------------------------------------------------------------------
+struct SellOp {
+	int N;
+	long total;
+	const int *width, *off, *col;
+};
+
+inline SellOp sell_of(const Mesh &m) { return SellOp{m.N, m.slTotal, m.slWidth, m.slOff, m.slCol}; }
+
+template <int B> constexpr int sell_vals() { return B == 3 ? 9 : B * B; }
+
+template <int B, typename TM>
+__device__ __forceinline__ void load_block(const TM *__restrict__ val, long total, long idx, TM (&a)[B * B]);
+
+template <> __device__ __forceinline__ void load_block<3, double>(const double *__restrict__ val, long total, long idx,
+                                                                  double (&a)[9])
+{
+	const double2 *p = reinterpret_cast<const double2 *>(val + idx * 8);
+	double2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3);
+	a[0] = q0.x; a[1] = q0.y; a[2] = q1.x; a[3] = q1.y; a[4] = q2.x; a[5] = q2.y; a[6] = q3.x; a[7] = q3.y;
+	a[8] = __ldg(val + total * 8 + idx);
+}
+template <> __device__ __forceinline__ void load_block<3, float>(const float *__restrict__ val, long total, long idx,
+                                                                 float (&a)[9])
+{
+	const float4 *p = reinterpret_cast<const float4 *>(val + idx * 8);
+	float4 q0 = __ldg(p), q1 = __ldg(p + 1);
+	a[0] = q0.x; a[1] = q0.y; a[2] = q0.z; a[3] = q0.w; a[4] = q1.x; a[5] = q1.y; a[6] = q1.z; a[7] = q1.w;
+	a[8] = __ldg(val + total * 8 + idx);
+}
+template <> __device__ __forceinline__ void load_block<2, double>(const double *__restrict__ val, long, long idx,
+                                                                  double (&a)[4])
+{
+	const double2 *p = reinterpret_cast<const double2 *>(val + idx * 4);
+	double2 q0 = __ldg(p), q1 = __ldg(p + 1);
+	a[0] = q0.x; a[1] = q0.y; a[2] = q1.x; a[3] = q1.y;
+}
+template <> __device__ __forceinline__ void load_block<2, float>(const float *__restrict__ val, long, long idx,
+                                                                 float (&a)[4])
+{
+	float4 q = __ldg(reinterpret_cast<const float4 *>(val + idx * 4));
+	a[0] = q.x; a[1] = q.y; a[2] = q.z; a[3] = q.w;
+}
+template <> __device__ __forceinline__ void load_block<1, double>(const double *__restrict__ val, long, long idx,
+                                                                  double (&a)[1])
+{ a[0] = __ldg(val + idx); }
+template <> __device__ __forceinline__ void load_block<1, float>(const float *__restrict__ val, long, long idx,
+                                                                 float (&a)[1])
+{ a[0] = __ldg(val + idx); }
+
+// store one assembled block into the sliced layout
+template <int B>
+__device__ __forceinline__ void store_block(double *val, long total, long idx, const double (&a)[B][B])
+{
+	if (B == 3) {
+		for (int e = 0; e < 8; ++e) val[idx * 8 + e] = a[e / 3][e % 3];
+		val[total * 8 + idx] = a[2][2];
+	} else {
+		for (int r = 0; r < B; ++r) for (int c = 0; c < B; ++c) val[idx * B * B + r * B + c] = a[r][c];
+	}
+}
+
+// acc = row i of A x
+template <int B, typename TM, typename TV>
+__device__ __forceinline__ void sell_row(const SellOp &A, const TM *__restrict__ val, int i,
+                                         const TV *__restrict__ x, TV (&acc)[B])
+{
+	for (int r = 0; r < B; ++r) acc[r] = (TV) 0;
+	int s = i >> 5, lane = i & 31;
+	int w = __ldg(A.width + s);
+	long base = __ldg(A.off + s) + lane;
+#pragma unroll 2
+	for (int k = 0; k < w; ++k) {
+		long idx = base + ((long) k << 5);
+		int j = __ldg(A.col + idx);
+		TV xj[B];
+		for (int c = 0; c < B; ++c) xj[c] = x[(long) j * B + c];
+		TM a[B * B];
+		load_block<B, TM>(val, A.total, idx, a);
+		for (int r = 0; r < B; ++r)
+			for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
+	}
+}
+
+// --------------------------------------------------------------------------
 // kernels and launchers (defined in the .cu files)
 // --------------------------------------------------------------------------
 template <int D> void launch_elem_geom(const Mesh &m, const Model &md, const double *x, Geom &g,
@@ -204,9 +302,6 @@ template <int D> void launch_advance(int N, const double *x, const double *v, do
                                      double *trajSlot, cudaStream_t s);
 void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_t s);
 
-// block-CSR matvec y = A x (B = block size 1..3), FP64
-template <int B> void launch_bsr_spmv(const Mesh &m, const double *blk, const double *x, double *y,
-                                      cudaStream_t s);
 
 // --------------------------------------------------------------------------
 // CG solvers

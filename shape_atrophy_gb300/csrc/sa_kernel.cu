@@ -261,23 +261,17 @@ __global__ void k_kp_bnorm(int N, const double *__restrict__ b, double *part, KS
 
 // r = b - (ldm w + Bx0), (r, r)
 template <int D>
-__global__ void k_kp_init_r(int N, const int *__restrict__ rowPtr, const int *__restrict__ col,
-                            const double *__restrict__ blk, const double *__restrict__ b,
+__global__ void k_kp_init_r(SellOp A, const double *__restrict__ blk, const double *__restrict__ b,
                             const double *__restrict__ x, const double *__restrict__ w, double *__restrict__ r,
                             double *part, KScal *sc)
 {
 	if (sc->done) return;
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int N = A.N;
 	double v[1] = {0.0};
 	if (i < N) {
 		double acc[D];
-		for (int d = 0; d < D; ++d) acc[d] = 0.0;
-		for (int z = rowPtr[i]; z < rowPtr[i + 1]; ++z) {
-			int j = col[z];
-			const double *a = blk + (long) z * D * D;
-			for (int rr = 0; rr < D; ++rr)
-				for (int c = 0; c < D; ++c) acc[rr] += a[rr * D + c] * x[(long) j * D + c];
-		}
+		sell_row<D, double, double>(A, blk, i, x, acc);
 		for (int d = 0; d < D; ++d) {
 			long k = (long) i * D + d;
 			double Ax = sc->ldmWgt * w[k] + acc[d];
@@ -337,22 +331,16 @@ __global__ void k_kp_dir(int N, const double *__restrict__ r, const double *__re
 
 // Bd = (E + btm P) d; Ad = ldm Kid + Bd; (d, Ad) -> alpha
 template <int D>
-__global__ void k_kp_ad(int N, const int *__restrict__ rowPtr, const int *__restrict__ col,
-                        const double *__restrict__ blk, const double *__restrict__ dv, const double *__restrict__ Kid,
-                        double *__restrict__ Ad, double *part, KScal *sc)
+__global__ void k_kp_ad(SellOp A, const double *__restrict__ blk, const double *__restrict__ dv,
+                        const double *__restrict__ Kid, double *__restrict__ Ad, double *part, KScal *sc)
 {
 	if (sc->done) return;
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int N = A.N;
 	double v[1] = {0.0};
 	if (i < N) {
 		double acc[D];
-		for (int d = 0; d < D; ++d) acc[d] = 0.0;
-		for (int z = rowPtr[i]; z < rowPtr[i + 1]; ++z) {
-			int j = col[z];
-			const double *a = blk + (long) z * D * D;
-			for (int rr = 0; rr < D; ++rr)
-				for (int c = 0; c < D; ++c) acc[rr] += a[rr * D + c] * dv[(long) j * D + c];
-		}
+		sell_row<D, double, double>(A, blk, i, dv, acc);
 		for (int d = 0; d < D; ++d) {
 			long k = (long) i * D + d;
 			double a = sc->ldmWgt * Kid[k] + 1.0 * acc[d];
@@ -427,14 +415,14 @@ int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, con
 	k_kp_bnorm<D><<<nb, kKBlock, 0, s>>>(N, b, wk.part, sc);
 	// warm start x0 = K w (w = K^{-1} v of the previous step)
 	launch_dense_matvec<D>(N, K, wk.wK, x, dpart, s);
-	k_kp_init_r<D><<<nb, kKBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, b, x, wk.wK, wk.r, wk.part, sc);
+	k_kp_init_r<D><<<nb, kKBlock, 0, s>>>(sell_of(m), blk, b, x, wk.wK, wk.r, wk.part, sc);
 	launch_dense_matvec<D>(N, K, wk.r, wk.Kr, dpart, s);
 	k_kp_rkr<D><<<nb, kKBlock, 0, s>>>(N, wk.r, wk.Kr, wk.part, sc, 1);
 	k_kp_dir<D><<<grid_for(n), kBlock, 0, s>>>(N, wk.r, wk.Kr, wk.Kid, wk.dv, sc, 1);
 	const int chunk = 8;
 	for (int it = 0; it < md.cgItrMax + chunk; it += chunk) {
 		for (int k = 0; k < chunk; ++k) {
-			k_kp_ad<D><<<nb, kKBlock, 0, s>>>(N, m.rowPtr, m.femVtx + m.Z, blk, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
+			k_kp_ad<D><<<nb, kKBlock, 0, s>>>(sell_of(m), blk, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
 			k_kp_step<D><<<nb, kKBlock, 0, s>>>(N, x, wk.wK, wk.r, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
 			launch_dense_matvec<D>(N, K, wk.r, wk.Kr, dpart, s);
 			k_kp_rkr<D><<<nb, kKBlock, 0, s>>>(N, wk.r, wk.Kr, wk.part, sc, 0);

@@ -318,6 +318,7 @@ __global__ void k_asm_elastic(int Z, int E, int asmCols, const int *__restrict__
                               int frame, FrameMod fm, const double *__restrict__ frm, const double *__restrict__ tsv,
                               const int *__restrict__ lyr, const double *__restrict__ lyrMod,
                               double btmWgt, const double *__restrict__ pd, int Nb,
+                              const int *__restrict__ slDest, long total,
                               double *__restrict__ blk, double *__restrict__ dinv)
 {
 	int z = blockIdx.x * blockDim.x + threadIdx.x;
@@ -366,8 +367,7 @@ __global__ void k_asm_elastic(int Z, int E, int asmCols, const int *__restrict__
 			dinv[(long) i * D + d] = 1.0 / acc[d][d];
 		}
 	}
-	double *o = blk + (long) z * D * D;
-	for (int r = 0; r < D; ++r) for (int c = 0; c < D; ++c) o[r * D + c] = acc[r][c];
+	store_block<D>(blk, total, slDest[z], acc);
 }
 
 template <int D>
@@ -378,7 +378,7 @@ void launch_assemble_elastic(const Mesh &m, const Model &md, const Geom &g, cons
 	for (int k = 0; k < 4; ++k) fm.m[k] = md.mod[k];
 	k_asm_elastic<D><<<grid_for(m.Z, 128), 128, 0, s>>>(m.Z, m.E, m.asmCols, m.femVtx, m.femIfo, m.asmTab, g.QI,
 	                                                     g.vol, md.frame, fm, g.frm, g.tsv, m.elmLyr, md.lyrMod,
-	                                                     md.btmWgt, pd, m.Nb, blk, dinv);
+	                                                     md.btmWgt, pd, m.Nb, m.slDest, m.slTotal, blk, dinv);
 }
 
 // ---------------------------------------------------------------------------
@@ -420,6 +420,7 @@ __global__ void k_asm_rd(int Z, int E, const int *__restrict__ femVtx, const int
                          const double *__restrict__ absDet, int frame, const double *__restrict__ frm,
                          const double *__restrict__ tsv, double spdTan, double spdTsv,
                          const int *__restrict__ lyr, const double *__restrict__ lyrSpd, double dt,
+                         const int *__restrict__ slDest,
                          double *__restrict__ Mval, double *__restrict__ Lval, double *__restrict__ dinv)
 {
 	int z = blockIdx.x * blockDim.x + threadIdx.x;
@@ -437,8 +438,8 @@ __global__ void k_asm_rd(int Z, int E, const int *__restrict__ femVtx, const int
 		Gs += ggd_value<D>(frame, e, E, lo, hi, G, ad, frm, tsv, spdTan, spdTsv, Dl);
 	}
 	double L = 1.0 * M + dt * Gs;
-	Mval[z] = M;
-	Lval[z] = L;
+	Mval[z] = M;                 // femVtxMat (CSR) order, read by the next step's right-hand side
+	Lval[slDest[z]] = L;         // sliced layout, read by the CG matvec
 	int i = femVtx[z];
 	if (i == femVtx[Z + z]) dinv[i] = 1.0 / L;
 }
@@ -448,8 +449,8 @@ void launch_assemble_rd(const Mesh &m, const Model &md, const Geom &g, double dt
                         double *dinv, cudaStream_t s)
 {
 	k_asm_rd<D><<<grid_for(m.Z), kBlock, 0, s>>>(m.Z, m.E, m.femVtx, m.femIfo, m.asmTab, g.QI, g.absDet, md.frame,
-	                                              g.frm, g.tsv, md.spdTan, md.spdTsv, m.elmLyr, md.lyrSpd, dt, Mval,
-	                                              Lval, dinv);
+	                                              g.frm, g.tsv, md.spdTan, md.spdTsv, m.elmLyr, md.lyrSpd, dt, m.slDest,
+	                                              Mval, Lval, dinv);
 }
 
 // rhs_i = (M_t tau_t)_i + dt * sum_{e ∋ i} (tau-weighted consistent mass load)
@@ -517,34 +518,6 @@ void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_
 	k_soa_to_aos<<<grid_for((long) N * D), kBlock, 0, s>>>(N, D, soa, aos);
 }
 
-// ---------------------------------------------------------------------------
-// block-CSR matvec (FP64), one thread per block row
-// ---------------------------------------------------------------------------
-template <int B>
-__global__ void k_bsr_spmv(int N, const int *__restrict__ rowPtr, const int *__restrict__ col,
-                           const double *__restrict__ blk, const double *__restrict__ x, double *__restrict__ y)
-{
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= N) return;
-	double acc[B];
-	for (int r = 0; r < B; ++r) acc[r] = 0.0;
-	for (int z = rowPtr[i]; z < rowPtr[i + 1]; ++z) {
-		int j = col[z];
-		const double *a = blk + (long) z * B * B;
-		for (int c = 0; c < B; ++c) {
-			double xc = x[(long) j * B + c];
-			for (int r = 0; r < B; ++r) acc[r] += a[r * B + c] * xc;
-		}
-	}
-	for (int r = 0; r < B; ++r) y[(long) i * B + r] = acc[r];
-}
-
-template <int B>
-void launch_bsr_spmv(const Mesh &m, const double *blk, const double *x, double *y, cudaStream_t s)
-{
-	k_bsr_spmv<B><<<grid_for(m.N), kBlock, 0, s>>>(m.N, m.rowPtr, m.femVtx + m.Z, blk, x, y);
-}
-
 // explicit instantiations
 #define SA_INST(D)                                                                                           \
 	template void launch_elem_geom<D>(const Mesh &, const Model &, const double *, Geom &, Status *, bool,     \
@@ -565,8 +538,5 @@ void launch_bsr_spmv(const Mesh &m, const double *blk, const double *x, double *
 	                                cudaStream_t);
 SA_INST(2)
 SA_INST(3)
-template void launch_bsr_spmv<1>(const Mesh &, const double *, const double *, double *, cudaStream_t);
-template void launch_bsr_spmv<2>(const Mesh &, const double *, const double *, double *, cudaStream_t);
-template void launch_bsr_spmv<3>(const Mesh &, const double *, const double *, double *, cudaStream_t);
 
 }  // namespace sa
