@@ -31,13 +31,15 @@ struct CgScal {
 	int pad;
 };
 
-constexpr int kCgBlock = 256;
+constexpr int kCgBlock = 256;      // vector kernels: one thread per vector entry
+constexpr int kTpr = 4;            // matvec: threads per row (one warp per slot phase)
+constexpr int kSpmvBlock = 32 * kTpr;
 
 // block-wide reduction of K values; writes part[k*nb + blockIdx.x]; returns true in the last block
-template <int K>
+template <int K, int NT>
 __device__ __forceinline__ bool reduce_partials(double (&v)[K], double *part, unsigned int *counter)
 {
-	__shared__ double sm[K][kCgBlock / 32];
+	__shared__ double sm[K][NT / 32];
 	__shared__ bool last;
 	int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	for (int k = 0; k < K; ++k)
@@ -47,7 +49,7 @@ __device__ __forceinline__ bool reduce_partials(double (&v)[K], double *part, un
 	if (threadIdx.x == 0) {
 		for (int k = 0; k < K; ++k) {
 			double s = 0.0;
-			for (int w = 0; w < kCgBlock / 32; ++w) s += sm[k][w];
+			for (int w = 0; w < NT / 32; ++w) s += sm[k][w];
 			part[k * gridDim.x + blockIdx.x] = s;
 		}
 		__threadfence();
@@ -72,26 +74,47 @@ __device__ __forceinline__ void finish_partials(double (&out)[K], const double *
 }
 
 // ---------------------------------------------------------------------------
-// matvec kernels: w = A u (+ partial (w, u))
+// matvec kernel: w = A u and the partial (w, u).  One CTA per 32-row slice;
+// warp p of the CTA takes block slots k = p, p + kTpr, ... of the slice, so
+// every load instruction of a warp reads 32 consecutive slots; the kTpr
+// partial rows are combined in shared memory in a fixed order.
 // ---------------------------------------------------------------------------
 template <int B, typename TM, typename TV>
-__global__ void __launch_bounds__(kCgBlock) k_cg_spmv(SellOp A, const TM *__restrict__ blk,
-                                                      const TV *__restrict__ u, TV *__restrict__ w,
-                                                      double *part, CgScal *sc)
+__global__ void __launch_bounds__(kSpmvBlock) k_cg_spmv(SellOp A, const TM *__restrict__ blk,
+                                                        const TV *__restrict__ u, TV *__restrict__ w,
+                                                        double *part, CgScal *sc)
 {
 	if (sc->done) return;
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	const int N = A.N;
+	__shared__ TV red[kTpr][B * 32];
+	const int sl = blockIdx.x, lane = threadIdx.x & 31, ph = threadIdx.x >> 5;
+	const int i = sl * 32 + lane;
+	const int wdt = __ldg(A.width + sl);
+	const long base = __ldg(A.off + sl) + lane;
+	TV acc[B];
+	for (int r = 0; r < B; ++r) acc[r] = (TV) 0;
+#pragma unroll 2
+	for (int k = ph; k < wdt; k += kTpr) {
+		long idx = base + ((long) k << 5);
+		int j = __ldg(A.col + idx);
+		TV xj[B];
+		for (int c = 0; c < B; ++c) xj[c] = u[(long) j * B + c];
+		TM a[B * B];
+		load_block<B, TM>(blk, A.total, idx, a);
+		for (int r = 0; r < B; ++r)
+			for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
+	}
+	for (int r = 0; r < B; ++r) red[ph][r * 32 + lane] = acc[r];
+	__syncthreads();
 	double v[1] = {0.0};
-	if (i < N) {
-		TV acc[B];
-		sell_row<B, TM, TV>(A, blk, i, u, acc);
+	if (ph == 0 && i < A.N) {
 		for (int r = 0; r < B; ++r) {
-			w[(long) i * B + r] = acc[r];
-			v[0] += (double) acc[r] * (double) u[(long) i * B + r];
+			TV o = red[0][r * 32 + lane];
+			for (int q = 1; q < kTpr; ++q) o += red[q][r * 32 + lane];
+			w[(long) i * B + r] = o;
+			v[0] += (double) o * (double) u[(long) i * B + r];
 		}
 	}
-	if (!reduce_partials<1>(v, part, &sc->counter)) return;
+	if (!reduce_partials<1, kSpmvBlock>(v, part, &sc->counter)) return;
 	double d[1];
 	finish_partials<1>(d, part);
 	if (threadIdx.x == 0) {
@@ -111,34 +134,32 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_spmv(SellOp A, const TM *__rest
 }
 
 // ---------------------------------------------------------------------------
-// vector kernel: p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^{-1} r
+// vector kernel, one thread per entry:
+// p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^{-1} r
 // ---------------------------------------------------------------------------
-template <int B, typename TV, typename TX>
-__global__ void __launch_bounds__(kCgBlock) k_cg_update(int N, TX *__restrict__ x, TV *__restrict__ r,
+template <typename TV, typename TX>
+__global__ void __launch_bounds__(kCgBlock) k_cg_update(long n, TX *__restrict__ x, TV *__restrict__ r,
                                                         TV *__restrict__ u, const TV *__restrict__ w,
                                                         TV *__restrict__ p, TV *__restrict__ s,
                                                         const TV *__restrict__ dinv, double *part, CgScal *sc)
 {
 	if (sc->done) return;
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
 	double v[2] = {0.0, 0.0};
-	if (i < N) {
+	if (k < n) {
 		TV al = (TV) sc->alpha, be = (TV) sc->beta;
-		for (int c = 0; c < B; ++c) {
-			long k = (long) i * B + c;
-			TV pk = u[k] + be * p[k];
-			TV sk = w[k] + be * s[k];
-			p[k] = pk; s[k] = sk;
-			x[k] = x[k] + (TX) al * (TX) pk;
-			TV rk = r[k] - al * sk;
-			r[k] = rk;
-			TV uk = dinv[k] * rk;
-			u[k] = uk;
-			v[0] += (double) rk * (double) uk;
-			v[1] += (double) rk * (double) rk;
-		}
+		TV pk = u[k] + be * p[k];
+		TV sk = w[k] + be * s[k];
+		p[k] = pk; s[k] = sk;
+		x[k] = x[k] + (TX) al * (TX) pk;
+		TV rk = r[k] - al * sk;
+		r[k] = rk;
+		TV uk = dinv[k] * rk;
+		u[k] = uk;
+		v[0] = (double) rk * (double) uk;
+		v[1] = (double) rk * (double) rk;
 	}
-	if (!reduce_partials<2>(v, part, &sc->counter)) return;
+	if (!reduce_partials<2, kCgBlock>(v, part, &sc->counter)) return;
 	double d[2];
 	finish_partials<2>(d, part);
 	if (threadIdx.x == 0) {
@@ -154,26 +175,23 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_update(int N, TX *__restrict__ 
 }
 
 // r = b - q, u = D^{-1} r, partials (b, b), (r, r), (r, u)
-template <int B, typename TV>
-__global__ void __launch_bounds__(kCgBlock) k_cg_init(int N, const double *__restrict__ b, const double *__restrict__ q,
+template <typename TV>
+__global__ void __launch_bounds__(kCgBlock) k_cg_init(long n, const double *__restrict__ b, const double *__restrict__ q,
                                                       const TV *__restrict__ dinv, TV *__restrict__ r,
                                                       TV *__restrict__ u, double *part, CgScal *sc)
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
 	double v[3] = {0.0, 0.0, 0.0};
-	if (i < N) {
-		for (int c = 0; c < B; ++c) {
-			long k = (long) i * B + c;
-			double rk = b[k] - q[k];
-			TV rt = (TV) rk;
-			TV uk = dinv[k] * rt;
-			r[k] = rt; u[k] = uk;
-			v[0] += b[k] * b[k];
-			v[1] += rk * rk;
-			v[2] += (double) rt * (double) uk;
-		}
+	if (k < n) {
+		double rk = b[k] - q[k];
+		TV rt = (TV) rk;
+		TV uk = dinv[k] * rt;
+		r[k] = rt; u[k] = uk;
+		v[0] = b[k] * b[k];
+		v[1] = rk * rk;
+		v[2] = (double) rt * (double) uk;
 	}
-	if (!reduce_partials<3>(v, part, &sc->counter)) return;
+	if (!reduce_partials<3, kCgBlock>(v, part, &sc->counter)) return;
 	double d[3];
 	finish_partials<3>(d, part);
 	if (threadIdx.x == 0) {
@@ -248,12 +266,13 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
                      TV *r, TV *u, TV *w, TV *p, TV *sv, double *part, CgScal *sc, int itrMax, double tolSqu,
                      double bb, cudaStream_t s, CgWork *prof = nullptr)
 {
-	int N = m.N, nb = grid_for(N, kCgBlock);
+	int N = m.N;
 	long n = (long) N * B;
+	int nb = grid_for(n, kCgBlock);
 	set_scal(sc, tolSqu, itrMax, bb, s);
 	SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
 	SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
-	k_cg_init<B, TV><<<nb, kCgBlock, 0, s>>>(N, b, q, dinv, r, u, part, sc);
+	k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
 	const int chunk = 16;
 	bool timing = prof && prof->profileEnabled && prof->profileOn;
 	if (timing && !prof->ev[0])
@@ -262,9 +281,9 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	for (int it = 0; it < itrMax + chunk; it += chunk) {
 		for (int k = 0; k < chunk; ++k) {
 			if (timing) SA_CHECK(cudaEventRecord(prof->ev[2 * k], s));
-			k_cg_spmv<B, TM, TV><<<nb, kCgBlock, 0, s>>>(sell_of(m), blk, u, w, part, sc);
+			k_cg_spmv<B, TM, TV><<<m.nslice, kSpmvBlock, 0, s>>>(sell_of(m), blk, u, w, part, sc);
 			if (timing) SA_CHECK(cudaEventRecord(prof->ev[2 * k + 1], s));
-			k_cg_update<B, TV, TX><<<nb, kCgBlock, 0, s>>>(N, x, r, u, w, p, sv, dinv, part, sc);
+			k_cg_update<TV, TX><<<nb, kCgBlock, 0, s>>>(n, x, r, u, w, p, sv, dinv, part, sc);
 		}
 		SA_CHECK(cudaGetLastError());
 		if (prof) prof->launches += 2 * chunk;
@@ -321,14 +340,14 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 	SA_CHECK(cudaMemsetAsync(zero, 0, sizeof(double) * n, s));
 	int total = 0, code = SA_ERR_NOT_CONVERGED;
 	double bb = -1.0;
-	const int nb = grid_for(N, kCgBlock);
+	const int nb = grid_for(n, kCgBlock);
 	for (int outer = 0; outer < 64; ++outer) {
 		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(sell_of(m), blk, x, q);
 		k_sub<<<grid_for(n), kBlock, 0, s>>>(n, b, q, rin);
 		wk.launches += 4;                     // spmv64, sub, init, axpy of this outer step
 		// outer test: |b - A x|^2 < tol^2 |b|^2 (k_cg_init with b and q gives both norms)
 		set_scal(sc, tolSqu, 1, bb, s);
-		k_cg_init<B, float><<<nb, kCgBlock, 0, s>>>(N, b, q, dinv32, r32, u32, wk.part, sc);
+		k_cg_init<float><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv32, r32, u32, wk.part, sc);
 		CgScal h0 = read_scal(sc, s);
 		if (bb < 0.0) bb = h0.bb;
 		if (h0.code == SA_ERR_NONFINITE) { code = SA_ERR_NONFINITE; break; }
