@@ -31,8 +31,13 @@ struct CgScal {
 	int pad;
 };
 
-constexpr int kCgBlock = 256;      // vector kernels: one thread per vector entry
-constexpr int kTpr = 4;            // matvec: threads per row (one warp per slot phase)
+// FP64 throughput on GB300 is 2 thread-DFMA per clock per SM, so the
+// kernels below avoid FP64 work that is not the algorithm's own: dot
+// products are shuffle-reduced only by warps that hold data, and vector
+// kernels reduce kVecPer entries per thread before any shuffle.
+constexpr int kCgBlock = 256;      // vector kernels
+constexpr int kVecPer = 4;         // vector entries per thread
+constexpr int kTpr = 2;            // matvec: threads per row (one warp per slot phase)
 constexpr int kSpmvBlock = 32 * kTpr;
 
 // block-wide reduction of K values; writes part[k*nb + blockIdx.x]; returns true in the last block
@@ -105,16 +110,25 @@ __global__ void __launch_bounds__(kSpmvBlock) k_cg_spmv(SellOp A, const TM *__re
 	}
 	for (int r = 0; r < B; ++r) red[ph][r * 32 + lane] = acc[r];
 	__syncthreads();
-	double v[1] = {0.0};
-	if (ph == 0 && i < A.N) {
-		for (int r = 0; r < B; ++r) {
-			TV o = red[0][r * 32 + lane];
-			for (int q = 1; q < kTpr; ++q) o += red[q][r * 32 + lane];
-			w[(long) i * B + r] = o;
-			v[0] += (double) o * (double) u[(long) i * B + r];
+	__shared__ bool last;
+	if (ph == 0) {             // warp 0 finishes the rows and reduces the slice's part of (w, u)
+		double v = 0.0;
+		if (i < A.N)
+			for (int r = 0; r < B; ++r) {
+				TV o = red[0][r * 32 + lane];
+				for (int q = 1; q < kTpr; ++q) o += red[q][r * 32 + lane];
+				w[(long) i * B + r] = o;
+				v += (double) o * (double) u[(long) i * B + r];
+			}
+		for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+		if (lane == 0) {
+			part[blockIdx.x] = v;
+			__threadfence();
+			last = (atomicAdd(&sc->counter, 1u) == gridDim.x - 1);
 		}
 	}
-	if (!reduce_partials<1, kSpmvBlock>(v, part, &sc->counter)) return;
+	__syncthreads();
+	if (!last) return;
 	double d[1];
 	finish_partials<1>(d, part);
 	if (threadIdx.x == 0) {
@@ -144,20 +158,24 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_update(long n, TX *__restrict__
                                                         const TV *__restrict__ dinv, double *part, CgScal *sc)
 {
 	if (sc->done) return;
-	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	const long stride = (long) gridDim.x * blockDim.x;
 	double v[2] = {0.0, 0.0};
-	if (k < n) {
-		TV al = (TV) sc->alpha, be = (TV) sc->beta;
-		TV pk = u[k] + be * p[k];
-		TV sk = w[k] + be * s[k];
-		p[k] = pk; s[k] = sk;
-		x[k] = x[k] + (TX) al * (TX) pk;
-		TV rk = r[k] - al * sk;
-		r[k] = rk;
-		TV uk = dinv[k] * rk;
-		u[k] = uk;
-		v[0] = (double) rk * (double) uk;
-		v[1] = (double) rk * (double) rk;
+	const TV al = (TV) sc->alpha, be = (TV) sc->beta;
+#pragma unroll
+	for (int j = 0; j < kVecPer; ++j) {
+		long k = blockIdx.x * (long) blockDim.x + threadIdx.x + j * stride;
+		if (k < n) {
+			TV pk = u[k] + be * p[k];
+			TV sk = w[k] + be * s[k];
+			p[k] = pk; s[k] = sk;
+			x[k] = x[k] + (TX) al * (TX) pk;
+			TV rk = r[k] - al * sk;
+			r[k] = rk;
+			TV uk = dinv[k] * rk;
+			u[k] = uk;
+			v[0] += (double) rk * (double) uk;
+			v[1] += (double) rk * (double) rk;
+		}
 	}
 	if (!reduce_partials<2, kCgBlock>(v, part, &sc->counter)) return;
 	double d[2];
@@ -180,16 +198,19 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_init(long n, const double *__re
                                                       const TV *__restrict__ dinv, TV *__restrict__ r,
                                                       TV *__restrict__ u, double *part, CgScal *sc)
 {
-	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	const long stride = (long) gridDim.x * blockDim.x;
 	double v[3] = {0.0, 0.0, 0.0};
-	if (k < n) {
-		double rk = b[k] - q[k];
-		TV rt = (TV) rk;
-		TV uk = dinv[k] * rt;
-		r[k] = rt; u[k] = uk;
-		v[0] = b[k] * b[k];
-		v[1] = rk * rk;
-		v[2] = (double) rt * (double) uk;
+	for (int j = 0; j < kVecPer; ++j) {
+		long k = blockIdx.x * (long) blockDim.x + threadIdx.x + j * stride;
+		if (k < n) {
+			double rk = b[k] - q[k];
+			TV rt = (TV) rk;
+			TV uk = dinv[k] * rt;
+			r[k] = rt; u[k] = uk;
+			v[0] += b[k] * b[k];
+			v[1] += rk * rk;
+			v[2] += (double) rt * (double) uk;
+		}
 	}
 	if (!reduce_partials<3, kCgBlock>(v, part, &sc->counter)) return;
 	double d[3];
@@ -268,32 +289,50 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 {
 	int N = m.N;
 	long n = (long) N * B;
-	int nb = grid_for(n, kCgBlock);
+	int nb = grid_for(n, kCgBlock * kVecPer);
 	set_scal(sc, tolSqu, itrMax, bb, s);
 	SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
 	SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
 	k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
 	const int chunk = 16;
 	bool timing = prof && prof->profileEnabled && prof->profileOn;
+	if (!prof->pinned) {
+		SA_CHECK(cudaHostAlloc(&prof->pinned, 2 * sizeof(CgScal), cudaHostAllocDefault));
+		for (int k = 0; k < 2; ++k) SA_CHECK(cudaEventCreateWithFlags(&prof->chunkEv[k], cudaEventDisableTiming));
+	}
 	if (timing && !prof->ev[0])
-		for (int k = 0; k < 2 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
-	int itersBefore = 0;
-	for (int it = 0; it < itrMax + chunk; it += chunk) {
+		for (int k = 0; k < 4 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
+	CgScal *hs = (CgScal *) prof->pinned;
+	// chunks of iterations are queued one ahead: while the host waits for the
+	// status of chunk c - 1, chunk c is already on the GPU (its kernels return
+	// at once if c - 1 converged), so the device never idles on the host
+	auto launch_chunk = [&](int set) {
 		for (int k = 0; k < chunk; ++k) {
-			if (timing) SA_CHECK(cudaEventRecord(prof->ev[2 * k], s));
+			if (timing) SA_CHECK(cudaEventRecord(prof->ev[set * 2 * chunk + 2 * k], s));
 			k_cg_spmv<B, TM, TV><<<m.nslice, kSpmvBlock, 0, s>>>(sell_of(m), blk, u, w, part, sc);
-			if (timing) SA_CHECK(cudaEventRecord(prof->ev[2 * k + 1], s));
+			if (timing) SA_CHECK(cudaEventRecord(prof->ev[set * 2 * chunk + 2 * k + 1], s));
 			k_cg_update<TV, TX><<<nb, kCgBlock, 0, s>>>(n, x, r, u, w, p, sv, dinv, part, sc);
 		}
+		SA_CHECK(cudaMemcpyAsync(hs + set, sc, sizeof(CgScal), cudaMemcpyDeviceToHost, s));
+		SA_CHECK(cudaEventRecord(prof->chunkEv[set], s));
 		SA_CHECK(cudaGetLastError());
-		if (prof) prof->launches += 2 * chunk;
-		CgScal h = read_scal(sc, s);
+		prof->launches += 2 * chunk;
+	};
+	const int maxChunks = (itrMax + chunk - 1) / chunk + 1;
+	int itersBefore = 0;
+	launch_chunk(0);
+	for (int c = 1; c <= maxChunks; ++c) {
+		if (c < maxChunks) launch_chunk(c & 1);
+		int prev = (c - 1) & 1;
+		SA_CHECK(cudaEventSynchronize(prof->chunkEv[prev]));
+		CgScal h = hs[prev];
 		if (timing) {
 			// matvec launches that did work in this chunk = iterations completed in it
 			int worked = std::min(chunk, h.iters - itersBefore);
 			for (int k = 0; k < worked; ++k) {
 				float ms = 0.f;
-				SA_CHECK(cudaEventElapsedTime(&ms, prof->ev[2 * k], prof->ev[2 * k + 1]));
+				SA_CHECK(cudaEventElapsedTime(&ms, prof->ev[prev * 2 * chunk + 2 * k],
+				                              prof->ev[prev * 2 * chunk + 2 * k + 1]));
 				prof->spmvMs += ms;
 			}
 			prof->spmvCount += worked;

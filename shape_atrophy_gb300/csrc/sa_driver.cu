@@ -668,10 +668,6 @@ struct Session : SessionBase {
 		st.start(x0d, tauVar.data());
 		SA_CHECK(cudaStreamSynchronize(s));
 	}
-	~Session() override
-	{
-		for (cudaEvent_t e : w.cw.ev) if (e) cudaEventDestroy(e);
-	}
 	double lastStepMs = 0.0;
 	int step(int n) override
 	{

@@ -320,6 +320,18 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	double spmvMs = 0.0;
 	long spmvCount = 0;
 	long long launches = 0;       // kernel launches issued (CG loops and the time stepper)
+	void *pinned = nullptr;       // two host copies of the CG status (chunk pipelining)
+	cudaEvent_t chunkEv[2] = {};
+
+	CgWork() = default;
+	CgWork(const CgWork &) = delete;
+	CgWork &operator=(const CgWork &) = delete;
+	~CgWork()
+	{
+		for (cudaEvent_t e : ev) if (e) cudaEventDestroy(e);
+		for (cudaEvent_t e : chunkEv) if (e) cudaEventDestroy(e);
+		if (pinned) cudaFreeHost(pinned);
+	}
 };
 
 template <int B> int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double *b,
