@@ -190,11 +190,12 @@ struct Model {
 };
 
 // --------------------------------------------------------------------------
-// sliced block-row matvec.  Values of a B x B block (row-major) are stored
-// in two regions so that every thread issues aligned vector loads: B = 3
-// puts entries 0..7 at val[8 slot + e] and entry 8 at val[8 total + slot];
-// B = 2 puts the 4 entries at val[4 slot + e]; B = 1 at val[slot].  A warp
-// covers one slice, so each load instruction reads one contiguous span.
+// sliced block-row matvec.  Slots are numbered slice by slice (slot idx of
+// lane l = idx % 32 in a 32-slot group starting at idx - l); entry e of the
+// row-major B x B block of slot idx sits at val[(idx - l) B^2 + 32 e + l].
+// For a fixed block slot and entry, the 32 lanes of a warp (32 consecutive
+// rows) therefore read 32 consecutive values: every load instruction of the
+// matvec is one fully used 256-byte (FP64) or 128-byte (FP32) span.
 // --------------------------------------------------------------------------
 struct SellOp {
 	int N;
@@ -204,57 +205,29 @@ struct SellOp {
 
 inline SellOp sell_of(const Mesh &m) { return SellOp{m.N, m.slTotal, m.slWidth, m.slOff, m.slCol}; }
 
-template <int B> constexpr int sell_vals() { return B == 3 ? 9 : B * B; }
+template <int B> constexpr int sell_vals() { return B * B; }
+
+__device__ __forceinline__ long sell_pos(long idx, int e, int BB)
+{
+	long lane = idx & 31;
+	return (idx - lane) * BB + 32L * e + lane;
+}
 
 template <int B, typename TM>
-__device__ __forceinline__ void load_block(const TM *__restrict__ val, long total, long idx, TM (&a)[B * B]);
-
-template <> __device__ __forceinline__ void load_block<3, double>(const double *__restrict__ val, long total, long idx,
-                                                                  double (&a)[9])
+__device__ __forceinline__ void load_block(const TM *__restrict__ val, long, long idx, TM (&a)[B * B])
 {
-	const double2 *p = reinterpret_cast<const double2 *>(val + idx * 8);
-	double2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3);
-	a[0] = q0.x; a[1] = q0.y; a[2] = q1.x; a[3] = q1.y; a[4] = q2.x; a[5] = q2.y; a[6] = q3.x; a[7] = q3.y;
-	a[8] = __ldg(val + total * 8 + idx);
+	const TM *p = val + sell_pos(idx, 0, B * B);
+#pragma unroll
+	for (int e = 0; e < B * B; ++e) a[e] = __ldg(p + 32 * e);
 }
-template <> __device__ __forceinline__ void load_block<3, float>(const float *__restrict__ val, long total, long idx,
-                                                                 float (&a)[9])
-{
-	const float4 *p = reinterpret_cast<const float4 *>(val + idx * 8);
-	float4 q0 = __ldg(p), q1 = __ldg(p + 1);
-	a[0] = q0.x; a[1] = q0.y; a[2] = q0.z; a[3] = q0.w; a[4] = q1.x; a[5] = q1.y; a[6] = q1.z; a[7] = q1.w;
-	a[8] = __ldg(val + total * 8 + idx);
-}
-template <> __device__ __forceinline__ void load_block<2, double>(const double *__restrict__ val, long, long idx,
-                                                                  double (&a)[4])
-{
-	const double2 *p = reinterpret_cast<const double2 *>(val + idx * 4);
-	double2 q0 = __ldg(p), q1 = __ldg(p + 1);
-	a[0] = q0.x; a[1] = q0.y; a[2] = q1.x; a[3] = q1.y;
-}
-template <> __device__ __forceinline__ void load_block<2, float>(const float *__restrict__ val, long, long idx,
-                                                                 float (&a)[4])
-{
-	float4 q = __ldg(reinterpret_cast<const float4 *>(val + idx * 4));
-	a[0] = q.x; a[1] = q.y; a[2] = q.z; a[3] = q.w;
-}
-template <> __device__ __forceinline__ void load_block<1, double>(const double *__restrict__ val, long, long idx,
-                                                                  double (&a)[1])
-{ a[0] = __ldg(val + idx); }
-template <> __device__ __forceinline__ void load_block<1, float>(const float *__restrict__ val, long, long idx,
-                                                                 float (&a)[1])
-{ a[0] = __ldg(val + idx); }
 
 // store one assembled block into the sliced layout
 template <int B>
-__device__ __forceinline__ void store_block(double *val, long total, long idx, const double (&a)[B][B])
+__device__ __forceinline__ void store_block(double *val, long, long idx, const double (&a)[B][B])
 {
-	if (B == 3) {
-		for (int e = 0; e < 8; ++e) val[idx * 8 + e] = a[e / 3][e % 3];
-		val[total * 8 + idx] = a[2][2];
-	} else {
-		for (int r = 0; r < B; ++r) for (int c = 0; c < B; ++c) val[idx * B * B + r * B + c] = a[r][c];
-	}
+	double *p = val + sell_pos(idx, 0, B * B);
+	for (int r = 0; r < B; ++r)
+		for (int c = 0; c < B; ++c) p[32 * (r * B + c)] = a[r][c];
 }
 
 // acc = row i of A x
