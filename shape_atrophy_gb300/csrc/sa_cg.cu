@@ -37,8 +37,8 @@ struct CgScal {
 // kernels reduce kVecPer entries per thread before any shuffle.
 constexpr int kCgBlock = 256;      // vector kernels
 constexpr int kVecPer = 4;         // vector entries per thread
-constexpr int kTpr = 2;            // matvec: threads per row (one warp per slot phase)
-constexpr int kSpmvBlock = 32 * kTpr;
+constexpr int kSlicesPerCta = 4;   // matvec: one warp per 32-row slice, one thread per row
+constexpr int kSpmvBlock = 32 * kSlicesPerCta;
 
 // block-wide reduction of K values; writes part[k*nb + blockIdx.x]; returns true in the last block
 template <int K, int NT>
@@ -90,42 +90,44 @@ __global__ void __launch_bounds__(kSpmvBlock) k_cg_spmv(SellOp A, const TM *__re
                                                         double *part, CgScal *sc)
 {
 	if (sc->done) return;
-	__shared__ TV red[kTpr][B * 32];
-	const int sl = blockIdx.x, lane = threadIdx.x & 31, ph = threadIdx.x >> 5;
-	const int i = sl * 32 + lane;
-	const int wdt = __ldg(A.width + sl);
-	const long base = __ldg(A.off + sl) + lane;
-	TV acc[B];
-	for (int r = 0; r < B; ++r) acc[r] = (TV) 0;
-#pragma unroll 2
-	for (int k = ph; k < wdt; k += kTpr) {
-		long idx = base + ((long) k << 5);
-		int j = __ldg(A.col + idx);
-		TV xj[B];
-		for (int c = 0; c < B; ++c) xj[c] = u[(long) j * B + c];
-		TM a[B * B];
-		load_block<B, TM>(blk, A.total, idx, a);
-		for (int r = 0; r < B; ++r)
-			for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
-	}
-	for (int r = 0; r < B; ++r) red[ph][r * 32 + lane] = acc[r];
-	__syncthreads();
+	__shared__ double wsum[kSlicesPerCta];
 	__shared__ bool last;
-	if (ph == 0) {             // warp 0 finishes the rows and reduces the slice's part of (w, u)
-		double v = 0.0;
+	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+	const int sl = blockIdx.x * kSlicesPerCta + wp;
+	const int nsl = (A.N + 31) >> 5;
+	double v = 0.0;
+	if (sl < nsl) {
+		const int i = sl * 32 + lane;
+		const int wdt = __ldg(A.width + sl);
+		const long base = __ldg(A.off + sl) + lane;
+		TV acc[B];
+		for (int r = 0; r < B; ++r) acc[r] = (TV) 0;
+#pragma unroll 4
+		for (int k = 0; k < wdt; ++k) {
+			long idx = base + ((long) k << 5);
+			int j = __ldg(A.col + idx);
+			TV xj[B];
+			for (int c = 0; c < B; ++c) xj[c] = u[(long) j * B + c];
+			TM a[B * B];
+			load_block<B, TM>(blk, A.total, idx, a);
+			for (int r = 0; r < B; ++r)
+				for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
+		}
 		if (i < A.N)
 			for (int r = 0; r < B; ++r) {
-				TV o = red[0][r * 32 + lane];
-				for (int q = 1; q < kTpr; ++q) o += red[q][r * 32 + lane];
-				w[(long) i * B + r] = o;
-				v += (double) o * (double) u[(long) i * B + r];
+				w[(long) i * B + r] = acc[r];
+				v += (double) acc[r] * (double) u[(long) i * B + r];
 			}
 		for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-		if (lane == 0) {
-			part[blockIdx.x] = v;
-			__threadfence();
-			last = (atomicAdd(&sc->counter, 1u) == gridDim.x - 1);
-		}
+	}
+	if (lane == 0) wsum[wp] = v;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double s = wsum[0];
+		for (int q = 1; q < kSlicesPerCta; ++q) s += wsum[q];
+		part[blockIdx.x] = s;
+		__threadfence();
+		last = (atomicAdd(&sc->counter, 1u) == gridDim.x - 1);
 	}
 	__syncthreads();
 	if (!last) return;
@@ -309,7 +311,8 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	auto launch_chunk = [&](int set) {
 		for (int k = 0; k < chunk; ++k) {
 			if (timing) SA_CHECK(cudaEventRecord(prof->ev[set * 2 * chunk + 2 * k], s));
-			k_cg_spmv<B, TM, TV><<<m.nslice, kSpmvBlock, 0, s>>>(sell_of(m), blk, u, w, part, sc);
+			k_cg_spmv<B, TM, TV><<<(m.nslice + kSlicesPerCta - 1) / kSlicesPerCta, kSpmvBlock, 0, s>>>(
+				sell_of(m), blk, u, w, part, sc);
 			if (timing) SA_CHECK(cudaEventRecord(prof->ev[set * 2 * chunk + 2 * k + 1], s));
 			k_cg_update<TV, TX><<<nb, kCgBlock, 0, s>>>(n, x, r, u, w, p, sv, dinv, part, sc);
 		}
