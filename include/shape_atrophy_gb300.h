@@ -140,6 +140,30 @@ int sa_forward(sa_context *ctx, const sa_element_object *obj, const double *lmkI
 int sa_varifold(sa_context *ctx, const sa_element_object *obj, const double *lmkMat,
                 const sa_target *tgt, int precision, double *obj_out, double *gradMat);
 
+/* Varifold objective without any device allocation (no counterpart in the
+ * reference).  For callers that must not allocate while they evaluate the
+ * objective: an optimiser's line search that calls it hundreds of times on
+ * a GPU whose memory is managed by someone else (MATLAB's gpuArray pool, a
+ * serving process with a fixed budget), where cudaMalloc can fail and
+ * cudaFree synchronises the whole device.  Same value as sa_varifold.
+ *   - All inputs must already be device memory (nodes: N x dim
+ *     column-major; vfdVtxMat: Vd x dim int32; target Vt x dim, Vt);
+ *     host pointers are rejected with SA_ERR_ARG (nothing is copied).
+ *   - Limit: vfdElmNum and tgtElmNum at most 32768 each; larger sizes
+ *     return SA_ERR_ARG.  The scratch is a fixed ~2.4 MB device array that
+ *     every GPU loading the library holds until the process exits.
+ *   - The first call on a device looks the array's device address up
+ *     (cudaGetSymbolAddress); make that first call before any stream
+ *     capture.  Runs on the given stream (NULL: the legacy default stream)
+ *     of the current device and waits for it before returning.
+ *   - All calls share the one array: calls that overlap on the GPU (other
+ *     threads, other streams) race; serialise them.
+ *   - objOut may be host or device memory. */
+int sa_varifold_noalloc(int dim, int lmkNum, const double *lmkMat, int vfdElmNum, const int *vfdVtxMat,
+                        int tgtElmNum, const double *tgtCenPosMat, const double *tgtUniDirMat,
+                        const double *tgtElmVolVec, char cenKnlType, double cenKnlWidth, char dirKnlType,
+                        double dirKnlWidth, void *stream, double *objOut);
+
 /* Stepwise solve of one parameter vector (no reference counterpart: the
  * reference runs all timeNum-1 steps inside one call).  A session keeps
  * mesh, state and solver work device-resident; sa_session_step advances up

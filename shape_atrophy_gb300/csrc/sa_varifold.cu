@@ -255,4 +255,143 @@ template double varifold<2>(const Mesh &, const Model &, const double *, const d
 template double varifold<3>(const Mesh &, const Model &, const double *, const double *, const double *,
                             const double *, int, double *, cudaStream_t, int, int *);
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the varifold objective (sa_varifold_noalloc).
+//
+// Its scratch -- boundary-element centres and directions (2 D Vd doubles),
+// element volumes (Vd), per-row pair sums (Vd + Vt) and the reduction buffer
+// (kSum + 1) -- lives in the file-scope device array below instead of device
+// memory obtained per call.  Every GPU that loads the library holds the
+// array (about 2.4 MB) until the process exits.  Host code never hands the
+// array's name to a kernel: on the host that name is only a stand-in, so the
+// device address is looked up once per device with cudaGetSymbolAddress and
+// that address is what the kernels receive.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocMaxElm = 32768;                       // max Vd and max Vt
+constexpr long kNoAllocDoubles = 9L * kNoAllocMaxElm + 1024;
+__device__ __align__(256) double g_noallocScratch[kNoAllocDoubles];
+
+// boundary elements from nodes in the reference's N x D column-major layout
+template <int D>
+__global__ void k_vfd_elems_soa(int N, int Vd, const int *__restrict__ vfdVtx, const double *__restrict__ x,
+                                double *__restrict__ cen, double *__restrict__ dir, double *__restrict__ vol)
+{
+	int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= Vd) return;
+	Vec<D> q[D];
+	for (int k = 0; k < D; ++k)
+		for (int d = 0; d < D; ++d) q[k].c[d] = x[(long) d * N + vfdVtx[(long) k * Vd + e]];
+	Vec<D> c, u;
+	double v;
+	if (D == 2) {
+		for (int d = 0; d < D; ++d) c.c[d] = 0.5 * (q[0].c[d] + q[1].c[d]);
+		u = vsub(q[1], q[0]);
+		v = sqrt(vdot(u, u));
+		for (int d = 0; d < D; ++d) u.c[d] /= v;
+		vol[e] = v;
+	} else {
+		Vec<3> a0, a1, a2;
+		for (int d = 0; d < 3; ++d) { a0.c[d] = q[0].c[d]; a1.c[d] = q[1].c[d]; a2.c[d] = q[2].c[d]; }
+		Vec<3> cr = vcross(vsub(a1, a0), vsub(a2, a0));
+		v = sqrt(vdot(cr, cr));
+		for (int d = 0; d < 3; ++d) { c.c[d] = (a0.c[d] + a1.c[d] + a2.c[d]) / 3.0; u.c[d] = cr.c[d] / v; }
+		vol[e] = 0.5 * v;
+	}
+	for (int d = 0; d < D; ++d) { cen[d * (long) Vd + e] = c.c[d]; dir[d * (long) Vd + e] = u.c[d]; }
+}
+
+template <int D>
+static double varifold_in_scratch(double *scr, int N, const double *x, int Vd, const int *vfdVtx, int Vt,
+                                  const double *tc, const double *tu, const double *tv, int ck, double cw, int dk,
+                                  double dw, cudaStream_t s)
+{
+	double *cen = scr, *dir = cen + (long) D * Vd, *vol = dir + (long) D * Vd, *vfd = vol + Vd;
+	double *sumScr = vfd + Vd + Vt;
+	k_vfd_elems_soa<D><<<grid_for(Vd), kBlock, 0, s>>>(N, Vd, vfdVtx, x, cen, dir, vol);
+	VfdSet Ds{cen, dir, vol, Vd}, Ts{tc, tu, tv, Vt}, E0{nullptr, nullptr, nullptr, 0};
+	const int blk = 128;
+	// same row/column roles as the allocating path (reference branch on Vd >= Vt)
+	if (Vd >= Vt) {
+		k_vfd_rows<D, double><<<grid_for(Vd, blk), blk, 0, s>>>(Ds, Ds, 1.0, Ts, -2.0, ck, cw, dk, dw, vfd, 0,
+		                                                        nullptr, nullptr);
+		k_vfd_rows<D, double><<<grid_for(Vt, blk), blk, 0, s>>>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, vfd + Vd, 0,
+		                                                        nullptr, nullptr);
+	} else {
+		k_vfd_rows<D, double><<<grid_for(Vt, blk), blk, 0, s>>>(Ts, Ts, 1.0, Ds, -2.0, ck, cw, dk, dw, vfd, 0,
+		                                                        nullptr, nullptr);
+		k_vfd_rows<D, double><<<grid_for(Vd, blk), blk, 0, s>>>(Ds, Ds, 1.0, E0, 0.0, ck, cw, dk, dw, vfd + Vt, 0,
+		                                                        nullptr, nullptr);
+	}
+	SA_CHECK(cudaGetLastError());
+	// device_sum clears the part of its buffer that accumulates before using it
+	return device_sum(vfd, Vd + Vt, sumScr, s);
+}
+
 }  // namespace sa
+
+#include <mutex>
+
+namespace {
+std::mutex g_noallocMutex;
+double *g_noallocAddr[128] = {};
+
+// device address of the scratch array on device dev (looked up on first use)
+int noalloc_scratch(int dev, double **out)
+{
+	if (dev < 0 || dev >= 128) return SA_ERR_UNSUPPORTED;
+	std::lock_guard<std::mutex> lock(g_noallocMutex);
+	if (!g_noallocAddr[dev]) {
+		void *p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, sa::g_noallocScratch);
+		if (e != cudaSuccess || !p) { cudaGetLastError(); return SA_ERR_CUDA; }
+		g_noallocAddr[dev] = (double *) p;
+	}
+	*out = g_noallocAddr[dev];
+	return SA_OK;
+}
+
+bool on_device(const void *p)
+{
+	cudaPointerAttributes a;
+	if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+}  // namespace
+
+extern "C" int sa_varifold_noalloc(int dim, int lmkNum, const double *lmkMat, int vfdElmNum, const int *vfdVtxMat,
+                                   int tgtElmNum, const double *tgtCenPosMat, const double *tgtUniDirMat,
+                                   const double *tgtElmVolVec, char cenKnlType, double cenKnlWidth, char dirKnlType,
+                                   double dirKnlWidth, void *stream, double *objOut)
+{
+	if (dim != 2 && dim != 3) return SA_ERR_ARG;
+	if (lmkNum <= 0 || vfdElmNum <= 0 || tgtElmNum <= 0 || !objOut) return SA_ERR_ARG;
+	if (vfdElmNum > sa::kNoAllocMaxElm || tgtElmNum > sa::kNoAllocMaxElm) return SA_ERR_ARG;   // scratch limit
+	if (cenKnlType != 'G' && cenKnlType != 'C' && cenKnlType != 'M') return SA_ERR_ARG;
+	if (dirKnlType != 'B' && dirKnlType != 'L' && dirKnlType != 'O' && dirKnlType != 'U') return SA_ERR_ARG;
+	if (!on_device(lmkMat) || !on_device(vfdVtxMat) || !on_device(tgtCenPosMat) || !on_device(tgtUniDirMat) ||
+	    !on_device(tgtElmVolVec))
+		return SA_ERR_ARG;                     // inputs must already be in device memory: nothing is copied
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SA_ERR_CUDA; }
+	double *scr = nullptr;
+	int rc = noalloc_scratch(dev, &scr);
+	if (rc != SA_OK) return rc;
+	cudaStream_t s = (cudaStream_t) stream;
+	try {
+		double v = dim == 2
+		    ? sa::varifold_in_scratch<2>(scr, lmkNum, lmkMat, vfdElmNum, vfdVtxMat, tgtElmNum, tgtCenPosMat,
+		                                 tgtUniDirMat, tgtElmVolVec, cenKnlType, cenKnlWidth, dirKnlType,
+		                                 dirKnlWidth, s)
+		    : sa::varifold_in_scratch<3>(scr, lmkNum, lmkMat, vfdElmNum, vfdVtxMat, tgtElmNum, tgtCenPosMat,
+		                                 tgtUniDirMat, tgtElmVolVec, cenKnlType, cenKnlWidth, dirKnlType,
+		                                 dirKnlWidth, s);
+		if (cudaMemcpy(objOut, &v, sizeof(double), cudaMemcpyDefault) != cudaSuccess) {
+			cudaGetLastError();
+			return SA_ERR_CUDA;
+		}
+	} catch (const sa::CudaError &) {
+		cudaGetLastError();
+		return SA_ERR_CUDA;
+	}
+	return SA_OK;
+}
