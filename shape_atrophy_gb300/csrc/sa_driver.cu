@@ -262,6 +262,19 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		m.slOff = P.alloc<int>(nsl);
 		m.slCol = P.alloc<int>(total);
 		m.slDest = P.alloc<int>(m.Z);
+		// slot of the transposed entry: row j of femVtxMat is sorted by column
+		// (checked above), so (j, i) is found by bisection
+		std::vector<int> tz(m.Z);
+		for (int z = 0; z < m.Z; ++z) {
+			int i = fv[z], j = fv[m.Z + z];
+			const int *b = fv.data() + m.Z + rp[j], *e = fv.data() + m.Z + rp[j + 1];
+			const int *q = std::lower_bound(b, e, i);
+			SA_REQUIRE(q != e && *q == i, "femVtxMat pattern is not symmetric");
+			tz[z] = rp[j] + (int) (q - b);
+			SA_REQUIRE(fi[z] == fi[tz[z]], "femIfoMat lists differ between (i, j) and (j, i)");
+		}
+		m.transZ = P.alloc<int>(m.Z);
+		SA_CHECK(cudaMemcpyAsync(m.transZ, tz.data(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slWidth, wid.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slOff, off.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slCol, col.data(), sizeof(int) * total, cudaMemcpyHostToDevice, s));
@@ -305,8 +318,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	w.Mnow = P.alloc<double>(Z); w.Mnxt = P.alloc<double>(Z); w.L = P.zeros<double>(T);
 	w.dinvRd = P.alloc<double>(N); w.rhs = P.alloc<double>(N);
 	for (Geom *g : {&w.g0, &w.g1}) {
-		g->QI = P.alloc<double>((size_t) (D + 1) * D * E);
-		g->absDet = P.alloc<double>(E); g->vol = P.alloc<double>(E);
+		g->rec = P.alloc<double>((size_t) rec_len<D>() * E);
 		if (md.frame) { g->frm = P.alloc<double>((size_t) D * E); g->tsv = P.alloc<double>((size_t) D * E); }
 	}
 	int nb = grid_for(N, 256);

@@ -83,22 +83,6 @@ template <> __device__ __forceinline__ Mat<3> inv_edges<3>(const Vec<3> *q, doub
 	return r;
 }
 
-// gradient of barycentric coordinate a (0..D) from Q^{-1} stored SoA: QI[(r*D+c)*E+e]
-template <int D> __device__ __forceinline__ Vec<D> bary_grad(const double *QI, int E, int e, int a)
-{
-	Vec<D> g;
-	if (a > 0) {
-		for (int c = 0; c < D; ++c) g.c[c] = QI[((a - 1) * D + c) * (long) E + e];
-	} else {
-		for (int c = 0; c < D; ++c) {
-			double s = -QI[(0 * D + c) * (long) E + e];
-			for (int r = 1; r < D; ++r) s = s - QI[(r * D + c) * (long) E + e];
-			g.c[c] = s;
-		}
-	}
-	return g;
-}
-
 // --------------------------------------------------------------------------
 // activity functions (inc/activity.h:4-38, 106-167)
 // --------------------------------------------------------------------------
@@ -158,16 +142,23 @@ struct Mesh {              // device copy of one element object + derived tables
 	int *slOff = nullptr;      // nslice: first slot of the slice
 	int *slCol = nullptr;      // slTotal: column (node) of each slot; padding points at the row itself
 	int *slDest = nullptr;     // Z: sliced slot of each femVtxMat slot
+	int *transZ = nullptr;     // Z: femVtxMat slot of the transposed entry (j, i)
 	int *asmTab = nullptr;     // femIfoCols/2-1 x Z: e*16 + a*4 + b, femIfo order
 	int asmCols = 0;
 	signed char *sign0 = nullptr;  // initial orientation of each element
 	std::vector<void *> owned;
 };
 
+// Per-element geometry record, one aligned record per element so that an
+// assembly contribution reads one cache line: gradients of the barycentric
+// coordinates (a = 0..D, component c at a*D + c), then the element volume
+// and |det Q|.  128 bytes in 3D, 64 bytes in 2D.
+template <int D> constexpr int rec_len() { return D == 3 ? 16 : 8; }
+template <int D> constexpr int rec_vol() { return (D + 1) * D; }
+template <int D> constexpr int rec_det() { return (D + 1) * D + 1; }
+
 struct Geom {              // per-element geometry of one configuration
-	double *QI = nullptr;      // D*D x E
-	double *absDet = nullptr;  // E   |det Q|
-	double *vol = nullptr;     // E   computeVolume
+	double *rec = nullptr;     // rec_len<D>() x E, element-major
 	double *frm = nullptr;     // D x E frame: tangent (2D) / normal (3D)
 	double *tsv = nullptr;     // D x E transverse direction
 };

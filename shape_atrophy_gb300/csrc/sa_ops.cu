@@ -25,7 +25,7 @@ namespace sa {
 // ---------------------------------------------------------------------------
 template <int D>
 __global__ void k_elem_geom(int E, const int *__restrict__ elmVtx, const double *__restrict__ x,
-                            double *__restrict__ G, double *__restrict__ absDet, double *__restrict__ vol,
+                            double *__restrict__ rec,
                             int frame, const int *__restrict__ frmVtx, const int *__restrict__ tsvVtx,
                             double *__restrict__ frm, double *__restrict__ tsv,
                             const signed char *__restrict__ sign0, int *inverted)
@@ -37,16 +37,20 @@ __global__ void k_elem_geom(int E, const int *__restrict__ elmVtx, const double 
 	for (int k = 0; k < D; ++k) q[k] = vsub(load_node<D>(x, elmVtx[(k + 1) * E + e]), q0);
 	double det = det_edges<D>(q);
 	Mat<D> QI = inv_edges<D>(q, det);
+	double r[rec_len<D>()];
 	// gradient of phi_0 is minus the column sums of Q^{-1} (reference order: -a - b - c)
 	for (int c = 0; c < D; ++c) {
 		double s = -QI.m[0][c];
-		for (int r = 1; r < D; ++r) s = s - QI.m[r][c];
-		G[(0 * D + c) * (long) E + e] = s;
-		for (int r = 0; r < D; ++r) G[((r + 1) * D + c) * (long) E + e] = QI.m[r][c];
+		for (int k = 1; k < D; ++k) s = s - QI.m[k][c];
+		r[c] = s;
+		for (int k = 0; k < D; ++k) r[(k + 1) * D + c] = QI.m[k][c];
 	}
 	double ad = fabs(det);
-	absDet[e] = ad;
-	vol[e] = (D == 2 ? 0.5 * ad : ad / 6.0);          // inc/utility.h:11-29
+	r[rec_vol<D>()] = (D == 2 ? 0.5 * ad : ad / 6.0);   // inc/utility.h:11-29
+	r[rec_det<D>()] = ad;
+	for (int k = rec_det<D>() + 1; k < rec_len<D>(); ++k) r[k] = 0.0;
+	double2 *o = reinterpret_cast<double2 *>(rec + (long) e * rec_len<D>());
+	for (int k = 0; k < rec_len<D>() / 2; ++k) o[k] = make_double2(r[2 * k], r[2 * k + 1]);
 	if (sign0) {
 		signed char sg = det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
 		if (sg != sign0[e]) atomicAdd(inverted, 1);
@@ -86,9 +90,8 @@ template <int D>
 void launch_elem_geom(const Mesh &m, const Model &md, const double *x, Geom &g, Status *st, bool check,
                       cudaStream_t s)
 {
-	k_elem_geom<D><<<grid_for(m.E), kBlock, 0, s>>>(m.E, m.elmVtx, x, g.QI, g.absDet, g.vol, md.frame,
-	                                                  m.frmVtx, m.tsvVtx, g.frm, g.tsv,
-	                                                  check ? m.sign0 : nullptr, &st->inverted);
+	k_elem_geom<D><<<grid_for(m.E), kBlock, 0, s>>>(m.E, m.elmVtx, x, g.rec, md.frame, m.frmVtx, m.tsvVtx, g.frm,
+	                                                  g.tsv, check ? m.sign0 : nullptr, &st->inverted);
 }
 
 // ---------------------------------------------------------------------------
@@ -183,8 +186,7 @@ void launch_tau_initial(const Mesh &m, const Model &md, const double *tv, const 
 // ---------------------------------------------------------------------------
 template <int D>
 __global__ void k_yank_rhs(int N, int E, const int *__restrict__ vtxElm, const int *__restrict__ elmVtx,
-                           const double *__restrict__ G, const double *__restrict__ vol,
-                           const double *__restrict__ fy, double *__restrict__ b)
+                           const double *__restrict__ rec, const double *__restrict__ fy, double *__restrict__ b)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= N) return;
@@ -196,8 +198,9 @@ __global__ void k_yank_rhs(int N, int E, const int *__restrict__ vtxElm, const i
 		double fs = fy[elmVtx[e]];
 		for (int k = 1; k <= D; ++k) fs = fs + fy[elmVtx[k * (long) E + e]];
 		double fc = fs / (D + 1);
-		double v = vol[e];
-		for (int d = 0; d < D; ++d) acc[d] = acc[d] + -fc * G[(l * D + d) * (long) E + e] * v;
+		const double *R = rec + (long) e * rec_len<D>();
+		double v = R[rec_vol<D>()];
+		for (int d = 0; d < D; ++d) acc[d] = acc[d] + -fc * R[l * D + d] * v;
 	}
 	for (int d = 0; d < D; ++d) b[(long) i * D + d] = acc[d];
 }
@@ -205,7 +208,7 @@ __global__ void k_yank_rhs(int N, int E, const int *__restrict__ vtxElm, const i
 template <int D>
 void launch_yank_rhs(const Mesh &m, const Geom &g, const double *fy, double *b, cudaStream_t s)
 {
-	k_yank_rhs<D><<<grid_for(m.N), kBlock, 0, s>>>(m.N, m.E, m.vtxElm, m.elmVtx, g.QI, g.vol, fy, b);
+	k_yank_rhs<D><<<grid_for(m.N), kBlock, 0, s>>>(m.N, m.E, m.vtxElm, m.elmVtx, g.rec, fy, b);
 }
 
 // ---------------------------------------------------------------------------
@@ -304,9 +307,11 @@ __device__ __forceinline__ void pre_frame(Mat<3> &pm, const Vec<3> &n, const Vec
 }
 
 // ---------------------------------------------------------------------------
-// elasticity block assembly: one thread per femVtxMat slot (i, j); the
-// contributions are the elements listed for the slot in femIfoMat (same
-// order), with ordered local indices (a, b) precomputed in asmTab.
+// elasticity block assembly: one thread per femVtxMat slot (i, j) with
+// i <= j; the contributions are the elements listed for the slot in
+// femIfoMat (same order), with ordered local indices (a, b) precomputed in
+// asmTab.  The block of (j, i) is the transpose and is written by the same
+// thread, so the assembled operator is exactly symmetric.
 //   isotropic: K_ab = vol (lambda g_a g_b^T + mu (g_a.g_b) I + mu g_b g_a^T)
 //   frame:     column c of K_ab = vol * preMat(sym(e_c (x) g_b))^T g_a
 // Diagonal slots add btmWgt * pd_i * I and write the Jacobi inverse.
@@ -314,34 +319,37 @@ __device__ __forceinline__ void pre_frame(Mat<3> &pm, const Vec<3> &n, const Vec
 template <int D>
 __global__ void k_asm_elastic(int Z, int E, int asmCols, const int *__restrict__ femVtx,
                               const int *__restrict__ femIfo, const int *__restrict__ asmTab,
-                              const double *__restrict__ G, const double *__restrict__ vol,
+                              const double *__restrict__ rec,
                               int frame, FrameMod fm, const double *__restrict__ frm, const double *__restrict__ tsv,
                               const int *__restrict__ lyr, const double *__restrict__ lyrMod,
                               double btmWgt, const double *__restrict__ pd, int Nb,
-                              const int *__restrict__ slDest, long total,
+                              const int *__restrict__ slDest, const int *__restrict__ transZ, long total,
                               double *__restrict__ blk, double *__restrict__ dinv)
 {
 	int z = blockIdx.x * blockDim.x + threadIdx.x;
 	if (z >= Z) return;
+	const int i = femVtx[z], j = femVtx[Z + z];
+	if (i > j) return;                       // written by the thread of (j, i)
 	double acc[D][D];
 	for (int r = 0; r < D; ++r) for (int c = 0; c < D; ++c) acc[r][c] = 0.0;
 	int cnt = femIfo[z];
 	for (int k = 0; k < cnt; ++k) {
 		int code = asmTab[k * (long) Z + z];
 		int e = code >> 4, a = (code >> 2) & 3, b = code & 3;
-		double v = vol[e];
+		const double *R = rec + (long) e * rec_len<D>();
+		double v = R[rec_vol<D>()];
 		Vec<D> ga, gb;
-		for (int c = 0; c < D; ++c) {
-			ga.c[c] = G[(a * D + c) * (long) E + e];
-			gb.c[c] = G[(b * D + c) * (long) E + e];
-		}
+		for (int c = 0; c < D; ++c) { ga.c[c] = R[a * D + c]; gb.c[c] = R[b * D + c]; }
 		if (!frame) {
 			int l = lyr[e];
-			double lam = lyrMod[2 * l], mu = lyrMod[2 * l + 1];
-			double gg = vdot(ga, gb);
-			for (int r = 0; r < D; ++r)
-				for (int c = 0; c < D; ++c)
-					acc[r][c] += v * (lam * ga.c[r] * gb.c[c] + mu * gb.c[r] * ga.c[c] + (r == c ? mu * gg : 0.0));
+			double vl = v * lyrMod[2 * l], vm = v * lyrMod[2 * l + 1];
+			double la[D], ma[D];
+			for (int r = 0; r < D; ++r) { la[r] = vl * ga.c[r]; ma[r] = vm * ga.c[r]; }
+			double dg = vm * vdot(ga, gb);
+			for (int r = 0; r < D; ++r) {
+				for (int c = 0; c < D; ++c) acc[r][c] += la[r] * gb.c[c] + gb.c[r] * ma[c];
+				acc[r][r] += dg;
+			}
 		} else {
 			Vec<D> fa, sa;
 			for (int d = 0; d < D; ++d) { fa.c[d] = frm[d * (long) E + e]; sa.c[d] = tsv[d * (long) E + e]; }
@@ -359,15 +367,19 @@ __global__ void k_asm_elastic(int Z, int E, int asmCols, const int *__restrict__
 			}
 		}
 	}
-	int i = femVtx[z], j = femVtx[Z + z];
 	if (i == j) {
 		double p = (i < Nb) ? btmWgt * pd[i] : 0.0;
 		for (int d = 0; d < D; ++d) {
 			acc[d][d] += p;
 			dinv[(long) i * D + d] = 1.0 / acc[d][d];
 		}
+		store_block<D>(blk, total, slDest[z], acc);
+		return;
 	}
 	store_block<D>(blk, total, slDest[z], acc);
+	double tr[D][D];
+	for (int r = 0; r < D; ++r) for (int c = 0; c < D; ++c) tr[r][c] = acc[c][r];
+	store_block<D>(blk, total, slDest[transZ[z]], tr);
 }
 
 template <int D>
@@ -376,9 +388,9 @@ void launch_assemble_elastic(const Mesh &m, const Model &md, const Geom &g, cons
 {
 	FrameMod fm;
 	for (int k = 0; k < 4; ++k) fm.m[k] = md.mod[k];
-	k_asm_elastic<D><<<grid_for(m.Z, 128), 128, 0, s>>>(m.Z, m.E, m.asmCols, m.femVtx, m.femIfo, m.asmTab, g.QI,
-	                                                     g.vol, md.frame, fm, g.frm, g.tsv, m.elmLyr, md.lyrMod,
-	                                                     md.btmWgt, pd, m.Nb, m.slDest, m.slTotal, blk, dinv);
+	k_asm_elastic<D><<<grid_for(m.Z, 128), 128, 0, s>>>(m.Z, m.E, m.asmCols, m.femVtx, m.femIfo, m.asmTab, g.rec,
+	                                                     md.frame, fm, g.frm, g.tsv, m.elmLyr, md.lyrMod, md.btmWgt,
+	                                                     pd, m.Nb, m.slDest, m.transZ, m.slTotal, blk, dinv);
 }
 
 // ---------------------------------------------------------------------------
@@ -386,12 +398,12 @@ void launch_assemble_elastic(const Mesh &m, const Model &md, const Geom &g, cons
 // values on the femVtxMat pattern, gathered in femIfoMat order
 // ---------------------------------------------------------------------------
 template <int D>
-__device__ __forceinline__ double ggd_value(int frame, int e, int E, int a, int b, const double *G,
+__device__ __forceinline__ double ggd_value(int frame, int e, int E, int a, int b, const double *R,
                                             double absDet, const double *frm, const double *tsv,
                                             double spdTan, double spdTsv, double Dl)
 {
 	Vec<D> ga, gb;
-	for (int c = 0; c < D; ++c) { ga.c[c] = G[(a * D + c) * (long) E + e]; gb.c[c] = G[(b * D + c) * (long) E + e]; }
+	for (int c = 0; c < D; ++c) { ga.c[c] = R[a * D + c]; gb.c[c] = R[b * D + c]; }
 	if (!frame) {
 		double mvol = (D == 2 ? 0.5 * absDet : absDet / 6.0);
 		return mvol * (Dl * vdot(ga, gb));
@@ -403,7 +415,7 @@ __device__ __forceinline__ double ggd_value(int frame, int e, int E, int a, int 
 	double fP[D + 1], sP[D + 1];
 	for (int k = 1; k <= D; ++k) {
 		Vec<D> gk;
-		for (int c = 0; c < D; ++c) gk.c[c] = G[(k * D + c) * (long) E + e];
+		for (int c = 0; c < D; ++c) gk.c[c] = R[k * D + c];
 		fP[k] = vdot(gk, f); sP[k] = vdot(gk, s);
 	}
 	fP[0] = -fP[1]; sP[0] = -sP[1];
@@ -414,17 +426,21 @@ __device__ __forceinline__ double ggd_value(int frame, int e, int E, int a, int 
 	return absDet / 6.0 * (spdTan * (gg - fP[a] * fP[b]) + spdTsv * sP[a] * sP[b]);
 }
 
+// one thread per slot (i, j) with i <= j; M and G are symmetric (the
+// femIfoMat lists of (i, j) and (j, i) hold the same elements in the same
+// order), so the thread writes both entries
 template <int D>
 __global__ void k_asm_rd(int Z, int E, const int *__restrict__ femVtx, const int *__restrict__ femIfo,
-                         const int *__restrict__ asmTab, const double *__restrict__ G,
-                         const double *__restrict__ absDet, int frame, const double *__restrict__ frm,
-                         const double *__restrict__ tsv, double spdTan, double spdTsv,
+                         const int *__restrict__ asmTab, const double *__restrict__ rec, int frame,
+                         const double *__restrict__ frm, const double *__restrict__ tsv, double spdTan, double spdTsv,
                          const int *__restrict__ lyr, const double *__restrict__ lyrSpd, double dt,
-                         const int *__restrict__ slDest,
+                         const int *__restrict__ slDest, const int *__restrict__ transZ,
                          double *__restrict__ Mval, double *__restrict__ Lval, double *__restrict__ dinv)
 {
 	int z = blockIdx.x * blockDim.x + threadIdx.x;
 	if (z >= Z) return;
+	const int i = femVtx[z], j = femVtx[Z + z];
+	if (i > j) return;
 	int cnt = femIfo[z];
 	double mul = femIfo[Z + z];
 	double M = 0.0, Gs = 0.0;
@@ -432,25 +448,28 @@ __global__ void k_asm_rd(int Z, int E, const int *__restrict__ femVtx, const int
 		int code = asmTab[k * (long) Z + z];
 		int e = code >> 4, a = (code >> 2) & 3, b = code & 3;
 		int lo = a < b ? a : b, hi = a < b ? b : a;
-		double ad = absDet[e];
+		const double *R = rec + (long) e * rec_len<D>();
+		double ad = R[rec_det<D>()];
 		M += mul * (ad / (D == 2 ? 24.0 : 120.0));
 		double Dl = frame ? 0.0 : lyrSpd[lyr[e]];
-		Gs += ggd_value<D>(frame, e, E, lo, hi, G, ad, frm, tsv, spdTan, spdTsv, Dl);
+		Gs += ggd_value<D>(frame, e, E, lo, hi, R, ad, frm, tsv, spdTan, spdTsv, Dl);
 	}
 	double L = 1.0 * M + dt * Gs;
 	Mval[z] = M;                 // femVtxMat (CSR) order, read by the next step's right-hand side
 	Lval[slDest[z]] = L;         // sliced layout, read by the CG matvec
-	int i = femVtx[z];
-	if (i == femVtx[Z + z]) dinv[i] = 1.0 / L;
+	if (i == j) { dinv[i] = 1.0 / L; return; }
+	int zt = transZ[z];
+	Mval[zt] = M;
+	Lval[slDest[zt]] = L;
 }
 
 template <int D>
 void launch_assemble_rd(const Mesh &m, const Model &md, const Geom &g, double dt, double *Mval, double *Lval,
                         double *dinv, cudaStream_t s)
 {
-	k_asm_rd<D><<<grid_for(m.Z), kBlock, 0, s>>>(m.Z, m.E, m.femVtx, m.femIfo, m.asmTab, g.QI, g.absDet, md.frame,
-	                                              g.frm, g.tsv, md.spdTan, md.spdTsv, m.elmLyr, md.lyrSpd, dt, m.slDest,
-	                                              Mval, Lval, dinv);
+	k_asm_rd<D><<<grid_for(m.Z), kBlock, 0, s>>>(m.Z, m.E, m.femVtx, m.femIfo, m.asmTab, g.rec, md.frame, g.frm,
+	                                              g.tsv, md.spdTan, md.spdTsv, m.elmLyr, md.lyrSpd, dt, m.slDest,
+	                                              m.transZ, Mval, Lval, dinv);
 }
 
 // rhs_i = (M_t tau_t)_i + dt * sum_{e ∋ i} (tau-weighted consistent mass load)
@@ -458,7 +477,7 @@ template <int D>
 __global__ void k_rd_rhs(int N, int E, const int *__restrict__ rowPtr, const int *__restrict__ col,
                          const double *__restrict__ Mnow, const double *__restrict__ tau,
                          const int *__restrict__ vtxElm, const int *__restrict__ elmVtx,
-                         const double *__restrict__ absDet, const double *__restrict__ fr, double dt,
+                         const double *__restrict__ rec, const double *__restrict__ fr, double dt,
                          double *__restrict__ rhs)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -474,7 +493,7 @@ __global__ void k_rd_rhs(int N, int E, const int *__restrict__ rowPtr, const int
 			double f = fr[elmVtx[k * (long) E + e]];
 			s = s + (k == l ? 2.0 * f : f);
 		}
-		rp += s * absDet[e] / (D == 2 ? 24.0 : 120.0);
+		rp += s * rec[(long) e * rec_len<D>() + rec_det<D>()] / (D == 2 ? 24.0 : 120.0);
 	}
 	rhs[i] = 1.0 * mt + dt * rp;
 }
@@ -484,7 +503,7 @@ void launch_rd_rhs(const Mesh &m, const Geom &gNow, const double *Mnow, const do
                    double dt, double *rhs, cudaStream_t s)
 {
 	k_rd_rhs<D><<<grid_for(m.N), kBlock, 0, s>>>(m.N, m.E, m.rowPtr, m.femVtx + m.Z, Mnow, tau, m.vtxElm, m.elmVtx,
-	                                             gNow.absDet, fr, dt, rhs);
+	                                             gNow.rec, fr, dt, rhs);
 }
 
 // ---------------------------------------------------------------------------
