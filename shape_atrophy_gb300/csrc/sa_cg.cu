@@ -9,10 +9,10 @@
 // with the dot (w, u)) and one vector kernel (p, s, x, r, u updates fused
 // with the dots (r, u) and (r, r)).  All scalars stay on the device; the
 // last block of each kernel finishes its reduction in a fixed order, so
-// results do not depend on block scheduling.  Kernel arguments never
-// change between iterations, so chunks of iterations are captured once in
-// a CUDA graph and replayed; the host reads the status word once per
-// chunk.  Stopping rule as the reference: |r|^2 < tol^2 |b|^2, b = 0
+// results do not depend on block scheduling.  Iterations are queued in
+// chunks of 16, one chunk ahead of the host's check of the status word (a
+// kernel returns at once when the solve has stopped), so the device does
+// not wait for the host.  Stopping rule as the reference: |r|^2 < tol^2 |b|^2, b = 0
 // gives x = 0.
 //
 // Mixed precision (SA_PREC_MIXED): FP32 operator values and FP32 vectors in
@@ -31,58 +31,88 @@ struct CgScal {
 	int pad;
 };
 
-// FP64 throughput on GB300 is 2 thread-DFMA per clock per SM, so the
-// kernels below avoid FP64 work that is not the algorithm's own: dot
-// products are shuffle-reduced only by warps that hold data, and vector
-// kernels reduce kVecPer entries per thread before any shuffle.
+// FP64 throughput on GB300 is 2 thread-DFMA per clock per SM (a warp
+// instruction occupies the SM's FP64 pipe for 16 cycles), so the kernels
+// below avoid FP64 work that is not the algorithm's own: block sums of the
+// dot products go through shared memory and are added by one warp, and the
+// vector kernels run on a grid of kVecCtasPerSm CTAs per SM, every SM taking
+// the same share of entries.
 constexpr int kCgBlock = 256;      // vector kernels
-constexpr int kVecPer = 4;         // vector entries per thread
+constexpr int kVecCtasPerSm = 4;   // vector kernels: CTAs per SM (grid-stride loops)
 constexpr int kSlicesPerCta = 4;   // matvec: one warp per 32-row slice, one thread per row
 constexpr int kSpmvBlock = 32 * kSlicesPerCta;
 
-// block-wide reduction of K values; writes part[k*nb + blockIdx.x]; returns true in the last block
+// fixed-order sum over the NT threads of a block of K values each; the
+// result is valid in thread 0.  Called by every thread of the block.
+template <int K, int NT>
+__device__ __forceinline__ void block_sum(double (&v)[K], double (&sm)[K][NT])
+{
+	const int lane = threadIdx.x & 31;
+	for (int k = 0; k < K; ++k) sm[k][threadIdx.x] = v[k];
+	__syncthreads();
+	if (threadIdx.x < 32)
+		for (int k = 0; k < K; ++k) {
+			double s = sm[k][lane];
+#pragma unroll
+			for (int q = 1; q < NT / 32; ++q) s += sm[k][lane + 32 * q];
+			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+			v[k] = s;
+		}
+}
+
+// block partials part[k * nb + blockIdx.x]; returns true in the block that
+// arrives last (the one that finishes the reduction)
 template <int K, int NT>
 __device__ __forceinline__ bool reduce_partials(double (&v)[K], double *part, unsigned int *counter)
 {
-	__shared__ double sm[K][NT / 32];
+	__shared__ double sm[K][NT];
 	__shared__ bool last;
-	int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-	for (int k = 0; k < K; ++k)
-		for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
-	if (lane == 0) for (int k = 0; k < K; ++k) sm[k][wid] = v[k];
-	__syncthreads();
+	block_sum<K, NT>(v, sm);
 	if (threadIdx.x == 0) {
-		for (int k = 0; k < K; ++k) {
-			double s = 0.0;
-			for (int w = 0; w < NT / 32; ++w) s += sm[k][w];
-			part[k * gridDim.x + blockIdx.x] = s;
-		}
+		for (int k = 0; k < K; ++k) part[k * gridDim.x + blockIdx.x] = v[k];
 		__threadfence();
-		unsigned int t = atomicAdd(counter, 1u);
-		last = (t == gridDim.x - 1);
+		last = (atomicAdd(counter, 1u) == gridDim.x - 1);
 	}
 	__syncthreads();
 	return last;
 }
 
-// fixed-order sum of the partials by warp 0 of the last block (result valid in lane 0)
-template <int K>
+// fixed-order sum of the partials by every thread of the last block
+// (thread t adds partials t, t + NT, ...; then block_sum); valid in thread 0
+template <int K, int NT>
 __device__ __forceinline__ void finish_partials(double (&out)[K], const double *part)
 {
-	int lane = threadIdx.x & 31;
+	__shared__ double sm[K][NT];
+	const int G = gridDim.x;
 	for (int k = 0; k < K; ++k) {
 		double s = 0.0;
-		for (int b = lane; b < (int) gridDim.x; b += 32) s += __ldcg(part + k * gridDim.x + b);
-		for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+#pragma unroll 8
+		for (int b = threadIdx.x; b < G; b += NT) s += __ldcg(part + (long) k * G + b);
 		out[k] = s;
 	}
+	block_sum<K, NT>(out, sm);
+}
+
+// one block slot of a row: acc += A_slot * u[col]
+template <int B, typename TM, typename TV>
+__device__ __forceinline__ void spmv_slot(const SellOp &A, const TM *__restrict__ blk, const TV *__restrict__ u,
+                                          long idx, TV (&acc)[B])
+{
+	int j = __ldg(A.col + idx);
+	TV xj[B];
+	for (int c = 0; c < B; ++c) xj[c] = u[(long) j * B + c];
+	TM a[B * B];
+	load_block<B, TM>(blk, A.total, idx, a);
+	for (int r = 0; r < B; ++r)
+		for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
 }
 
 // ---------------------------------------------------------------------------
-// matvec kernel: w = A u and the partial (w, u).  One CTA per 32-row slice;
-// warp p of the CTA takes block slots k = p, p + kTpr, ... of the slice, so
-// every load instruction of a warp reads 32 consecutive slots; the kTpr
-// partial rows are combined in shared memory in a fixed order.
+// matvec kernel: w = A u and the partial (w, u).  One warp per 32-row slice,
+// one thread per row, kSlicesPerCta slices per CTA; every load instruction
+// of a warp reads 32 consecutive slots.  Even and odd slots go to separate
+// accumulators (two independent load and FMA streams per thread).  The last
+// CTA to finish forms alpha and beta.
 // ---------------------------------------------------------------------------
 template <int B, typename TM, typename TV>
 __global__ void __launch_bounds__(kSpmvBlock) k_cg_spmv(SellOp A, const TM *__restrict__ blk,
@@ -100,23 +130,19 @@ __global__ void __launch_bounds__(kSpmvBlock) k_cg_spmv(SellOp A, const TM *__re
 		const int i = sl * 32 + lane;
 		const int wdt = __ldg(A.width + sl);
 		const long base = __ldg(A.off + sl) + lane;
-		TV acc[B];
-		for (int r = 0; r < B; ++r) acc[r] = (TV) 0;
-#pragma unroll 4
-		for (int k = 0; k < wdt; ++k) {
-			long idx = base + ((long) k << 5);
-			int j = __ldg(A.col + idx);
-			TV xj[B];
-			for (int c = 0; c < B; ++c) xj[c] = u[(long) j * B + c];
-			TM a[B * B];
-			load_block<B, TM>(blk, A.total, idx, a);
-			for (int r = 0; r < B; ++r)
-				for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
+		TV acc0[B], acc1[B];
+		for (int r = 0; r < B; ++r) { acc0[r] = (TV) 0; acc1[r] = (TV) 0; }
+		int k = 0;
+		for (; k + 2 <= wdt; k += 2) {
+			spmv_slot<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+			spmv_slot<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), acc1);
 		}
+		if (k < wdt) spmv_slot<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
 		if (i < A.N)
 			for (int r = 0; r < B; ++r) {
-				w[(long) i * B + r] = acc[r];
-				v += (double) acc[r] * (double) u[(long) i * B + r];
+				TV o = acc0[r] + acc1[r];
+				w[(long) i * B + r] = o;
+				v += (double) o * (double) u[(long) i * B + r];
 			}
 		for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
 	}
@@ -132,7 +158,7 @@ __global__ void __launch_bounds__(kSpmvBlock) k_cg_spmv(SellOp A, const TM *__re
 	__syncthreads();
 	if (!last) return;
 	double d[1];
-	finish_partials<1>(d, part);
+	finish_partials<1, kSpmvBlock>(d, part);
 	if (threadIdx.x == 0) {
 		double delta = d[0], gam = sc->gam, alpha, beta;
 		if (sc->first) { beta = 0.0; alpha = gam / delta; }
@@ -150,8 +176,9 @@ __global__ void __launch_bounds__(kSpmvBlock) k_cg_spmv(SellOp A, const TM *__re
 }
 
 // ---------------------------------------------------------------------------
-// vector kernel, one thread per entry:
+// vector kernel (grid-stride over entries):
 // p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^{-1} r
+// and the dots (r, u), (r, r)
 // ---------------------------------------------------------------------------
 template <typename TV, typename TX>
 __global__ void __launch_bounds__(kCgBlock) k_cg_update(long n, TX *__restrict__ x, TV *__restrict__ r,
@@ -163,25 +190,22 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_update(long n, TX *__restrict__
 	const long stride = (long) gridDim.x * blockDim.x;
 	double v[2] = {0.0, 0.0};
 	const TV al = (TV) sc->alpha, be = (TV) sc->beta;
-#pragma unroll
-	for (int j = 0; j < kVecPer; ++j) {
-		long k = blockIdx.x * (long) blockDim.x + threadIdx.x + j * stride;
-		if (k < n) {
-			TV pk = u[k] + be * p[k];
-			TV sk = w[k] + be * s[k];
-			p[k] = pk; s[k] = sk;
-			x[k] = x[k] + (TX) al * (TX) pk;
-			TV rk = r[k] - al * sk;
-			r[k] = rk;
-			TV uk = dinv[k] * rk;
-			u[k] = uk;
-			v[0] += (double) rk * (double) uk;
-			v[1] += (double) rk * (double) rk;
-		}
+#pragma unroll 2
+	for (long k = blockIdx.x * (long) blockDim.x + threadIdx.x; k < n; k += stride) {
+		TV pk = u[k] + be * p[k];
+		TV sk = w[k] + be * s[k];
+		p[k] = pk; s[k] = sk;
+		x[k] = x[k] + (TX) al * (TX) pk;
+		TV rk = r[k] - al * sk;
+		r[k] = rk;
+		TV uk = dinv[k] * rk;
+		u[k] = uk;
+		v[0] += (double) rk * (double) uk;
+		v[1] += (double) rk * (double) rk;
 	}
 	if (!reduce_partials<2, kCgBlock>(v, part, &sc->counter)) return;
 	double d[2];
-	finish_partials<2>(d, part);
+	finish_partials<2, kCgBlock>(d, part);
 	if (threadIdx.x == 0) {
 		sc->gamPrev = sc->gam;
 		sc->gam = d[0];
@@ -202,21 +226,18 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_init(long n, const double *__re
 {
 	const long stride = (long) gridDim.x * blockDim.x;
 	double v[3] = {0.0, 0.0, 0.0};
-	for (int j = 0; j < kVecPer; ++j) {
-		long k = blockIdx.x * (long) blockDim.x + threadIdx.x + j * stride;
-		if (k < n) {
-			double rk = b[k] - q[k];
-			TV rt = (TV) rk;
-			TV uk = dinv[k] * rt;
-			r[k] = rt; u[k] = uk;
-			v[0] += b[k] * b[k];
-			v[1] += rk * rk;
-			v[2] += (double) rt * (double) uk;
-		}
+	for (long k = blockIdx.x * (long) blockDim.x + threadIdx.x; k < n; k += stride) {
+		double rk = b[k] - q[k];
+		TV rt = (TV) rk;
+		TV uk = dinv[k] * rt;
+		r[k] = rt; u[k] = uk;
+		v[0] += b[k] * b[k];
+		v[1] += rk * rk;
+		v[2] += (double) rt * (double) uk;
 	}
 	if (!reduce_partials<3, kCgBlock>(v, part, &sc->counter)) return;
 	double d[3];
-	finish_partials<3>(d, part);
+	finish_partials<3, kCgBlock>(d, part);
 	if (threadIdx.x == 0) {
 		if (sc->bb < 0.0) sc->bb = d[0];       // bb < 0: take |b|^2 from this rhs
 		sc->rr = d[1]; sc->gam = d[2];
@@ -265,6 +286,13 @@ __global__ void k_spmv64(SellOp A, const double *__restrict__ blk, const double 
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
+// CTAs of the vector kernels: kVecCtasPerSm per SM, fewer for short vectors
+static int vec_grid(long n, int smCount)
+{
+	int need = grid_for(n, kCgBlock);
+	return std::max(1, std::min(need, kVecCtasPerSm * std::max(1, smCount)));
+}
+
 static void set_scal(CgScal *d, double tolSqu, int itrMax, double bb, cudaStream_t s)
 {
 	CgScal h{};
@@ -291,7 +319,7 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 {
 	int N = m.N;
 	long n = (long) N * B;
-	int nb = grid_for(n, kCgBlock * kVecPer);
+	int nb = vec_grid(n, prof->smCount);
 	set_scal(sc, tolSqu, itrMax, bb, s);
 	SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
 	SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
@@ -382,7 +410,7 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 	SA_CHECK(cudaMemsetAsync(zero, 0, sizeof(double) * n, s));
 	int total = 0, code = SA_ERR_NOT_CONVERGED;
 	double bb = -1.0;
-	const int nb = grid_for(n, kCgBlock);
+	const int nb = vec_grid(n, wk.smCount);
 	for (int outer = 0; outer < 64; ++outer) {
 		k_spmv64<B><<<grid_for(N), kBlock, 0, s>>>(sell_of(m), blk, x, q);
 		k_sub<<<grid_for(n), kBlock, 0, s>>>(n, b, q, rin);

@@ -275,6 +275,16 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		}
 		m.transZ = P.alloc<int>(m.Z);
 		SA_CHECK(cudaMemcpyAsync(m.transZ, tz.data(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
+		// assembly order: the N diagonal slots (many elements each) first, then
+		// the strictly upper slots (few elements each), so a warp's threads
+		// loop over similar element counts
+		std::vector<int> ord;
+		ord.reserve((m.Z + m.N) / 2 + 1);
+		for (int z = 0; z < m.Z; ++z) if (fv[z] == fv[m.Z + z]) ord.push_back(z);
+		for (int z = 0; z < m.Z; ++z) if (fv[z] < fv[m.Z + z]) ord.push_back(z);
+		m.nAsm = (int) ord.size();
+		m.asmOrder = P.alloc<int>(ord.size());
+		SA_CHECK(cudaMemcpyAsync(m.asmOrder, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slWidth, wid.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slOff, off.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slCol, col.data(), sizeof(int) * total, cudaMemcpyHostToDevice, s));
@@ -328,6 +338,11 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	// partial sums: up to 3 per CTA of the widest CG kernel grid (entries / 256, or one CTA per slice)
 	int nbCg = std::max(grid_for(n, 256), std::max(m.nslice, nb));
 	c.part = P.alloc<double>((size_t) 3 * nbCg + 64); c.scal = P.zeros<double>(32); c.maxBlocks = nbCg;
+	{
+		int dev = 0;
+		SA_CHECK(cudaGetDevice(&dev));
+		SA_CHECK(cudaDeviceGetAttribute(&c.smCount, cudaDevAttrMultiProcessorCount, dev));
+	}
 	c.xr = P.alloc<double>((size_t) 3 * n);
 	if (md.precision == SA_PREC_MIXED) {
 		c.blk32 = P.alloc<float>((size_t) T * sell_vals<D>());

@@ -143,6 +143,8 @@ struct Mesh {              // device copy of one element object + derived tables
 	int *slCol = nullptr;      // slTotal: column (node) of each slot; padding points at the row itself
 	int *slDest = nullptr;     // Z: sliced slot of each femVtxMat slot
 	int *transZ = nullptr;     // Z: femVtxMat slot of the transposed entry (j, i)
+	int *asmOrder = nullptr;   // nAsm: slots assembled (diagonal slots, then i < j)
+	int nAsm = 0;
 	int *asmTab = nullptr;     // femIfoCols/2-1 x Z: e*16 + a*4 + b, femIfo order
 	int asmCols = 0;
 	signed char *sign0 = nullptr;  // initial orientation of each element
@@ -275,6 +277,7 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	double *part;                 // partial sums: 3 x maxBlocks
 	double *scal;                 // device scalars
 	int maxBlocks;
+	int smCount = 1;              // SMs of the device (grid of the vector kernels)
 	float *blk32 = nullptr;       // FP32 copy of the operator (mixed precision)
 	float *f32 = nullptr;         // 7 n FP32 vectors of the inner solve (mixed precision)
 	double *xr = nullptr;         // 3 n FP64 refinement scratch

@@ -308,7 +308,7 @@ __device__ __forceinline__ void pre_frame(Mat<3> &pm, const Vec<3> &n, const Vec
 
 // ---------------------------------------------------------------------------
 // elasticity block assembly: one thread per femVtxMat slot (i, j) with
-// i <= j; the contributions are the elements listed for the slot in
+// i <= j, diagonal slots first (Mesh::asmOrder); the contributions are the elements listed for the slot in
 // femIfoMat (same order), with ordered local indices (a, b) precomputed in
 // asmTab.  The block of (j, i) is the transpose and is written by the same
 // thread, so the assembled operator is exactly symmetric.
@@ -324,10 +324,12 @@ __global__ void k_asm_elastic(int Z, int E, int asmCols, const int *__restrict__
                               const int *__restrict__ lyr, const double *__restrict__ lyrMod,
                               double btmWgt, const double *__restrict__ pd, int Nb,
                               const int *__restrict__ slDest, const int *__restrict__ transZ, long total,
+                              const int *__restrict__ order, int nOrd,
                               double *__restrict__ blk, double *__restrict__ dinv)
 {
-	int z = blockIdx.x * blockDim.x + threadIdx.x;
-	if (z >= Z) return;
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= nOrd) return;
+	const int z = order[t];
 	const int i = femVtx[z], j = femVtx[Z + z];
 	if (i > j) return;                       // written by the thread of (j, i)
 	double acc[D][D];
@@ -388,9 +390,10 @@ void launch_assemble_elastic(const Mesh &m, const Model &md, const Geom &g, cons
 {
 	FrameMod fm;
 	for (int k = 0; k < 4; ++k) fm.m[k] = md.mod[k];
-	k_asm_elastic<D><<<grid_for(m.Z, 128), 128, 0, s>>>(m.Z, m.E, m.asmCols, m.femVtx, m.femIfo, m.asmTab, g.rec,
-	                                                     md.frame, fm, g.frm, g.tsv, m.elmLyr, md.lyrMod, md.btmWgt,
-	                                                     pd, m.Nb, m.slDest, m.transZ, m.slTotal, blk, dinv);
+	k_asm_elastic<D><<<grid_for(m.nAsm, 128), 128, 0, s>>>(m.Z, m.E, m.asmCols, m.femVtx, m.femIfo, m.asmTab, g.rec,
+	                                                        md.frame, fm, g.frm, g.tsv, m.elmLyr, md.lyrMod, md.btmWgt,
+	                                                        pd, m.Nb, m.slDest, m.transZ, m.slTotal, m.asmOrder,
+	                                                        m.nAsm, blk, dinv);
 }
 
 // ---------------------------------------------------------------------------
@@ -435,10 +438,12 @@ __global__ void k_asm_rd(int Z, int E, const int *__restrict__ femVtx, const int
                          const double *__restrict__ frm, const double *__restrict__ tsv, double spdTan, double spdTsv,
                          const int *__restrict__ lyr, const double *__restrict__ lyrSpd, double dt,
                          const int *__restrict__ slDest, const int *__restrict__ transZ,
+                         const int *__restrict__ order, int nOrd,
                          double *__restrict__ Mval, double *__restrict__ Lval, double *__restrict__ dinv)
 {
-	int z = blockIdx.x * blockDim.x + threadIdx.x;
-	if (z >= Z) return;
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= nOrd) return;
+	const int z = order[t];
 	const int i = femVtx[z], j = femVtx[Z + z];
 	if (i > j) return;
 	int cnt = femIfo[z];
@@ -467,9 +472,9 @@ template <int D>
 void launch_assemble_rd(const Mesh &m, const Model &md, const Geom &g, double dt, double *Mval, double *Lval,
                         double *dinv, cudaStream_t s)
 {
-	k_asm_rd<D><<<grid_for(m.Z), kBlock, 0, s>>>(m.Z, m.E, m.femVtx, m.femIfo, m.asmTab, g.rec, md.frame, g.frm,
-	                                              g.tsv, md.spdTan, md.spdTsv, m.elmLyr, md.lyrSpd, dt, m.slDest,
-	                                              m.transZ, Mval, Lval, dinv);
+	k_asm_rd<D><<<grid_for(m.nAsm), kBlock, 0, s>>>(m.Z, m.E, m.femVtx, m.femIfo, m.asmTab, g.rec, md.frame, g.frm,
+	                                                 g.tsv, md.spdTan, md.spdTsv, m.elmLyr, md.lyrSpd, dt, m.slDest,
+	                                                 m.transZ, m.asmOrder, m.nAsm, Mval, Lval, dinv);
 }
 
 // rhs_i = (M_t tau_t)_i + dt * sum_{e ∋ i} (tau-weighted consistent mass load)
