@@ -126,8 +126,11 @@ class ClockSampler:
 def spec_for(args, steps: int):
     from shape_atrophy_gb300 import problems
     if args.workload == "annulus":
-        return problems.annulus_layered(steps=steps)
-    return problems.shell_layered(steps=steps)
+        spec = problems.annulus_layered(steps=steps)
+    else:
+        spec = problems.shell_layered(steps=steps)
+    spec["cgKernel"] = getattr(args, "cg_kernel", "auto")
+    return spec
 
 
 def cpu_sample(spec_full, seconds: float = 25.0, max_steps: int = 3):
@@ -176,6 +179,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="shell", choices=["shell", "annulus"])
+    ap.add_argument("--cg-kernel", default="auto", choices=["auto", "persistent", "two-kernel"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     args = ap.parse_args()
@@ -194,8 +198,9 @@ def main():
     spec = spec_for(args, W + K)
     sess = api.Session(spec, precision=args.precision, objective=False, device=local)
     sess.step(W)                                       # untimed warm-up steps
-    sess.profile(1)                                    # CUDA-event timing of the velocity matvec
-    launches0 = sess.info()["kernelLaunches"]
+    sess.profile(1)                                    # CUDA-event timing of the velocity CG kernel
+    info0 = sess.info()
+    launches0, iters0 = info0["kernelLaunches"], info0["cgIterTotal"]
     clk = ClockSampler(local)
     clk.start()
     barrier(dist)
@@ -207,32 +212,38 @@ def main():
     ms_dev = info["lastStepMs"]
     ms_max = reduce_max(ms_dev, dist, local)
     barrier(dist)
-    spmv_ms, spmv_cnt, spmv_bytes = sess.profile(0)
+    k_ms, k_cnt, k_bytes, k_flops = sess.profile(0)
     launches = info["kernelLaunches"] - launches0
-    cg_iters = info["cgIterTotal"]
+    cg_iters = info["cgIterTotal"] - iters0
     sess.close()
 
     value = ws * K / (ms_max / 1000.0)
     hbm, peak_kind = peaks()
-    avg_launch_s = (spmv_ms / spmv_cnt) / 1000.0 if spmv_cnt else float("nan")
-    achieved = spmv_bytes / avg_launch_s / 1e9 if spmv_cnt else None
-    D = 3
-    Z = spec["elmObj"]["femVtxMat"].shape[1]
-    fp64_flops = 2.0 * Z * D * D if args.precision == "fp64" else None
+    persistent = 0 < 4 * k_cnt < cg_iters              # one launch per solve, not one per iteration
+    kname = ("k_cg_persist (whole velocity CG solve: matvec, vector updates, dots)" if persistent
+             else "k_cg_spmv (velocity block matvec + dot)")
+    avg_launch_s = (k_ms / k_cnt) / 1000.0 if k_cnt else float("nan")
+    bytes_per_launch = k_bytes / k_cnt if k_cnt else None
+    achieved = bytes_per_launch / avg_launch_s / 1e9 if k_cnt else None
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "k_cg_spmv_shell_l5_traffic.txt")
-    if os.path.exists(tfile) and args.precision == "fp64" and args.workload == "shell":
+    tfile = os.path.join(ROOT, "profiles", ("k_cg_persist" if persistent else "k_cg_spmv") +
+                         f"_shell_l5_{args.precision}_traffic.txt")
+    if os.path.exists(tfile) and args.workload == "shell":
         for line in open(tfile):
-            if line.startswith("dram_bytes_per_launch:"):
-                traffic = float(line.split(":")[1])
+            if line.startswith("dram_bytes_per_iteration:") and cg_iters:
+                traffic = float(line.split(":")[1]) * (cg_iters / k_cnt if persistent else 1.0)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-                "kernel": "k_cg_spmv (velocity block-CSR matvec + dot)", "peak_source": peak_kind,
-                "bytes_per_launch": spmv_bytes, "avg_launch_us": avg_launch_s * 1e6, "launches": spmv_cnt}
-    if fp64_flops:
-        roofline["fp64_pipe"] = {"achieved_tflops": fp64_flops / avg_launch_s / 1e12, "peak_tflops": 1.19,
-                                 "frac": fp64_flops / avg_launch_s / 1e12 / 1.19,
-                                 "peak_source": "measured FP64 FMA loop on this pool's GB300"}
+                "kernel": kname, "peak_source": peak_kind,
+                "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6, "launches": k_cnt}
+    if k_cnt:
+        fl = k_flops / k_cnt / avg_launch_s / 1e12
+        if args.precision == "fp64":
+            roofline["fp64_pipe"] = {"achieved_tflops": fl, "peak_tflops": 1.19, "frac": fl / 1.19,
+                                     "peak_source": "measured FP64 FMA loop on this pool's GB300"}
+        else:
+            roofline["fp32_pipe"] = {"achieved_tflops": fl, "peak_tflops": 69.5, "frac": fl / 69.5,
+                                     "peak_source": "measured FP32 FMA loop on this pool's GB300"}
 
     e2e = None
     if not args.no_e2e and rank == 0:

@@ -44,12 +44,17 @@ extern "C" {
 #define SA_ERR_NOT_CONVERGED  4   /* per-solve status: CG hit its iteration cap */
 #define SA_ERR_BREAKDOWN      5   /* per-solve status: CG breakdown (zero curvature) */
 #define SA_ERR_NONFINITE      6   /* per-solve status: NaN/Inf in a solve */
+#define SA_ERR_TIMEOUT        7   /* a bounded device-side wait (grid barrier) gave up */
 
 #define SA_ELA_FRAME          0   /* reference frame elasticity, K-preconditioned CG */
 #define SA_ELA_ISOTROPIC      1   /* layered isotropic elasticity, Jacobi-PCG */
 
 #define SA_PREC_FP64          0   /* all arithmetic in FP64 */
 #define SA_PREC_MIXED         1   /* FP32 operators, FP64 dots/residuals + refinement */
+
+#define SA_CG_AUTO            0   /* persistent CG kernel when the grid fits on the GPU, else two kernels */
+#define SA_CG_PERSISTENT      1   /* same as AUTO (falls back when the grid does not fit) */
+#define SA_CG_TWO_KERNEL      2   /* matvec + vector kernel per iteration */
 
 typedef struct sa_context sa_context;
 
@@ -93,6 +98,7 @@ typedef struct sa_params {
 	double cgTolSqu;
 	int rdItrMax;                       /* isotropic reaction-diffusion PCG (frame: same as cgItrMax) */
 	double rdTolSqu;                    /* isotropic RD PCG tolerance squared (frame: 1e-28) */
+	int cgKernel;                       /* SA_CG_AUTO (0), SA_CG_PERSISTENT or SA_CG_TWO_KERNEL */
 } sa_params;
 
 /* Varifold target and kernels (computeObjfcn prhs[13..20]). */
@@ -171,9 +177,11 @@ int sa_varifold_noalloc(int dim, int lmkNum, const double *lmkMat, int vfdElmNum
  * solve), sa_session_state copies the current nodes (N x dim) and
  * concentration (N), sa_session_objective evaluates the varifold objective
  * of the current shape (needs a target at creation).  sa_session_profile
- * switches CUDA-event timing of the velocity matvec kernel on or off and
- * returns its accumulated time, launch count and algorithmic bytes per
- * launch. */
+ * switches CUDA-event timing of the velocity CG's dominant kernel on or off
+ * (the persistent CG kernel, or the matvec kernel on the two-kernel path;
+ * enable = -1 leaves it as it is) and returns, since it was last switched,
+ * the kernel's accumulated device time, its launch count and the
+ * algorithmic bytes and flops of those launches. */
 typedef struct sa_session sa_session;
 int sa_session_create(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat,
                       const sa_params *prm, const sa_target *tgt, const double *tauVarVec, int tauVarNum,
@@ -182,7 +190,8 @@ int sa_session_step(sa_session *s, int nsteps, int *stepsDone);
 int sa_session_state(sa_session *s, double *lmkMat, double *tauVec, int *step);
 int sa_session_objective(sa_session *s, double *obj);
 int sa_session_info(sa_session *s, sa_solve_info *info);
-int sa_session_profile(sa_session *s, int enable, double *spmvMs, long long *spmvCount, double *spmvBytes);
+int sa_session_profile(sa_session *s, int enable, double *kernelMs, long long *launches, double *bytes,
+                       double *flops);
 int sa_session_destroy(sa_session *s);
 
 /* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and

@@ -17,7 +17,8 @@ _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
 
 SA_OK, SA_ERR_ARG, SA_ERR_CUDA, SA_ERR_UNSUPPORTED = 0, 1, 2, 3
-SA_ERR_NOT_CONVERGED, SA_ERR_BREAKDOWN, SA_ERR_NONFINITE = 4, 5, 6
+SA_ERR_NOT_CONVERGED, SA_ERR_BREAKDOWN, SA_ERR_NONFINITE, SA_ERR_TIMEOUT = 4, 5, 6, 7
+SA_CG_AUTO, SA_CG_PERSISTENT, SA_CG_TWO_KERNEL = 0, 1, 2
 SA_ELA_FRAME, SA_ELA_ISOTROPIC = 0, 1
 SA_PREC_FP64, SA_PREC_MIXED = 0, 1
 
@@ -42,7 +43,7 @@ class Params(C.Structure):
         ("modVec", _dp), ("modNum", C.c_int), ("spdTanVal", C.c_double), ("spdTsvVal", C.c_double),
         ("spdLyrVec", _dp), ("lyrNum", C.c_int), ("ynkActPrmVec", _dp), ("reaActPrmVec", _dp),
         ("btmWgt", C.c_double), ("timeStp", C.c_double), ("timeNum", C.c_int), ("cgItrMax", C.c_int),
-        ("cgTolSqu", C.c_double), ("rdItrMax", C.c_int), ("rdTolSqu", C.c_double),
+        ("cgTolSqu", C.c_double), ("rdItrMax", C.c_int), ("rdTolSqu", C.c_double), ("cgKernel", C.c_int),
     ]
 
 
@@ -88,7 +89,7 @@ def load():
     lib.sa_session_state.argtypes = [vp, _dp, _dp, _ip]
     lib.sa_session_objective.argtypes = [vp, _dp]
     lib.sa_session_info.argtypes = [vp, C.POINTER(SolveInfo)]
-    lib.sa_session_profile.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp]
+    lib.sa_session_profile.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]
     lib.sa_session_destroy.argtypes = [vp]
     _LIB = lib
     return lib

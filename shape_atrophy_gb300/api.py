@@ -98,6 +98,8 @@ def _params(spec: dict, K: _Keep, precision: str) -> _lib.Params:
     p.cgItrMax, p.cgTolSqu = int(spec["cgItrMax"]), float(spec["cgTolSqu"])
     p.rdItrMax = int(spec.get("rdItrMax", 0))
     p.rdTolSqu = float(spec.get("rdTolSqu", 0.0))
+    p.cgKernel = {"auto": _lib.SA_CG_AUTO, "persistent": _lib.SA_CG_PERSISTENT,
+                  "two-kernel": _lib.SA_CG_TWO_KERNEL}[spec.get("cgKernel", "auto")]
     return p
 
 
@@ -218,11 +220,12 @@ class Session:
                     invertedElements=i.invertedElements, lastStepMs=i.elapsedMs, kernelLaunches=i.kernelLaunches)
 
     def profile(self, enable: int = -1):
-        """enable=1/0 switches matvec timing on/off (and resets it); returns (ms, launches, bytes/launch)."""
-        ms, cnt, by = C.c_double(), C.c_longlong(), C.c_double()
+        """enable=1/0 switches timing of the velocity CG's dominant kernel on/off (and resets the totals);
+        returns (ms, launches, algorithmic bytes, flops) accumulated over the timed launches."""
+        ms, cnt, by, fl = C.c_double(), C.c_longlong(), C.c_double(), C.c_double()
         self.ctx.check(self.ctx.lib.sa_session_profile(self.h, int(enable), C.byref(ms), C.byref(cnt),
-                                                       C.byref(by)), "sa_session_profile")
-        return ms.value, cnt.value, by.value
+                                                       C.byref(by), C.byref(fl)), "sa_session_profile")
+        return ms.value, cnt.value, by.value, fl.value
 
     def close(self):
         if self.h:

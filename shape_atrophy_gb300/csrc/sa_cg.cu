@@ -43,18 +43,19 @@ constexpr int kSlicesPerCta = 4;   // matvec: one warp per 32-row slice, one thr
 constexpr int kSpmvBlock = 32 * kSlicesPerCta;
 
 // fixed-order sum over the NT threads of a block of K values each; the
-// result is valid in thread 0.  Called by every thread of the block.
+// result is valid in thread 0.  Called by every thread of the block; sm
+// holds K * NT doubles of shared memory.
 template <int K, int NT>
-__device__ __forceinline__ void block_sum(double (&v)[K], double (&sm)[K][NT])
+__device__ __forceinline__ void block_sum(double (&v)[K], double *sm)
 {
 	const int lane = threadIdx.x & 31;
-	for (int k = 0; k < K; ++k) sm[k][threadIdx.x] = v[k];
+	for (int k = 0; k < K; ++k) sm[k * NT + threadIdx.x] = v[k];
 	__syncthreads();
 	if (threadIdx.x < 32)
 		for (int k = 0; k < K; ++k) {
-			double s = sm[k][lane];
+			double s = sm[k * NT + lane];
 #pragma unroll
-			for (int q = 1; q < NT / 32; ++q) s += sm[k][lane + 32 * q];
+			for (int q = 1; q < NT / 32; ++q) s += sm[k * NT + lane + 32 * q];
 			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
 			v[k] = s;
 		}
@@ -65,7 +66,7 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double (&sm)[K][NT])
 template <int K, int NT>
 __device__ __forceinline__ bool reduce_partials(double (&v)[K], double *part, unsigned int *counter)
 {
-	__shared__ double sm[K][NT];
+	__shared__ double sm[K * NT];
 	__shared__ bool last;
 	block_sum<K, NT>(v, sm);
 	if (threadIdx.x == 0) {
@@ -82,7 +83,7 @@ __device__ __forceinline__ bool reduce_partials(double (&v)[K], double *part, un
 template <int K, int NT>
 __device__ __forceinline__ void finish_partials(double (&out)[K], const double *part)
 {
-	__shared__ double sm[K][NT];
+	__shared__ double sm[K * NT];
 	const int G = gridDim.x;
 	for (int k = 0; k < K; ++k) {
 		double s = 0.0;
@@ -284,6 +285,197 @@ __global__ void k_spmv64(SellOp A, const double *__restrict__ blk, const double 
 }
 
 // ---------------------------------------------------------------------------
+// Persistent CG: one cooperative launch runs the whole solve.  Each thread
+// owns one row (3 entries for the velocity, 1 for reaction-diffusion) and
+// keeps x, r, u, p, s and D^{-1} of that row in registers; only u goes
+// through global memory, because the matvec gathers the neighbours' u.
+// Per iteration two grid-wide reductions (delta = (w, u); gamma = (r, u)
+// and (r, r)) double as the grid barriers that order the u reads and
+// writes.  The CTA that arrives last at a reduction adds the per-CTA
+// partials in a fixed order and publishes the sums; every CTA then forms
+// the same alpha, beta and stopping decision.  Waits are bounded: a CTA
+// that waits longer than kBarWaitNs (or sees another CTA give up) stops
+// with SA_ERR_TIMEOUT.
+// ---------------------------------------------------------------------------
+struct GridBar {
+	unsigned int count, gen, abort, pad;
+	double val[4];
+};
+constexpr unsigned long long kBarWaitNs = 1000000000ull;   // 1 s
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+__device__ __forceinline__ unsigned int load_volatile(const unsigned int *p)
+{
+	return *(const volatile unsigned int *) p;
+}
+
+// sum of K values over the nctas CTAs of the launch (fixed order) and a
+// grid barrier; every thread returns the sums in v.  false: the wait gave up.
+template <int K, int NT>
+__device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int nctas, GridBar *bar,
+                                            unsigned int &gen, double *sm)
+{
+	__shared__ int lastS, okS;
+	block_sum<K, NT>(v, sm);
+	if (threadIdx.x == 0) {
+		for (int k = 0; k < K; ++k) part[k * nctas + blockIdx.x] = v[k];
+		__threadfence();
+		lastS = (atomicAdd(&bar->count, 1u) == (unsigned int) nctas - 1);
+	}
+	__syncthreads();
+	if (lastS) {
+		double t[K];
+		for (int k = 0; k < K; ++k) {
+			double a = 0.0;
+#pragma unroll 8
+			for (int b = threadIdx.x; b < nctas; b += NT) a += __ldcg(part + (long) k * nctas + b);
+			t[k] = a;
+		}
+		block_sum<K, NT>(t, sm);
+		if (threadIdx.x == 0) {
+			for (int k = 0; k < K; ++k) bar->val[k] = t[k];
+			atomicExch(&bar->count, 0u);
+			__threadfence();
+			atomicExch(&bar->gen, gen + 1);
+			okS = 1;
+		}
+	} else if (threadIdx.x == 0) {
+		int ok = 1;
+		unsigned long long t0 = global_ns();
+		while (load_volatile(&bar->gen) == gen) {
+			if (load_volatile(&bar->abort)) { ok = 0; break; }
+			if (global_ns() - t0 > kBarWaitNs) { atomicExch(&bar->abort, 1u); ok = 0; break; }
+			__nanosleep(32);
+		}
+		__threadfence();
+		okS = ok;
+	}
+	__syncthreads();
+	gen += 1;
+	if (!okS) return false;
+	for (int k = 0; k < K; ++k) v[k] = __ldcg(bar->val + k);
+	return true;
+}
+
+template <int B, typename TM, typename TV>
+__device__ __forceinline__ void spmv_slot_cg(const SellOp &A, const TM *__restrict__ blk, const TV *u, long idx,
+                                             TV (&acc)[B])
+{
+	int j = __ldg(A.col + idx);
+	TV xj[B];
+	for (int c = 0; c < B; ++c) xj[c] = __ldcg(u + (long) j * B + c);   // written during the launch
+	TM a[B * B];
+	load_block<B, TM>(blk, A.total, idx, a);
+	for (int r = 0; r < B; ++r)
+		for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
+}
+
+constexpr int kPersistMinCtas = 5;   // CTAs of kSpmvBlock threads resident per SM (register budget)
+
+template <int B, typename TM, typename TV, typename TX>
+__global__ void __launch_bounds__(kSpmvBlock, kPersistMinCtas)
+k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, TX *x, const TV *r0, TV *u,
+             double *part, CgScal *sc, GridBar *bar)
+{
+	__shared__ double sm[2 * kSpmvBlock];
+	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
+	const int nctas = gridDim.x;
+	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+	const int sl = blockIdx.x * kSlicesPerCta + wp;
+	const int nsl = (A.N + 31) >> 5;
+	const int i = sl * 32 + lane;
+	const bool own = sl < nsl && i < A.N;
+	const int wdt = sl < nsl ? __ldg(A.width + sl) : 0;
+	const long base = sl < nsl ? __ldg(A.off + sl) + lane : 0;
+	const double bb = sc->bb, tolSqu = sc->tolSqu;
+	const int itrMax = sc->itrMax;
+	double gam = sc->gam, rr = sc->rr, gamPrev = 0.0, alphaPrev = 1.0;
+	unsigned int gen = load_volatile(&bar->gen);
+	TX xv[B];
+	TV rv[B], uv[B], pv[B], sv[B], dv[B];
+	for (int c = 0; c < B; ++c) {
+		xv[c] = (TX) 0; rv[c] = uv[c] = pv[c] = sv[c] = dv[c] = (TV) 0;
+		if (own) {
+			long k = (long) i * B + c;
+			xv[c] = x[k]; rv[c] = r0[k]; uv[c] = u[k]; dv[c] = dinv[k];
+		}
+	}
+	int it = 0, code = SA_OK;
+	bool first = true;
+	for (;;) {
+		// w = A u and (w, u)
+		TV acc0[B], acc1[B];
+		for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
+		int k = 0;
+		for (; k + 2 <= wdt; k += 2) {
+			spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+			spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), acc1);
+		}
+		if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+		TV wv[B];
+		double d1[1] = {0.0};
+		for (int c = 0; c < B; ++c) {
+			wv[c] = acc0[c] + acc1[c];
+			if (own) d1[0] += (double) wv[c] * (double) uv[c];
+		}
+		if (!grid_reduce<1, kSpmvBlock>(d1, part, nctas, bar, gen, sm)) {
+			code = SA_ERR_TIMEOUT;
+			break;
+		}
+		const double delta = d1[0];
+		double alpha, beta;
+		if (first) { beta = 0.0; alpha = gam / delta; }
+		else {
+			beta = gam / gamPrev;
+			alpha = gam / (delta - beta * gam / alphaPrev);
+		}
+		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
+			code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
+			break;
+		}
+		// p, s, x, r, u of the own row; (r, u) and (r, r)
+		double d2[2] = {0.0, 0.0};
+		if (own) {
+			const TV al = (TV) alpha, be = (TV) beta;
+			for (int c = 0; c < B; ++c) {
+				pv[c] = uv[c] + be * pv[c];
+				sv[c] = wv[c] + be * sv[c];
+				xv[c] = xv[c] + (TX) al * (TX) pv[c];
+				rv[c] = rv[c] - al * sv[c];
+				uv[c] = dv[c] * rv[c];
+				u[(long) i * B + c] = uv[c];
+				d2[0] += (double) rv[c] * (double) uv[c];
+				d2[1] += (double) rv[c] * (double) rv[c];
+			}
+		}
+		if (!grid_reduce<2, kSpmvBlock>(d2, part + nctas, nctas, bar, gen, sm)) {
+			code = SA_ERR_TIMEOUT;
+			break;
+		}
+		gamPrev = gam;
+		gam = d2[0];
+		rr = d2[1];
+		alphaPrev = alpha;
+		first = false;
+		++it;
+		if (!isfinite(gam) || !isfinite(rr)) { code = SA_ERR_NONFINITE; break; }
+		if (rr < tolSqu * bb) { code = SA_OK; break; }
+		if (it >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
+	}
+	if (own)
+		for (int c = 0; c < B; ++c) x[(long) i * B + c] = xv[c];
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		sc->iters = it; sc->code = code; sc->rr = rr; sc->gam = gam; sc->done = 1;
+	}
+}
+
+// ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
 // CTAs of the vector kernels: kVecCtasPerSm per SM, fewer for short vectors
@@ -303,6 +495,23 @@ static void set_scal(CgScal *d, double tolSqu, int itrMax, double bb, cudaStream
 	SA_CHECK(cudaMemcpyAsync(d, &h, sizeof(CgScal), cudaMemcpyHostToDevice, s));
 }
 
+// CTAs of k_cg_persist that can be resident at once (0: the kernel cannot run)
+template <int B, typename TM, typename TV, typename TX>
+static int persist_capacity(int smCount)
+{
+	static int perSm = -1;
+	if (perSm < 0) {
+		int v = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist<B, TM, TV, TX>, kSpmvBlock, 0) !=
+		    cudaSuccess) {
+			cudaGetLastError();
+			v = 0;
+		}
+		perSm = v;
+	}
+	return perSm * smCount;
+}
+
 static CgScal read_scal(const CgScal *d, cudaStream_t s)
 {
 	CgScal h;
@@ -320,18 +529,55 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	int N = m.N;
 	long n = (long) N * B;
 	int nb = vec_grid(n, prof->smCount);
+	const int chunk = 16;
+	bool timing = prof->profileEnabled && prof->profileOn;
+	if (timing && !prof->ev[0])
+		for (int k = 0; k < 4 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
 	set_scal(sc, tolSqu, itrMax, bb, s);
+	const int nctas = (m.nslice + kSlicesPerCta - 1) / kSlicesPerCta;
+	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
+	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount);
+	if (persist) {
+		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first)
+		k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
+		GridBar *bar = (GridBar *) prof->bar;
+		SA_CHECK(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
+		SellOp A = sell_of(m);
+		const TV *r0 = r;
+		void *args[] = {&A, (void *) &blk, (void *) &dinv, (void *) &x, (void *) &r0, (void *) &u, (void *) &part,
+		                (void *) &sc, (void *) &bar};
+		if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
+		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
+		                                     dim3(kSpmvBlock), args, 0, s));
+		if (timing) SA_CHECK(cudaEventRecord(prof->ev[1], s));
+		k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
+		prof->launches += 3;
+		unsigned int gaveUp = 0;
+		SA_CHECK(cudaMemcpyAsync(&gaveUp, &bar->abort, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+		CgScal h = read_scal(sc, s);
+		if (timing && h.iters > 0) {
+			float ms = 0.f;
+			SA_CHECK(cudaEventElapsedTime(&ms, prof->ev[0], prof->ev[1]));
+			prof->spmvMs += ms;
+			prof->spmvCount += 1;
+			// per iteration: operator values, column indices and slice table once, u gathered once and
+			// written once (x, r, p, s, D^-1 stay in registers); per launch: x, r, u, D^-1 in, x out
+			prof->profBytes += (double) h.iters * ((double) m.slTotal * (B * B * sizeof(TM) + 4.0) +
+			                                       8.0 * m.nslice + 2.0 * sizeof(TV) * n) +
+			                   4.0 * sizeof(TV) * n + sizeof(TX) * n;
+			prof->profFlops += (double) h.iters * 2.0 * ((double) B * B * m.slTotal + 8.0 * n);
+		}
+		// any CTA that gave up leaves the abort flag set, whatever CTA 0 reported
+		if (gaveUp || h.code == SA_ERR_TIMEOUT) throw DeviceWaitError{"persistent CG grid barrier"};
+		return h;
+	}
 	SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
 	SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
 	k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
-	const int chunk = 16;
-	bool timing = prof && prof->profileEnabled && prof->profileOn;
 	if (!prof->pinned) {
 		SA_CHECK(cudaHostAlloc(&prof->pinned, 2 * sizeof(CgScal), cudaHostAllocDefault));
 		for (int k = 0; k < 2; ++k) SA_CHECK(cudaEventCreateWithFlags(&prof->chunkEv[k], cudaEventDisableTiming));
 	}
-	if (timing && !prof->ev[0])
-		for (int k = 0; k < 4 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
 	CgScal *hs = (CgScal *) prof->pinned;
 	// chunks of iterations are queued one ahead: while the host waits for the
 	// status of chunk c - 1, chunk c is already on the GPU (its kernels return
@@ -367,6 +613,10 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 				prof->spmvMs += ms;
 			}
 			prof->spmvCount += worked;
+			// per matvec: operator values, column indices, slice table, u read and w written once
+			prof->profBytes += worked * ((double) m.slTotal * (B * B * sizeof(TM) + 4.0) + 8.0 * m.nslice +
+			                             2.0 * sizeof(TV) * n);
+			prof->profFlops += worked * 2.0 * B * B * (double) m.slTotal;
 			itersBefore = h.iters;
 		}
 		if (h.done) break;

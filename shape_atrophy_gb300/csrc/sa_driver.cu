@@ -338,6 +338,8 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	// partial sums: up to 3 per CTA of the widest CG kernel grid (entries / 256, or one CTA per slice)
 	int nbCg = std::max(grid_for(n, 256), std::max(m.nslice, nb));
 	c.part = P.alloc<double>((size_t) 3 * nbCg + 64); c.scal = P.zeros<double>(32); c.maxBlocks = nbCg;
+	c.bar = P.zeros<double>(8);
+	c.cgKernel = md.cgKernel;
 	{
 		int dev = 0;
 		SA_CHECK(cudaGetDevice(&dev));
@@ -520,6 +522,8 @@ static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *
 	SA_REQUIRE(md.timeNum >= 1, "timeNum must be >= 1");
 	md.rdItrMax = p->rdItrMax > 0 ? p->rdItrMax : std::max(p->cgItrMax, 1000);
 	md.rdTolSqu = p->rdTolSqu > 0.0 ? p->rdTolSqu : (md.frame ? 1e-26 : p->cgTolSqu);
+	SA_REQUIRE(p->cgKernel >= SA_CG_AUTO && p->cgKernel <= SA_CG_TWO_KERNEL, "cgKernel must be 0, 1 or 2");
+	md.cgKernel = p->cgKernel;
 	if (tgt) {
 		md.cenKnl = tgt->cenKnlType; md.dirKnl = tgt->dirKnlType;
 		md.cenWidth = tgt->cenKnlWidth; md.dirWidth = tgt->dirKnlWidth;
@@ -651,7 +655,7 @@ struct SessionBase {
 	virtual void state(double *lmk, double *tau, int *t) = 0;
 	virtual double objective() = 0;
 	virtual void info(sa_solve_info *i) = 0;
-	virtual void profile(int enable, double *ms, long long *cnt, double *bytes) = 0;
+	virtual void profile(int enable, double *ms, long long *cnt, double *bytes, double *flops) = 0;
 };
 
 template <int D>
@@ -744,20 +748,18 @@ struct Session : SessionBase {
 		i->elapsedMs = lastStepMs;             // device time of the last sa_session_step call
 		i->kernelLaunches = w.cw.launches;
 	}
-	void profile(int enable, double *ms, long long *cnt, double *bytes) override
+	void profile(int enable, double *ms, long long *cnt, double *bytes, double *flops) override
 	{
 		if (ms) *ms = w.cw.spmvMs;
 		if (cnt) *cnt = w.cw.spmvCount;
-		if (bytes) {
-			double val = md.precision == SA_PREC_MIXED ? 4.0 : 8.0;
-			// block values + column index per sliced slot (padding included), slice table, u read and w
-			// written once
-			*bytes = (double) m.slTotal * (sell_vals<D>() * val + 4.0) + 8.0 * m.nslice + 2.0 * val * m.N * D;
-		}
+		if (bytes) *bytes = w.cw.profBytes;
+		if (flops) *flops = w.cw.profFlops;
 		if (enable >= 0) {
 			w.cw.profileEnabled = enable;
 			w.cw.spmvMs = 0.0;
 			w.cw.spmvCount = 0;
+			w.cw.profBytes = 0.0;
+			w.cw.profFlops = 0.0;
 		}
 	}
 };
@@ -778,6 +780,9 @@ static int guarded(sa_context *ctx, F &&f)
 		ctx->err = std::string(e.where) + ": " + cudaGetErrorString(e.e);
 		cudaGetLastError();
 		return SA_ERR_CUDA;
+	} catch (const DeviceWaitError &e) {
+		ctx->err = std::string(e.where) + ": a device-side wait gave up after its time limit";
+		return SA_ERR_TIMEOUT;
 	} catch (const std::bad_alloc &) {
 		ctx->err = "host allocation failed";
 		return SA_ERR_CUDA;
@@ -902,10 +907,11 @@ int sa_session_info(sa_session *s, sa_solve_info *info)
 	return sa::guarded(s->impl->ctx, [&]() { s->impl->info(info); return SA_OK; });
 }
 
-int sa_session_profile(sa_session *s, int enable, double *spmvMs, long long *spmvCount, double *spmvBytes)
+int sa_session_profile(sa_session *s, int enable, double *kernelMs, long long *launches, double *bytes,
+                       double *flops)
 {
-	if (!s) return SA_ERR_ARG;
-	return sa::guarded(s->impl->ctx, [&]() { s->impl->profile(enable, spmvMs, spmvCount, spmvBytes); return SA_OK; });
+	if (!s || !s->impl) return SA_ERR_ARG;
+	return sa::guarded(s->impl->ctx, [&]() { s->impl->profile(enable, kernelMs, launches, bytes, flops); return SA_OK; });
 }
 
 int sa_session_destroy(sa_session *s)

@@ -180,6 +180,7 @@ struct Model {
 	int rdItrMax; double rdTolSqu;
 	char cenKnl, dirKnl; double cenWidth, dirWidth;
 	int precision;             // SA_PREC_FP64 or SA_PREC_MIXED
+	int cgKernel = 0;          // SA_CG_AUTO / SA_CG_PERSISTENT / SA_CG_TWO_KERNEL
 };
 
 // --------------------------------------------------------------------------
@@ -278,6 +279,9 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	double *scal;                 // device scalars
 	int maxBlocks;
 	int smCount = 1;              // SMs of the device (grid of the vector kernels)
+	int cgKernel = 0;             // SA_CG_AUTO / SA_CG_PERSISTENT / SA_CG_TWO_KERNEL
+	void *bar = nullptr;          // grid barrier of the persistent CG kernel (64 bytes, device)
+	double profBytes = 0.0, profFlops = 0.0;   // algorithmic bytes / flops of the timed launches
 	float *blk32 = nullptr;       // FP32 copy of the operator (mixed precision)
 	float *f32 = nullptr;         // 7 n FP32 vectors of the inner solve (mixed precision)
 	double *xr = nullptr;         // 3 n FP64 refinement scratch
@@ -325,6 +329,7 @@ double device_sum(const double *v, long n, double *scratch, cudaStream_t s);
 
 // error helpers
 struct CudaError { cudaError_t e; const char *where; };
+struct DeviceWaitError { const char *where; };   // a bounded device-side wait gave up
 #define SA_CHECK(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) throw ::sa::CudaError{_e, #x}; } while (0)
 
 }  // namespace sa

@@ -1,0 +1,89 @@
+"""Solver variants on the GPU against the oracle.
+
+- persistent CG kernel (one cooperative launch per solve) and the two-kernel
+  CG (matvec + vector kernel per iteration) both match the FP64 oracle to
+  1e-10 relative, and each other to 1e-12;
+- mixed precision (FP32 operators and vectors, FP64 dots and iterative
+  refinement) stays within 1e-6 relative of the FP64 oracle in node
+  positions, concentration and objective;
+- a stepwise session reproduces the one-call forward trajectory exactly.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+MIXED_TOL = 1e-6
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
+
+
+def _case(name):
+    from shape_atrophy_gb300 import problems
+    if name == "annulus":
+        return problems.annulus_layered(angNum=48, radNum=7, steps=6, cgTolVal=1e-12)
+    return problems.shell_layered(level=2, lyrCntNum=4, steps=4, cgTolVal=1e-12)
+
+
+@pytest.fixture(scope="module")
+def oracle_runs():
+    from oracle.oracle import Problem
+    out = {}
+    for name in ("annulus", "shell"):
+        spec = _case(name)
+        out[name] = Problem(spec).forward(spec["tauVarVec"], with_obj=True)
+    return out
+
+
+@pytest.mark.parametrize("name", ["annulus", "shell"])
+def test_cg_paths_match_oracle_and_each_other(name, oracle_runs):
+    from shape_atrophy_gb300 import api
+    want = oracle_runs[name]
+    runs = {}
+    for path in ("persistent", "two-kernel"):
+        spec = _case(name)
+        spec["cgKernel"] = path
+        got = api.forward(spec, trajectory=True, objective=True)
+        assert got["info"]["status"] == 0
+        assert rel(got["lmkStk"], want["lmkStk"]) < TOL, path
+        assert rel(got["tauMat"], want["tauMat"]) < TOL, path
+        assert abs(got["obj"][0] - want["obj"]) <= TOL * abs(want["obj"]), path
+        runs[path] = got
+    a, b = runs["persistent"], runs["two-kernel"]
+    assert rel(a["lmkStk"], b["lmkStk"]) < 1e-12
+    assert rel(a["tauMat"], b["tauMat"]) < 1e-12
+    assert a["info"]["cgIterTotal"] == pytest.approx(b["info"]["cgIterTotal"], abs=2 * 4)
+
+
+@pytest.mark.parametrize("name", ["annulus", "shell"])
+@pytest.mark.parametrize("path", ["persistent", "two-kernel"])
+def test_mixed_precision_error_against_fp64_oracle(name, path, oracle_runs):
+    from shape_atrophy_gb300 import api
+    want = oracle_runs[name]
+    spec = _case(name)
+    spec["cgTolSqu"] = 1e-16                 # the workload tolerance, 1e-8 relative residual
+    spec["cgKernel"] = path
+    got = api.forward(spec, trajectory=True, objective=True, precision="mixed")
+    assert got["info"]["status"] == 0
+    assert rel(got["lmkStk"], want["lmkStk"]) < MIXED_TOL
+    assert rel(got["tauMat"], want["tauMat"]) < MIXED_TOL
+    assert abs(got["obj"][0] - want["obj"]) <= MIXED_TOL * abs(want["obj"])
+
+
+def test_session_steps_reproduce_forward():
+    from shape_atrophy_gb300 import api
+    spec = _case("shell")
+    full = api.forward(spec, trajectory=True, objective=False)
+    sess = api.Session(spec, objective=False)
+    T = spec["timeNum"]
+    for t in range(1, T):
+        assert sess.step(1) == 1
+        x, tau, step = sess.state()
+        assert step == t
+        np.testing.assert_array_equal(x, full["lmkStk"][t])
+        np.testing.assert_array_equal(tau, full["tauMat"][t])
+    assert sess.step(1) == 0                 # never past timeNum - 1
+    sess.close()
