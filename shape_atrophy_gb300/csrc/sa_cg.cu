@@ -289,19 +289,22 @@ __global__ void k_spmv64(SellOp A, const double *__restrict__ blk, const double 
 // owns one row (3 entries for the velocity, 1 for reaction-diffusion) and
 // keeps x, r, u, p, s and D^{-1} of that row in registers; only u goes
 // through global memory, because the matvec gathers the neighbours' u.
+// One CTA per SM (up to kPersistMaxWarps warps, one 32-row slice per warp).
 // Per iteration two grid-wide reductions (delta = (w, u); gamma = (r, u)
 // and (r, r)) double as the grid barriers that order the u reads and
-// writes.  The CTA that arrives last at a reduction adds the per-CTA
-// partials in a fixed order and publishes the sums; every CTA then forms
-// the same alpha, beta and stopping decision.  Waits are bounded: a CTA
-// that waits longer than kBarWaitNs (or sees another CTA give up) stops
-// with SA_ERR_TIMEOUT.
+// writes: every CTA publishes its partial sums, counts itself in, waits for
+// the count of the whole grid and then adds all partials in the same fixed
+// order, so every CTA forms the same alpha, beta and stopping decision.
+// Waits are bounded: a CTA that waits longer than kBarWaitNs (or sees
+// another CTA give up) stops with SA_ERR_TIMEOUT.
 // ---------------------------------------------------------------------------
 struct GridBar {
-	unsigned int count, gen, abort, pad;
-	double val[4];
+	unsigned int count, pad0[31];      // arrivals, grows by nctas per reduction (zeroed per launch)
+	unsigned int abort, pad1[31];      // set by a CTA that gave up
 };
+static_assert(sizeof(GridBar) <= kGridBarBytes, "grid barrier larger than its allocation");
 constexpr unsigned long long kBarWaitNs = 1000000000ull;   // 1 s
+constexpr int kPersistMaxWarps = 20;                       // CTA size limit (96 registers per thread)
 
 __device__ __forceinline__ unsigned long long global_ns()
 {
@@ -310,56 +313,66 @@ __device__ __forceinline__ unsigned long long global_ns()
 	return t;
 }
 
-__device__ __forceinline__ unsigned int load_volatile(const unsigned int *p)
+__device__ __forceinline__ unsigned int load_acquire(const unsigned int *p)
 {
-	return *(const volatile unsigned int *) p;
+	unsigned int v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
 }
 
-// sum of K values over the nctas CTAs of the launch (fixed order) and a
-// grid barrier; every thread returns the sums in v.  false: the wait gave up.
-template <int K, int NT>
-__device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int nctas, GridBar *bar,
-                                            unsigned int &gen, double *sm)
+// block sum for a block of any multiple of 32 threads (at most 32 * kPersistMaxWarps); valid in thread 0
+template <int K>
+__device__ __forceinline__ void block_sum_any(double (&v)[K], double *sm)
 {
-	__shared__ int lastS, okS;
-	block_sum<K, NT>(v, sm);
+	const int lane = threadIdx.x & 31, NT = blockDim.x;
+	for (int k = 0; k < K; ++k) sm[k * NT + threadIdx.x] = v[k];
+	__syncthreads();
+	if (threadIdx.x < 32)
+		for (int k = 0; k < K; ++k) {
+			double s = sm[k * NT + lane];
+			for (int q = 32 + lane; q < NT; q += 32) s += sm[k * NT + q];
+			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+			v[k] = s;
+		}
+}
+
+// sum of K values over all threads of the nctas CTAs (fixed order) plus a
+// grid barrier; every thread returns the sums in v.  false: the wait gave up.
+template <int K>
+__device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int nctas, GridBar *bar,
+                                            unsigned int &target, double *sm)
+{
+	__shared__ int okS;
+	__shared__ double tot[K];
+	block_sum_any<K>(v, sm);
+	target += (unsigned int) nctas;
 	if (threadIdx.x == 0) {
 		for (int k = 0; k < K; ++k) part[k * nctas + blockIdx.x] = v[k];
 		__threadfence();
-		lastS = (atomicAdd(&bar->count, 1u) == (unsigned int) nctas - 1);
-	}
-	__syncthreads();
-	if (lastS) {
-		double t[K];
-		for (int k = 0; k < K; ++k) {
-			double a = 0.0;
-#pragma unroll 8
-			for (int b = threadIdx.x; b < nctas; b += NT) a += __ldcg(part + (long) k * nctas + b);
-			t[k] = a;
-		}
-		block_sum<K, NT>(t, sm);
-		if (threadIdx.x == 0) {
-			for (int k = 0; k < K; ++k) bar->val[k] = t[k];
-			atomicExch(&bar->count, 0u);
-			__threadfence();
-			atomicExch(&bar->gen, gen + 1);
-			okS = 1;
-		}
-	} else if (threadIdx.x == 0) {
+		atomicAdd(&bar->count, 1u);
 		int ok = 1;
-		unsigned long long t0 = global_ns();
-		while (load_volatile(&bar->gen) == gen) {
-			if (load_volatile(&bar->abort)) { ok = 0; break; }
+		const unsigned long long t0 = global_ns();
+		while ((int) (load_acquire(&bar->count) - target) < 0) {
+			if (load_acquire(&bar->abort)) { ok = 0; break; }
 			if (global_ns() - t0 > kBarWaitNs) { atomicExch(&bar->abort, 1u); ok = 0; break; }
-			__nanosleep(32);
 		}
 		__threadfence();
 		okS = ok;
 	}
 	__syncthreads();
-	gen += 1;
 	if (!okS) return false;
-	for (int k = 0; k < K; ++k) v[k] = __ldcg(bar->val + k);
+	if (threadIdx.x < 32) {
+		const int lane = threadIdx.x;
+		for (int k = 0; k < K; ++k) {
+			double s = 0.0;
+#pragma unroll 8
+			for (int b = lane; b < nctas; b += 32) s += __ldcg(part + (long) k * nctas + b);
+			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+			if (lane == 0) tot[k] = s;
+		}
+	}
+	__syncthreads();
+	for (int k = 0; k < K; ++k) v[k] = tot[k];
 	return true;
 }
 
@@ -376,18 +389,16 @@ __device__ __forceinline__ void spmv_slot_cg(const SellOp &A, const TM *__restri
 		for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
 }
 
-constexpr int kPersistMinCtas = 5;   // CTAs of kSpmvBlock threads resident per SM (register budget)
-
 template <int B, typename TM, typename TV, typename TX>
-__global__ void __launch_bounds__(kSpmvBlock, kPersistMinCtas)
+__global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
 k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, TX *x, const TV *r0, TV *u,
              double *part, CgScal *sc, GridBar *bar)
 {
-	__shared__ double sm[2 * kSpmvBlock];
+	__shared__ double sm[2 * 32 * kPersistMaxWarps];
 	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
 	const int nctas = gridDim.x;
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-	const int sl = blockIdx.x * kSlicesPerCta + wp;
+	const int sl = blockIdx.x * (blockDim.x >> 5) + wp;
 	const int nsl = (A.N + 31) >> 5;
 	const int i = sl * 32 + lane;
 	const bool own = sl < nsl && i < A.N;
@@ -396,7 +407,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	const double bb = sc->bb, tolSqu = sc->tolSqu;
 	const int itrMax = sc->itrMax;
 	double gam = sc->gam, rr = sc->rr, gamPrev = 0.0, alphaPrev = 1.0;
-	unsigned int gen = load_volatile(&bar->gen);
+	unsigned int target = 0;                     // bar->count is zeroed before the launch
 	TX xv[B];
 	TV rv[B], uv[B], pv[B], sv[B], dv[B];
 	for (int c = 0; c < B; ++c) {
@@ -424,7 +435,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			wv[c] = acc0[c] + acc1[c];
 			if (own) d1[0] += (double) wv[c] * (double) uv[c];
 		}
-		if (!grid_reduce<1, kSpmvBlock>(d1, part, nctas, bar, gen, sm)) {
+		if (!grid_reduce<1>(d1, part, nctas, bar, target, sm)) {
 			code = SA_ERR_TIMEOUT;
 			break;
 		}
@@ -454,7 +465,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 				d2[1] += (double) rv[c] * (double) rv[c];
 			}
 		}
-		if (!grid_reduce<2, kSpmvBlock>(d2, part + nctas, nctas, bar, gen, sm)) {
+		if (!grid_reduce<2>(d2, part + nctas, nctas, bar, target, sm)) {
 			code = SA_ERR_TIMEOUT;
 			break;
 		}
@@ -495,21 +506,24 @@ static void set_scal(CgScal *d, double tolSqu, int itrMax, double bb, cudaStream
 	SA_CHECK(cudaMemcpyAsync(d, &h, sizeof(CgScal), cudaMemcpyHostToDevice, s));
 }
 
-// CTAs of k_cg_persist that can be resident at once (0: the kernel cannot run)
+// CTAs of k_cg_persist with `warps` warps each that can be resident at once (0: it cannot run)
 template <int B, typename TM, typename TV, typename TX>
-static int persist_capacity(int smCount)
+static int persist_capacity(int smCount, int warps)
 {
-	static int perSm = -1;
-	if (perSm < 0) {
+	static int perSm[kPersistMaxWarps + 1] = {};
+	static bool known[kPersistMaxWarps + 1] = {};
+	if (warps < 1 || warps > kPersistMaxWarps) return 0;
+	if (!known[warps]) {
 		int v = 0;
-		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist<B, TM, TV, TX>, kSpmvBlock, 0) !=
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist<B, TM, TV, TX>, 32 * warps, 0) !=
 		    cudaSuccess) {
 			cudaGetLastError();
 			v = 0;
 		}
-		perSm = v;
+		perSm[warps] = v;
+		known[warps] = true;
 	}
-	return perSm * smCount;
+	return perSm[warps] * smCount;
 }
 
 static CgScal read_scal(const CgScal *d, cudaStream_t s)
@@ -534,9 +548,11 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	if (timing && !prof->ev[0])
 		for (int k = 0; k < 4 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
 	set_scal(sc, tolSqu, itrMax, bb, s);
-	const int nctas = (m.nslice + kSlicesPerCta - 1) / kSlicesPerCta;
+	// persistent launch: one CTA per SM, one slice per warp
+	const int pw = std::max(1, std::min(kPersistMaxWarps, (m.nslice + prof->smCount - 1) / prof->smCount));
+	const int nctas = (m.nslice + pw - 1) / pw;
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
-	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount);
+	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw);
 	if (persist) {
 		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first)
 		k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
@@ -548,7 +564,7 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		                (void *) &sc, (void *) &bar};
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
 		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
-		                                     dim3(kSpmvBlock), args, 0, s));
+		                                     dim3(32 * pw), args, 0, s));
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[1], s));
 		k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
 		prof->launches += 3;

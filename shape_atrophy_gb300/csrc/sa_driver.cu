@@ -338,7 +338,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	// partial sums: up to 3 per CTA of the widest CG kernel grid (entries / 256, or one CTA per slice)
 	int nbCg = std::max(grid_for(n, 256), std::max(m.nslice, nb));
 	c.part = P.alloc<double>((size_t) 3 * nbCg + 64); c.scal = P.zeros<double>(32); c.maxBlocks = nbCg;
-	c.bar = P.zeros<double>(8);
+	c.bar = P.zeros<char>(kGridBarBytes);
 	c.cgKernel = md.cgKernel;
 	{
 		int dev = 0;

@@ -273,6 +273,8 @@ void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_
 // --------------------------------------------------------------------------
 // CG solvers
 // --------------------------------------------------------------------------
+constexpr int kGridBarBytes = 512;   // device memory of the persistent CG's grid barrier
+
 struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	double *r, *u, *w, *p, *sv;   // n each
 	double *part;                 // partial sums: 3 x maxBlocks
@@ -280,7 +282,7 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	int maxBlocks;
 	int smCount = 1;              // SMs of the device (grid of the vector kernels)
 	int cgKernel = 0;             // SA_CG_AUTO / SA_CG_PERSISTENT / SA_CG_TWO_KERNEL
-	void *bar = nullptr;          // grid barrier of the persistent CG kernel (64 bytes, device)
+	void *bar = nullptr;          // grid barrier of the persistent CG kernel (kGridBarBytes, device)
 	double profBytes = 0.0, profFlops = 0.0;   // algorithmic bytes / flops of the timed launches
 	float *blk32 = nullptr;       // FP32 copy of the operator (mixed precision)
 	float *f32 = nullptr;         // 7 n FP32 vectors of the inner solve (mixed precision)
