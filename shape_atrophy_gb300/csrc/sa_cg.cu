@@ -320,17 +320,21 @@ __device__ __forceinline__ unsigned int load_acquire(const unsigned int *p)
 	return v;
 }
 
-// block sum for a block of any multiple of 32 threads (at most 32 * kPersistMaxWarps); valid in thread 0
+// block sum for a block of any multiple of 32 threads (at most 32 * kPersistMaxWarps); valid in thread 0.
+// Each warp reduces its 32 values by shuffles, then warp 0 reduces the warp sums.
 template <int K>
 __device__ __forceinline__ void block_sum_any(double (&v)[K], double *sm)
 {
-	const int lane = threadIdx.x & 31, NT = blockDim.x;
-	for (int k = 0; k < K; ++k) sm[k * NT + threadIdx.x] = v[k];
+	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	for (int k = 0; k < K; ++k) {
+		double s = v[k];
+		for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+		if (lane == 0) sm[k * 32 + wp] = s;
+	}
 	__syncthreads();
 	if (threadIdx.x < 32)
 		for (int k = 0; k < K; ++k) {
-			double s = sm[k * NT + lane];
-			for (int q = 32 + lane; q < NT; q += 32) s += sm[k * NT + q];
+			double s = lane < nw ? sm[k * 32 + lane] : 0.0;
 			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
 			v[k] = s;
 		}
@@ -394,7 +398,7 @@ __global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
 k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, TX *x, const TV *r0, TV *u,
              double *part, CgScal *sc, GridBar *bar)
 {
-	__shared__ double sm[2 * 32 * kPersistMaxWarps];
+	__shared__ double sm[2 * 32];                 // block_sum_any scratch (K <= 2, at most 32 warps)
 	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
 	const int nctas = gridDim.x;
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
