@@ -194,6 +194,52 @@ int sa_session_profile(sa_session *s, int enable, double *kernelMs, long long *l
                        double *flops);
 int sa_session_destroy(sa_session *s);
 
+/* Serving (no reference counterpart: the reference solves one request per
+ * MEX call).  A server owns a loop thread and its own stream on the
+ * context's GPU and runs layered-model forward solves (elaType
+ * SA_ELA_ISOTROPIC, one parameter vector each) with continuous batching:
+ * requests are admitted in arrival order while their device footprint fits
+ * hbmBudgetBytes and fewer than maxInstances run; every running instance
+ * keeps its mesh, state and CG vectors on the device; each tick advances all
+ * running instances one time step, with one batched persistent CG launch for
+ * all their velocity solves (per precision and dimension) and one for all
+ * their reaction-diffusion solves.  Finished instances free their memory at
+ * the end of a tick; queued requests enter at the start of the next.  A
+ * request's result does not depend on which other requests run with it.
+ *
+ * sa_server_submit copies every input (host or device memory) before it
+ * returns.  sa_server_result returns, once the request is DONE, the final
+ * node positions (lmkNum x dim, column-major), the final concentration
+ * (lmkNum), the varifold objective (0 without a target; DBL_MAX when a solve
+ * failed, with info->status telling which), the solve diagnostics
+ * (info->elapsedMs = admission to completion) and the latency from
+ * submission to completion; it releases the request.  A FAILED request
+ * (invalid input, device error) returns its error code and message.
+ * sa_server_destroy finishes the queued and running requests first. */
+#define SA_REQ_QUEUED   0
+#define SA_REQ_RUNNING  1
+#define SA_REQ_DONE     2
+#define SA_REQ_FAILED   3
+
+typedef struct sa_server sa_server;
+typedef struct sa_server_counters {
+	long long submitted, completed, failed;
+	int queued, running;
+	double bytesInUse, peakBytes;   /* device bytes held by running instances (now, peak) */
+	long long ticks;                /* batched time steps executed */
+	double busyMs;                  /* host wall time spent in ticks */
+} sa_server_counters;
+
+int sa_server_create(sa_context *ctx, double hbmBudgetBytes, int maxInstances, sa_server **out);
+int sa_server_submit(sa_server *sv, const sa_element_object *obj, const double *lmkIniMat, const sa_params *prm,
+                     const sa_target *tgt, const double *tauVarVec, int tauVarNum, long long *requestId);
+int sa_server_poll(sa_server *sv, long long requestId, int *state);
+int sa_server_wait(sa_server *sv, long long requestId, double timeoutMs, int *state);   /* timeoutMs < 0: no limit */
+int sa_server_result(sa_server *sv, long long requestId, double *lmkMat, double *tauVec, double *objOut,
+                     sa_solve_info *info, double *latencyMs);
+int sa_server_stats(sa_server *sv, sa_server_counters *stats);
+int sa_server_destroy(sa_server *sv);
+
 /* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and
  * deformation_3D_frame (dim 3): arguments in prhs order
  * (CUDA/2D_frame/deformation.cu:24-50), outputs plhs[0..2]

@@ -62,6 +62,17 @@ class SolveInfo(C.Structure):
     ]
 
 
+class ServerCounters(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
+        ("queued", C.c_int), ("running", C.c_int), ("bytesInUse", C.c_double), ("peakBytes", C.c_double),
+        ("ticks", C.c_longlong), ("busyMs", C.c_double),
+    ]
+
+
+SA_REQ_QUEUED, SA_REQ_RUNNING, SA_REQ_DONE, SA_REQ_FAILED = 0, 1, 2, 3
+
+
 def library_path() -> str:
     return _build.LIB
 
@@ -91,6 +102,14 @@ def load():
     lib.sa_session_info.argtypes = [vp, C.POINTER(SolveInfo)]
     lib.sa_session_profile.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]
     lib.sa_session_destroy.argtypes = [vp]
+    lib.sa_server_create.argtypes = [vp, C.c_double, C.c_int, C.POINTER(vp)]
+    lib.sa_server_submit.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Params), C.POINTER(Target), _dp,
+                                     C.c_int, C.POINTER(C.c_longlong)]
+    lib.sa_server_poll.argtypes = [vp, C.c_longlong, _ip]
+    lib.sa_server_wait.argtypes = [vp, C.c_longlong, C.c_double, _ip]
+    lib.sa_server_result.argtypes = [vp, C.c_longlong, _dp, _dp, _dp, C.POINTER(SolveInfo), _dp]
+    lib.sa_server_stats.argtypes = [vp, C.POINTER(ServerCounters)]
+    lib.sa_server_destroy.argtypes = [vp]
     _LIB = lib
     return lib
 

@@ -289,3 +289,78 @@ def computeObjfcn(h_tauVarMat, h_tauPrmVec, elaType, h_lmkIniMat, elmObj, tgtObj
     tv = np.asarray(h_tauVarMat, dtype=np.float64)
     tv = tv.T if tv.ndim == 2 else tv[None, :]
     return forward(spec, tv, trajectory=False, objective=True)["obj"]
+
+
+class Server:
+    """Continuous-batching solver service (layered model): submit() returns at once; result() waits.
+
+    hbm_budget: device bytes the running instances may hold; max_instances: limit on concurrent solves.
+    """
+
+    def __init__(self, hbm_budget: float = 64e9, max_instances: int = 256, device: int = 0):
+        self.ctx = context(device)
+        self.h = C.c_void_p()
+        self.ctx.check(self.ctx.lib.sa_server_create(self.ctx.h, float(hbm_budget), int(max_instances),
+                                                     C.byref(self.h)), "sa_server_create")
+        self.meta = {}
+
+    def submit(self, spec: dict, tauVarVec=None, precision: str = "fp64", objective: bool = True) -> int:
+        D = int(spec["dim"])
+        K = _Keep()
+        lmk = np.ascontiguousarray(np.asarray(spec["lmkIniMat"], dtype=np.float64))
+        N = lmk.shape[1]
+        with_obj = objective and spec.get("tgt") is not None
+        o = _element_object(spec["elmObj"], D, N, K, with_vfd=with_obj)
+        if "elmLyrVec" in spec:
+            o.elmLyrVec = K.i32(spec["elmLyrVec"])
+        p = _params(spec, K, precision)
+        t = _target(spec, K) if with_obj else None
+        tv = np.ascontiguousarray(np.asarray(spec["tauVarVec"] if tauVarVec is None else tauVarVec,
+                                             dtype=np.float64).reshape(-1))
+        rid = C.c_longlong()
+        self.ctx.check(self.ctx.lib.sa_server_submit(self.h, C.byref(o), lmk.ctypes.data_as(_lib._dp), C.byref(p),
+                                                     C.byref(t) if t is not None else None,
+                                                     tv.ctypes.data_as(_lib._dp), tv.size, C.byref(rid)),
+                       "sa_server_submit")
+        self.meta[rid.value] = (D, N)
+        return rid.value
+
+    def poll(self, rid: int) -> int:
+        st = C.c_int()
+        self.ctx.check(self.ctx.lib.sa_server_poll(self.h, int(rid), C.byref(st)), "sa_server_poll")
+        return st.value
+
+    def result(self, rid: int, timeout_ms: float = -1.0) -> dict:
+        """Waits for the request, then returns dict(lmk (D, N), tau (N,), obj, info, latency_ms)."""
+        st = C.c_int()
+        self.ctx.check(self.ctx.lib.sa_server_wait(self.h, int(rid), float(timeout_ms), C.byref(st)),
+                       "sa_server_wait")
+        if st.value not in (_lib.SA_REQ_DONE, _lib.SA_REQ_FAILED):
+            raise TimeoutError(f"request {rid} not finished")
+        D, N = self.meta.pop(rid)
+        lmk, tau = np.zeros((D, N)), np.zeros(N)
+        obj, lat = C.c_double(), C.c_double()
+        info = _lib.SolveInfo()
+        self.ctx.check(self.ctx.lib.sa_server_result(self.h, int(rid), lmk.ctypes.data_as(_lib._dp),
+                                                     tau.ctypes.data_as(_lib._dp), C.byref(obj), C.byref(info),
+                                                     C.byref(lat)), "sa_server_result")
+        return dict(lmk=lmk, tau=tau, obj=obj.value, latency_ms=lat.value,
+                    info=dict(status=info.status, cgIterTotal=info.cgIterTotal, rdIterTotal=info.rdIterTotal,
+                              cgIterMax=info.cgIterMax, invertedElements=info.invertedElements,
+                              elapsedMs=info.elapsedMs))
+
+    def stats(self) -> dict:
+        c = _lib.ServerCounters()
+        self.ctx.check(self.ctx.lib.sa_server_stats(self.h, C.byref(c)), "sa_server_stats")
+        return {k: getattr(c, k) for k, _ in c._fields_}
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.sa_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -340,10 +340,11 @@ __device__ __forceinline__ void block_sum_any(double (&v)[K], double *sm)
 		}
 }
 
-// sum of K values over all threads of the nctas CTAs (fixed order) plus a
-// grid barrier; every thread returns the sums in v.  false: the wait gave up.
+// sum of K values over all threads of the nctas CTAs of one solve (fixed
+// order) plus a barrier among them; lc is the CTA's index within the solve.
+// Every thread returns the sums in v.  false: the wait gave up.
 template <int K>
-__device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int nctas, GridBar *bar,
+__device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int lc, int nctas, GridBar *bar,
                                             unsigned int &target, double *sm)
 {
 	__shared__ int okS;
@@ -351,7 +352,7 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int nc
 	block_sum_any<K>(v, sm);
 	target += (unsigned int) nctas;
 	if (threadIdx.x == 0) {
-		for (int k = 0; k < K; ++k) part[k * nctas + blockIdx.x] = v[k];
+		for (int k = 0; k < K; ++k) part[k * nctas + lc] = v[k];
 		__threadfence();
 		atomicAdd(&bar->count, 1u);
 		int ok = 1;
@@ -439,7 +440,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			wv[c] = acc0[c] + acc1[c];
 			if (own) d1[0] += (double) wv[c] * (double) uv[c];
 		}
-		if (!grid_reduce<1>(d1, part, nctas, bar, target, sm)) {
+		if (!grid_reduce<1>(d1, part, blockIdx.x, nctas, bar, target, sm)) {
 			code = SA_ERR_TIMEOUT;
 			break;
 		}
@@ -469,7 +470,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 				d2[1] += (double) rv[c] * (double) rv[c];
 			}
 		}
-		if (!grid_reduce<2>(d2, part + nctas, nctas, bar, target, sm)) {
+		if (!grid_reduce<2>(d2, part + nctas, blockIdx.x, nctas, bar, target, sm)) {
 			code = SA_ERR_TIMEOUT;
 			break;
 		}
@@ -486,6 +487,124 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	if (own)
 		for (int c = 0; c < B; ++c) x[(long) i * B + c] = xv[c];
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		sc->iters = it; sc->code = code; sc->rr = rr; sc->gam = gam; sc->done = 1;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Batched persistent CG: one cooperative launch advances many independent
+// solves (the instances of a serving batch).  Job j owns the CTAs
+// [cta0, cta0 + nctas) of the launch; its warps stride over its slices, its
+// CTAs reduce and synchronise only among themselves (own partials, own
+// barrier, own scalars), and they stop when their solve stops.  Vectors live
+// in global memory (a job may have more slices than warps); each row is
+// updated by the thread that computed its matvec entry, so only u is read
+// across threads.
+// ---------------------------------------------------------------------------
+constexpr int kBatchBlock = 256;
+constexpr int kBatchMinCtas = 4;
+constexpr int kBatchSlicesPerWarp = 2;     // slices (of 32 rows) per warp when a solve's CTAs are sized
+
+template <int B, typename TM, typename TV, typename TX>
+__global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const CgJob *__restrict__ jobs, int njobs)
+{
+	__shared__ double sm[2 * 32];
+	__shared__ int jS;
+	if (threadIdx.x == 0) {                      // last job with cta0 <= blockIdx.x
+		int lo = 0, hi = njobs - 1;
+		while (lo < hi) {
+			int mid = (lo + hi + 1) >> 1;
+			if (jobs[mid].cta0 <= (int) blockIdx.x) lo = mid;
+			else hi = mid - 1;
+		}
+		jS = lo;
+	}
+	__syncthreads();
+	const CgJob &J = jobs[jS];
+	const int lc = (int) blockIdx.x - J.cta0, nctas = J.nctas;
+	if (lc < 0 || lc >= nctas) return;           // no job owns this CTA (launch padding)
+	CgScal *sc = (CgScal *) J.sc;
+	if (sc->done) return;
+	const SellOp A = J.A;
+	const TM *blk = (const TM *) J.blk;
+	const TV *dinv = (const TV *) J.dinv;
+	TX *x = (TX *) J.x;
+	TV *r = (TV *) J.r, *u = (TV *) J.u, *w = (TV *) J.w, *p = (TV *) J.p, *sv = (TV *) J.s;
+	GridBar *bar = (GridBar *) J.bar;
+	double *part = J.part;
+	const int lane = threadIdx.x & 31, W = blockDim.x >> 5;
+	const int wj = lc * W + (threadIdx.x >> 5), WJ = nctas * W;
+	const int nsl = (A.N + 31) >> 5;
+	const double bb = sc->bb, tolSqu = sc->tolSqu;
+	const int itrMax = sc->itrMax;
+	double gam = sc->gam, rr = sc->rr, gamPrev = 0.0, alphaPrev = 1.0;
+	unsigned int target = 0;
+	int it = 0, code = SA_OK;
+	bool first = true;
+	for (;;) {
+		double d1[1] = {0.0};
+		for (int sl = wj; sl < nsl; sl += WJ) {
+			const int i = sl * 32 + lane;
+			const int wdt = __ldg(A.width + sl);
+			const long base = __ldg(A.off + sl) + lane;
+			TV acc0[B], acc1[B];
+			for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
+			int k = 0;
+			for (; k + 2 <= wdt; k += 2) {
+				spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+				spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), acc1);
+			}
+			if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+			if (i < A.N)
+				for (int c = 0; c < B; ++c) {
+					TV o = acc0[c] + acc1[c];
+					w[(long) i * B + c] = o;
+					d1[0] += (double) o * (double) __ldcg(u + (long) i * B + c);
+				}
+		}
+		if (!grid_reduce<1>(d1, part, lc, nctas, bar, target, sm)) { code = SA_ERR_TIMEOUT; break; }
+		const double delta = d1[0];
+		double alpha, beta;
+		if (first) { beta = 0.0; alpha = gam / delta; }
+		else {
+			beta = gam / gamPrev;
+			alpha = gam / (delta - beta * gam / alphaPrev);
+		}
+		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
+			code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
+			break;
+		}
+		double d2[2] = {0.0, 0.0};
+		const TV al = (TV) alpha, be = (TV) beta;
+		for (int sl = wj; sl < nsl; sl += WJ) {
+			const int i = sl * 32 + lane;
+			if (i >= A.N) continue;
+			for (int c = 0; c < B; ++c) {
+				const long k = (long) i * B + c;
+				TV pk = __ldcg(u + k) + be * p[k];
+				TV sk = w[k] + be * sv[k];
+				p[k] = pk; sv[k] = sk;
+				x[k] = x[k] + (TX) al * (TX) pk;
+				TV rk = r[k] - al * sk;
+				r[k] = rk;
+				TV uk = dinv[k] * rk;
+				u[k] = uk;
+				d2[0] += (double) rk * (double) uk;
+				d2[1] += (double) rk * (double) rk;
+			}
+		}
+		if (!grid_reduce<2>(d2, part + nctas, lc, nctas, bar, target, sm)) { code = SA_ERR_TIMEOUT; break; }
+		gamPrev = gam;
+		gam = d2[0];
+		rr = d2[1];
+		alphaPrev = alpha;
+		first = false;
+		++it;
+		if (!isfinite(gam) || !isfinite(rr)) { code = SA_ERR_NONFINITE; break; }
+		if (rr < tolSqu * bb) { code = SA_OK; break; }
+		if (it >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
+	}
+	if (lc == 0 && threadIdx.x == 0) {
 		sc->iters = it; sc->code = code; sc->rr = rr; sc->gam = gam; sc->done = 1;
 	}
 }
@@ -707,6 +826,163 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 	if (itersOut) *itersOut = total;
 	return code;
 }
+
+// ---------------------------------------------------------------------------
+// batched CG (serving): per-solve preparation, one launch for all solves
+// ---------------------------------------------------------------------------
+template <int B>
+void cg_prepare_fp64(const Mesh &m, const double *blk, const double *dinv, const double *b, double *x, int itrMax,
+                     double tolSqu, CgWork &w, cudaStream_t s)
+{
+	long n = (long) m.N * B;
+	double *q = w.xr;
+	k_spmv64<B><<<grid_for(m.N), kBlock, 0, s>>>(sell_of(m), blk, x, q);
+	set_scal((CgScal *) w.scal, tolSqu, itrMax, -1.0, s);
+	SA_CHECK(cudaMemsetAsync(w.p, 0, sizeof(double) * n, s));
+	SA_CHECK(cudaMemsetAsync(w.sv, 0, sizeof(double) * n, s));
+	k_cg_init<double><<<vec_grid(n, w.smCount), kCgBlock, 0, s>>>(n, b, q, dinv, w.r, w.u, w.part,
+	                                                                (CgScal *) w.scal);
+	w.launches += 2;
+}
+
+template <int B>
+void cg_finish_fp64(const Mesh &m, double *x, CgWork &w, cudaStream_t s)
+{
+	long n = (long) m.N * B;
+	k_cg_zero<double><<<grid_for(n), kBlock, 0, s>>>(n, x, (const CgScal *) w.scal);
+	w.launches += 1;
+}
+
+template <int B>
+void cg_mixed_outer(const Mesh &m, const double *blk, const double *dinv, const double *b, const double *x,
+                    double bb, int first, CgWork &w, cudaStream_t s)
+{
+	long n = (long) m.N * B;
+	float *r32 = w.f32, *u32 = r32 + n, *dinv32 = r32 + 5 * n;
+	double *q = w.xr, *rin = w.xr + n;
+	if (first) k_convert<double, float><<<grid_for(n), kBlock, 0, s>>>(n, dinv, dinv32);
+	k_spmv64<B><<<grid_for(m.N), kBlock, 0, s>>>(sell_of(m), blk, x, q);
+	k_sub<<<grid_for(n), kBlock, 0, s>>>(n, b, q, rin);
+	set_scal((CgScal *) w.scal, 1.0, 1, bb, s);
+	k_cg_init<float><<<vec_grid(n, w.smCount), kCgBlock, 0, s>>>(n, b, q, dinv32, r32, u32, w.part,
+	                                                               (CgScal *) w.scal);
+	w.launches += 3 + (first ? 1 : 0);
+}
+
+template <int B>
+void cg_mixed_inner(const Mesh &m, int itrMax, double innerTolSqu, CgWork &w, cudaStream_t s)
+{
+	long n = (long) m.N * B;
+	float *r32 = w.f32, *u32 = r32 + n, *p32 = r32 + 3 * n, *s32 = r32 + 4 * n;
+	float *dinv32 = r32 + 5 * n, *d32 = r32 + 6 * n;
+	double *rin = w.xr + n, *zero = w.xr + 2 * n;
+	SA_CHECK(cudaMemsetAsync(zero, 0, sizeof(double) * n, s));
+	SA_CHECK(cudaMemsetAsync(d32, 0, sizeof(float) * n, s));
+	SA_CHECK(cudaMemsetAsync(p32, 0, sizeof(float) * n, s));
+	SA_CHECK(cudaMemsetAsync(s32, 0, sizeof(float) * n, s));
+	set_scal((CgScal *) w.scal, innerTolSqu, itrMax, -1.0, s);
+	k_cg_init<float><<<vec_grid(n, w.smCount), kCgBlock, 0, s>>>(n, rin, zero, dinv32, r32, u32, w.part,
+	                                                               (CgScal *) w.scal);
+	w.launches += 1;
+}
+
+void cg_mixed_apply(long n, double *x, const CgWork &w, cudaStream_t s)
+{
+	k_axpy_f32<<<grid_for(n), kBlock, 0, s>>>(n, x, w.f32 + 6 * n);
+}
+
+CgState cg_state(const CgWork &w, cudaStream_t s)
+{
+	CgScal h = read_scal((const CgScal *) w.scal, s);
+	return CgState{h.code, h.iters, h.zero, h.done, h.rr, h.bb};
+}
+
+// CTAs of k_cg_batch resident at once
+template <int B, typename TM, typename TV, typename TX>
+static int batch_capacity(int smCount)
+{
+	static int perSm = -1;
+	if (perSm < 0) {
+		int v = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_batch<B, TM, TV, TX>, kBatchBlock, 0) !=
+		    cudaSuccess) {
+			cudaGetLastError();
+			v = 0;
+		}
+		perSm = v;
+	}
+	return perSm * smCount;
+}
+
+template <int B, typename TM, typename TV, typename TX>
+void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJobs, int maxJobs, cudaStream_t s)
+{
+	const int cap = batch_capacity<B, TM, TV, TX>(smCount);
+	if (cap <= 0) throw CudaError{cudaErrorLaunchOutOfResources, "k_cg_batch occupancy"};
+	const int W = kBatchBlock / 32;
+	size_t k0 = 0;
+	while (k0 < solves.size()) {
+		// CTAs of a solve: one per kBatchSlicesPerWarp slices per warp, from its own size only (its partial
+		// sums, and so its result, do not depend on the other solves); solves [k0, k1) share one launch
+		std::vector<CgJob> jobs;
+		int cta = 0;
+		size_t k1 = k0;
+		for (; k1 < solves.size() && (int) jobs.size() < maxJobs; ++k1) {
+			const BatchSolve &b = solves[k1];
+			const Mesh &m = *b.m;
+			const int per = W * kBatchSlicesPerWarp;
+			const int want = std::max(1, std::min(cap, (m.nslice + per - 1) / per));
+			if (cta + want > cap) break;
+			CgWork &w = *b.cw;
+			CgJob j;
+			j.A = sell_of(m);
+			j.blk = b.blk; j.dinv = b.dinv; j.x = b.x;
+			if (sizeof(TV) == sizeof(double)) {
+				j.r = w.r; j.u = w.u; j.w = w.w; j.p = w.p; j.s = w.sv;
+			} else {
+				long n = (long) m.N * B;
+				float *f = w.f32;
+				j.r = f; j.u = f + n; j.w = f + 2 * n; j.p = f + 3 * n; j.s = f + 4 * n;
+			}
+			j.part = w.part; j.sc = w.scal; j.bar = w.bar;
+			j.cta0 = cta; j.nctas = want;
+			cta += want;
+			SA_CHECK(cudaMemsetAsync(w.bar, 0, sizeof(GridBar), s));
+			w.launches += 1;
+			jobs.push_back(j);
+		}
+		SA_CHECK(cudaMemcpyAsync(devJobs, jobs.data(), sizeof(CgJob) * jobs.size(), cudaMemcpyHostToDevice, s));
+		int nj = (int) jobs.size();
+		const CgJob *dj = devJobs;
+		void *args[] = {(void *) &dj, (void *) &nj};
+		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_batch<B, TM, TV, TX>, dim3(cta), dim3(kBatchBlock),
+		                                     args, 0, s));
+		// the job table is read by the kernel: wait before the host vector goes away or is rewritten
+		SA_CHECK(cudaStreamSynchronize(s));
+		for (const CgJob &j : jobs) {
+			unsigned int gaveUp = 0;
+			SA_CHECK(cudaMemcpy(&gaveUp, &((GridBar *) j.bar)->abort, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+			if (gaveUp) throw DeviceWaitError{"batched CG grid barrier"};
+		}
+		k0 = k1;
+	}
+}
+
+#define SA_BATCH_INST(B)                                                                                          \
+	template void cg_prepare_fp64<B>(const Mesh &, const double *, const double *, const double *, double *, int, \
+	                                 double, CgWork &, cudaStream_t);                                             \
+	template void cg_finish_fp64<B>(const Mesh &, double *, CgWork &, cudaStream_t);                             \
+	template void cg_mixed_outer<B>(const Mesh &, const double *, const double *, const double *, const double *, \
+	                                double, int, CgWork &, cudaStream_t);                                         \
+	template void cg_mixed_inner<B>(const Mesh &, int, double, CgWork &, cudaStream_t);                          \
+	template void cg_batch_run<B, double, double, double>(const std::vector<BatchSolve> &, int, CgJob *, int,    \
+	                                                      cudaStream_t);                                          \
+	template void cg_batch_run<B, float, float, float>(const std::vector<BatchSolve> &, int, CgJob *, int,       \
+	                                                   cudaStream_t);
+SA_BATCH_INST(1)
+SA_BATCH_INST(2)
+SA_BATCH_INST(3)
+#undef SA_BATCH_INST
 
 template int cg_jacobi<1>(const Mesh &, const double *, const double *, const double *, double *, int, double,
                           CgWork &, Status *, int *, cudaStream_t, int);

@@ -17,6 +17,13 @@
 #include <cmath>
 #include <string>
 #include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
 
 struct sa_context {
 	int device = 0;
@@ -41,6 +48,7 @@ static bool is_device_ptr(const void *p)
 struct Pool {                 // device allocations of one call, freed at the end
 	std::vector<void *> ptrs;
 	cudaStream_t s;
+	size_t bytes = 0;         // device bytes allocated
 	explicit Pool(cudaStream_t st) : s(st) {}
 	~Pool() { for (void *p : ptrs) cudaFree(p); }
 	template <typename T> T *alloc(size_t n)
@@ -48,6 +56,7 @@ struct Pool {                 // device allocations of one call, freed at the en
 		void *p = nullptr;
 		SA_CHECK(cudaMalloc(&p, sizeof(T) * (n ? n : 1)));
 		ptrs.push_back(p);
+		bytes += sizeof(T) * (n ? n : 1);
 		return (T *) p;
 	}
 	template <typename T> T *zeros(size_t n)
@@ -410,26 +419,56 @@ struct Stepper {
 		xn = w.xa; xx = w.xb;
 	}
 
+	double *tau_now() const { return w.trajT + (long) t * m.N; }
+	double *tau_next() const { return w.trajT + (long) (t + 1) * m.N; }
+
+	// step part 1: loads and the velocity operator at the current shape
+	void pre_velocity()
+	{
+		launch_activity<D>(m, md, tau_now(), w.fy, w.fr, s);
+		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
+		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, s);
+		launch_yank_rhs<D>(m, *gn, w.fy, w.b, s);
+		if (useK) launch_kernel_matrix<D>(md, m.N, xn, w.K, s);
+		else if (md.precision == SA_PREC_MIXED)
+			k_to_f32<<<grid_for(m.slTotal * sell_vals<D>()), kBlock, 0, s>>>(m.slTotal * sell_vals<D>(), w.blk,
+			                                                                  w.cw.blk32);
+		// activity, (penalty), elastic assembly, yank, (kernel matrix or FP32 copy)
+		w.cw.launches += 3 + (m.Bt > 0 && md.btmWgt != 0.0) + (useK || md.precision == SA_PREC_MIXED);
+	}
+
+	// step part 2 (after the velocity solve): new shape, reaction-diffusion operator and right-hand side
+	void post_velocity()
+	{
+		long n = (long) m.N * D;
+		double dt = md.timeStp;
+		launch_advance<D>(m.N, xn, w.v, dt, xx, w.trajX ? w.trajX + (long) (t + 1) * n : nullptr, s);
+		launch_elem_geom<D>(m, md, xx, *gx, st, true, s);
+		launch_assemble_rd<D>(m, md, *gx, dt, w.Mnxt, w.L, w.dinvRd, s);
+		launch_rd_rhs<D>(m, *gn, w.Mnow, tau_now(), w.fr, dt, w.rhs, s);
+		SA_CHECK(cudaMemcpyAsync(tau_next(), tau_now(), sizeof(double) * m.N, cudaMemcpyDeviceToDevice, s));
+		w.cw.launches += 4;                 // advance, geometry, rd assembly, rd rhs
+	}
+
+	// step part 3 (after the reaction-diffusion solve)
+	void end_step()
+	{
+		std::swap(gn, gx);
+		std::swap(xn, xx);
+		std::swap(w.Mnow, w.Mnxt);
+		++t;
+	}
+
 	// returns the number of steps taken; stops early at timeNum - 1 or on a failed solve
 	int step(int nsteps)
 	{
-		int N = m.N, T = md.timeNum, done = 0;
-		long n = (long) N * D;
-		double dt = md.timeStp;
+		int T = md.timeNum, done = 0;
 		while (done < nsteps && t < T - 1 && out.status == SA_OK) {
-			double *tauNow = w.trajT + (long) t * N, *tauNxt = w.trajT + (long) (t + 1) * N;
-			launch_activity<D>(m, md, tauNow, w.fy, w.fr, s);
-			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
-			launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, s);
-			launch_yank_rhs<D>(m, *gn, w.fy, w.b, s);
+			pre_velocity();
 			int its = 0, code;
 			if (useK) {
-				launch_kernel_matrix<D>(md, N, xn, w.K, s);
 				code = kpcg<D>(m, md, w.blk, w.K, w.b, w.v, w.kw, st, &its, s);
 			} else {
-				if (md.precision == SA_PREC_MIXED)
-					k_to_f32<<<grid_for(m.slTotal * sell_vals<D>()), kBlock, 0, s>>>(m.slTotal * sell_vals<D>(), w.blk,
-					                                                                  w.cw.blk32);
 				w.cw.profileOn = 1;
 				code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st, &its, s,
 				                    md.precision);
@@ -438,22 +477,13 @@ struct Stepper {
 			out.cgTotal += its;
 			out.cgMax = std::max(out.cgMax, its);
 			if (code != SA_OK) { out.status = code; break; }
-			launch_advance<D>(N, xn, w.v, dt, xx, w.trajX ? w.trajX + (long) (t + 1) * n : nullptr, s);
-			launch_elem_geom<D>(m, md, xx, *gx, st, true, s);
-			launch_assemble_rd<D>(m, md, *gx, dt, w.Mnxt, w.L, w.dinvRd, s);
-			launch_rd_rhs<D>(m, *gn, w.Mnow, tauNow, w.fr, dt, w.rhs, s);
-			SA_CHECK(cudaMemcpyAsync(tauNxt, tauNow, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+			post_velocity();
 			int rits = 0;
-			code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, tauNxt, md.rdItrMax, md.rdTolSqu, w.cw, st, &rits, s,
+			code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, st, &rits, s,
 			                    SA_PREC_FP64);
 			out.rdTotal += rits;
 			if (code != SA_OK) { out.status = code; break; }
-			// activity, (penalty), elastic assembly, yank, (to_f32), advance, geometry, rd assembly, rd rhs
-			w.cw.launches += 8 + (m.Bt > 0 && md.btmWgt != 0.0) + (!useK && md.precision == SA_PREC_MIXED);
-			std::swap(gn, gx);
-			std::swap(xn, xx);
-			std::swap(w.Mnow, w.Mnxt);
-			++t;
+			end_step();
 			++done;
 		}
 		return done;
@@ -789,6 +819,479 @@ static int guarded(sa_context *ctx, F &&f)
 	}
 }
 
+
+// ---------------------------------------------------------------------------
+// serving: continuous batching of forward solves (layered model)
+//
+// A request is copied at submission.  The loop thread admits queued
+// requests in arrival order while their device footprint fits the budget
+// (and fewer than maxInstances run), keeps each admitted instance's mesh,
+// state and solver vectors device-resident, and advances all running
+// instances one time step per tick: element kernels per instance, then ONE
+// batched persistent CG launch for all velocity solves of a precision and
+// dimension, then one batched launch for all reaction-diffusion solves.
+// Instances that finish (or fail) leave at the end of a tick and free their
+// memory; queued requests enter at the start of the next one.  The CTAs a
+// solve gets depend only on its own size, so its result does not depend on
+// what else runs in the batch.
+// ---------------------------------------------------------------------------
+struct Request {
+	long long id = 0;
+	int dim = 0;
+	sa_element_object obj{};
+	sa_params prm{};
+	sa_target tgt{};
+	bool hasTgt = false;
+	std::vector<int> elmVtx, vtxElm, btmVtx, vtxBtm, femVtx, femIfo, vfdVtx, elmLyr;
+	std::vector<double> lmk, tauPrm, mod, spdLyr, ynk, rea, tauVar, cen, dir, vol;
+	int state = SA_REQ_QUEUED;
+	int status = SA_OK;
+	std::string err;
+	std::vector<double> lmkOut, tauOut;
+	double objOut = 0.0;
+	sa_solve_info info{};
+	size_t estBytes = 0;
+	std::chrono::steady_clock::time_point tSubmit, tStart, tDone;
+};
+
+template <typename T> static void copy_in(std::vector<T> &dst, const T *src, size_t n)
+{
+	dst.resize(n);
+	if (n) {
+		SA_REQUIRE(src, "missing input array");
+		SA_CHECK(cudaMemcpy(dst.data(), src, sizeof(T) * n, cudaMemcpyDefault));
+	}
+}
+
+// device bytes an instance will hold, from the request's sizes (before the sliced layout exists)
+static size_t estimate_bytes(const Request &r)
+{
+	const sa_element_object &o = r.obj;
+	size_t D = r.dim, N = o.lmkNum, E = o.elmNum, Z = o.nzrNum, T = r.prm.timeNum;
+	size_t slots = Z + Z / 8 + 32 * (N / 32 + 1);                 // sliced slots incl. padding (bound)
+	size_t ints = E * (D + 1) + N * o.vtxElmCols + Z * (2 + o.femIfoCols) + Z * 4 + slots + 2 * E +
+	              (size_t) o.btmElmNum * D + (size_t) o.btmLmkNum * o.vtxBtmCols + (size_t) o.vfdElmNum * D;
+	size_t dbl = slots * (D * D + 1) + 2 * Z + 2 * E * (D == 3 ? 16 : 8) + 20 * N * D + 8 * N + T * N;
+	if (r.prm.precision == SA_PREC_MIXED) dbl += (slots * D * D + 7 * N * D) / 2;
+	if (r.hasTgt) dbl += (size_t) r.tgt.tgtElmNum * (2 * D + 1) + (size_t) o.vfdElmNum * (3 * D + 2);
+	return 4 * ints + 8 * dbl + (1 << 20);
+}
+
+struct InstBase {
+	Request *req = nullptr;
+	size_t bytes = 0;
+	int failed = 0;
+	int its = 0, rits = 0;
+	double bb = -1.0, innerTol = 0.0;
+	int mixedTotal = 0, mixedDone = 0;
+	virtual ~InstBase() {}
+	virtual int dim() const = 0;
+	virtual int precision() const = 0;
+	virtual bool finished() const = 0;
+	virtual void pre_velocity() = 0;
+	virtual void prepare_velocity_fp64() = 0;
+	virtual void finish_velocity_fp64() = 0;
+	virtual BatchSolve velocity_fp64() = 0;
+	virtual void mixed_outer(int first) = 0;
+	virtual void mixed_inner() = 0;
+	virtual BatchSolve velocity_mixed() = 0;
+	virtual void mixed_apply() = 0;
+	virtual void zero_velocity() = 0;
+	virtual void prepare_rd() = 0;
+	virtual BatchSolve rd_solve() = 0;
+	virtual void finish_rd() = 0;
+	virtual void end_step() = 0;
+	virtual CgWork &cg() = 0;
+	virtual const Model &model() const = 0;
+	virtual void results() = 0;              // final state, objective and diagnostics into the request
+	virtual void account(int velIts, int rdIts) = 0;
+	virtual void set_status(int code) = 0;
+};
+
+template <int D>
+struct Inst : InstBase {
+	Pool P;
+	Mesh m;
+	Model md;
+	Work w;
+	Stepper<D> st;
+	cudaStream_t s;
+	const double *tc = nullptr, *tu = nullptr, *tvl = nullptr;
+	int Vt = 0;
+
+	Inst(Request *r, cudaStream_t s_) : P(s_), st(m, md, w, s_), s(s_)
+	{
+		req = r;
+		fill_model(md, D, &r->prm, r->hasTgt ? &r->tgt : nullptr, P);
+		SA_REQUIRE(!md.frame && md.ldmWgt == 0.0, "the server runs the layered model (elaType isotropic, ldmWgt 0)");
+		build_mesh(m, &r->obj, r->hasTgt, false, true, md.lyrNum, P);
+		SA_REQUIRE(r->tauVar.size() >= (size_t) D + 2, "tauVarVec too small");
+		const double *x0 = P.dev(r->lmk.data(), (size_t) m.N * D);
+		if (r->hasTgt) {
+			Vt = r->tgt.tgtElmNum;
+			tc = P.dev(r->cen.data(), (size_t) Vt * D);
+			tu = P.dev(r->dir.data(), (size_t) Vt * D);
+			tvl = P.dev(r->vol.data(), (size_t) Vt);
+		}
+		alloc_work<D>(w, m, md, false, P);
+		double *xa = P.alloc<double>((size_t) m.N * D);
+		launch_soa_to_aos(m.N, D, x0, xa, s);
+		k_init_sign<D><<<grid_for(m.E), kBlock, 0, s>>>(m.E, m.elmVtx, xa, m.sign0);
+		st.start(x0, r->tauVar.data());
+		SA_CHECK(cudaStreamSynchronize(s));
+		bytes = P.bytes;
+	}
+	int dim() const override { return D; }
+	int precision() const override { return md.precision; }
+	bool finished() const override { return failed || st.t >= md.timeNum - 1; }
+	void pre_velocity() override { st.pre_velocity(); }
+	void prepare_velocity_fp64() override
+	{
+		cg_prepare_fp64<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, s);
+	}
+	void finish_velocity_fp64() override { cg_finish_fp64<D>(m, w.v, w.cw, s); }
+	BatchSolve velocity_fp64() override { return BatchSolve{&m, &w.cw, w.blk, w.dinv, w.v}; }
+	void mixed_outer(int first) override { cg_mixed_outer<D>(m, w.blk, w.dinv, w.b, w.v, bb, first, w.cw, s); }
+	void mixed_inner() override { cg_mixed_inner<D>(m, md.cgItrMax - mixedTotal, innerTol, w.cw, s); }
+	BatchSolve velocity_mixed() override
+	{
+		long n = (long) m.N * D;
+		return BatchSolve{&m, &w.cw, w.cw.blk32, w.cw.f32 + 5 * n, w.cw.f32 + 6 * n};
+	}
+	void mixed_apply() override { cg_mixed_apply((long) m.N * D, w.v, w.cw, s); }
+	void zero_velocity() override { SA_CHECK(cudaMemsetAsync(w.v, 0, sizeof(double) * m.N * D, s)); }
+	void prepare_rd() override
+	{
+		st.post_velocity();
+		cg_prepare_fp64<1>(m, w.L, w.dinvRd, w.rhs, st.tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, s);
+	}
+	BatchSolve rd_solve() override { return BatchSolve{&m, &w.cw, w.L, w.dinvRd, st.tau_next()}; }
+	void finish_rd() override { cg_finish_fp64<1>(m, st.tau_next(), w.cw, s); }
+	void end_step() override { st.end_step(); }
+	CgWork &cg() override { return w.cw; }
+	const Model &model() const override { return md; }
+	void set_status(int code) override { st.out.status = code; }
+	void account(int velIts, int rdIts) override
+	{
+		st.out.cgTotal += velIts;
+		st.out.cgMax = std::max(st.out.cgMax, velIts);
+		st.out.rdTotal += rdIts;
+	}
+	void results() override
+	{
+		Request &r = *req;
+		Status hs;
+		SA_CHECK(cudaMemcpyAsync(&hs, st.st, sizeof(Status), cudaMemcpyDeviceToHost, s));
+		std::vector<double> h = to_host(st.xn, (size_t) m.N * D, s);
+		r.lmkOut.assign((size_t) m.N * D, 0.0);
+		for (int i = 0; i < m.N; ++i)
+			for (int d = 0; d < D; ++d) r.lmkOut[(size_t) d * m.N + i] = h[(size_t) i * D + d];
+		r.tauOut = to_host(w.trajT + (long) st.t * m.N, (size_t) m.N, s);
+		r.status = st.out.status;
+		r.objOut = 0.0;
+		if (r.hasTgt) {
+			if (st.out.status != SA_OK) r.objOut = DBL_MAX;
+			else {
+				int err = SA_OK;
+				r.objOut = varifold<D>(m, md, st.xn, tc, tu, tvl, Vt, nullptr, s, md.precision, &err);
+				SA_REQUIRE(err == SA_OK, "varifold arguments");
+			}
+		}
+		r.info.status = st.out.status;
+		r.info.cgIterTotal = st.out.cgTotal;
+		r.info.rdIterTotal = st.out.rdTotal;
+		r.info.cgIterMax = st.out.cgMax;
+		r.info.invertedElements = hs.inverted;
+		r.info.kernelLaunches = w.cw.launches;
+	}
+};
+
+struct Server {
+	sa_context *ctx;
+	cudaStream_t s = nullptr;
+	size_t budget;
+	int maxInst;
+	std::mutex mu;
+	std::condition_variable cv;
+	std::deque<Request *> queue;
+	std::map<long long, std::unique_ptr<Request>> reqs;
+	std::vector<std::unique_ptr<InstBase>> active;
+	long long nextId = 1, submitted = 0, completed = 0, failedCount = 0, ticks = 0;
+	size_t inUse = 0, peak = 0;
+	double busyMs = 0.0;
+	bool stop = false;
+	std::string loopErr;
+	CgJob *devJobs = nullptr;
+	int smCount = 1;
+	std::thread th;
+
+	static constexpr int kMaxJobs = 4096;
+
+	Server(sa_context *c, size_t budgetBytes, int maxInstances) : ctx(c), budget(budgetBytes), maxInst(maxInstances)
+	{
+		SA_CHECK(cudaSetDevice(ctx->device));
+		SA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+		SA_CHECK(cudaMalloc(&devJobs, sizeof(CgJob) * kMaxJobs));
+		SA_CHECK(cudaDeviceGetAttribute(&smCount, cudaDevAttrMultiProcessorCount, ctx->device));
+		th = std::thread([this] { loop(); });
+	}
+	~Server()
+	{
+		{
+			std::lock_guard<std::mutex> g(mu);
+			stop = true;
+		}
+		cv.notify_all();
+		if (th.joinable()) th.join();
+		active.clear();
+		cudaSetDevice(ctx->device);
+		if (devJobs) cudaFree(devJobs);
+		if (s) cudaStreamDestroy(s);
+	}
+
+	// a solve that did not converge (or broke down): the instance stops, the request completes with that
+	// per-solve status and objective DBL_MAX, as sa_forward reports it
+	void fail(InstBase &in, int code)
+	{
+		in.failed = 1;
+		in.set_status(code);
+	}
+
+	// one time step of every running instance
+	void tick()
+	{
+		std::vector<InstBase *> run;
+		for (auto &u : active) if (!u->finished()) run.push_back(u.get());
+		for (InstBase *in : run) { in->its = 0; in->rits = 0; in->pre_velocity(); }
+		// velocity: FP64 instances, one batched launch per dimension
+		for (int D = 2; D <= 3; ++D) {
+			std::vector<InstBase *> g;
+			for (InstBase *in : run) if (in->dim() == D && in->precision() == SA_PREC_FP64) g.push_back(in);
+			if (g.empty()) continue;
+			std::vector<BatchSolve> bs;
+			for (InstBase *in : g) { in->prepare_velocity_fp64(); bs.push_back(in->velocity_fp64()); }
+			if (D == 2) cg_batch_run<2, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
+			else cg_batch_run<3, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
+			for (InstBase *in : g) in->finish_velocity_fp64();
+			for (InstBase *in : g) {
+				CgState c = cg_state(in->cg(), s);
+				in->its = c.iters;
+				if (c.code != SA_OK) fail(*in, c.code);
+			}
+		}
+		// velocity: mixed precision, FP64 iterative refinement around batched FP32 solves
+		for (int D = 2; D <= 3; ++D) {
+			std::vector<InstBase *> g;
+			for (InstBase *in : run) if (in->dim() == D && in->precision() == SA_PREC_MIXED) g.push_back(in);
+			if (g.empty()) continue;
+			for (InstBase *in : g) { in->bb = -1.0; in->mixedTotal = 0; in->mixedDone = 0; }
+			for (int outer = 0; outer < 64 && !g.empty(); ++outer) {
+				for (InstBase *in : g) in->mixed_outer(outer == 0);
+				std::vector<InstBase *> inner;
+				for (InstBase *in : g) {
+					CgState c = cg_state(in->cg(), s);
+					const Model &md = in->model();
+					if (in->bb < 0.0) in->bb = c.bb;
+					if (c.code == SA_ERR_NONFINITE) { fail(*in, SA_ERR_NONFINITE); continue; }
+					if (c.zero) { in->zero_velocity(); continue; }
+					if (c.rr < md.cgTolSqu * in->bb) continue;
+					if (in->mixedTotal >= md.cgItrMax) { fail(*in, SA_ERR_NOT_CONVERGED); continue; }
+					double need = 0.01 * md.cgTolSqu * in->bb / c.rr;
+					in->innerTol = need > 1e-10 ? need : 1e-10;
+					inner.push_back(in);
+				}
+				if (inner.empty()) break;
+				std::vector<BatchSolve> bs;
+				for (InstBase *in : inner) { in->mixed_inner(); bs.push_back(in->velocity_mixed()); }
+				if (D == 2) cg_batch_run<2, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
+				else cg_batch_run<3, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
+				std::vector<InstBase *> next;
+				for (InstBase *in : inner) {
+					CgState c = cg_state(in->cg(), s);
+					in->mixedTotal += c.iters;
+					if (c.code == SA_ERR_NONFINITE) { fail(*in, SA_ERR_NONFINITE); continue; }
+					in->mixed_apply();
+					next.push_back(in);
+				}
+				g.swap(next);
+				if (outer == 63)
+					for (InstBase *in : g) fail(*in, SA_ERR_NOT_CONVERGED);
+			}
+			for (InstBase *in : run)
+				if (in->dim() == D && in->precision() == SA_PREC_MIXED) in->its = in->mixedTotal;
+		}
+		// reaction-diffusion: one batched launch for every instance still running
+		std::vector<InstBase *> rd;
+		for (InstBase *in : run) if (!in->failed) rd.push_back(in);
+		if (!rd.empty()) {
+			std::vector<BatchSolve> bs;
+			for (InstBase *in : rd) { in->prepare_rd(); bs.push_back(in->rd_solve()); }
+			cg_batch_run<1, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
+			for (InstBase *in : rd) in->finish_rd();
+			for (InstBase *in : rd) {
+				CgState c = cg_state(in->cg(), s);
+				in->rits = c.iters;
+				if (c.code != SA_OK) fail(*in, c.code);
+			}
+		}
+		for (InstBase *in : run) {
+			in->account(in->its, in->rits);
+			if (!in->failed) in->end_step();
+		}
+		++ticks;
+	}
+
+	void admit(std::unique_lock<std::mutex> &lk)
+	{
+		while (!queue.empty() && (int) active.size() < maxInst) {
+			Request *r = queue.front();
+			if (!active.empty() && inUse + r->estBytes > budget) break;     // wait for memory
+			queue.pop_front();
+			r->state = SA_REQ_RUNNING;
+			r->tStart = std::chrono::steady_clock::now();
+			lk.unlock();
+			std::unique_ptr<InstBase> in;
+			std::string err;
+			int code = SA_OK;
+			try {
+				if (r->dim == 2) in.reset(new Inst<2>(r, s));
+				else in.reset(new Inst<3>(r, s));
+			} catch (const ArgError &e) { code = SA_ERR_ARG; err = e.msg; }
+			catch (const CudaError &e) { code = SA_ERR_CUDA; err = std::string(e.where) + ": " + cudaGetErrorString(e.e); cudaGetLastError(); }
+			catch (const std::bad_alloc &) { code = SA_ERR_CUDA; err = "host allocation failed"; }
+			lk.lock();
+			if (!in) {
+				r->status = code; r->err = err; r->state = SA_REQ_FAILED;
+				r->tDone = std::chrono::steady_clock::now();
+				++failedCount;
+				cv.notify_all();
+				continue;
+			}
+			inUse += in->bytes;
+			peak = std::max(peak, inUse);
+			active.push_back(std::move(in));
+		}
+	}
+
+	void retire(std::unique_lock<std::mutex> &lk)
+	{
+		for (size_t k = 0; k < active.size();) {
+			InstBase *in = active[k].get();
+			if (!in->finished()) { ++k; continue; }
+			Request *r = in->req;
+			lk.unlock();
+			std::string err;
+			try { in->results(); }
+			catch (const ArgError &e) { err = e.msg; }
+			catch (const CudaError &e) { err = std::string(e.where) + ": " + cudaGetErrorString(e.e); cudaGetLastError(); }
+			lk.lock();
+			if (!err.empty() && r->err.empty()) { r->status = SA_ERR_CUDA; r->err = err; }
+			bool ok = r->err.empty();
+			r->state = ok ? SA_REQ_DONE : SA_REQ_FAILED;
+			r->tDone = std::chrono::steady_clock::now();
+			if (ok) ++completed; else ++failedCount;
+			inUse -= in->bytes;
+			active.erase(active.begin() + k);
+			cv.notify_all();
+		}
+	}
+
+	void loop()
+	{
+		cudaSetDevice(ctx->device);
+		std::unique_lock<std::mutex> lk(mu);
+		while (true) {
+			if (stop && queue.empty() && active.empty()) break;
+			admit(lk);
+			if (active.empty()) {
+				if (stop) break;
+				cv.wait(lk, [this] { return stop || !queue.empty(); });
+				continue;
+			}
+			lk.unlock();
+			auto t0 = std::chrono::steady_clock::now();
+			std::string err;
+			int code = SA_OK;
+			try { tick(); }
+			catch (const CudaError &e) { code = SA_ERR_CUDA; err = std::string(e.where) + ": " + cudaGetErrorString(e.e); cudaGetLastError(); }
+			catch (const DeviceWaitError &e) { code = SA_ERR_TIMEOUT; err = std::string(e.where) + ": a device-side wait gave up"; }
+			catch (const ArgError &e) { code = SA_ERR_ARG; err = e.msg; }
+			busyMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+			lk.lock();
+			if (code != SA_OK) {             // an error, not a solve status: the running requests fail
+				loopErr = err;
+				for (auto &u : active)
+					if (!u->finished()) { u->failed = 1; u->set_status(code); u->req->status = code; u->req->err = err; }
+			}
+			retire(lk);
+		}
+	}
+
+	long long submit(int dim, const sa_element_object *o, const double *lmkIni, const sa_params *p,
+	                 const sa_target *t, const double *tauVar, int tauVarNum)
+	{
+		SA_REQUIRE(o && lmkIni && p && tauVar, "missing argument");
+		SA_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+		SA_REQUIRE(o->dim == dim, "element object dimension");
+		SA_REQUIRE(p->elaType == SA_ELA_ISOTROPIC, "the server runs the layered model (elaType isotropic)");
+		SA_REQUIRE(o->lmkNum > 0 && o->elmNum > 0 && o->nzrNum > 0 && p->timeNum >= 1, "empty problem");
+		std::unique_ptr<Request> r(new Request);
+		r->dim = dim;
+		size_t N = o->lmkNum, E = o->elmNum, Z = o->nzrNum;
+		copy_in(r->elmVtx, o->elmVtxMat, E * (dim + 1));
+		copy_in(r->vtxElm, o->vtxElmMat, N * o->vtxElmCols);
+		copy_in(r->btmVtx, o->btmVtxMat, (size_t) o->btmElmNum * dim);
+		copy_in(r->vtxBtm, o->vtxBtmMat, (size_t) o->btmLmkNum * o->vtxBtmCols);
+		copy_in(r->femVtx, o->femVtxMat, Z * 2);
+		copy_in(r->femIfo, o->femIfoMat, Z * o->femIfoCols);
+		copy_in(r->elmLyr, o->elmLyrVec, E);
+		r->obj = *o;
+		r->obj.elmVtxMat = r->elmVtx.data(); r->obj.vtxElmMat = r->vtxElm.data();
+		r->obj.frmVtxMat = nullptr; r->obj.tsvVtxMat = nullptr; r->obj.bdrVtxMat = nullptr;
+		r->obj.vtxBdrMat = nullptr; r->obj.vfdIfoMat = nullptr;
+		r->obj.btmVtxMat = r->btmVtx.empty() ? nullptr : r->btmVtx.data();
+		r->obj.vtxBtmMat = r->vtxBtm.empty() ? nullptr : r->vtxBtm.data();
+		r->obj.femVtxMat = r->femVtx.data(); r->obj.femIfoMat = r->femIfo.data();
+		r->obj.elmLyrVec = r->elmLyr.data();
+		copy_in(r->lmk, lmkIni, N * dim);
+		copy_in(r->tauVar, tauVar, (size_t) tauVarNum);
+		r->prm = *p;
+		copy_in(r->tauPrm, p->tauPrmVec, p->tauPrmVec ? (size_t) p->tauPrmNum : 0);
+		copy_in(r->mod, p->modVec, (size_t) p->modNum);
+		copy_in(r->spdLyr, p->spdLyrVec, (size_t) p->lyrNum);
+		copy_in(r->ynk, p->ynkActPrmVec, 1);
+		copy_in(r->rea, p->reaActPrmVec, 1);
+		r->prm.tauPrmVec = r->tauPrm.empty() ? nullptr : r->tauPrm.data();
+		r->prm.modVec = r->mod.data(); r->prm.spdLyrVec = r->spdLyr.data();
+		r->prm.ynkActPrmVec = r->ynk.data(); r->prm.reaActPrmVec = r->rea.data();
+		if (t) {
+			r->hasTgt = true;
+			size_t Vt = t->tgtElmNum, Vd = o->vfdElmNum;
+			copy_in(r->vfdVtx, o->vfdVtxMat, Vd * dim);
+			r->obj.vfdVtxMat = r->vfdVtx.data();
+			copy_in(r->cen, t->cenPosMat, Vt * dim);
+			copy_in(r->dir, t->uniDirMat, Vt * dim);
+			copy_in(r->vol, t->elmVolVec, Vt);
+			r->tgt = *t;
+			r->tgt.cenPosMat = r->cen.data(); r->tgt.uniDirMat = r->dir.data(); r->tgt.elmVolVec = r->vol.data();
+		} else {
+			r->obj.vfdVtxMat = nullptr;
+		}
+		r->estBytes = estimate_bytes(*r);
+		SA_REQUIRE(r->estBytes <= budget, "request larger than the server's device memory budget");
+		r->tSubmit = std::chrono::steady_clock::now();
+		std::lock_guard<std::mutex> g(mu);
+		SA_REQUIRE(!stop, "server is stopping");
+		long long id = nextId++;
+		r->id = id;
+		queue.push_back(r.get());
+		reqs[id] = std::move(r);
+		++submitted;
+		cv.notify_all();
+		return id;
+	}
+};
+
 }  // namespace sa
 
 // ===========================================================================
@@ -1007,6 +1510,119 @@ int sa_computeObjfcn_frame(sa_context *ctx, int dim, const double *tauVarMat, in
 	t.dirKnlType = (char) dirKnlType; t.dirKnlWidth = dirKnlWidth;
 	return sa_forward(ctx, &o, lmkIniMat, &p, &t, tauVarMat, tauVarNum, objTotNum, nullptr, nullptr, objVec,
 	                  nullptr);
+}
+
+
+// ---------------------------------------------------------------------------
+// serving
+// ---------------------------------------------------------------------------
+struct sa_server {
+	sa_context *ctx;
+	sa::Server *impl;
+	std::string err;
+};
+
+int sa_server_create(sa_context *ctx, double hbmBudgetBytes, int maxInstances, sa_server **out)
+{
+	if (!out) return SA_ERR_ARG;
+	*out = nullptr;
+	return sa::guarded(ctx, [&]() {
+		SA_REQUIRE(hbmBudgetBytes > 0.0 && maxInstances > 0, "budget and instance limit must be positive");
+		std::unique_ptr<sa_server> sv(new sa_server{ctx, nullptr, std::string()});
+		sv->impl = new sa::Server(ctx, (size_t) hbmBudgetBytes, maxInstances);
+		*out = sv.release();
+		return SA_OK;
+	});
+}
+
+int sa_server_submit(sa_server *sv, const sa_element_object *obj, const double *lmkIniMat, const sa_params *prm,
+                     const sa_target *tgt, const double *tauVarVec, int tauVarNum, long long *requestId)
+{
+	if (!sv || !requestId || !obj) return SA_ERR_ARG;
+	return sa::guarded(sv->ctx, [&]() {
+		*requestId = sv->impl->submit(obj->dim, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum);
+		return SA_OK;
+	});
+}
+
+int sa_server_poll(sa_server *sv, long long requestId, int *state)
+{
+	if (!sv || !state) return SA_ERR_ARG;
+	std::lock_guard<std::mutex> g(sv->impl->mu);
+	auto it = sv->impl->reqs.find(requestId);
+	if (it == sv->impl->reqs.end()) return SA_ERR_ARG;
+	*state = it->second->state;
+	return SA_OK;
+}
+
+int sa_server_wait(sa_server *sv, long long requestId, double timeoutMs, int *state)
+{
+	if (!sv || !state) return SA_ERR_ARG;
+	sa::Server &S = *sv->impl;
+	std::unique_lock<std::mutex> lk(S.mu);
+	auto it = S.reqs.find(requestId);
+	if (it == S.reqs.end()) return SA_ERR_ARG;
+	sa::Request *r = it->second.get();
+	auto done = [r] { return r->state == SA_REQ_DONE || r->state == SA_REQ_FAILED; };
+	if (timeoutMs < 0) S.cv.wait(lk, done);
+	else S.cv.wait_for(lk, std::chrono::duration<double, std::milli>(timeoutMs), done);
+	*state = r->state;
+	return SA_OK;
+}
+
+int sa_server_result(sa_server *sv, long long requestId, double *lmkMat, double *tauVec, double *objOut,
+                     sa_solve_info *info, double *latencyMs)
+{
+	if (!sv) return SA_ERR_ARG;
+	sa::Server &S = *sv->impl;
+	std::unique_ptr<sa::Request> r;
+	{
+		std::lock_guard<std::mutex> g(S.mu);
+		auto it = S.reqs.find(requestId);
+		if (it == S.reqs.end()) return SA_ERR_ARG;
+		if (it->second->state != SA_REQ_DONE && it->second->state != SA_REQ_FAILED) return SA_ERR_ARG;
+		r = std::move(it->second);
+		S.reqs.erase(it);
+	}
+	if (r->state == SA_REQ_FAILED) {
+		sv->ctx->err = r->err;
+		if (latencyMs) *latencyMs = std::chrono::duration<double, std::milli>(r->tDone - r->tSubmit).count();
+		return r->status != SA_OK ? r->status : SA_ERR_CUDA;
+	}
+	if (lmkMat && !r->lmkOut.empty()) memcpy(lmkMat, r->lmkOut.data(), sizeof(double) * r->lmkOut.size());
+	if (tauVec && !r->tauOut.empty()) memcpy(tauVec, r->tauOut.data(), sizeof(double) * r->tauOut.size());
+	if (objOut) *objOut = r->objOut;
+	if (info) {
+		*info = r->info;
+		info->elapsedMs = std::chrono::duration<double, std::milli>(r->tDone - r->tStart).count();
+	}
+	if (latencyMs) *latencyMs = std::chrono::duration<double, std::milli>(r->tDone - r->tSubmit).count();
+	return SA_OK;
+}
+
+int sa_server_stats(sa_server *sv, sa_server_counters *st)
+{
+	if (!sv || !st) return SA_ERR_ARG;
+	sa::Server &S = *sv->impl;
+	std::lock_guard<std::mutex> g(S.mu);
+	st->submitted = S.submitted;
+	st->completed = S.completed;
+	st->failed = S.failedCount;
+	st->queued = (int) S.queue.size();
+	st->running = (int) S.active.size();
+	st->bytesInUse = (double) S.inUse;
+	st->peakBytes = (double) S.peak;
+	st->ticks = S.ticks;
+	st->busyMs = S.busyMs;
+	return SA_OK;
+}
+
+int sa_server_destroy(sa_server *sv)
+{
+	if (!sv) return SA_OK;
+	delete sv->impl;
+	delete sv;
+	return SA_OK;
 }
 
 }  // extern "C"

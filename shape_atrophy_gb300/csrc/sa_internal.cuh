@@ -311,6 +311,39 @@ template <int B> int cg_jacobi(const Mesh &m, const double *blk, const double *d
                                double *x, int itrMax, double tolSqu, CgWork &w, Status *st,
                                int *itersOut, cudaStream_t s, int precision);
 
+// ---- batched CG (many independent solves in one persistent launch) ----
+struct CgJob {                 // one solve of a batched launch (device-visible)
+	SellOp A;
+	const void *blk, *dinv;    // operator values (TM), Jacobi inverse (TV)
+	void *x, *r, *u, *w, *p, *s;   // solution (TX) and CG vectors (TV)
+	double *part;              // 3 x nctas partial sums
+	void *sc, *bar;            // scalars, grid barrier
+	int cta0, nctas;           // CTAs of the launch that belong to this solve
+};
+struct CgState { int code, iters, zero, done; double rr, bb; };   // host copy of a solve's scalars
+enum CgVec { kCgFp64, kCgFp32 };     // which vector set of CgWork a batched solve uses
+struct BatchSolve { const Mesh *m; CgWork *cw; const void *blk; const void *dinv; void *x; };
+
+// FP64 solve A x = b (x holds the initial guess): q = A x, r = b - q, u = D^-1 r, scalars; zeroes p, s
+template <int B> void cg_prepare_fp64(const Mesh &m, const double *blk, const double *dinv, const double *b,
+                                      double *x, int itrMax, double tolSqu, CgWork &w, cudaStream_t s);
+// mixed precision, outer step: rin = b - A x (FP64 operator), |b|^2 (bb < 0: take it from b) and |rin|^2,
+// and the FP32 Jacobi inverse on the first call (first != 0)
+template <int B> void cg_mixed_outer(const Mesh &m, const double *blk, const double *dinv, const double *b,
+                                     const double *x, double bb, int first, CgWork &w, cudaStream_t s);
+// mixed precision, inner FP32 solve A d = rin to the relative tolerance innerTolSqu (d = 0 first)
+template <int B> void cg_mixed_inner(const Mesh &m, int itrMax, double innerTolSqu, CgWork &w, cudaStream_t s);
+// mixed precision: x += d
+void cg_mixed_apply(long n, double *x, const CgWork &w, cudaStream_t s);
+// one launch (or several, when the CTAs do not fit at once) over all solves
+template <int B, typename TM, typename TV, typename TX>
+void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJobs, int maxJobs,
+                  cudaStream_t s);
+// x = 0 where the right-hand side was zero (after a batched FP64 solve)
+template <int B> void cg_finish_fp64(const Mesh &m, double *x, CgWork &w, cudaStream_t s);
+// host copy of the scalars (synchronises s)
+CgState cg_state(const CgWork &w, cudaStream_t s);
+
 // frame mode K-preconditioned CG (2D/ipcg.cu:11-100) with dense K
 struct KpcgWork {
 	double *Ad, *Kid, *r, *Kr, *dv, *wK;  // wK tracks K^{-1} x
