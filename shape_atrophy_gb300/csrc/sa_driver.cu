@@ -132,16 +132,20 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 	m.dim = D; m.V = D + 1; m.N = o->lmkNum; m.E = o->elmNum; m.Z = o->nzrNum;
 	m.Bt = o->btmElmNum; m.Nb = o->btmLmkNum; m.Vd = needVfd ? o->vfdElmNum : 0;
 	SA_REQUIRE(m.N > 0 && m.E > 0 && m.Z >= m.N, "empty mesh or femVtxMat smaller than the node count");
-	SA_REQUIRE(o->elmVtxMat && o->vtxElmMat && o->frmVtxMat && o->tsvVtxMat && o->femVtxMat && o->femIfoMat,
-	           "missing element-object array");
+	SA_REQUIRE(o->elmVtxMat && o->vtxElmMat && o->femVtxMat && o->femIfoMat, "missing element-object array");
+	// the frame arrays are read by the frame model only
+	SA_REQUIRE(layered || (o->frmVtxMat && o->tsvVtxMat), "frame model needs tanVtxMat/nmlVtxMat and tsvVtxMat");
+	const bool haveFrame = o->frmVtxMat && o->tsvVtxMat;
 	SA_REQUIRE(o->vtxElmCols >= 1 && o->femIfoCols >= 2, "adjacency matrices need a count column");
 	SA_REQUIRE((long) m.E * 16 < (1L << 31), "too many elements for the 32-bit assembly table");
 	m.vtxElmCols = o->vtxElmCols; m.femIfoCols = o->femIfoCols;
 	int frmCols = D == 2 ? 4 : 6;
 	m.elmVtx = (int *) P.dev(o->elmVtxMat, (size_t) m.E * m.V);
 	m.vtxElm = (int *) P.dev(o->vtxElmMat, (size_t) m.N * o->vtxElmCols);
-	m.frmVtx = (int *) P.dev(o->frmVtxMat, (size_t) m.E * frmCols);
-	m.tsvVtx = (int *) P.dev(o->tsvVtxMat, (size_t) m.E * frmCols);
+	if (haveFrame) {
+		m.frmVtx = (int *) P.dev(o->frmVtxMat, (size_t) m.E * frmCols);
+		m.tsvVtx = (int *) P.dev(o->tsvVtxMat, (size_t) m.E * frmCols);
+	}
 	m.femVtx = (int *) P.dev(o->femVtxMat, (size_t) m.Z * 2);
 	m.femIfo = (int *) P.dev(o->femIfoMat, (size_t) m.Z * o->femIfoCols);
 	if (m.Bt > 0) {
@@ -195,10 +199,12 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 			           "vtxElmMat entry does not match elmVtxMat");
 		}
 	}
-	std::vector<int> fr = to_host(m.frmVtx, (size_t) m.E * frmCols, s);
-	for (int v : fr) SA_REQUIRE(v >= 0 && v < m.N, "tan/nmlVtxMat index out of range");
-	std::vector<int> ts = to_host(m.tsvVtx, (size_t) m.E * frmCols, s);
-	for (int v : ts) SA_REQUIRE(v >= 0 && v < m.N, "tsvVtxMat index out of range");
+	if (haveFrame) {
+		std::vector<int> fr = to_host(m.frmVtx, (size_t) m.E * frmCols, s);
+		for (int v : fr) SA_REQUIRE(v >= 0 && v < m.N, "tan/nmlVtxMat index out of range");
+		std::vector<int> ts = to_host(m.tsvVtx, (size_t) m.E * frmCols, s);
+		for (int v : ts) SA_REQUIRE(v >= 0 && v < m.N, "tsvVtxMat index out of range");
+	}
 	if (m.Bt > 0) {
 		std::vector<int> bv = to_host(m.btmVtx, (size_t) m.Bt * D, s);
 		for (int v : bv) SA_REQUIRE(v >= 0 && v < m.N, "btmVtxMat index out of range");
