@@ -10,8 +10,12 @@
 //   dsum (2D_frame/dsum.cu:6-73)                     -> device_sum (same 512-wide tree order)
 // The Matern-3/2 centre kernel 'M' (1 + r/w) exp(-r/w) is the layered model's addition.
 //
-// Mixed precision: pair terms in FP32 with FP32 sums inside each column tile,
-// tile sums accumulated in FP64 per row, FP64 final reduction.
+// Mixed precision: pair terms in FP32 with compensated (Kahan) FP32 sums
+// inside each column tile, tile sums accumulated in FP64 per row, FP64 final
+// reduction.  Centres are carried as two floats (value and remainder), so a
+// centre difference keeps FP32 precision relative to the difference itself
+// rather than to the coordinates (the kernel widths are small against the
+// shape's extent).
 #include "sa_internal.cuh"
 #include <cmath>
 
@@ -75,12 +79,15 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
                            double dw, double *__restrict__ out, int grad, double *__restrict__ dc,
                            double *__restrict__ dt)
 {
-	__shared__ T sc[kVfdTile * D], su[kVfdTile * D], sv[kVfdTile];
+	constexpr bool kSplit = sizeof(T) < sizeof(double);     // two-float centres in FP32
+	__shared__ T sc[kVfdTile * D], su[kVfdTile * D], sv[kVfdTile], sl[kSplit ? kVfdTile * D : 1];
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	bool act = i < R.n;
-	T ci[D], ui[D], vi = 0;
+	T ci[D], cl[D], ui[D], vi = 0;
 	for (int d = 0; d < D; ++d) {
-		ci[d] = act ? (T) R.cen[d * (long) R.n + i] : (T) 0;
+		double c = act ? R.cen[d * (long) R.n + i] : 0.0;
+		ci[d] = (T) c;
+		cl[d] = kSplit ? (T) (c - (double) ci[d]) : (T) 0;
 		ui[d] = act ? (T) R.dir[d * (long) R.n + i] : (T) 0;
 	}
 	if (act) vi = (T) R.vol[i];
@@ -99,29 +106,43 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 			__syncthreads();
 			for (int t = threadIdx.x; t < nt; t += blockDim.x) {
 				for (int d = 0; d < D; ++d) {
-					sc[t * D + d] = (T) S.cen[d * (long) S.n + j0 + t];
+					double c = S.cen[d * (long) S.n + j0 + t];
+					sc[t * D + d] = (T) c;
+					if (kSplit) sl[t * D + d] = (T) (c - (double) sc[t * D + d]);
 					su[t * D + d] = (T) S.dir[d * (long) S.n + j0 + t];
 				}
 				sv[t] = (T) S.vol[j0 + t];
 			}
 			__syncthreads();
 			if (!act) continue;
-			T tile = 0, tgc[D], tgt[D];
+			T tile = 0, comp = 0, tgc[D], tgt[D];
 			for (int d = 0; d < D; ++d) { tgc[d] = 0; tgt[d] = 0; }
 			for (int jj = 0; jj < nt; ++jj) {
-				T d2 = (ci[0] - sc[jj * D]) * (ci[0] - sc[jj * D]);
-				for (int d = 1; d < D; ++d) d2 = d2 + (ci[d] - sc[jj * D + d]) * (ci[d] - sc[jj * D + d]);
+				T df[D];
+				for (int d = 0; d < D; ++d) {
+					df[d] = ci[d] - sc[jj * D + d];
+					if (kSplit) df[d] = df[d] + (cl[d] - sl[jj * D + d]);
+				}
+				T d2 = df[0] * df[0];
+				for (int d = 1; d < D; ++d) d2 = d2 + df[d] * df[d];
 				T ang = ui[0] * su[jj * D];
 				for (int d = 1; d < D; ++d) ang = ang + ui[d] * su[jj * D + d];
 				T d1c, d1d;
 				T kc = cen_knl<T>(ck, cwT, d2, d1c);
 				T kd = dir_knl<T>(dk, dwT, ang, d1d);
 				T vj = sv[jj];
-				tile += coef * kc * kd * vi * vj;
+				const T term = coef * kc * kd * vi * vj;
+				if (kSplit) {                  // Kahan: the FP32 tile sum keeps its lost low bits
+					T y = term - comp, t = tile + y;
+					comp = (t - tile) - y;
+					tile = t;
+				} else {
+					tile += term;
+				}
 				if (grad) {
 					// geometricFunction/grassmanFunction gradients and dqVfd_DD_DT accumulation
 					for (int d = 0; d < D; ++d) {
-						T dK = d1c * (ci[d] - sc[jj * D + d]);
+						T dK = d1c * df[d];
 						T tK = d1d / nLen * (-ang * ui[d] + su[jj * D + d]);
 						tgc[d] += gco * dK * kd * vi * vj;
 						tgt[d] += gco * kc * (tK * vi + kd * half * ui[d]) * vj;
