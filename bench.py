@@ -156,6 +156,74 @@ def cpu_sample(spec_full, seconds: float = 25.0, max_steps: int = 3):
     return steps / t_total, cores, f"first {steps} time step(s) of the same shell workload, {t_total:.1f} s"
 
 
+SERVED = ("Poisson stream of forward solves: 3D layered shells, icosphere level 3-5 x 4/8/12 prism layers "
+          "(3210-133146 nodes), 20-60 steps each, random bump centre, Lame (lambda, mu=lambda/2) log-uniform in "
+          "[0.5, 10] and diffusivity log-uniform in [0.005, 0.1] per material layer, Matern-3/2 varifold objective; "
+          "the same stream served in FP64 and in mixed precision")
+
+
+def served_requests(n: int, seed: int = 7, mean_gap_s: float = 0.04):
+    """Seeded request stream (specs + Poisson inter-arrival gaps); meshes are shared between requests."""
+    import numpy as np
+    from shape_atrophy_gb300 import problems
+    rng = np.random.default_rng(seed)
+    cache, out = {}, []
+    for _ in range(n):
+        level = int(rng.choice([3, 4, 5], p=[0.4, 0.4, 0.2]))
+        layers = int(rng.choice([4, 8, 12]))
+        steps = int(rng.integers(20, 61))
+        key = (level, layers)
+        if key not in cache:
+            cache[key] = problems.shell_layered(level=level, lyrCntNum=layers + 1, steps=steps)
+        sp = dict(cache[key])
+        sp["timeNum"] = steps + 1
+        lam = 10.0 ** rng.uniform(np.log10(0.5), 1.0, 3)
+        sp["modVec"] = np.column_stack([lam, lam / 2]).reshape(-1)
+        sp["spdLyrVec"] = 10.0 ** rng.uniform(np.log10(0.005), np.log10(0.1), 3)
+        c = rng.normal(size=3)
+        c /= np.linalg.norm(c)
+        sp["tauVarVec"] = np.array([c[0], c[1], c[2], 1.0, 0.15])
+        out.append((sp, float(rng.exponential(mean_gap_s))))
+    return out
+
+
+def served_leg(device: int, n: int = 32):
+    """The same Poisson stream through the continuous-batching server in FP64 and in mixed precision."""
+    import numpy as np
+    from shape_atrophy_gb300 import api
+    reqs = served_requests(n)
+    runs = {}
+    for prec in ("fp64", "mixed"):
+        sv = api.Server(hbm_budget=200e9, max_instances=64, device=device)
+        t0 = time.perf_counter()
+        t_next, ids = t0, []
+        for sp, gap in reqs:
+            t_next += gap
+            now = time.perf_counter()
+            if t_next > now:
+                time.sleep(t_next - now)
+            ids.append(sv.submit(sp, precision=prec))
+        res = [sv.result(i) for i in ids]
+        wall = time.perf_counter() - t0
+        st = sv.stats()
+        sv.close()
+        lat = np.array([r["latency_ms"] for r in res])
+        runs[prec] = dict(res=res, line={
+            "solves_per_s": len(res) / wall, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "wall_s": wall,
+            "steps_per_s": sum(sp["timeNum"] - 1 for sp, _ in reqs) / wall,
+            "ok": int(sum(r["info"]["status"] == 0 for r in res)), "peak_device_gb": st["peakBytes"] / 1e9,
+            "ticks": st["ticks"]})
+    ep = eo = 0.0
+    for a, b in zip(runs["mixed"]["res"], runs["fp64"]["res"]):
+        ep = max(ep, float(np.abs(a["lmk"] - b["lmk"]).max() / np.abs(b["lmk"]).max()))
+        eo = max(eo, abs(a["obj"] - b["obj"]) / abs(b["obj"]))
+    return {"workload": SERVED, "requests": n, "mean_gap_ms": 40.0, "fp64": runs["fp64"]["line"],
+            "mixed": runs["mixed"]["line"],
+            "mixed_over_fp64_solves": runs["mixed"]["line"]["solves_per_s"] / runs["fp64"]["line"]["solves_per_s"],
+            "mixed_vs_fp64_max_rel_err": {"positions": ep, "objective": eo}}
+
+
 def run_reference(args, rank, ws, dist):
     """CPU restatement of the model on the host cores (the reference has no CPU path of its own)."""
     if rank != 0:
@@ -182,6 +250,8 @@ def main():
     ap.add_argument("--cg-kernel", default="auto", choices=["auto", "persistent", "two-kernel"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
+    ap.add_argument("--served-requests", type=int, default=32)
     args = ap.parse_args()
     rank, local, ws, dist = dist_init()
     if args.impl == "reference":
@@ -259,6 +329,10 @@ def main():
                "what": f"one sa_forward call ({K} steps + objective) with host buffers: mesh upload and set-up, "
                        "solve, trajectory download"}
 
+    served = None
+    if not args.no_served and rank == 0 and args.workload == "shell":
+        served = served_leg(local, args.served_requests)
+
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:
         v, cores, sample = cpu_sample(spec_for(args, 4))
@@ -273,7 +347,7 @@ def main():
                            "elements": spec["elmObj"]["elmVtxMat"].shape[1], "cg_iters_per_step": cg_iters / K,
                            "l2": "per-step working set (~0.3 GB) larger than the 129 MB L2",
                            "parallelism": f"replicas x{ws}"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "served": served, "clocks": clocks,
                 "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     if dist is not None:
