@@ -343,9 +343,12 @@ __device__ __forceinline__ void block_sum_any(double (&v)[K], double *sm)
 // sum of K values over all threads of the nctas CTAs of one solve (fixed
 // order) plus a barrier among them; lc is the CTA's index within the solve.
 // Every thread returns the sums in v.  false: the wait gave up.
-template <int K>
+// post(sums) runs in thread 0 before the sums are broadcast (scalar work once per CTA, not per thread).
+struct NoPost { __device__ void operator()(const double *) const {} };
+
+template <int K, typename Post = NoPost>
 __device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int lc, int nctas, GridBar *bar,
-                                            unsigned int &target, double *sm)
+                                            unsigned int &target, double *sm, Post post = Post())
 {
 	__shared__ int okS;
 	__shared__ double tot[K];
@@ -375,10 +378,39 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int lc
 			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
 			if (lane == 0) tot[k] = s;
 		}
+		if (lane == 0) post(tot);
 	}
 	__syncthreads();
 	for (int k = 0; k < K; ++k) v[k] = tot[k];
 	return true;
+}
+
+// Chronopoulos-Gear step lengths from delta = (w, u) (thread 0 of each CTA; the same in every CTA)
+__device__ __forceinline__ void cg_step_lengths(double delta, double gam, double gamPrev, double alphaPrev,
+                                                bool first, double *out)
+{
+	double alpha, beta;
+	if (first) { beta = 0.0; alpha = gam / delta; }
+	else {
+		beta = gam / gamPrev;
+		alpha = gam / (delta - beta * gam / alphaPrev);
+	}
+	out[0] = alpha;
+	out[1] = beta;
+}
+
+// a row's contribution to a dot product: FP64 operands fold each product into the FP64 sum; FP32
+// operands form the row's (at most 3-term) FP32 sum first and add it to the FP64 sum once
+template <int B, typename TV>
+__device__ __forceinline__ void dot_row(double &acc, const TV (&a)[B], const TV (&b)[B])
+{
+	if (sizeof(TV) == sizeof(double)) {
+		for (int c = 0; c < B; ++c) acc += (double) a[c] * (double) b[c];
+	} else {
+		TV s = a[0] * b[0];
+		for (int c = 1; c < B; ++c) s += a[c] * b[c];
+		acc += (double) s;
+	}
 }
 
 template <int B, typename TM, typename TV>
@@ -400,6 +432,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
              double *part, CgScal *sc, GridBar *bar)
 {
 	__shared__ double sm[2 * 32];                 // block_sum_any scratch (K <= 2, at most 32 warps)
+	__shared__ double ab[2];                      // alpha, beta of the iteration
 	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
 	const int nctas = gridDim.x;
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
@@ -436,21 +469,15 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 		if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
 		TV wv[B];
 		double d1[1] = {0.0};
-		for (int c = 0; c < B; ++c) {
-			wv[c] = acc0[c] + acc1[c];
-			if (own) d1[0] += (double) wv[c] * (double) uv[c];
-		}
-		if (!grid_reduce<1>(d1, part, blockIdx.x, nctas, bar, target, sm)) {
+		for (int c = 0; c < B; ++c) wv[c] = acc0[c] + acc1[c];
+		if (own) dot_row<B, TV>(d1[0], wv, uv);
+		if (!grid_reduce<1>(d1, part, blockIdx.x, nctas, bar, target, sm, [&](const double *t) {
+			    cg_step_lengths(t[0], gam, gamPrev, alphaPrev, first, ab);
+		    })) {
 			code = SA_ERR_TIMEOUT;
 			break;
 		}
-		const double delta = d1[0];
-		double alpha, beta;
-		if (first) { beta = 0.0; alpha = gam / delta; }
-		else {
-			beta = gam / gamPrev;
-			alpha = gam / (delta - beta * gam / alphaPrev);
-		}
+		const double delta = d1[0], alpha = ab[0], beta = ab[1];
 		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
 			code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
 			break;
@@ -466,9 +493,9 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 				rv[c] = rv[c] - al * sv[c];
 				uv[c] = dv[c] * rv[c];
 				u[(long) i * B + c] = uv[c];
-				d2[0] += (double) rv[c] * (double) uv[c];
-				d2[1] += (double) rv[c] * (double) rv[c];
 			}
+			dot_row<B, TV>(d2[0], rv, uv);
+			dot_row<B, TV>(d2[1], rv, rv);
 		}
 		if (!grid_reduce<2>(d2, part + nctas, blockIdx.x, nctas, bar, target, sm)) {
 			code = SA_ERR_TIMEOUT;
@@ -509,6 +536,7 @@ template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const CgJob *__restrict__ jobs, int njobs)
 {
 	__shared__ double sm[2 * 32];
+	__shared__ double ab[2];                      // alpha, beta of the iteration
 	__shared__ int jS;
 	if (threadIdx.x == 0) {                      // last job with cta0 <= blockIdx.x
 		int lo = 0, hi = njobs - 1;
@@ -555,21 +583,23 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 				spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), acc1);
 			}
 			if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
-			if (i < A.N)
+			if (i < A.N) {
+				TV o[B], ui[B];
 				for (int c = 0; c < B; ++c) {
-					TV o = acc0[c] + acc1[c];
-					w[(long) i * B + c] = o;
-					d1[0] += (double) o * (double) __ldcg(u + (long) i * B + c);
+					o[c] = acc0[c] + acc1[c];
+					w[(long) i * B + c] = o[c];
+					ui[c] = __ldcg(u + (long) i * B + c);
 				}
+				dot_row<B, TV>(d1[0], o, ui);
+			}
 		}
-		if (!grid_reduce<1>(d1, part, lc, nctas, bar, target, sm)) { code = SA_ERR_TIMEOUT; break; }
-		const double delta = d1[0];
-		double alpha, beta;
-		if (first) { beta = 0.0; alpha = gam / delta; }
-		else {
-			beta = gam / gamPrev;
-			alpha = gam / (delta - beta * gam / alphaPrev);
+		if (!grid_reduce<1>(d1, part, lc, nctas, bar, target, sm, [&](const double *t) {
+			    cg_step_lengths(t[0], gam, gamPrev, alphaPrev, first, ab);
+		    })) {
+			code = SA_ERR_TIMEOUT;
+			break;
 		}
+		const double delta = d1[0], alpha = ab[0], beta = ab[1];
 		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
 			code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
 			break;
@@ -579,19 +609,20 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 		for (int sl = wj; sl < nsl; sl += WJ) {
 			const int i = sl * 32 + lane;
 			if (i >= A.N) continue;
+			TV rk[B], uk[B];
 			for (int c = 0; c < B; ++c) {
 				const long k = (long) i * B + c;
 				TV pk = __ldcg(u + k) + be * p[k];
 				TV sk = w[k] + be * sv[k];
 				p[k] = pk; sv[k] = sk;
 				x[k] = x[k] + (TX) al * (TX) pk;
-				TV rk = r[k] - al * sk;
-				r[k] = rk;
-				TV uk = dinv[k] * rk;
-				u[k] = uk;
-				d2[0] += (double) rk * (double) uk;
-				d2[1] += (double) rk * (double) rk;
+				rk[c] = r[k] - al * sk;
+				r[k] = rk[c];
+				uk[c] = dinv[k] * rk[c];
+				u[k] = uk[c];
 			}
+			dot_row<B, TV>(d2[0], rk, uk);
+			dot_row<B, TV>(d2[1], rk, rk);
 		}
 		if (!grid_reduce<2>(d2, part + nctas, lc, nctas, bar, target, sm)) { code = SA_ERR_TIMEOUT; break; }
 		gamPrev = gam;
