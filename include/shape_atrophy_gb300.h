@@ -240,6 +240,13 @@ int sa_server_result(sa_server *sv, long long requestId, double *lmkMat, double 
 int sa_server_stats(sa_server *sv, sa_server_counters *stats);
 int sa_server_destroy(sa_server *sv);
 
+/* Self-test of the bounded device-side waits (no reference counterpart).
+ * Launches two cooperative CTAs on a grid barrier whose arrival count can
+ * never reach its target; each CTA must give up after the 1 s limit the CG
+ * kernels use, set the abort flag and return, leaving the context usable.
+ * *ctasGaveUp = CTAs that gave up (2 when the mechanism works). */
+int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs);
+
 /* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and
  * deformation_3D_frame (dim 3): arguments in prhs order
  * (CUDA/2D_frame/deformation.cu:24-50), outputs plhs[0..2]

@@ -641,6 +641,52 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 }
 
 // ---------------------------------------------------------------------------
+// Self-test of the bounded grid wait: a cooperative launch whose barrier
+// count starts 2^31 away from its target, so the arrivals never reach it (a
+// flag that nothing sets).  Every CTA must give up after kBarWaitNs and report it;
+// no fault, no hang, the context stays usable.
+// ---------------------------------------------------------------------------
+__global__ void k_barrier_probe(double *part, GridBar *bar, int *gaveUp)
+{
+	__shared__ double sm[2 * 32];
+	unsigned int target = 0;
+	double v[1] = {1.0};
+	bool ok = grid_reduce<1>(v, part, blockIdx.x, gridDim.x, bar, target, sm);
+	if (threadIdx.x == 0 && !ok) atomicAdd(gaveUp, 1);
+}
+
+int barrier_selftest(cudaStream_t s, int *ctasGaveUp, int *abortFlag)
+{
+	const int nctas = 2, nt = 64;
+	int per = 0;
+	SA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_barrier_probe, nt, 0));
+	if (per < 1) return SA_ERR_UNSUPPORTED;
+	char *mem = nullptr;
+	SA_CHECK(cudaMalloc(&mem, kGridBarBytes + 256));
+	GridBar *bar = (GridBar *) mem;
+	double *part = (double *) (mem + kGridBarBytes);
+	int *gave = (int *) (mem + kGridBarBytes + 128);
+	GridBar h{};
+	// count - target stays in [2^31, 2^32) for every number of arrivals, i.e. "not yet" as a signed
+	// difference: the wait can only end by its time limit
+	h.count = 0x80000000u + (unsigned int) nctas;
+	SA_CHECK(cudaMemcpyAsync(bar, &h, sizeof(GridBar), cudaMemcpyHostToDevice, s));
+	SA_CHECK(cudaMemsetAsync(gave, 0, sizeof(int), s));
+	void *args[] = {(void *) &part, (void *) &bar, (void *) &gave};
+	cudaError_t e = cudaLaunchCooperativeKernel((const void *) k_barrier_probe, dim3(nctas), dim3(nt), args, 0, s);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+	GridBar out{};
+	int g = 0;
+	if (e == cudaSuccess) e = cudaMemcpy(&out, bar, sizeof(GridBar), cudaMemcpyDeviceToHost);
+	if (e == cudaSuccess) e = cudaMemcpy(&g, gave, sizeof(int), cudaMemcpyDeviceToHost);
+	cudaFree(mem);
+	SA_CHECK(e);
+	*ctasGaveUp = g;
+	*abortFlag = (int) out.abort;
+	return SA_OK;
+}
+
+// ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
 // CTAs of the vector kernels: kVecCtasPerSm per SM, fewer for short vectors

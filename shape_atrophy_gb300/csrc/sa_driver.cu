@@ -1631,4 +1631,20 @@ int sa_server_destroy(sa_server *sv)
 	return SA_OK;
 }
 
+
+int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs)
+{
+	if (!ctasGaveUp) return SA_ERR_ARG;
+	return sa::guarded(ctx, [&]() {
+		int gave = 0, abortFlag = 0;
+		auto t0 = std::chrono::steady_clock::now();
+		int rc = sa::barrier_selftest(ctx->stream, &gave, &abortFlag);
+		if (elapsedMs) *elapsedMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+		*ctasGaveUp = gave;
+		if (rc != SA_OK) return rc;
+		SA_REQUIRE(abortFlag == 1, "the poisoned barrier did not record an abort");
+		return SA_OK;
+	});
+}
+
 }  // extern "C"

@@ -343,6 +343,8 @@ void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *dev
 template <int B> void cg_finish_fp64(const Mesh &m, double *x, CgWork &w, cudaStream_t s);
 // host copy of the scalars (synchronises s)
 CgState cg_state(const CgWork &w, cudaStream_t s);
+// bounded grid wait self-test: CTAs that gave up, and the abort flag they left
+int barrier_selftest(cudaStream_t s, int *ctasGaveUp, int *abortFlag);
 
 // frame mode K-preconditioned CG (2D/ipcg.cu:11-100) with dense K
 struct KpcgWork {
