@@ -174,7 +174,7 @@ def served_requests(n: int, seed: int = 7, mean_gap_s: float = 0.04):
         steps = int(rng.integers(20, 61))
         key = (level, layers)
         if key not in cache:
-            cache[key] = problems.shell_layered(level=level, lyrCntNum=layers + 1, steps=steps)
+            cache[key] = problems.shell_layered(level=level, lyrCntNum=layers + 1, steps=steps, native=True)
         sp = dict(cache[key])
         sp["timeNum"] = steps + 1
         lam = 10.0 ** rng.uniform(np.log10(0.5), 1.0, 3)

@@ -240,6 +240,28 @@ int sa_server_result(sa_server *sv, long long requestId, double *lmkMat, double 
 int sa_server_stats(sa_server *sv, sa_server_counters *stats);
 int sa_server_destroy(sa_server *sv);
 
+/* Element-object builders (host code, no device needed): the arrays of
+ * CUDA/generateElementObject2D.m, CUDA/generateElementObject3D.m and
+ * CUDA/tri2tetra.m, bit for bit (same orders: column-major find lists,
+ * sortrows pattern, femIfoMat element lists ascending), built in
+ * O(E log E) instead of the MATLAB find-per-node loops.  The object owns its
+ * arrays; sa_elmobj_view fills an sa_element_object that points into them
+ * (valid until sa_elmobj_free) and can be passed to every entry point.
+ * vfdIfoMat (the varifold gradient gather table) is included.  tri2tetra:
+ * triVtxMat T x 3 -> tetVtxMat E x 4, nmlVtxMat E x 6, tsvVtxMat E x 6,
+ * E = 3 T (lyrCntNum - 1), arrays allocated by the caller.  2D: periodic != 0
+ * closes every node layer into a ring (annulus). */
+typedef struct sa_elmobj sa_elmobj;
+int sa_tri2tetra(const int *triVtxMat, int triNum, int lyrCntNum, int *tetVtxMat, int *nmlVtxMat, int *tsvVtxMat);
+int sa_build_element_object_3d(const int *tetVtxMat, int elmNum, const int *btmVtxMat, int btmElmNum,
+                               const int *nmlVtxMat, const int *tsvVtxMat, const int *vfdLyrVec, int vfdLyrNum,
+                               sa_elmobj **out);
+int sa_build_element_object_2d(int lyrLmkNum, int lyrCntNum, const int *vfdLyrVec, int vfdLyrNum, int periodic,
+                               sa_elmobj **out);
+int sa_elmobj_view(const sa_elmobj *obj, sa_element_object *view);
+int sa_elmobj_layers(const sa_elmobj *obj, int *lyrLmkNum, int *lyrCntNum, int *elmPerLayer);
+int sa_elmobj_free(sa_elmobj *obj);
+
 /* Self-test of the bounded device-side waits (no reference counterpart).
  * Launches two cooperative CTAs on a grid barrier whose arrival count can
  * never reach its target; each CTA must give up after the 1 s limit the CG

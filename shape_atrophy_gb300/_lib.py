@@ -102,6 +102,12 @@ def load():
     lib.sa_session_info.argtypes = [vp, C.POINTER(SolveInfo)]
     lib.sa_session_profile.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]
     lib.sa_session_destroy.argtypes = [vp]
+    lib.sa_tri2tetra.argtypes = [_ip, C.c_int, C.c_int, _ip, _ip, _ip]
+    lib.sa_build_element_object_3d.argtypes = [_ip, C.c_int, _ip, C.c_int, _ip, _ip, _ip, C.c_int, C.POINTER(vp)]
+    lib.sa_build_element_object_2d.argtypes = [C.c_int, C.c_int, _ip, C.c_int, C.c_int, C.POINTER(vp)]
+    lib.sa_elmobj_view.argtypes = [vp, C.POINTER(ElementObject)]
+    lib.sa_elmobj_layers.argtypes = [vp, _ip, _ip, _ip]
+    lib.sa_elmobj_free.argtypes = [vp]
     lib.sa_server_create.argtypes = [vp, C.c_double, C.c_int, C.POINTER(vp)]
     lib.sa_server_submit.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Params), C.POINTER(Target), _dp,
                                      C.c_int, C.POINTER(C.c_longlong)]

@@ -364,3 +364,78 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# --------------------------------------------------------------------------
+# native element-object builders (host code of the C library)
+# --------------------------------------------------------------------------
+def _i32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+
+
+def _elmobj_dict(h, lib, dim: int) -> dict:
+    """Copy a built sa_elmobj into the dict layout of mesh.generate_element_object_2d/3d."""
+    v = _lib.ElementObject()
+    lib.sa_elmobj_view(h, C.byref(v))
+    N, E = v.lmkNum, v.elmNum
+
+    def arr(ptr, rows, cols):
+        return np.ctypeslib.as_array(ptr, shape=(rows, cols)).copy()
+
+    fcols = 4 if dim == 2 else 6
+    obj = {"elmVtxMat": arr(v.elmVtxMat, dim + 1, E), "vtxElmMat": arr(v.vtxElmMat, v.vtxElmCols, N),
+           ("tanVtxMat" if dim == 2 else "nmlVtxMat"): arr(v.frmVtxMat, fcols, E),
+           "tsvVtxMat": arr(v.tsvVtxMat, fcols, E), "bdrVtxMat": arr(v.bdrVtxMat, dim, v.bdrElmNum),
+           "vtxBdrMat": arr(v.vtxBdrMat, v.vtxBdrCols, N), "btmVtxMat": arr(v.btmVtxMat, dim, v.btmElmNum),
+           "vtxBtmMat": arr(v.vtxBtmMat, v.vtxBtmCols, v.btmLmkNum), "femVtxMat": arr(v.femVtxMat, 2, v.nzrNum),
+           "femIfoMat": arr(v.femIfoMat, v.femIfoCols, v.nzrNum), "vfdVtxMat": arr(v.vfdVtxMat, dim, v.vfdElmNum),
+           "vfdIfoMat": arr(v.vfdIfoMat, v.vfdIfoCols, N), "dim": dim}
+    L, Cn, per = C.c_int(), C.c_int(), C.c_int()
+    lib.sa_elmobj_layers(h, C.byref(L), C.byref(Cn), C.byref(per))
+    obj["lyrLmkNum"], obj["lyrCntNum"], obj["elmPerLayer"] = L.value, Cn.value, per.value
+    return obj
+
+
+def tri2tetra(triVtxMat, lyrCntNum: int):
+    """tri2tetra.m in the C library: (3, T) triangles -> tet (4, E), nml (6, E), tsv (6, E)."""
+    lib = _lib.load()
+    tri = _i32(triVtxMat)
+    T = tri.shape[1]
+    E = 3 * T * (int(lyrCntNum) - 1)
+    tet, nml, tsv = np.zeros((4, E), np.int32), np.zeros((6, E), np.int32), np.zeros((6, E), np.int32)
+    rc = lib.sa_tri2tetra(tri.ctypes.data_as(_lib._ip), T, int(lyrCntNum), tet.ctypes.data_as(_lib._ip),
+                          nml.ctypes.data_as(_lib._ip), tsv.ctypes.data_as(_lib._ip))
+    if rc != _lib.SA_OK:
+        raise ValueError(f"sa_tri2tetra failed (code {rc})")
+    return tet, nml, tsv
+
+
+def build_element_object_3d(tetVtxMat, btmVtxMat, nmlVtxMat, tsvVtxMat, vfdLyrVec) -> dict:
+    """generateElementObject3D.m in the C library (same arrays as mesh.generate_element_object_3d)."""
+    lib = _lib.load()
+    tet, btm, nml, tsv, vl = (_i32(a) for a in (tetVtxMat, btmVtxMat, nmlVtxMat, tsvVtxMat, vfdLyrVec))
+    h = C.c_void_p()
+    rc = lib.sa_build_element_object_3d(tet.ctypes.data_as(_lib._ip), tet.shape[1], btm.ctypes.data_as(_lib._ip),
+                                        btm.shape[1], nml.ctypes.data_as(_lib._ip), tsv.ctypes.data_as(_lib._ip),
+                                        vl.ctypes.data_as(_lib._ip), vl.size, C.byref(h))
+    if rc != _lib.SA_OK:
+        raise ValueError(f"sa_build_element_object_3d failed (code {rc})")
+    try:
+        return _elmobj_dict(h, lib, 3)
+    finally:
+        lib.sa_elmobj_free(h)
+
+
+def build_element_object_2d(lyrLmkNum: int, lyrCntNum: int, vfdLyrVec, periodic: bool = False) -> dict:
+    """generateElementObject2D.m in the C library (same arrays as mesh.generate_element_object_2d)."""
+    lib = _lib.load()
+    vl = _i32(vfdLyrVec)
+    h = C.c_void_p()
+    rc = lib.sa_build_element_object_2d(int(lyrLmkNum), int(lyrCntNum), vl.ctypes.data_as(_lib._ip), vl.size,
+                                        int(bool(periodic)), C.byref(h))
+    if rc != _lib.SA_OK:
+        raise ValueError(f"sa_build_element_object_2d failed (code {rc})")
+    try:
+        return _elmobj_dict(h, lib, 2)
+    finally:
+        lib.sa_elmobj_free(h)

@@ -323,12 +323,19 @@ def shell_nodes(surf: np.ndarray, lyrCntNum: int, r0: float, r1: float) -> np.nd
     return np.concatenate([surf * rk for rk in r], axis=1)
 
 
-def shell_element_object(level: int, lyrCntNum: int, vfdLyrVec=None):
-    """Icosphere-level shell: (nodes (3, N), elmObj) with bottom = inner surface."""
+def shell_element_object(level: int, lyrCntNum: int, vfdLyrVec=None, native: bool = False):
+    """Icosphere-level shell: (nodes (3, N), elmObj) with bottom = inner surface.
+
+    native=True builds tri2tetra and the element object with the C library's
+    builders (the same arrays, bit for bit, much faster for large meshes)."""
     surf, tri = icosphere(level)
-    tet, nml, tsv = tri2tetra(tri, lyrCntNum)
     if vfdLyrVec is None:
         vfdLyrVec = [lyrCntNum]
+    if native:
+        from . import api
+        tet, nml, tsv = api.tri2tetra(tri, lyrCntNum)
+        return surf, tri, tet, nml, tsv, api.build_element_object_3d(tet, tri, nml, tsv, vfdLyrVec)
+    tet, nml, tsv = tri2tetra(tri, lyrCntNum)
     return surf, tri, tet, nml, tsv, generate_element_object_3d(tet, tri, nml, tsv, vfdLyrVec)
 
 

@@ -101,9 +101,10 @@ def annulus_layered(angNum: int = 256, radNum: int = 16, steps: int = 50, timeSt
 
 def shell_layered(level: int = 5, lyrCntNum: int = 9, steps: int = 100, timeStp: float = 0.01,
                   cgTolVal: float = 1e-8, btmWgt: float = 10.0, target_seed: int = 2,
-                  material_of_prism=None) -> dict:
-    """Layered 3D shell, radii 0.7-1.0; default = icosphere 5 x 8 prism layers."""
-    surf, tri, tet, nml, tsv, obj = mesh.shell_element_object(level, lyrCntNum)
+                  material_of_prism=None, native: bool = False) -> dict:
+    """Layered 3D shell, radii 0.7-1.0; default = icosphere 5 x 8 prism layers.
+    native=True builds the element object with the C library (identical arrays)."""
+    surf, tri, tet, nml, tsv, obj = mesh.shell_element_object(level, lyrCntNum, native=native)
     lmk = mesh.shell_nodes(surf, lyrCntNum, 0.7, 1.0)
     E = obj["elmVtxMat"].shape[1]
     nl = lyrCntNum - 1
