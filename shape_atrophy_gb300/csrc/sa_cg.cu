@@ -519,126 +519,6 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 }
 
 // ---------------------------------------------------------------------------
-// Pipelined persistent CG (Ghysels & Vanroose's preconditioned pipelined CG)
-// for the FP32 inner solves of mixed precision: ONE grid reduction per
-// iteration.  The recurrences carry w = A u, z = A q and q = D^-1 s, so the
-// iteration's only matvec n = A m (m = D^-1 w) does not wait for the step
-// lengths: the reduction of (r, u), (w, u), (r, r) is also the barrier that
-// makes m visible, and the matvec follows it directly.  m is double
-// buffered (the iteration writes m_{i+1} while other CTAs may still gather
-// m_i), and so are the partial sums.  Eight vectors per row stay in
-// registers.  FP32 only: the refinement loop around it recomputes the true
-// residual in FP64, so the recurrences' drift is corrected there.
-// ---------------------------------------------------------------------------
-template <int B, typename TM, typename TV, typename TX>
-__global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
-k_cg_persist_pipe(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, TX *x, const TV *r0,
-                  const TV *u0, TV *m0, TV *m1, double *part, CgScal *sc, GridBar *bar)
-{
-	__shared__ double sm[3 * 32];
-	__shared__ double ab[2];
-	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
-	const int nctas = gridDim.x;
-	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-	const int sl = blockIdx.x * (blockDim.x >> 5) + wp;
-	const int nsl = (A.N + 31) >> 5;
-	const int i = sl * 32 + lane;
-	const bool own = sl < nsl && i < A.N;
-	const int wdt = sl < nsl ? __ldg(A.width + sl) : 0;
-	const long base = sl < nsl ? __ldg(A.off + sl) + lane : 0;
-	const double bb = sc->bb, tolSqu = sc->tolSqu;
-	const int itrMax = sc->itrMax;
-	double gam = 0.0, rr = sc->rr, gamPrev = 0.0, alphaPrev = 1.0;
-	unsigned int target = 0;
-	TX xv[B];
-	TV rv[B], uv[B], wv[B], pv[B], sv[B], qv[B], zv[B], dv[B];
-	for (int c = 0; c < B; ++c) {
-		xv[c] = (TX) 0; rv[c] = uv[c] = wv[c] = pv[c] = sv[c] = qv[c] = zv[c] = dv[c] = (TV) 0;
-		if (own) {
-			long k = (long) i * B + c;
-			xv[c] = x[k]; rv[c] = r0[k]; uv[c] = u0[k]; dv[c] = dinv[k];
-		}
-	}
-	// w_0 = A u_0 (u_0 written by k_cg_init before this launch), m_0 = D^-1 w_0
-	{
-		TV acc0[B], acc1[B];
-		for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
-		int k = 0;
-		for (; k + 2 <= wdt; k += 2) {
-			spmv_slot_cg<B, TM, TV>(A, blk, u0, base + ((long) k << 5), acc0);
-			spmv_slot_cg<B, TM, TV>(A, blk, u0, base + ((long) (k + 1) << 5), acc1);
-		}
-		if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u0, base + ((long) k << 5), acc0);
-		for (int c = 0; c < B; ++c) {
-			wv[c] = acc0[c] + acc1[c];
-			if (own) m0[(long) i * B + c] = dv[c] * wv[c];
-		}
-	}
-	int it = 0, code = SA_OK;
-	bool first = true;
-	for (;;) {
-		TV *mc = (it & 1) ? m1 : m0, *mn = (it & 1) ? m0 : m1;      // m_i, m_{i+1}
-		double d3[3] = {0.0, 0.0, 0.0};
-		if (own) {
-			dot_row<B, TV>(d3[0], rv, uv);
-			dot_row<B, TV>(d3[1], wv, uv);
-			dot_row<B, TV>(d3[2], rv, rv);
-		}
-		double *pt = part + (it & 1) * 3 * nctas;
-		if (!grid_reduce<3>(d3, pt, blockIdx.x, nctas, bar, target, sm, [&](const double *t) {
-			    cg_step_lengths(t[1], t[0], gamPrev, alphaPrev, first, ab);
-		    })) {
-			code = SA_ERR_TIMEOUT;
-			break;
-		}
-		gam = d3[0];
-		rr = d3[2];
-		const double delta = d3[1], alpha = ab[0], beta = ab[1];
-		if (!isfinite(gam) || !isfinite(rr)) { code = SA_ERR_NONFINITE; break; }
-		if (rr < tolSqu * bb) { code = SA_OK; break; }
-		if (it >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
-		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
-			code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
-			break;
-		}
-		// n = A m_i (m_i of every row written before the reduction)
-		TV acc0[B], acc1[B];
-		for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
-		int k = 0;
-		for (; k + 2 <= wdt; k += 2) {
-			spmv_slot_cg<B, TM, TV>(A, blk, mc, base + ((long) k << 5), acc0);
-			spmv_slot_cg<B, TM, TV>(A, blk, mc, base + ((long) (k + 1) << 5), acc1);
-		}
-		if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, mc, base + ((long) k << 5), acc0);
-		if (own) {
-			const TV al = (TV) alpha, be = (TV) beta;
-			for (int c = 0; c < B; ++c) {
-				TV nv = acc0[c] + acc1[c];
-				TV mv = dv[c] * wv[c];
-				zv[c] = nv + be * zv[c];
-				qv[c] = mv + be * qv[c];
-				sv[c] = wv[c] + be * sv[c];
-				pv[c] = uv[c] + be * pv[c];
-				xv[c] = xv[c] + (TX) al * (TX) pv[c];
-				rv[c] = rv[c] - al * sv[c];
-				uv[c] = uv[c] - al * qv[c];
-				wv[c] = wv[c] - al * zv[c];
-				mn[(long) i * B + c] = dv[c] * wv[c];
-			}
-		}
-		gamPrev = gam;
-		alphaPrev = alpha;
-		first = false;
-		++it;
-	}
-	if (own)
-		for (int c = 0; c < B; ++c) x[(long) i * B + c] = xv[c];
-	if (blockIdx.x == 0 && threadIdx.x == 0) {
-		sc->iters = it; sc->code = code; sc->rr = rr; sc->gam = gam; sc->done = 1;
-	}
-}
-
-// ---------------------------------------------------------------------------
 // Batched persistent CG: one cooperative launch advances many independent
 // solves (the instances of a serving batch).  Job j owns the CTAs
 // [cta0, cta0 + nctas) of the launch; its warps stride over its slices, its
@@ -826,9 +706,8 @@ static void set_scal(CgScal *d, double tolSqu, int itrMax, double bb, cudaStream
 	SA_CHECK(cudaMemcpyAsync(d, &h, sizeof(CgScal), cudaMemcpyHostToDevice, s));
 }
 
-// CTAs of the persistent CG kernel (pipelined form when PIPE) with `warps` warps each that can be resident
-// at once (0: it cannot run)
-template <int B, typename TM, typename TV, typename TX, bool PIPE>
+// CTAs of k_cg_persist with `warps` warps each that can be resident at once (0: it cannot run)
+template <int B, typename TM, typename TV, typename TX>
 static int persist_capacity(int smCount, int warps)
 {
 	static int perSm[kPersistMaxWarps + 1] = {};
@@ -836,12 +715,8 @@ static int persist_capacity(int smCount, int warps)
 	if (warps < 1 || warps > kPersistMaxWarps) return 0;
 	if (!known[warps]) {
 		int v = 0;
-		cudaError_t e;
-		if constexpr (PIPE)
-			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist_pipe<B, TM, TV, TX>, 32 * warps, 0);
-		else
-			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist<B, TM, TV, TX>, 32 * warps, 0);
-		if (e != cudaSuccess) {
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist<B, TM, TV, TX>, 32 * warps, 0) !=
+		    cudaSuccess) {
 			cudaGetLastError();
 			v = 0;
 		}
@@ -876,30 +751,20 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	// persistent launch: one CTA per SM, one slice per warp
 	const int pw = std::max(1, std::min(kPersistMaxWarps, (m.nslice + prof->smCount - 1) / prof->smCount));
 	const int nctas = (m.nslice + pw - 1) / pw;
-	// FP32 solves (the inner solves of mixed precision) use the pipelined form: one grid reduction per
-	// iteration; FP64 solves the Chronopoulos-Gear form
-	constexpr bool kPipe = sizeof(TV) < sizeof(double);
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
-	                     nctas <= persist_capacity<B, TM, TV, TX, kPipe>(prof->smCount, pw);
+	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw);
 	if (persist) {
 		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first)
 		k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
 		GridBar *bar = (GridBar *) prof->bar;
 		SA_CHECK(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
 		SellOp A = sell_of(m);
-		const TV *r0 = r, *u0 = u;
-		TV *m0 = w, *m1 = p;                          // the pipelined form's double-buffered D^-1 w
+		const TV *r0 = r;
 		void *args[] = {&A, (void *) &blk, (void *) &dinv, (void *) &x, (void *) &r0, (void *) &u, (void *) &part,
 		                (void *) &sc, (void *) &bar};
-		void *argsPipe[] = {&A, (void *) &blk, (void *) &dinv, (void *) &x, (void *) &r0, (void *) &u0, (void *) &m0,
-		                    (void *) &m1, (void *) &part, (void *) &sc, (void *) &bar};
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
-		if constexpr (kPipe)
-			SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist_pipe<B, TM, TV, TX>, dim3(nctas),
-			                                     dim3(32 * pw), argsPipe, 0, s));
-		else
-			SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
-			                                     dim3(32 * pw), args, 0, s));
+		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
+		                                     dim3(32 * pw), args, 0, s));
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[1], s));
 		k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
 		prof->launches += 3;

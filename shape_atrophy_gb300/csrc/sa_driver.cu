@@ -350,10 +350,9 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	CgWork &c = w.cw;
 	c.r = P.alloc<double>(n); c.u = P.alloc<double>(n); c.w = P.alloc<double>(n);
 	c.p = P.alloc<double>(n); c.sv = P.alloc<double>(n);
-	// partial sums per CTA of the widest CG kernel grid (entries / 256, or one CTA per slice)
+	// partial sums: up to 3 per CTA of the widest CG kernel grid (entries / 256, or one CTA per slice)
 	int nbCg = std::max(grid_for(n, 256), std::max(m.nslice, nb));
-	// 3 values per CTA, double-buffered by the pipelined CG
-	c.part = P.alloc<double>((size_t) 6 * nbCg + 64); c.scal = P.zeros<double>(32); c.maxBlocks = nbCg;
+	c.part = P.alloc<double>((size_t) 3 * nbCg + 64); c.scal = P.zeros<double>(32); c.maxBlocks = nbCg;
 	c.bar = P.zeros<char>(kGridBarBytes);
 	c.cgKernel = md.cgKernel;
 	{
