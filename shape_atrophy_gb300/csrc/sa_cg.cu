@@ -61,6 +61,22 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *sm)
 		}
 }
 
+// u = M^-1 r for one row: point Jacobi (dv = D^-1 of the row) or, when bv is given, the row's B x B
+// block-Jacobi inverse (FP32 inner solves of mixed precision)
+template <int B, typename TV>
+__device__ __forceinline__ void apply_prec(const TV (&dv)[B], const TV *bv, const TV (&r)[B], TV (&u)[B])
+{
+	if (bv) {
+		for (int a = 0; a < B; ++a) {
+			TV t = bv[a * B] * r[0];
+			for (int c = 1; c < B; ++c) t += bv[a * B + c] * r[c];
+			u[a] = t;
+		}
+	} else {
+		for (int c = 0; c < B; ++c) u[c] = dv[c] * r[c];
+	}
+}
+
 // block partials part[k * nb + blockIdx.x]; returns true in the block that
 // arrives last (the one that finishes the reduction)
 template <int K, int NT>
@@ -251,6 +267,48 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_init(long n, const double *__re
 	}
 }
 
+// k_cg_init for the FP32 inner solves with the block-Jacobi preconditioner: one row (B entries) per
+// thread, r = b - q, u = Binv r, partials (b, b), (r, r), (r, u)
+template <int B>
+__global__ void __launch_bounds__(kCgBlock) k_cg_init_blk(int N, const double *__restrict__ b,
+                                                          const double *__restrict__ q,
+                                                          const float *__restrict__ binv, float *__restrict__ r,
+                                                          float *__restrict__ u, double *part, CgScal *sc)
+{
+	const int stride = gridDim.x * blockDim.x;
+	double v[3] = {0.0, 0.0, 0.0};
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+		float rt[B], ut[B], unused[B];
+		for (int c = 0; c < B; ++c) {
+			const long k = (long) i * B + c;
+			double rk = b[k] - q[k];
+			rt[c] = (float) rk;
+			r[k] = rt[c];
+			v[0] += b[k] * b[k];
+			v[1] += rk * rk;
+			unused[c] = 0.0f;
+		}
+		apply_prec<B, float>(unused, binv + (long) i * B * B, rt, ut);
+		for (int c = 0; c < B; ++c) {
+			u[(long) i * B + c] = ut[c];
+			v[2] += (double) rt[c] * (double) ut[c];
+		}
+	}
+	if (!reduce_partials<3, kCgBlock>(v, part, &sc->counter)) return;
+	double d[3];
+	finish_partials<3, kCgBlock>(d, part);
+	if (threadIdx.x == 0) {
+		if (sc->bb < 0.0) sc->bb = d[0];
+		sc->rr = d[1]; sc->gam = d[2];
+		sc->first = 1; sc->done = 0; sc->code = SA_OK;
+		if (!isfinite(d[0]) || !isfinite(d[1])) { sc->code = SA_ERR_NONFINITE; sc->done = 1; }
+		else if (sc->bb == 0.0) { sc->zero = 1; sc->done = 1; }
+		else if (d[1] < sc->tolSqu * sc->bb) sc->done = 1;
+		else if (sc->itrMax <= 0) { sc->code = SA_ERR_NOT_CONVERGED; sc->done = 1; }
+		sc->counter = 0;
+	}
+}
+
 template <typename TX>
 __global__ void k_cg_zero(long n, TX *x, const CgScal *sc)
 {
@@ -428,8 +486,8 @@ __device__ __forceinline__ void spmv_slot_cg(const SellOp &A, const TM *__restri
 
 template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
-k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, TX *x, const TV *r0, TV *u,
-             double *part, CgScal *sc, GridBar *bar)
+k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, const TV *__restrict__ binv, TX *x,
+             const TV *r0, TV *u, double *part, CgScal *sc, GridBar *bar)
 {
 	__shared__ double sm[2 * 32];                 // block_sum_any scratch (K <= 2, at most 32 warps)
 	__shared__ double ab[2];                      // alpha, beta of the iteration
@@ -447,7 +505,10 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	double gam = sc->gam, rr = sc->rr, gamPrev = 0.0, alphaPrev = 1.0;
 	unsigned int target = 0;                     // bar->count is zeroed before the launch
 	TX xv[B];
-	TV rv[B], uv[B], pv[B], sv[B], dv[B];
+	// block-Jacobi only for FP32 vectors (the mixed inner solves); FP64 keeps point Jacobi and its registers
+	constexpr int kBV = sizeof(TV) == sizeof(float) ? B * B : 1;
+	TV rv[B], uv[B], pv[B], sv[B], dv[B], bv[kBV];
+	const bool blockPrec = kBV > 1 && binv != nullptr;   // the same in every thread
 	for (int c = 0; c < B; ++c) {
 		xv[c] = (TX) 0; rv[c] = uv[c] = pv[c] = sv[c] = dv[c] = (TV) 0;
 		if (own) {
@@ -455,6 +516,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			xv[c] = x[k]; rv[c] = r0[k]; uv[c] = u[k]; dv[c] = dinv[k];
 		}
 	}
+	for (int t = 0; t < kBV; ++t) bv[t] = (own && blockPrec) ? binv[(long) i * B * B + t] : (TV) 0;
 	int it = 0, code = SA_OK;
 	bool first = true;
 	for (;;) {
@@ -491,9 +553,10 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 				sv[c] = wv[c] + be * sv[c];
 				xv[c] = xv[c] + (TX) al * (TX) pv[c];
 				rv[c] = rv[c] - al * sv[c];
-				uv[c] = dv[c] * rv[c];
-				u[(long) i * B + c] = uv[c];
 			}
+			if constexpr (kBV > 1) apply_prec<B, TV>(dv, blockPrec ? bv : nullptr, rv, uv);
+			else for (int c = 0; c < B; ++c) uv[c] = dv[c] * rv[c];
+			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uv[c];
 			dot_row<B, TV>(d2[0], rv, uv);
 			dot_row<B, TV>(d2[1], rv, rv);
 		}
@@ -556,6 +619,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 	const SellOp A = J.A;
 	const TM *blk = (const TM *) J.blk;
 	const TV *dinv = (const TV *) J.dinv;
+	const TV *binv = (const TV *) J.binv;
 	TX *x = (TX *) J.x;
 	TV *r = (TV *) J.r, *u = (TV *) J.u, *w = (TV *) J.w, *p = (TV *) J.p, *sv = (TV *) J.s;
 	GridBar *bar = (GridBar *) J.bar;
@@ -609,7 +673,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 		for (int sl = wj; sl < nsl; sl += WJ) {
 			const int i = sl * 32 + lane;
 			if (i >= A.N) continue;
-			TV rk[B], uk[B];
+			TV rk[B], uk[B], dk[B];
 			for (int c = 0; c < B; ++c) {
 				const long k = (long) i * B + c;
 				TV pk = __ldcg(u + k) + be * p[k];
@@ -618,9 +682,10 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 				x[k] = x[k] + (TX) al * (TX) pk;
 				rk[c] = r[k] - al * sk;
 				r[k] = rk[c];
-				uk[c] = dinv[k] * rk[c];
-				u[k] = uk[c];
+				dk[c] = dinv[k];
 			}
+			apply_prec<B, TV>(dk, binv ? binv + (long) i * B * B : nullptr, rk, uk);
+			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uk[c];
 			dot_row<B, TV>(d2[0], rk, uk);
 			dot_row<B, TV>(d2[1], rk, rk);
 		}
@@ -754,14 +819,22 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
 	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw);
 	if (persist) {
-		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first)
-		k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
+		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first).  FP32
+		// inner solves of mixed precision are block-Jacobi preconditioned (3x3 node blocks)
+		const TV *binv = nullptr;
+		if constexpr (sizeof(TV) == sizeof(float)) binv = prof->binv32;
+		if (binv) {
+			if constexpr (sizeof(TV) == sizeof(float))
+				k_cg_init_blk<B><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
+		} else {
+			k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
+		}
 		GridBar *bar = (GridBar *) prof->bar;
 		SA_CHECK(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
 		SellOp A = sell_of(m);
 		const TV *r0 = r;
-		void *args[] = {&A, (void *) &blk, (void *) &dinv, (void *) &x, (void *) &r0, (void *) &u, (void *) &part,
-		                (void *) &sc, (void *) &bar};
+		void *args[] = {&A, (void *) &blk, (void *) &dinv, (void *) &binv, (void *) &x, (void *) &r0, (void *) &u,
+		                (void *) &part, (void *) &sc, (void *) &bar};
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
 		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
 		                                     dim3(32 * pw), args, 0, s));
@@ -958,8 +1031,12 @@ void cg_mixed_inner(const Mesh &m, int itrMax, double innerTolSqu, CgWork &w, cu
 	SA_CHECK(cudaMemsetAsync(p32, 0, sizeof(float) * n, s));
 	SA_CHECK(cudaMemsetAsync(s32, 0, sizeof(float) * n, s));
 	set_scal((CgScal *) w.scal, innerTolSqu, itrMax, -1.0, s);
-	k_cg_init<float><<<vec_grid(n, w.smCount), kCgBlock, 0, s>>>(n, rin, zero, dinv32, r32, u32, w.part,
-	                                                               (CgScal *) w.scal);
+	if (w.binv32)
+		k_cg_init_blk<B><<<vec_grid(m.N, w.smCount), kCgBlock, 0, s>>>(m.N, rin, zero, w.binv32, r32, u32, w.part,
+		                                                                (CgScal *) w.scal);
+	else
+		k_cg_init<float><<<vec_grid(n, w.smCount), kCgBlock, 0, s>>>(n, rin, zero, dinv32, r32, u32, w.part,
+		                                                               (CgScal *) w.scal);
 	w.launches += 1;
 }
 
@@ -1013,7 +1090,7 @@ void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *dev
 			CgWork &w = *b.cw;
 			CgJob j;
 			j.A = sell_of(m);
-			j.blk = b.blk; j.dinv = b.dinv; j.x = b.x;
+			j.blk = b.blk; j.dinv = b.dinv; j.binv = b.binv; j.x = b.x;
 			if (sizeof(TV) == sizeof(double)) {
 				j.r = w.r; j.u = w.u; j.w = w.w; j.p = w.p; j.s = w.sv;
 			} else {

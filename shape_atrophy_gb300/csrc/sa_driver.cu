@@ -363,6 +363,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	c.xr = P.alloc<double>((size_t) 3 * n);
 	if (md.precision == SA_PREC_MIXED) {
 		c.blk32 = P.alloc<float>((size_t) T * sell_vals<D>());
+		c.binv32 = P.alloc<float>((size_t) N * D * D);
 		c.f32 = P.alloc<float>((size_t) 7 * n);
 	}
 	bool useK = md.frame || md.ldmWgt != 0.0;
@@ -433,7 +434,7 @@ struct Stepper {
 	{
 		launch_activity<D>(m, md, tau_now(), w.fy, w.fr, s);
 		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
-		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, s);
+		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, w.cw.binv32, s);
 		launch_yank_rhs<D>(m, *gn, w.fy, w.b, s);
 		if (useK) launch_kernel_matrix<D>(md, m.N, xn, w.K, s);
 		else if (md.precision == SA_PREC_MIXED)
@@ -956,13 +957,13 @@ struct Inst : InstBase {
 		cg_prepare_fp64<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, s);
 	}
 	void finish_velocity_fp64() override { cg_finish_fp64<D>(m, w.v, w.cw, s); }
-	BatchSolve velocity_fp64() override { return BatchSolve{&m, &w.cw, w.blk, w.dinv, w.v}; }
+	BatchSolve velocity_fp64() override { return BatchSolve{&m, &w.cw, w.blk, w.dinv, w.v, nullptr}; }
 	void mixed_outer(int first) override { cg_mixed_outer<D>(m, w.blk, w.dinv, w.b, w.v, bb, first, w.cw, s); }
 	void mixed_inner() override { cg_mixed_inner<D>(m, md.cgItrMax - mixedTotal, innerTol, w.cw, s); }
 	BatchSolve velocity_mixed() override
 	{
 		long n = (long) m.N * D;
-		return BatchSolve{&m, &w.cw, w.cw.blk32, w.cw.f32 + 5 * n, w.cw.f32 + 6 * n};
+		return BatchSolve{&m, &w.cw, w.cw.blk32, w.cw.f32 + 5 * n, w.cw.f32 + 6 * n, w.cw.binv32};
 	}
 	void mixed_apply() override { cg_mixed_apply((long) m.N * D, w.v, w.cw, s); }
 	void zero_velocity() override { SA_CHECK(cudaMemsetAsync(w.v, 0, sizeof(double) * m.N * D, s)); }
@@ -971,7 +972,7 @@ struct Inst : InstBase {
 		st.post_velocity();
 		cg_prepare_fp64<1>(m, w.L, w.dinvRd, w.rhs, st.tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, s);
 	}
-	BatchSolve rd_solve() override { return BatchSolve{&m, &w.cw, w.L, w.dinvRd, st.tau_next()}; }
+	BatchSolve rd_solve() override { return BatchSolve{&m, &w.cw, w.L, w.dinvRd, st.tau_next(), nullptr}; }
 	void finish_rd() override { cg_finish_fp64<1>(m, st.tau_next(), w.cw, s); }
 	void end_step() override { st.end_step(); }
 	CgWork &cg() override { return w.cw; }

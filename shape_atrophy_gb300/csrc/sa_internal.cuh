@@ -83,6 +83,35 @@ template <> __device__ __forceinline__ Mat<3> inv_edges<3>(const Vec<3> *q, doub
 	return r;
 }
 
+// inverse of a small dense matrix by cofactors (diagonal blocks of the operator; SPD, well away from 0)
+template <int D> __device__ __forceinline__ Mat<D> mat_inverse(const Mat<D> &a);
+template <> __device__ __forceinline__ Mat<2> mat_inverse<2>(const Mat<2> &a)
+{
+	Mat<2> r;
+	double det = a.m[0][0] * a.m[1][1] - a.m[0][1] * a.m[1][0];
+	r.m[0][0] = a.m[1][1] / det; r.m[0][1] = -a.m[0][1] / det;
+	r.m[1][0] = -a.m[1][0] / det; r.m[1][1] = a.m[0][0] / det;
+	return r;
+}
+template <> __device__ __forceinline__ Mat<3> mat_inverse<3>(const Mat<3> &a)
+{
+	Mat<3> r;
+	double c00 = a.m[1][1] * a.m[2][2] - a.m[1][2] * a.m[2][1];
+	double c01 = a.m[1][2] * a.m[2][0] - a.m[1][0] * a.m[2][2];
+	double c02 = a.m[1][0] * a.m[2][1] - a.m[1][1] * a.m[2][0];
+	double det = a.m[0][0] * c00 + a.m[0][1] * c01 + a.m[0][2] * c02;
+	r.m[0][0] = c00 / det;
+	r.m[1][0] = c01 / det;
+	r.m[2][0] = c02 / det;
+	r.m[0][1] = (a.m[0][2] * a.m[2][1] - a.m[0][1] * a.m[2][2]) / det;
+	r.m[1][1] = (a.m[0][0] * a.m[2][2] - a.m[0][2] * a.m[2][0]) / det;
+	r.m[2][1] = (a.m[0][1] * a.m[2][0] - a.m[0][0] * a.m[2][1]) / det;
+	r.m[0][2] = (a.m[0][1] * a.m[1][2] - a.m[0][2] * a.m[1][1]) / det;
+	r.m[1][2] = (a.m[0][2] * a.m[1][0] - a.m[0][0] * a.m[1][2]) / det;
+	r.m[2][2] = (a.m[0][0] * a.m[1][1] - a.m[0][1] * a.m[1][0]) / det;
+	return r;
+}
+
 // --------------------------------------------------------------------------
 // activity functions (inc/activity.h:4-38, 106-167)
 // --------------------------------------------------------------------------
@@ -259,8 +288,10 @@ template <int D> void launch_yank_rhs(const Mesh &m, const Geom &g, const double
                                       cudaStream_t s);
 template <int D> void launch_penalty_diag(const Mesh &m, const Model &md, const double *x, double *pd,
                                           cudaStream_t s);
+// binv32 (optional, N x D x D): FP32 inverses of the diagonal blocks (block-Jacobi of the FP32 inner solves)
 template <int D> void launch_assemble_elastic(const Mesh &m, const Model &md, const Geom &g,
-                                              const double *pd, double *blk, double *dinv, cudaStream_t s);
+                                              const double *pd, double *blk, double *dinv, float *binv32,
+                                              cudaStream_t s);
 template <int D> void launch_assemble_rd(const Mesh &m, const Model &md, const Geom &g, double dt,
                                          double *Mval, double *Lval, double *dinv, cudaStream_t s);
 template <int D> void launch_rd_rhs(const Mesh &m, const Geom &gNow, const double *Mnow, const double *tau,
@@ -285,6 +316,7 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	void *bar = nullptr;          // grid barrier of the persistent CG kernel (kGridBarBytes, device)
 	double profBytes = 0.0, profFlops = 0.0;   // algorithmic bytes / flops of the timed launches
 	float *blk32 = nullptr;       // FP32 copy of the operator (mixed precision)
+	float *binv32 = nullptr;      // FP32 inverses of its diagonal blocks (block-Jacobi, mixed precision)
 	float *f32 = nullptr;         // 7 n FP32 vectors of the inner solve (mixed precision)
 	double *xr = nullptr;         // 3 n FP64 refinement scratch
 	// optional CUDA-event timing of the velocity matvec kernel (k_cg_spmv)
@@ -315,6 +347,7 @@ template <int B> int cg_jacobi(const Mesh &m, const double *blk, const double *d
 struct CgJob {                 // one solve of a batched launch (device-visible)
 	SellOp A;
 	const void *blk, *dinv;    // operator values (TM), Jacobi inverse (TV)
+	const void *binv;          // block-Jacobi inverses (TV, B x B per row) or null
 	void *x, *r, *u, *w, *p, *s;   // solution (TX) and CG vectors (TV)
 	double *part;              // 3 x nctas partial sums
 	void *sc, *bar;            // scalars, grid barrier
@@ -322,7 +355,7 @@ struct CgJob {                 // one solve of a batched launch (device-visible)
 };
 struct CgState { int code, iters, zero, done; double rr, bb; };   // host copy of a solve's scalars
 enum CgVec { kCgFp64, kCgFp32 };     // which vector set of CgWork a batched solve uses
-struct BatchSolve { const Mesh *m; CgWork *cw; const void *blk; const void *dinv; void *x; };
+struct BatchSolve { const Mesh *m; CgWork *cw; const void *blk; const void *dinv; void *x; const void *binv; };
 
 // FP64 solve A x = b (x holds the initial guess): q = A x, r = b - q, u = D^-1 r, scalars; zeroes p, s
 template <int B> void cg_prepare_fp64(const Mesh &m, const double *blk, const double *dinv, const double *b,
