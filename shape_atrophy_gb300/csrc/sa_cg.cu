@@ -61,21 +61,20 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *sm)
 		}
 }
 
-// u = M^-1 r for one row: point Jacobi (dv = D^-1 of the row) or, when bv is given, the row's B x B
-// block-Jacobi inverse (FP32 inner solves of mixed precision)
+// u = M^-1 r for one row with the row's B x B block-Jacobi inverse bv (row-major); the FP32 inner
+// solves of mixed precision use it, the FP64 solves point Jacobi
 template <int B, typename TV>
-__device__ __forceinline__ void apply_prec(const TV (&dv)[B], const TV *bv, const TV (&r)[B], TV (&u)[B])
+__device__ __forceinline__ void prec_block(const TV *bv, const TV (&r)[B], TV (&u)[B])
 {
-	if (bv) {
-		for (int a = 0; a < B; ++a) {
-			TV t = bv[a * B] * r[0];
-			for (int c = 1; c < B; ++c) t += bv[a * B + c] * r[c];
-			u[a] = t;
-		}
-	} else {
-		for (int c = 0; c < B; ++c) u[c] = dv[c] * r[c];
+	for (int a = 0; a < B; ++a) {
+		TV t = bv[a * B] * r[0];
+		for (int c = 1; c < B; ++c) t += bv[a * B + c] * r[c];
+		u[a] = t;
 	}
 }
+
+// block-Jacobi is chosen at compile time: FP32 vectors (mixed-precision inner solves) only
+template <typename TV> constexpr bool block_prec() { return sizeof(TV) == sizeof(float); }
 
 // block partials part[k * nb + blockIdx.x]; returns true in the block that
 // arrives last (the one that finishes the reduction)
@@ -278,7 +277,7 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_init_blk(int N, const double *_
 	const int stride = gridDim.x * blockDim.x;
 	double v[3] = {0.0, 0.0, 0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
-		float rt[B], ut[B], unused[B];
+		float rt[B], ut[B];
 		for (int c = 0; c < B; ++c) {
 			const long k = (long) i * B + c;
 			double rk = b[k] - q[k];
@@ -286,9 +285,8 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_init_blk(int N, const double *_
 			r[k] = rt[c];
 			v[0] += b[k] * b[k];
 			v[1] += rk * rk;
-			unused[c] = 0.0f;
 		}
-		apply_prec<B, float>(unused, binv + (long) i * B * B, rt, ut);
+		prec_block<B, float>(binv + (long) i * B * B, rt, ut);
 		for (int c = 0; c < B; ++c) {
 			u[(long) i * B + c] = ut[c];
 			v[2] += (double) rt[c] * (double) ut[c];
@@ -505,10 +503,10 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	double gam = sc->gam, rr = sc->rr, gamPrev = 0.0, alphaPrev = 1.0;
 	unsigned int target = 0;                     // bar->count is zeroed before the launch
 	TX xv[B];
-	// block-Jacobi only for FP32 vectors (the mixed inner solves); FP64 keeps point Jacobi and its registers
-	constexpr int kBV = sizeof(TV) == sizeof(float) ? B * B : 1;
+	// block-Jacobi for FP32 vectors (the mixed inner solves, binv given); FP64 point Jacobi
+	constexpr bool kBlk = block_prec<TV>();
+	constexpr int kBV = kBlk ? B * B : 1;
 	TV rv[B], uv[B], pv[B], sv[B], dv[B], bv[kBV];
-	const bool blockPrec = kBV > 1 && binv != nullptr;   // the same in every thread
 	for (int c = 0; c < B; ++c) {
 		xv[c] = (TX) 0; rv[c] = uv[c] = pv[c] = sv[c] = dv[c] = (TV) 0;
 		if (own) {
@@ -516,7 +514,8 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			xv[c] = x[k]; rv[c] = r0[k]; uv[c] = u[k]; dv[c] = dinv[k];
 		}
 	}
-	for (int t = 0; t < kBV; ++t) bv[t] = (own && blockPrec) ? binv[(long) i * B * B + t] : (TV) 0;
+	if constexpr (kBlk)
+		for (int t = 0; t < kBV; ++t) bv[t] = own ? binv[(long) i * B * B + t] : (TV) 0;
 	int it = 0, code = SA_OK;
 	bool first = true;
 	for (;;) {
@@ -554,7 +553,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 				xv[c] = xv[c] + (TX) al * (TX) pv[c];
 				rv[c] = rv[c] - al * sv[c];
 			}
-			if constexpr (kBV > 1) apply_prec<B, TV>(dv, blockPrec ? bv : nullptr, rv, uv);
+			if constexpr (kBlk) prec_block<B, TV>(bv, rv, uv);
 			else for (int c = 0; c < B; ++c) uv[c] = dv[c] * rv[c];
 			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uv[c];
 			dot_row<B, TV>(d2[0], rv, uv);
@@ -619,7 +618,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 	const SellOp A = J.A;
 	const TM *blk = (const TM *) J.blk;
 	const TV *dinv = (const TV *) J.dinv;
-	const TV *binv = (const TV *) J.binv;
+	const TV *binv = (const TV *) J.binv;          // FP32 solves only (block-Jacobi), never read in FP64
 	TX *x = (TX *) J.x;
 	TV *r = (TV *) J.r, *u = (TV *) J.u, *w = (TV *) J.w, *p = (TV *) J.p, *sv = (TV *) J.s;
 	GridBar *bar = (GridBar *) J.bar;
@@ -684,7 +683,8 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 				r[k] = rk[c];
 				dk[c] = dinv[k];
 			}
-			apply_prec<B, TV>(dk, binv ? binv + (long) i * B * B : nullptr, rk, uk);
+			if constexpr (block_prec<TV>()) prec_block<B, TV>(binv + (long) i * B * B, rk, uk);
+			else for (int c = 0; c < B; ++c) uk[c] = dk[c] * rk[c];
 			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uk[c];
 			dot_row<B, TV>(d2[0], rk, uk);
 			dot_row<B, TV>(d2[1], rk, rk);
@@ -817,15 +817,15 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	const int pw = std::max(1, std::min(kPersistMaxWarps, (m.nslice + prof->smCount - 1) / prof->smCount));
 	const int nctas = (m.nslice + pw - 1) / pw;
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
+	                     (!block_prec<TV>() || prof->binv32) &&
 	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw);
 	if (persist) {
 		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first).  FP32
 		// inner solves of mixed precision are block-Jacobi preconditioned (3x3 node blocks)
 		const TV *binv = nullptr;
-		if constexpr (sizeof(TV) == sizeof(float)) binv = prof->binv32;
-		if (binv) {
-			if constexpr (sizeof(TV) == sizeof(float))
-				k_cg_init_blk<B><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
+		if constexpr (block_prec<TV>()) {
+			binv = prof->binv32;
+			k_cg_init_blk<B><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
 		} else {
 			k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
 		}
@@ -1031,12 +1031,10 @@ void cg_mixed_inner(const Mesh &m, int itrMax, double innerTolSqu, CgWork &w, cu
 	SA_CHECK(cudaMemsetAsync(p32, 0, sizeof(float) * n, s));
 	SA_CHECK(cudaMemsetAsync(s32, 0, sizeof(float) * n, s));
 	set_scal((CgScal *) w.scal, innerTolSqu, itrMax, -1.0, s);
-	if (w.binv32)
-		k_cg_init_blk<B><<<vec_grid(m.N, w.smCount), kCgBlock, 0, s>>>(m.N, rin, zero, w.binv32, r32, u32, w.part,
-		                                                                (CgScal *) w.scal);
-	else
-		k_cg_init<float><<<vec_grid(n, w.smCount), kCgBlock, 0, s>>>(n, rin, zero, dinv32, r32, u32, w.part,
-		                                                               (CgScal *) w.scal);
+	if (!w.binv32) throw CudaError{cudaErrorInvalidValue, "mixed precision without block inverses"};
+	(void) dinv32;
+	k_cg_init_blk<B><<<vec_grid(m.N, w.smCount), kCgBlock, 0, s>>>(m.N, rin, zero, w.binv32, r32, u32, w.part,
+	                                                                (CgScal *) w.scal);
 	w.launches += 1;
 }
 
@@ -1090,6 +1088,7 @@ void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *dev
 			CgWork &w = *b.cw;
 			CgJob j;
 			j.A = sell_of(m);
+			if (block_prec<TV>() && !b.binv) throw CudaError{cudaErrorInvalidValue, "batched FP32 CG without block inverses"};
 			j.blk = b.blk; j.dinv = b.dinv; j.binv = b.binv; j.x = b.x;
 			if (sizeof(TV) == sizeof(double)) {
 				j.r = w.r; j.u = w.u; j.w = w.w; j.p = w.p; j.s = w.sv;
