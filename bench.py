@@ -27,6 +27,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -266,7 +268,7 @@ def main():
 
     K, W = args.steps, max(3, args.warmup)
     spec = spec_for(args, W + K)
-    sess = api.Session(spec, precision=args.precision, objective=False, device=local)
+    sess = api.Session(spec, precision=args.precision, objective=True, device=local)
     sess.step(W)                                       # untimed warm-up steps
     sess.profile(1)                                    # CUDA-event timing of the velocity CG kernel
     info0 = sess.info()
@@ -285,6 +287,22 @@ def main():
     k_ms, k_cnt, k_bytes, k_flops = sess.profile(0)
     launches = info["kernelLaunches"] - launches0
     cg_iters = info["cgIterTotal"] - iters0
+    # the objective (varifold of the current shape against the target): pair evaluations per second
+    objective = None
+    if rank == 0:
+        sess.objective()                               # warm-up
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            sess.objective()
+            ts.append(time.perf_counter() - t0)
+        Vd = spec["elmObj"]["vfdVtxMat"].shape[1]
+        Vt = np.asarray(spec["tgt"][2]).size
+        pairs = float(Vd + Vt) ** 2
+        t_obj = statistics.median(ts)
+        objective = {"kernel": "k_vfd_rows (varifold pair sums, Matern-3/2 x Binet)", "deformed": Vd, "target": Vt,
+                     "pairs": pairs, "ms": t_obj * 1e3, "pairs_per_s": pairs / t_obj,
+                     "what": "one sa_session_objective call (synchronous, host clock), median of 3"}
     sess.close()
 
     value = ws * K / (ms_max / 1000.0)
@@ -347,7 +365,8 @@ def main():
                            "elements": spec["elmObj"]["elmVtxMat"].shape[1], "cg_iters_per_step": cg_iters / K,
                            "l2": "per-step working set (~0.3 GB) larger than the 129 MB L2",
                            "parallelism": f"replicas x{ws}"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "served": served, "clocks": clocks,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "objective": objective, "served": served,
+                "clocks": clocks,
                 "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     if dist is not None:

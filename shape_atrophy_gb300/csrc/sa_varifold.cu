@@ -18,6 +18,7 @@
 // shape's extent).
 #include "sa_internal.cuh"
 #include <cmath>
+#include <algorithm>
 
 namespace sa {
 
@@ -73,7 +74,10 @@ __global__ void k_vfd_elems(int N, int Vd, const int *__restrict__ vfdVtx, const
 struct VfdSet { const double *cen, *dir, *vol; int n; };
 
 // out[i] = sum_j c1 K(i, j) over set A  +  sum_j c2 K(i, j) over set B (B may be empty);
-// gradient rows (dc, dt) when grad != 0 (rows must be the deformed set).
+// gradient rows (dc, dt) when grad != 0 (rows must be the deformed set).  blockIdx.y splits the
+// columns of each set into gridDim.y contiguous chunks (more CTAs than rows alone give); chunk c
+// writes its partial row sums at out + c * R.n (dc, dt at + c * D * R.n), summed in chunk order by
+// k_vfd_chunks.  One chunk: the reference's per-row order exactly.
 template <int D, typename T>
 __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, int ck, double cw, int dk,
                            double dw, double *__restrict__ out, int grad, double *__restrict__ dc,
@@ -95,14 +99,18 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 	double acc = 0.0, gc[D], gt[D];
 	for (int d = 0; d < D; ++d) { gc[d] = 0.0; gt[d] = 0.0; }
 	const T cwT = (T) cw, dwT = (T) dw;
+	const int C = gridDim.y, cy = blockIdx.y;
+	out += (long) cy * R.n;
+	if (grad) { dc += (long) cy * D * R.n; dt += (long) cy * D * R.n; }
 	for (int set = 0; set < 2; ++set) {
 		const VfdSet &S = set == 0 ? A : Bs;
 		T coef = (T) (set == 0 ? cA : cB);
+		const int jBeg = (int) ((long) S.n * cy / C), jEnd = (int) ((long) S.n * (cy + 1) / C);
 		// gradient weights of dqVfd_DD_DT: +2 for the deformed-deformed term (both ends move), -2 for
 		// the deformed-target term
 		T gco = (T) (set == 0 ? 2.0 * cA : cB);
-		for (int j0 = 0; j0 < S.n; j0 += kVfdTile) {
-			int nt = min(kVfdTile, S.n - j0);
+		for (int j0 = jBeg; j0 < jEnd; j0 += kVfdTile) {
+			int nt = min(kVfdTile, jEnd - j0);
 			__syncthreads();
 			for (int t = threadIdx.x; t < nt; t += blockDim.x) {
 				for (int d = 0; d < D; ++d) {
@@ -157,6 +165,30 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 	out[i] = acc;
 	if (grad)
 		for (int d = 0; d < D; ++d) { dc[d * (long) R.n + i] = gc[d]; dt[d * (long) R.n + i] = gt[d]; }
+}
+
+// row sums of the column chunks of k_vfd_rows, chunk order fixed (K values per row: 1, or 1 + 2D with the
+// gradient rows laid out [chunk][d][row])
+template <int D>
+__global__ void k_vfd_chunks(int n, int C, const double *__restrict__ part, double *__restrict__ out, int grad,
+                             const double *__restrict__ pdc, const double *__restrict__ pdt, double *__restrict__ dc,
+                             double *__restrict__ dt)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	double a = part[i];
+	for (int c = 1; c < C; ++c) a += part[(long) c * n + i];
+	out[i] = a;
+	if (!grad) return;
+	for (int d = 0; d < D; ++d) {
+		double x = pdc[(long) d * n + i], y = pdt[(long) d * n + i];
+		for (int c = 1; c < C; ++c) {
+			x += pdc[((long) c * D + d) * n + i];
+			y += pdt[((long) c * D + d) * n + i];
+		}
+		dc[(long) d * n + i] = x;
+		dt[(long) d * n + i] = y;
+	}
 }
 
 // node gradient gather (2D_frame/varifold.cu:435-466, 3D_frame :492-528)
@@ -239,30 +271,44 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 	int Vd = m.Vd;
 	*err = SA_OK;
 	if (grad && !m.vfdIfo) { *err = SA_ERR_ARG; return 0.0; }
+	// column chunks: enough CTAs to fill the GPU (the pair sums are latency bound at one CTA per SM)
+	int dev = 0, sms = 1;
+	SA_CHECK(cudaGetDevice(&dev));
+	SA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	const int blk = 128;
+	const int rowMax = std::max(Vd, Vt), colMin = std::min(Vd, Vt);
+	int C = std::max(1, (8 * sms + grid_for(rowMax, blk) - 1) / std::max(1, grid_for(rowMax, blk)));
+	C = std::min(C, std::max(1, colMin / (2 * kVfdTile)));
+	C = std::min(C, 32);
 	double *buf = nullptr;
-	size_t need = (size_t) Vd * (2 * D + 1) + (size_t) (Vd + Vt) + kSum + 1 + (grad ? (size_t) 2 * D * Vd : 0);
+	const size_t rows = (size_t) (Vd + Vt);
+	size_t need = (size_t) Vd * (2 * D + 1) + rows + kSum + 1 + (grad ? (size_t) 2 * D * Vd : 0) +
+	              (size_t) C * rowMax * (1 + (grad ? 2 * D : 0));
 	SA_CHECK(cudaMallocAsync(&buf, sizeof(double) * need, s));
 	double *cen = buf, *dir = cen + (long) D * Vd, *vol = dir + (long) D * Vd, *vfd = vol + Vd;
 	double *scr = vfd + Vd + Vt, *dc = scr + kSum + 1, *dt = dc + (long) D * Vd;
+	double *part = grad ? dt + (long) D * Vd : dc;
+	double *pdc = part + (long) C * rowMax, *pdt = pdc + (long) C * D * rowMax;
 	k_vfd_elems<D><<<grid_for(Vd), kBlock, 0, s>>>(m.N, Vd, m.vfdVtx, x, cen, dir, vol);
 	VfdSet Ds{cen, dir, vol, Vd}, Ts{tgtCen, tgtDir, tgtVol, Vt}, E0{nullptr, nullptr, nullptr, 0};
 	int ck = md.cenKnl, dk = md.dirKnl;
-	const int blk = 128;
-	auto rows = [&](VfdSet R, VfdSet A, double cA, VfdSet B, double cB, double *out, int g) {
+	auto rows_of = [&](VfdSet R, VfdSet A, double cA, VfdSet B, double cB, double *out, int g) {
 		if (R.n == 0) return;
+		dim3 grid(grid_for(R.n, blk), C);
 		if (precision == SA_PREC_MIXED)
-			k_vfd_rows<D, float><<<grid_for(R.n, blk), blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk,
-			                                                        md.dirWidth, out, g, dc, dt);
+			k_vfd_rows<D, float><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk, md.dirWidth, part, g,
+			                                          pdc, pdt);
 		else
-			k_vfd_rows<D, double><<<grid_for(R.n, blk), blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk,
-			                                                         md.dirWidth, out, g, dc, dt);
+			k_vfd_rows<D, double><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk, md.dirWidth, part, g,
+			                                           pdc, pdt);
+		k_vfd_chunks<D><<<grid_for(R.n), kBlock, 0, s>>>(R.n, C, part, out, g, pdc, pdt, dc, dt);
 	};
 	if (grad || Vd >= Vt) {
-		rows(Ds, Ds, 1.0, Ts, -2.0, vfd, grad ? 1 : 0);      // vfd_DD_DT / dqVfd_DD_DT
-		rows(Ts, Ts, 1.0, E0, 0.0, vfd + Vd, 0);             // vfd_TT
+		rows_of(Ds, Ds, 1.0, Ts, -2.0, vfd, grad ? 1 : 0);      // vfd_DD_DT / dqVfd_DD_DT
+		rows_of(Ts, Ts, 1.0, E0, 0.0, vfd + Vd, 0);             // vfd_TT
 	} else {
-		rows(Ts, Ts, 1.0, Ds, -2.0, vfd, 0);                 // vfd_TT_TD
-		rows(Ds, Ds, 1.0, E0, 0.0, vfd + Vt, 0);             // vfd_DD
+		rows_of(Ts, Ts, 1.0, Ds, -2.0, vfd, 0);                 // vfd_TT_TD
+		rows_of(Ds, Ds, 1.0, E0, 0.0, vfd + Vt, 0);             // vfd_DD
 	}
 	SA_CHECK(cudaGetLastError());
 	double obj = device_sum(vfd, Vd + Vt, scr, s);
