@@ -606,6 +606,8 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 	}
 	std::vector<double> objs(objNum, 0.0);
 	SolveOut last{};
+	VfdTargetCache vcache;                    // target-target varifold rows, shared by the columns
+	if (tgt) { vcache.rows = P.alloc<double>((size_t) tgt->tgtElmNum); vcache.capacity = tgt->tgtElmNum; }
 	SA_CHECK(cudaEventRecord(ctx->e0, s));
 	for (int k = 0; k < objNum; ++k) {
 		const double *tvk = tv.data() + (size_t) k * tauVarNum;
@@ -618,7 +620,8 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 		if (tgt) {
 			int err = SA_OK;
 			// the interleaved final positions sit in w.xa after forward_one
-			objs[k] = varifold<D>(m, md, w.xa, tc, tu, tvl, tgt->tgtElmNum, nullptr, s, md.precision, &err);
+			objs[k] = varifold<D>(m, md, w.xa, tc, tu, tvl, tgt->tgtElmNum, nullptr, s, md.precision, &err,
+			                      &vcache);
 			SA_REQUIRE(err == SA_OK, "varifold arguments");
 		}
 	}
@@ -705,6 +708,7 @@ struct Session : SessionBase {
 	const double *tc = nullptr, *tu = nullptr, *tvl = nullptr;
 	int Vt = 0;
 	std::vector<double> tauVar;
+	VfdTargetCache vcache;                    // target-target varifold rows, kept across objective() calls
 
 	Session(sa_context *c, const sa_element_object *obj, const double *lmkIni, const sa_params *prm,
 	        const sa_target *tgt, const double *tv, int tvNum)
@@ -768,7 +772,8 @@ struct Session : SessionBase {
 		SA_REQUIRE(tc, "session has no target");
 		if (st.out.status != SA_OK) return DBL_MAX;
 		int err = SA_OK;
-		double v = varifold<D>(m, md, st.xn, tc, tu, tvl, Vt, nullptr, ctx->stream, md.precision, &err);
+		if (!vcache.rows) { vcache.rows = P.alloc<double>((size_t) Vt); vcache.capacity = Vt; }
+		double v = varifold<D>(m, md, st.xn, tc, tu, tvl, Vt, nullptr, ctx->stream, md.precision, &err, &vcache);
 		SA_REQUIRE(err == SA_OK, "varifold arguments");
 		return v;
 	}

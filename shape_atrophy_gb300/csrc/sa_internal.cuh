@@ -389,10 +389,19 @@ template <int D> int kpcg(const Mesh &m, const Model &md, const double *blk, con
                           double *x, KpcgWork &w, Status *st, int *itersOut, cudaStream_t s);
 template <int D> void launch_kernel_matrix(const Model &md, int N, const double *x, double *K, cudaStream_t s);
 
-// varifold objective (and node gradient) of a shape
+// the target-target rows of the varifold objective (they depend on the target only), kept between calls
+struct VfdTargetCache {
+	double *rows = nullptr;    // device, capacity doubles
+	int capacity = 0;
+	bool valid = false;
+	int Vt = 0, precision = -1, ck = 0, dk = 0;
+	double cw = 0.0, dw = 0.0;
+};
+
+// varifold objective (and node gradient) of a shape; cache (optional) keeps the target-target rows
 template <int D> double varifold(const Mesh &m, const Model &md, const double *x, const double *tgtCen,
                                  const double *tgtDir, const double *tgtVol, int Vt, double *grad,
-                                 cudaStream_t s, int precision, int *err);
+                                 cudaStream_t s, int precision, int *err, VfdTargetCache *cache = nullptr);
 
 // deterministic sum of n doubles on the device (returned via host)
 double device_sum(const double *v, long n, double *scratch, cudaStream_t s);

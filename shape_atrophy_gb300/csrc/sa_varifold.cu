@@ -78,10 +78,12 @@ struct VfdSet { const double *cen, *dir, *vol; int n; };
 // columns of each set into gridDim.y contiguous chunks (more CTAs than rows alone give); chunk c
 // writes its partial row sums at out + c * R.n (dc, dt at + c * D * R.n), summed in chunk order by
 // k_vfd_chunks.  One chunk: the reference's per-row order exactly.
+// symA != 0 (objective only, set A is the row set itself): K is symmetric, so row i takes the pairs
+// j >= i of set A with weight 2 (1 on the diagonal) -- the same total with half the pair evaluations.
 template <int D, typename T>
 __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, int ck, double cw, int dk,
                            double dw, double *__restrict__ out, int grad, double *__restrict__ dc,
-                           double *__restrict__ dt)
+                           double *__restrict__ dt, int symA = 0)
 {
 	constexpr bool kSplit = sizeof(T) < sizeof(double);     // two-float centres in FP32
 	__shared__ T sc[kVfdTile * D], su[kVfdTile * D], sv[kVfdTile], sl[kSplit ? kVfdTile * D : 1];
@@ -105,7 +107,10 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 	for (int set = 0; set < 2; ++set) {
 		const VfdSet &S = set == 0 ? A : Bs;
 		T coef = (T) (set == 0 ? cA : cB);
-		const int jBeg = (int) ((long) S.n * cy / C), jEnd = (int) ((long) S.n * (cy + 1) / C);
+		const bool sym = set == 0 && symA;
+		const int lo = sym ? (int) (blockIdx.x * blockDim.x) : 0;   // columns below the CTA's rows: none
+		const int span = S.n > lo ? S.n - lo : 0;
+		const int jBeg = lo + (int) ((long) span * cy / C), jEnd = lo + (int) ((long) span * (cy + 1) / C);
 		// gradient weights of dqVfd_DD_DT: +2 for the deformed-deformed term (both ends move), -2 for
 		// the deformed-target term
 		T gco = (T) (set == 0 ? 2.0 * cA : cB);
@@ -126,6 +131,12 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 			T tile = 0, comp = 0, tgc[D], tgt[D];
 			for (int d = 0; d < D; ++d) { tgc[d] = 0; tgt[d] = 0; }
 			for (int jj = 0; jj < nt; ++jj) {
+				T wgt = (T) 1;
+				if (sym) {
+					const int j = j0 + jj;
+					if (j < i) continue;
+					if (j > i) wgt = (T) 2;
+				}
 				T df[D];
 				for (int d = 0; d < D; ++d) {
 					df[d] = ci[d] - sc[jj * D + d];
@@ -139,7 +150,7 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 				T kc = cen_knl<T>(ck, cwT, d2, d1c);
 				T kd = dir_knl<T>(dk, dwT, ang, d1d);
 				T vj = sv[jj];
-				const T term = coef * kc * kd * vi * vj;
+				const T term = wgt * coef * kc * kd * vi * vj;
 				if (kSplit) {                  // Kahan: the FP32 tile sum keeps its lost low bits
 					T y = term - comp, t = tile + y;
 					comp = (t - tile) - y;
@@ -266,7 +277,8 @@ double device_sum(const double *v, long n, double *scratch, cudaStream_t s)
 
 template <int D>
 double varifold(const Mesh &m, const Model &md, const double *x, const double *tgtCen, const double *tgtDir,
-                const double *tgtVol, int Vt, double *grad, cudaStream_t s, int precision, int *err)
+                const double *tgtVol, int Vt, double *grad, cudaStream_t s, int precision, int *err,
+                VfdTargetCache *cache)
 {
 	int Vd = m.Vd;
 	*err = SA_OK;
@@ -292,20 +304,36 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 	k_vfd_elems<D><<<grid_for(Vd), kBlock, 0, s>>>(m.N, Vd, m.vfdVtx, x, cen, dir, vol);
 	VfdSet Ds{cen, dir, vol, Vd}, Ts{tgtCen, tgtDir, tgtVol, Vt}, E0{nullptr, nullptr, nullptr, 0};
 	int ck = md.cenKnl, dk = md.dirKnl;
+	// rows_of: per-row sums of R against A (coefficient cA) and B (cB); the self term R = A uses the
+	// symmetric half when no gradient rows are wanted
 	auto rows_of = [&](VfdSet R, VfdSet A, double cA, VfdSet B, double cB, double *out, int g) {
 		if (R.n == 0) return;
 		dim3 grid(grid_for(R.n, blk), C);
+		const int sym = g ? 0 : 1;
 		if (precision == SA_PREC_MIXED)
 			k_vfd_rows<D, float><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk, md.dirWidth, part, g,
-			                                          pdc, pdt);
+			                                          pdc, pdt, sym);
 		else
 			k_vfd_rows<D, double><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk, md.dirWidth, part, g,
-			                                           pdc, pdt);
+			                                           pdc, pdt, sym);
 		k_vfd_chunks<D><<<grid_for(R.n), kBlock, 0, s>>>(R.n, C, part, out, g, pdc, pdt, dc, dt);
 	};
 	if (grad || Vd >= Vt) {
 		rows_of(Ds, Ds, 1.0, Ts, -2.0, vfd, grad ? 1 : 0);      // vfd_DD_DT / dqVfd_DD_DT
-		rows_of(Ts, Ts, 1.0, E0, 0.0, vfd + Vd, 0);             // vfd_TT
+		// vfd_TT depends on the target only: a cache (same target, same kernels, same precision) keeps
+		// its rows between calls
+		bool hit = cache && cache->rows && cache->valid && cache->Vt == Vt && cache->precision == precision &&
+		           cache->ck == ck && cache->dk == dk && cache->cw == md.cenWidth && cache->dw == md.dirWidth;
+		if (hit) {
+			SA_CHECK(cudaMemcpyAsync(vfd + Vd, cache->rows, sizeof(double) * Vt, cudaMemcpyDeviceToDevice, s));
+		} else {
+			rows_of(Ts, Ts, 1.0, E0, 0.0, vfd + Vd, 0);
+			if (cache && cache->rows && cache->capacity >= Vt) {
+				SA_CHECK(cudaMemcpyAsync(cache->rows, vfd + Vd, sizeof(double) * Vt, cudaMemcpyDeviceToDevice, s));
+				cache->valid = true; cache->Vt = Vt; cache->precision = precision;
+				cache->ck = ck; cache->dk = dk; cache->cw = md.cenWidth; cache->dw = md.dirWidth;
+			}
+		}
 	} else {
 		rows_of(Ts, Ts, 1.0, Ds, -2.0, vfd, 0);                 // vfd_TT_TD
 		rows_of(Ds, Ds, 1.0, E0, 0.0, vfd + Vt, 0);             // vfd_DD
@@ -318,9 +346,9 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 }
 
 template double varifold<2>(const Mesh &, const Model &, const double *, const double *, const double *,
-                            const double *, int, double *, cudaStream_t, int, int *);
+                            const double *, int, double *, cudaStream_t, int, int *, VfdTargetCache *);
 template double varifold<3>(const Mesh &, const Model &, const double *, const double *, const double *,
-                            const double *, int, double *, cudaStream_t, int, int *);
+                            const double *, int, double *, cudaStream_t, int, int *, VfdTargetCache *);
 
 // ---------------------------------------------------------------------------
 // Allocation-free variant of the varifold objective (sa_varifold_noalloc).
