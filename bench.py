@@ -300,9 +300,12 @@ def main():
         Vt = np.asarray(spec["tgt"][2]).size
         pairs = float(Vd + Vt) ** 2
         t_obj = statistics.median(ts)
+        evaluated = 0.5 * Vd * (Vd + 1) + float(Vd) * Vt      # symmetric DD half + DT; TT rows cached
         objective = {"kernel": "k_vfd_rows (varifold pair sums, Matern-3/2 x Binet)", "deformed": Vd, "target": Vt,
-                     "pairs": pairs, "ms": t_obj * 1e3, "pairs_per_s": pairs / t_obj,
-                     "what": "one sa_session_objective call (synchronous, host clock), median of 3"}
+                     "pairs": pairs, "evaluated_pairs": evaluated, "ms": t_obj * 1e3, "pairs_per_s": pairs / t_obj,
+                     "evaluated_pairs_per_s": evaluated / t_obj,
+                     "what": "one sa_session_objective call (synchronous, host clock), median of 3 after one "
+                             "warm-up; pairs = (Vd + Vt)^2 as the reference evaluates them"}
     sess.close()
 
     value = ws * K / (ms_max / 1000.0)
