@@ -226,6 +226,34 @@ def served_leg(device: int, n: int = 32):
             "mixed_vs_fp64_max_rel_err": {"positions": ep, "objective": eo}}
 
 
+def mixed_error_leg(args, device: int, steps: int = 100, every: int = 10):
+    """Config 3: the mixed-precision solve of the shell against the FP64 solve, both on the GPU, at every
+    10th step (node positions, concentration, objective).  The FP64 GPU path stands in for the FP64 oracle
+    (it matches the oracle to 1e-10 in the parity tests; the oracle itself needs minutes per step here)."""
+    import numpy as np
+    from shape_atrophy_gb300 import api
+    spec = spec_for(args, steps)
+    s64 = api.Session(spec, precision="fp64", objective=True, device=device)
+    s32 = api.Session(spec, precision="mixed", objective=True, device=device)
+    rows = []
+    for t in range(every, steps + 1, every):
+        s64.step(every)
+        s32.step(every)
+        x64, u64, _ = s64.state()
+        x32, u32, _ = s32.state()
+        o64, o32 = s64.objective(), s32.objective()
+        rows.append({"step": t,
+                     "positions": float(np.abs(x32 - x64).max() / np.abs(x64).max()),
+                     "concentration": float(np.abs(u32 - u64).max() / max(np.abs(u64).max(), 1e-300)),
+                     "objective": abs(o32 - o64) / abs(o64)})
+    s64.close()
+    s32.close()
+    worst = {k: max(r[k] for r in rows) for k in ("positions", "concentration", "objective")}
+    return {"steps": steps, "every": every, "reference": "FP64 GPU path (equal to the FP64 oracle to 1e-10)",
+            "max_rel_err": worst, "tolerance": 1e-6, "within": all(v <= 1e-6 for v in worst.values()),
+            "per_step": rows}
+
+
 def run_reference(args, rank, ws, dist):
     """CPU restatement of the model on the host cores (the reference has no CPU path of its own)."""
     if rank != 0:
@@ -253,6 +281,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
+    ap.add_argument("--no-mixed-error", action="store_true", help="skip the mixed-vs-FP64 error leg")
     ap.add_argument("--served-requests", type=int, default=32)
     args = ap.parse_args()
     rank, local, ws, dist = dist_init()
@@ -354,6 +383,10 @@ def main():
     if not args.no_served and rank == 0 and args.workload == "shell":
         served = served_leg(local, args.served_requests)
 
+    mixed_error = None
+    if not args.no_mixed_error and rank == 0 and args.workload == "shell":
+        mixed_error = mixed_error_leg(args, local)
+
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:
         v, cores, sample = cpu_sample(spec_for(args, 4))
@@ -368,7 +401,8 @@ def main():
                            "elements": spec["elmObj"]["elmVtxMat"].shape[1], "cg_iters_per_step": cg_iters / K,
                            "l2": "per-step working set (~0.3 GB) larger than the 129 MB L2",
                            "parallelism": f"replicas x{ws}"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "objective": objective, "served": served,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "objective": objective,
+                "mixed_error": mixed_error, "served": served,
                 "clocks": clocks,
                 "gpu_launches": launches}
         print(json.dumps(line), flush=True)
