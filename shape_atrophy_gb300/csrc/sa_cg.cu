@@ -377,20 +377,20 @@ __device__ __forceinline__ unsigned int load_acquire(const unsigned int *p)
 }
 
 // block sum for a block of any multiple of 32 threads (at most 32 * kPersistMaxWarps); valid in thread 0.
-// Each warp reduces its 32 values by shuffles, then warp 0 reduces the warp sums.
+// Every thread stores its values in shared memory and warp 0 adds them (lane l takes l, l + 32, ...,
+// then a shuffle tree): one FP64 add per value instead of a five-step shuffle tree in every warp, which
+// matters on a 2 DFMA/clk/SM FP64 pipe.  sm holds K * 32 * kPersistMaxWarps doubles.
 template <int K>
 __device__ __forceinline__ void block_sum_any(double (&v)[K], double *sm)
 {
-	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	for (int k = 0; k < K; ++k) {
-		double s = v[k];
-		for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-		if (lane == 0) sm[k * 32 + wp] = s;
-	}
+	const int lane = threadIdx.x & 31, NT = blockDim.x;
+	for (int k = 0; k < K; ++k) sm[k * 32 * kPersistMaxWarps + threadIdx.x] = v[k];
 	__syncthreads();
 	if (threadIdx.x < 32)
 		for (int k = 0; k < K; ++k) {
-			double s = lane < nw ? sm[k * 32 + lane] : 0.0;
+			const double *row = sm + k * 32 * kPersistMaxWarps;
+			double s = row[lane];
+			for (int q = lane + 32; q < NT; q += 32) s += row[q];
 			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
 			v[k] = s;
 		}
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
 k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, const TV *__restrict__ binv, TX *x,
              const TV *r0, TV *u, double *part, CgScal *sc, GridBar *bar)
 {
-	__shared__ double sm[2 * 32];                 // block_sum_any scratch (K <= 2, at most 32 warps)
+	__shared__ double sm[2 * 32 * kPersistMaxWarps];   // block_sum_any scratch (K <= 2)
 	__shared__ double ab[2];                      // alpha, beta of the iteration
 	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
 	const int nctas = gridDim.x;
@@ -597,7 +597,7 @@ constexpr int kBatchSlicesPerWarp = 2;     // slices (of 32 rows) per warp when 
 template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const CgJob *__restrict__ jobs, int njobs)
 {
-	__shared__ double sm[2 * 32];
+	__shared__ double sm[2 * 32 * kPersistMaxWarps];   // block_sum_any scratch (K <= 2)
 	__shared__ double ab[2];                      // alpha, beta of the iteration
 	__shared__ int jS;
 	if (threadIdx.x == 0) {                      // last job with cta0 <= blockIdx.x
@@ -713,7 +713,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 // ---------------------------------------------------------------------------
 __global__ void k_barrier_probe(double *part, GridBar *bar, int *gaveUp)
 {
-	__shared__ double sm[2 * 32];
+	__shared__ double sm[2 * 32 * kPersistMaxWarps];
 	unsigned int target = 0;
 	double v[1] = {1.0};
 	bool ok = grid_reduce<1>(v, part, blockIdx.x, gridDim.x, bar, target, sm);
