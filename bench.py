@@ -164,16 +164,27 @@ SERVED = ("Poisson stream of forward solves: 3D layered shells, icosphere level 
           "the same stream served in FP64 and in mixed precision")
 
 
-def served_requests(n: int, seed: int = 7, mean_gap_s: float = 0.04):
-    """Seeded request stream (specs + Poisson inter-arrival gaps); meshes are shared between requests."""
+SERVED_FULL = ("Poisson stream of forward solves over the whole config-5 range: 3D layered shells, icosphere "
+               "level 3-6 x 4-12 prism layers (up to 532k nodes, 2.95M tets), 20-100 steps each, random bump, "
+               "Lame and diffusivity per layer; served in FP64 and in mixed precision")
+
+
+def served_requests(n: int, seed: int = 7, mean_gap_s: float = 0.04, full: bool = False):
+    """Seeded request stream (specs + Poisson inter-arrival gaps); meshes are shared between requests.
+    full=True draws from the whole config-5 range (icosphere 3-6, 4-12 layers, 20-100 steps)."""
     import numpy as np
     from shape_atrophy_gb300 import problems
     rng = np.random.default_rng(seed)
     cache, out = {}, []
     for _ in range(n):
-        level = int(rng.choice([3, 4, 5], p=[0.4, 0.4, 0.2]))
-        layers = int(rng.choice([4, 8, 12]))
-        steps = int(rng.integers(20, 61))
+        if full:
+            level = int(rng.choice([3, 4, 5, 6], p=[0.3, 0.3, 0.25, 0.15]))
+            layers = int(rng.integers(4, 13))
+            steps = int(rng.integers(20, 101))
+        else:
+            level = int(rng.choice([3, 4, 5], p=[0.4, 0.4, 0.2]))
+            layers = int(rng.choice([4, 8, 12]))
+            steps = int(rng.integers(20, 61))
         key = (level, layers)
         if key not in cache:
             cache[key] = problems.shell_layered(level=level, lyrCntNum=layers + 1, steps=steps, native=True)
@@ -189,11 +200,11 @@ def served_requests(n: int, seed: int = 7, mean_gap_s: float = 0.04):
     return out
 
 
-def served_leg(device: int, n: int = 32):
+def served_leg(device: int, n: int = 32, full: bool = False):
     """The same Poisson stream through the continuous-batching server in FP64 and in mixed precision."""
     import numpy as np
     from shape_atrophy_gb300 import api
-    reqs = served_requests(n)
+    reqs = served_requests(n, full=full)
     runs = {}
     for prec in ("fp64", "mixed"):
         sv = api.Server(hbm_budget=200e9, max_instances=64, device=device)
@@ -220,7 +231,8 @@ def served_leg(device: int, n: int = 32):
     for a, b in zip(runs["mixed"]["res"], runs["fp64"]["res"]):
         ep = max(ep, float(np.abs(a["lmk"] - b["lmk"]).max() / np.abs(b["lmk"]).max()))
         eo = max(eo, abs(a["obj"] - b["obj"]) / abs(b["obj"]))
-    return {"workload": SERVED, "requests": n, "mean_gap_ms": 40.0, "fp64": runs["fp64"]["line"],
+    return {"workload": SERVED_FULL if full else SERVED, "requests": n, "mean_gap_ms": 40.0,
+            "fp64": runs["fp64"]["line"],
             "mixed": runs["mixed"]["line"],
             "mixed_over_fp64_solves": runs["mixed"]["line"]["solves_per_s"] / runs["fp64"]["line"]["solves_per_s"],
             "mixed_vs_fp64_max_rel_err": {"positions": ep, "objective": eo}}
@@ -283,6 +295,8 @@ def main():
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
     ap.add_argument("--no-mixed-error", action="store_true", help="skip the mixed-vs-FP64 error leg")
     ap.add_argument("--served-requests", type=int, default=32)
+    ap.add_argument("--served-full", action="store_true",
+                    help="served stream over the whole config-5 range (levels 3-6, 20-100 steps; minutes)")
     args = ap.parse_args()
     rank, local, ws, dist = dist_init()
     if args.impl == "reference":
@@ -381,7 +395,7 @@ def main():
 
     served = None
     if not args.no_served and rank == 0 and args.workload == "shell":
-        served = served_leg(local, args.served_requests)
+        served = served_leg(local, args.served_requests, full=args.served_full)
 
     mixed_error = None
     if not args.no_mixed_error and rank == 0 and args.workload == "shell":
