@@ -262,6 +262,21 @@ int sa_elmobj_view(const sa_elmobj *obj, sa_element_object *view);
 int sa_elmobj_layers(const sa_elmobj *obj, int *lyrLmkNum, int *lyrCntNum, int *elmPerLayer);
 int sa_elmobj_free(sa_elmobj *obj);
 
+/* Launch-shape tuning (process-wide; no reference counterpart).  Names:
+ * "persistMaxWarps" (1..20, warps per CTA cap of the persistent CG),
+ * "batchBlock" (128 or 256, threads per CTA of the batched CG),
+ * "batchSlicesPerWarp" (1..16, 32-row slices per warp when a batched solve's
+ * CTAs are sized), "vfdCtasPerSm" (1..32, CTAs per SM of the varifold pair
+ * sums).  shape_atrophy_gb300/autotune.py measures them on the GPU and writes
+ * shape_atrophy_gb300/tuning.json, which the Python API applies; the compiled
+ * defaults are the values measured best on GB300.  They change how partial
+ * sums are grouped: results are reproducible for a given setting.  Set them
+ * before creating sessions or servers. */
+int sa_set_tuning(const char *name, int value);
+int sa_get_tuning(const char *name, int *value);
+/* Name and SM count of a CUDA device (the key of the tuning table). */
+int sa_device_name(int device, char *buf, int len, int *smCount);
+
 /* Self-test of the bounded device-side waits (no reference counterpart).
  * Launches two cooperative CTAs on a grid barrier whose arrival count can
  * never reach its target; each CTA must give up after the 1 s limit the CG

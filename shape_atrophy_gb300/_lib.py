@@ -116,6 +116,9 @@ def load():
     lib.sa_server_result.argtypes = [vp, C.c_longlong, _dp, _dp, _dp, C.POINTER(SolveInfo), _dp]
     lib.sa_server_stats.argtypes = [vp, C.POINTER(ServerCounters)]
     lib.sa_server_destroy.argtypes = [vp]
+    lib.sa_set_tuning.argtypes = [C.c_char_p, C.c_int]
+    lib.sa_get_tuning.argtypes = [C.c_char_p, _ip]
+    lib.sa_device_name.argtypes = [C.c_int, C.c_char_p, C.c_int, _ip]
     _LIB = lib
     return lib
 

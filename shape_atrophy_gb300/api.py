@@ -19,7 +19,9 @@ Two layers:
 from __future__ import annotations
 
 import ctypes as C
+import json
 import math
+import os
 
 import numpy as np
 
@@ -27,10 +29,71 @@ from . import _lib
 
 _CTX = {}
 
+TUNING_NAMES = ("persistMaxWarps", "batchBlock", "batchSlicesPerWarp", "vfdCtasPerSm")
+TUNING_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+_TUNED = {"applied": None}
+
+
+def device_name(device: int = 0):
+    """(name, SM count) of a CUDA device: the key of the tuning table."""
+    lib = _lib.load()
+    buf = C.create_string_buffer(256)
+    sms = C.c_int()
+    rc = lib.sa_device_name(int(device), buf, 256, C.byref(sms))
+    if rc != _lib.SA_OK:
+        raise RuntimeError(f"sa_device_name failed with code {rc}")
+    return buf.value.decode(), sms.value
+
+
+def set_tuning(**values):
+    """Set launch shapes (process-wide; see TUNING_NAMES).  Raises on an unknown name or a value out of range."""
+    lib = _lib.load()
+    for k, v in values.items():
+        if lib.sa_set_tuning(k.encode(), int(v)) != _lib.SA_OK:
+            raise ValueError(f"bad tuning {k}={v}")
+
+
+def get_tuning() -> dict:
+    lib = _lib.load()
+    out = {}
+    for k in TUNING_NAMES:
+        v = C.c_int()
+        if lib.sa_get_tuning(k.encode(), C.byref(v)) != _lib.SA_OK:
+            raise RuntimeError(f"sa_get_tuning({k}) failed")
+        out[k] = v.value
+    return out
+
+
+def tuning_entry(device: int = 0, path: str = TUNING_FILE):
+    """The tuning-table entry for this device (matched by name and SM count), or None."""
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        table = json.load(f)
+    name, sms = device_name(device)
+    for e in table.get("devices", []):
+        if e.get("name") == name and int(e.get("smCount", -1)) == sms:
+            return e
+    return None
+
+
+def apply_tuning(device: int = 0, path: str = TUNING_FILE):
+    """Apply the autotuner's table for this device (compiled defaults stay when it has no entry).
+    Set SA_TUNING=off in the environment to keep the compiled defaults."""
+    if os.environ.get("SA_TUNING", "").lower() == "off":
+        return None
+    e = tuning_entry(device, path)
+    if e is not None:
+        set_tuning(**{k: e["values"][k] for k in TUNING_NAMES if k in e["values"]})
+    _TUNED["applied"] = e
+    return e
+
 
 def context(device: int = 0) -> _lib.Context:
     if device not in _CTX:
         _CTX[device] = _lib.Context(device)
+        if _TUNED["applied"] is None:
+            apply_tuning(device)
     return _CTX[device]
 
 

@@ -590,9 +590,8 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 // updated by the thread that computed its matvec entry, so only u is read
 // across threads.
 // ---------------------------------------------------------------------------
-constexpr int kBatchBlock = 256;
+constexpr int kBatchBlock = 256;           // largest CTA of the batched CG (the tuned size is at most this)
 constexpr int kBatchMinCtas = 4;
-constexpr int kBatchSlicesPerWarp = 2;     // slices (of 32 rows) per warp when a solve's CTAs are sized
 
 template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const CgJob *__restrict__ jobs, int njobs)
@@ -814,7 +813,8 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		for (int k = 0; k < 4 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
 	set_scal(sc, tolSqu, itrMax, bb, s);
 	// persistent launch: one CTA per SM, one slice per warp
-	const int pw = std::max(1, std::min(kPersistMaxWarps, (m.nslice + prof->smCount - 1) / prof->smCount));
+	const int pwCap = std::max(1, std::min(kPersistMaxWarps, tuning().persistMaxWarps));
+	const int pw = std::max(1, std::min(pwCap, (m.nslice + prof->smCount - 1) / prof->smCount));
 	const int nctas = (m.nslice + pw - 1) / pw;
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
 	                     (!block_prec<TV>() || prof->binv32) &&
@@ -1049,29 +1049,33 @@ CgState cg_state(const CgWork &w, cudaStream_t s)
 	return CgState{h.code, h.iters, h.zero, h.done, h.rr, h.bb};
 }
 
-// CTAs of k_cg_batch resident at once
+// CTAs of k_cg_batch (block threads per CTA, at most kBatchBlock) resident at once
 template <int B, typename TM, typename TV, typename TX>
-static int batch_capacity(int smCount)
+static int batch_capacity(int smCount, int block)
 {
-	static int perSm = -1;
-	if (perSm < 0) {
+	static int perSm[kBatchBlock / 32 + 1];
+	static bool known[kBatchBlock / 32 + 1] = {};
+	const int w = block / 32;
+	if (w < 1 || w > kBatchBlock / 32 || block % 32) return 0;
+	if (!known[w]) {
 		int v = 0;
-		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_batch<B, TM, TV, TX>, kBatchBlock, 0) !=
-		    cudaSuccess) {
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_batch<B, TM, TV, TX>, block, 0) != cudaSuccess) {
 			cudaGetLastError();
 			v = 0;
 		}
-		perSm = v;
+		perSm[w] = v;
+		known[w] = true;
 	}
-	return perSm * smCount;
+	return perSm[w] * smCount;
 }
 
 template <int B, typename TM, typename TV, typename TX>
 void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJobs, int maxJobs, cudaStream_t s)
 {
-	const int cap = batch_capacity<B, TM, TV, TX>(smCount);
+	const int block = std::max(32, std::min(kBatchBlock, tuning().batchBlock / 32 * 32));
+	const int cap = batch_capacity<B, TM, TV, TX>(smCount, block);
 	if (cap <= 0) throw CudaError{cudaErrorLaunchOutOfResources, "k_cg_batch occupancy"};
-	const int W = kBatchBlock / 32;
+	const int W = block / 32;
 	size_t k0 = 0;
 	while (k0 < solves.size()) {
 		// CTAs of a solve: one per kBatchSlicesPerWarp slices per warp, from its own size only (its partial
@@ -1082,7 +1086,7 @@ void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *dev
 		for (; k1 < solves.size() && (int) jobs.size() < maxJobs; ++k1) {
 			const BatchSolve &b = solves[k1];
 			const Mesh &m = *b.m;
-			const int per = W * kBatchSlicesPerWarp;
+			const int per = W * std::max(1, tuning().batchSlicesPerWarp);
 			const int want = std::max(1, std::min(cap, (m.nslice + per - 1) / per));
 			if (cta + want > cap) break;
 			CgWork &w = *b.cw;
@@ -1108,7 +1112,7 @@ void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *dev
 		int nj = (int) jobs.size();
 		const CgJob *dj = devJobs;
 		void *args[] = {(void *) &dj, (void *) &nj};
-		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_batch<B, TM, TV, TX>, dim3(cta), dim3(kBatchBlock),
+		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_batch<B, TM, TV, TX>, dim3(cta), dim3(block),
 		                                     args, 0, s));
 		// the job table is read by the kernel: wait before the host vector goes away or is rewritten
 		SA_CHECK(cudaStreamSynchronize(s));

@@ -13,6 +13,7 @@
 // reference's activity polynomials, and the velocity solved by the
 // K-preconditioned CG with the dense RKHS matrix of x_t.
 #include "sa_internal.cuh"
+#include <cstdio>
 #include <cstring>
 #include <cmath>
 #include <string>
@@ -1304,6 +1305,12 @@ struct Server {
 	}
 };
 
+Tuning &tuning()
+{
+	static Tuning t;
+	return t;
+}
+
 }  // namespace sa
 
 // ===========================================================================
@@ -1651,6 +1658,46 @@ int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs
 		SA_REQUIRE(abortFlag == 1, "the poisoned barrier did not record an abort");
 		return SA_OK;
 	});
+}
+
+
+int sa_set_tuning(const char *name, int value)
+{
+	if (!name) return SA_ERR_ARG;
+	sa::Tuning &t = sa::tuning();
+	std::string n(name);
+	if (n == "persistMaxWarps" && value >= 1 && value <= 20) t.persistMaxWarps = value;
+	else if (n == "batchBlock" && (value == 128 || value == 256)) t.batchBlock = value;
+	else if (n == "batchSlicesPerWarp" && value >= 1 && value <= 16) t.batchSlicesPerWarp = value;
+	else if (n == "vfdCtasPerSm" && value >= 1 && value <= 32) t.vfdCtasPerSm = value;
+	else return SA_ERR_ARG;
+	return SA_OK;
+}
+
+int sa_device_name(int device, char *buf, int len, int *smCount)
+{
+	if (!buf || len < 1) return SA_ERR_ARG;
+	cudaDeviceProp prop;
+	if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+		cudaGetLastError();
+		return SA_ERR_CUDA;
+	}
+	std::snprintf(buf, (size_t) len, "%s", prop.name);
+	if (smCount) *smCount = prop.multiProcessorCount;
+	return SA_OK;
+}
+
+int sa_get_tuning(const char *name, int *value)
+{
+	if (!name || !value) return SA_ERR_ARG;
+	const sa::Tuning &t = sa::tuning();
+	std::string n(name);
+	if (n == "persistMaxWarps") *value = t.persistMaxWarps;
+	else if (n == "batchBlock") *value = t.batchBlock;
+	else if (n == "batchSlicesPerWarp") *value = t.batchSlicesPerWarp;
+	else if (n == "vfdCtasPerSm") *value = t.vfdCtasPerSm;
+	else return SA_ERR_ARG;
+	return SA_OK;
 }
 
 }  // extern "C"

@@ -306,6 +306,18 @@ void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_
 // --------------------------------------------------------------------------
 constexpr int kGridBarBytes = 512;   // device memory of the persistent CG's grid barrier
 
+// Launch shapes chosen by the autotuner (shape_atrophy_gb300/autotune.py, which writes
+// shape_atrophy_gb300/tuning.json; the Python API applies it with sa_set_tuning).  The defaults are the
+// values it measured best on GB300.  They change how partial sums are grouped, so results are
+// reproducible for a given setting.
+struct Tuning {
+	int persistMaxWarps = 20;      // warps per CTA cap of the persistent CG (CTAs per SM follow)
+	int batchBlock = 256;          // threads per CTA of the batched (serving) CG: 128 or 256
+	int batchSlicesPerWarp = 2;    // 32-row slices per warp when a batched solve's CTAs are sized
+	int vfdCtasPerSm = 8;          // CTAs per SM of the varifold pair sums (column chunks)
+};
+Tuning &tuning();
+
 struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	double *r, *u, *w, *p, *sv;   // n each
 	double *part;                 // partial sums: 3 x maxBlocks

@@ -289,7 +289,8 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 	SA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 	const int blk = 128;
 	const int rowMax = std::max(Vd, Vt), colMin = std::min(Vd, Vt);
-	int C = std::max(1, (8 * sms + grid_for(rowMax, blk) - 1) / std::max(1, grid_for(rowMax, blk)));
+	const int perSm = std::max(1, tuning().vfdCtasPerSm);
+	int C = std::max(1, (perSm * sms + grid_for(rowMax, blk) - 1) / std::max(1, grid_for(rowMax, blk)));
 	C = std::min(C, std::max(1, colMin / (2 * kVfdTile)));
 	C = std::min(C, 32);
 	double *buf = nullptr;
