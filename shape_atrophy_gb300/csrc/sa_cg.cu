@@ -19,6 +19,7 @@
 // an inner CG with FP64 dot products, inside an FP64 iterative-refinement
 // loop whose residual b - A x is recomputed with the FP64 operator.
 #include "sa_internal.cuh"
+#include "sa_fixsum.cuh"
 #include <algorithm>
 #include <cmath>
 
@@ -349,8 +350,9 @@ __global__ void k_spmv64(SellOp A, const double *__restrict__ blk, const double 
 // Per iteration two grid-wide reductions (delta = (w, u); gamma = (r, u)
 // and (r, r)) double as the grid barriers that order the u reads and
 // writes: every CTA publishes its partial sums, counts itself in, waits for
-// the count of the whole grid and then adds all partials in the same fixed
-// order, so every CTA forms the same alpha, beta and stopping decision.
+// the count of the whole grid and then adds all partials exactly in 128-bit
+// fixed point (sa_fixsum.cuh: order-independent, rounded once), so every CTA
+// forms the same alpha, beta and stopping decision.
 // Waits are bounded: a CTA that waits longer than kBarWaitNs (or sees
 // another CTA give up) stops with SA_ERR_TIMEOUT.
 // ---------------------------------------------------------------------------
@@ -376,42 +378,84 @@ __device__ __forceinline__ unsigned int load_acquire(const unsigned int *p)
 	return v;
 }
 
-// block sum for a block of any multiple of 32 threads (at most 32 * kPersistMaxWarps); valid in thread 0.
-// Every thread stores its values in shared memory and warp 0 adds them (lane l takes l, l + 32, ...,
-// then a shuffle tree): one FP64 add per value instead of a five-step shuffle tree in every warp, which
-// matters on a 2 DFMA/clk/SM FP64 pipe.  sm holds K * 32 * kPersistMaxWarps doubles.
-template <int K>
-__device__ __forceinline__ void block_sum_any(double (&v)[K], double *sm)
+// Per-CTA scratch of the fixed-point reductions (K <= 2 values, up to 32 warps).
+struct FxScratch {
+	int e[2][32];          // per-warp largest exponent
+	Fx f[2][32];           // per-warp fixed-point sums
+	double tot[2];         // grid sums, broadcast to the CTA
+	int ok;                // the barrier wait ended normally
+};
+
+// Sum of K values over the threads of the CTA (any multiple of 32 threads, every thread calls), exact in
+// 128-bit fixed point (sa_fixsum.cuh), rounded once; valid in thread 0.  Integer pipes only: the FP64 pipe
+// (2 adds per clock per SM on GB300) would make a tree of FP64 adds the longest part of a grid reduction.
+template <int K, typename T>
+__device__ __forceinline__ void block_fx_sum(const T (&v)[K], FxScratch &fs, double (&out)[K])
 {
-	const int lane = threadIdx.x & 31, NT = blockDim.x;
-	for (int k = 0; k < K; ++k) sm[k * 32 * kPersistMaxWarps + threadIdx.x] = v[k];
+	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, W = blockDim.x >> 5;
+	int e[K];
+	for (int k = 0; k < K; ++k) {
+		e[k] = fx_warp_max(fx_exp(v[k]));
+		if (lane == 0) fs.e[k][wp] = e[k];
+	}
 	__syncthreads();
-	if (threadIdx.x < 32)
+	for (int k = 0; k < K; ++k) {
+		e[k] = fx_warp_max(lane < W ? fs.e[k][lane] : 1);
+		const Fx t = fx_warp_sum(fx_from(v[k], e[k]));
+		if (lane == 0) fs.f[k][wp] = t;
+	}
+	__syncthreads();
+	if (wp == 0)
 		for (int k = 0; k < K; ++k) {
-			const double *row = sm + k * 32 * kPersistMaxWarps;
-			double s = row[lane];
-			for (int q = lane + 32; q < NT; q += 32) s += row[q];
-			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-			v[k] = s;
+			const Fx t = fx_warp_sum(lane < W ? fs.f[k][lane] : fx_zero());
+			if (lane == 0) out[k] = fx_to_double(t, e[k]);
 		}
 }
 
-// sum of K values over all threads of the nctas CTAs of one solve (fixed
-// order) plus a barrier among them; lc is the CTA's index within the solve.
-// Every thread returns the sums in v.  false: the wait gave up.
-// post(sums) runs in thread 0 before the sums are broadcast (scalar work once per CTA, not per thread).
+// Sum of nctas partials of one value by one warp, in fixed point (exact, then rounded once; the same in
+// every CTA because it does not depend on the order); lane 0 returns it.
+constexpr int kFxRegs = 5;     // partials held in registers per lane (nctas <= 160); more take two passes
+__device__ __forceinline__ double warp_fx_partials(const double *part, int nctas)
+{
+	const int lane = threadIdx.x & 31;
+	Fx t = fx_zero();
+	int em;
+	if (nctas <= 32 * kFxRegs) {
+		double r[kFxRegs];
+		int e = 1;
+#pragma unroll
+		for (int q = 0; q < kFxRegs; ++q) {
+			const int b = lane + 32 * q;
+			r[q] = b < nctas ? __ldcg(part + b) : 0.0;
+			e = max(e, fx_exp(r[q]));
+		}
+		em = fx_warp_max(e);
+#pragma unroll
+		for (int q = 0; q < kFxRegs; ++q) t = fx_add(t, fx_from(r[q], em));
+	} else {
+		int e = 1;
+		for (int b = lane; b < nctas; b += 32) e = max(e, fx_exp(__ldcg(part + b)));
+		em = fx_warp_max(e);
+		for (int b = lane; b < nctas; b += 32) t = fx_add(t, fx_from(__ldcg(part + b), em));
+	}
+	t = fx_warp_sum(t);
+	return fx_to_double(t, em);
+}
+
+// sum of K values over all threads of the nctas CTAs of one solve plus a barrier among them; lc is the
+// CTA's index within the solve.  Every thread gets the sums in res.  false: the wait gave up.
+// post(sums) runs once per CTA (lane 0 of warp 0) before the sums are broadcast.
 struct NoPost { __device__ void operator()(const double *) const {} };
 
-template <int K, typename Post = NoPost>
-__device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int lc, int nctas, GridBar *bar,
-                                            unsigned int &target, double *sm, Post post = Post())
+template <int K, typename T, typename Post = NoPost>
+__device__ __forceinline__ bool grid_reduce(const T (&v)[K], double (&res)[K], double *part, int lc, int nctas,
+                                            GridBar *bar, unsigned int &target, FxScratch &fs, Post post = Post())
 {
-	__shared__ int okS;
-	__shared__ double tot[K];
-	block_sum_any<K>(v, sm);
+	double cta[K];
+	block_fx_sum<K, T>(v, fs, cta);
 	target += (unsigned int) nctas;
 	if (threadIdx.x == 0) {
-		for (int k = 0; k < K; ++k) part[k * nctas + lc] = v[k];
+		for (int k = 0; k < K; ++k) part[k * nctas + lc] = cta[k];
 		__threadfence();
 		atomicAdd(&bar->count, 1u);
 		int ok = 1;
@@ -421,23 +465,18 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[K], double *part, int lc
 			if (global_ns() - t0 > kBarWaitNs) { atomicExch(&bar->abort, 1u); ok = 0; break; }
 		}
 		__threadfence();
-		okS = ok;
+		fs.ok = ok;
 	}
 	__syncthreads();
-	if (!okS) return false;
-	if (threadIdx.x < 32) {
-		const int lane = threadIdx.x;
-		for (int k = 0; k < K; ++k) {
-			double s = 0.0;
-#pragma unroll 8
-			for (int b = lane; b < nctas; b += 32) s += __ldcg(part + (long) k * nctas + b);
-			for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-			if (lane == 0) tot[k] = s;
-		}
-		if (lane == 0) post(tot);
+	if (!fs.ok) return false;
+	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, W = blockDim.x >> 5;
+	for (int k = wp; k < K; k += W) {            // one warp per value
+		const double t = warp_fx_partials(part + (long) k * nctas, nctas);
+		if (lane == 0) fs.tot[k] = t;
 	}
+	if (threadIdx.x == 0) post(fs.tot);          // K == 1 with a post: warp 0 wrote tot[0] itself
 	__syncthreads();
-	for (int k = 0; k < K; ++k) v[k] = tot[k];
+	for (int k = 0; k < K; ++k) res[k] = fs.tot[k];
 	return true;
 }
 
@@ -453,6 +492,15 @@ __device__ __forceinline__ void cg_step_lengths(double delta, double gam, double
 	}
 	out[0] = alpha;
 	out[1] = beta;
+}
+
+// the (at most 3-term) dot product of one row, in the vector type
+template <int B, typename TV>
+__device__ __forceinline__ TV row_dot(const TV (&a)[B], const TV (&b)[B])
+{
+	TV s = a[0] * b[0];
+	for (int c = 1; c < B; ++c) s += a[c] * b[c];
+	return s;
 }
 
 // a row's contribution to a dot product: FP64 operands fold each product into the FP64 sum; FP32
@@ -487,7 +535,7 @@ __global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
 k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, const TV *__restrict__ binv, TX *x,
              const TV *r0, TV *u, double *part, CgScal *sc, GridBar *bar)
 {
-	__shared__ double sm[2 * 32 * kPersistMaxWarps];   // block_sum_any scratch (K <= 2)
+	__shared__ FxScratch fs;                      // grid-reduction scratch
 	__shared__ double ab[2];                      // alpha, beta of the iteration
 	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
 	const int nctas = gridDim.x;
@@ -529,22 +577,24 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 		}
 		if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
 		TV wv[B];
-		double d1[1] = {0.0};
+		TV d1[1] = {(TV) 0};
+		double g1[1];
 		for (int c = 0; c < B; ++c) wv[c] = acc0[c] + acc1[c];
-		if (own) dot_row<B, TV>(d1[0], wv, uv);
-		if (!grid_reduce<1>(d1, part, blockIdx.x, nctas, bar, target, sm, [&](const double *t) {
+		if (own) d1[0] = row_dot<B, TV>(wv, uv);
+		if (!grid_reduce<1, TV>(d1, g1, part, blockIdx.x, nctas, bar, target, fs, [&](const double *t) {
 			    cg_step_lengths(t[0], gam, gamPrev, alphaPrev, first, ab);
 		    })) {
 			code = SA_ERR_TIMEOUT;
 			break;
 		}
-		const double delta = d1[0], alpha = ab[0], beta = ab[1];
+		const double delta = g1[0], alpha = ab[0], beta = ab[1];
 		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
 			code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
 			break;
 		}
 		// p, s, x, r, u of the own row; (r, u) and (r, r)
-		double d2[2] = {0.0, 0.0};
+		TV d2[2] = {(TV) 0, (TV) 0};
+		double g2[2];
 		if (own) {
 			const TV al = (TV) alpha, be = (TV) beta;
 			for (int c = 0; c < B; ++c) {
@@ -556,16 +606,16 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			if constexpr (kBlk) prec_block<B, TV>(bv, rv, uv);
 			else for (int c = 0; c < B; ++c) uv[c] = dv[c] * rv[c];
 			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uv[c];
-			dot_row<B, TV>(d2[0], rv, uv);
-			dot_row<B, TV>(d2[1], rv, rv);
+			d2[0] = row_dot<B, TV>(rv, uv);
+			d2[1] = row_dot<B, TV>(rv, rv);
 		}
-		if (!grid_reduce<2>(d2, part + nctas, blockIdx.x, nctas, bar, target, sm)) {
+		if (!grid_reduce<2, TV>(d2, g2, part + nctas, blockIdx.x, nctas, bar, target, fs)) {
 			code = SA_ERR_TIMEOUT;
 			break;
 		}
 		gamPrev = gam;
-		gam = d2[0];
-		rr = d2[1];
+		gam = g2[0];
+		rr = g2[1];
 		alphaPrev = alpha;
 		first = false;
 		++it;
@@ -596,7 +646,7 @@ constexpr int kBatchMinCtas = 4;
 template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const CgJob *__restrict__ jobs, int njobs)
 {
-	__shared__ double sm[2 * 32 * kPersistMaxWarps];   // block_sum_any scratch (K <= 2)
+	__shared__ FxScratch fs;                      // grid-reduction scratch
 	__shared__ double ab[2];                      // alpha, beta of the iteration
 	__shared__ int jS;
 	if (threadIdx.x == 0) {                      // last job with cta0 <= blockIdx.x
@@ -655,13 +705,14 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 				dot_row<B, TV>(d1[0], o, ui);
 			}
 		}
-		if (!grid_reduce<1>(d1, part, lc, nctas, bar, target, sm, [&](const double *t) {
+		double g1[1];
+		if (!grid_reduce<1, double>(d1, g1, part, lc, nctas, bar, target, fs, [&](const double *t) {
 			    cg_step_lengths(t[0], gam, gamPrev, alphaPrev, first, ab);
 		    })) {
 			code = SA_ERR_TIMEOUT;
 			break;
 		}
-		const double delta = d1[0], alpha = ab[0], beta = ab[1];
+		const double delta = g1[0], alpha = ab[0], beta = ab[1];
 		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
 			code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
 			break;
@@ -688,10 +739,11 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 			dot_row<B, TV>(d2[0], rk, uk);
 			dot_row<B, TV>(d2[1], rk, rk);
 		}
-		if (!grid_reduce<2>(d2, part + nctas, lc, nctas, bar, target, sm)) { code = SA_ERR_TIMEOUT; break; }
+		double g2[2];
+		if (!grid_reduce<2, double>(d2, g2, part + nctas, lc, nctas, bar, target, fs)) { code = SA_ERR_TIMEOUT; break; }
 		gamPrev = gam;
-		gam = d2[0];
-		rr = d2[1];
+		gam = g2[0];
+		rr = g2[1];
 		alphaPrev = alpha;
 		first = false;
 		++it;
@@ -712,10 +764,10 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 // ---------------------------------------------------------------------------
 __global__ void k_barrier_probe(double *part, GridBar *bar, int *gaveUp)
 {
-	__shared__ double sm[2 * 32 * kPersistMaxWarps];
+	__shared__ FxScratch fs;
 	unsigned int target = 0;
-	double v[1] = {1.0};
-	bool ok = grid_reduce<1>(v, part, blockIdx.x, gridDim.x, bar, target, sm);
+	double v[1] = {1.0}, t[1];
+	bool ok = grid_reduce<1, double>(v, t, part, blockIdx.x, gridDim.x, bar, target, fs);
 	if (threadIdx.x == 0 && !ok) atomicAdd(gaveUp, 1);
 }
 
