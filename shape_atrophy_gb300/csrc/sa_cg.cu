@@ -346,7 +346,8 @@ __global__ void k_spmv64(SellOp A, const double *__restrict__ blk, const double 
 // owns one row (3 entries for the velocity, 1 for reaction-diffusion) and
 // keeps x, r, u, p, s and D^{-1} of that row in registers; only u goes
 // through global memory, because the matvec gathers the neighbours' u.
-// One CTA per SM (up to kPersistMaxWarps warps, one 32-row slice per warp).
+// One CTA per SM (up to kPersistMaxWarps warps: one 32-row slice per row
+// warp plus one reducer warp that does the grid-wide work, see below).
 // Per iteration two grid-wide reductions (delta = (w, u); gamma = (r, u)
 // and (r, r)) double as the grid barriers that order the u reads and
 // writes: every CTA publishes its partial sums, counts itself in, waits for
@@ -387,10 +388,10 @@ struct FxScratch {
 };
 
 // Sum of K values over the threads of the CTA (any multiple of 32 threads, every thread calls), exact in
-// 128-bit fixed point (sa_fixsum.cuh), rounded once; valid in thread 0.  Integer pipes only: the FP64 pipe
+// 128-bit fixed point (sa_fixsum.cuh), rounded once; valid in lane 0 of warp sumWarp.  Integer pipes only: the FP64 pipe
 // (2 adds per clock per SM on GB300) would make a tree of FP64 adds the longest part of a grid reduction.
 template <int K, typename T>
-__device__ __forceinline__ void block_fx_sum(const T (&v)[K], FxScratch &fs, double (&out)[K])
+__device__ __forceinline__ void block_fx_sum(const T (&v)[K], FxScratch &fs, double (&out)[K], int sumWarp = 0)
 {
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, W = blockDim.x >> 5;
 	int e[K];
@@ -405,7 +406,7 @@ __device__ __forceinline__ void block_fx_sum(const T (&v)[K], FxScratch &fs, dou
 		if (lane == 0) fs.f[k][wp] = t;
 	}
 	__syncthreads();
-	if (wp == 0)
+	if (wp == sumWarp)
 		for (int k = 0; k < K; ++k) {
 			const Fx t = fx_warp_sum(lane < W ? fs.f[k][lane] : fx_zero());
 			if (lane == 0) out[k] = fx_to_double(t, e[k]);
@@ -530,26 +531,50 @@ __device__ __forceinline__ void spmv_slot_cg(const SellOp &A, const TM *__restri
 		for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
 }
 
+// One reducer warp per CTA (the last warp, no rows) takes the grid-wide parts of the iteration off the
+// rows' critical path: while the row warps run the matvec it adds up the (r, u), (r, r) partials of the
+// previous update and forms beta and the constant part of alpha; while they update p and s it publishes
+// the CTA's (w, u), waits for the grid and forms alpha.  The row warps wait only for the barrier that makes
+// u complete (before the matvec) and for alpha (before x, r, u).  The convergence test of an update runs
+// after the next matvec (that matvec is discarded), so iterates and iteration counts are those of the
+// plain Chronopoulos-Gear loop.
+__device__ __forceinline__ bool wait_grid(GridBar *bar, unsigned int target)
+{
+	const unsigned long long t0 = global_ns();
+	while ((int) (load_acquire(&bar->count) - target) < 0) {
+		if (load_acquire(&bar->abort)) return false;
+		if (global_ns() - t0 > kBarWaitNs) { atomicExch(&bar->abort, 1u); return false; }
+	}
+	return true;
+}
+
 template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
 k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, const TV *__restrict__ binv, TX *x,
              const TV *r0, TV *u, double *part, CgScal *sc, GridBar *bar)
 {
-	__shared__ FxScratch fs;                      // grid-reduction scratch
-	__shared__ double ab[2];                      // alpha, beta of the iteration
+	__shared__ FxScratch fs;                     // block sums; fs.tot = gamma, rr of the last update
+	__shared__ double nx[4];                     // next gamma, rr, beta, beta * gamma / alphaPrev
+	__shared__ double al[2];                     // alpha, delta of the iteration
+	__shared__ int gaveUp;
 	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
-	const int nctas = gridDim.x;
+	const int nctas = gridDim.x, lc = blockIdx.x;
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-	const int sl = blockIdx.x * (blockDim.x >> 5) + wp;
+	const int H = (blockDim.x >> 5) - 1;         // the reducer warp; warps 0 .. H-1 own one slice each
+	const bool reducer = wp == H;
+	const int sl = lc * H + wp;
 	const int nsl = (A.N + 31) >> 5;
 	const int i = sl * 32 + lane;
-	const bool own = sl < nsl && i < A.N;
-	const int wdt = sl < nsl ? __ldg(A.width + sl) : 0;
-	const long base = sl < nsl ? __ldg(A.off + sl) + lane : 0;
+	const bool rowWarp = !reducer && sl < nsl;
+	const bool own = rowWarp && i < A.N;
+	const int wdt = rowWarp ? __ldg(A.width + sl) : 0;
+	const long base = rowWarp ? __ldg(A.off + sl) + lane : 0;
 	const double bb = sc->bb, tolSqu = sc->tolSqu;
 	const int itrMax = sc->itrMax;
-	double gam = sc->gam, rr = sc->rr, gamPrev = 0.0, alphaPrev = 1.0;
+	double gam = sc->gam, rr = sc->rr, alpha = 1.0, beta = 0.0;
+	double *partD = part, *partG = part + nctas;  // (w, u) partials; (r, u) then (r, r) partials
 	unsigned int target = 0;                     // bar->count is zeroed before the launch
+	if (threadIdx.x == 0) gaveUp = 0;
 	TX xv[B];
 	// block-Jacobi for FP32 vectors (the mixed inner solves, binv given); FP64 point Jacobi
 	constexpr bool kBlk = block_prec<TV>();
@@ -565,67 +590,113 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	if constexpr (kBlk)
 		for (int t = 0; t < kBV; ++t) bv[t] = own ? binv[(long) i * B * B + t] : (TV) 0;
 	int it = 0, code = SA_OK;
-	bool first = true;
+	bool first = true, pending = false;
 	for (;;) {
-		// w = A u and (w, u)
-		TV acc0[B], acc1[B];
-		for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
-		int k = 0;
-		for (; k + 2 <= wdt; k += 2) {
-			spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
-			spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), acc1);
-		}
-		if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+		// (1) rows: w = A u and (w, u).  Reducer: the sums of the last update, beta, beta * gamma / alpha
 		TV wv[B];
 		TV d1[1] = {(TV) 0};
-		double g1[1];
-		for (int c = 0; c < B; ++c) wv[c] = acc0[c] + acc1[c];
-		if (own) d1[0] = row_dot<B, TV>(wv, uv);
-		if (!grid_reduce<1, TV>(d1, g1, part, blockIdx.x, nctas, bar, target, fs, [&](const double *t) {
-			    cg_step_lengths(t[0], gam, gamPrev, alphaPrev, first, ab);
-		    })) {
-			code = SA_ERR_TIMEOUT;
-			break;
+		for (int c = 0; c < B; ++c) wv[c] = (TV) 0;
+		if (rowWarp) {
+			TV acc0[B], acc1[B];
+			for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
+			int k = 0;
+			for (; k + 2 <= wdt; k += 2) {
+				spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+				spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), acc1);
+			}
+			if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+			for (int c = 0; c < B; ++c) wv[c] = acc0[c] + acc1[c];
+			if (own) d1[0] = row_dot<B, TV>(wv, uv);
+		} else if (pending) {
+			// one set after the other: the loads are hidden behind the rows' matvec, registers are not spare
+			const double g = warp_fx_partials(partG, nctas);
+			const double q = warp_fx_partials(partG + nctas, nctas);
+			if (lane == 0) {
+				nx[0] = g;
+				nx[1] = q;
+				nx[2] = g / gam;                     // beta
+				nx[3] = nx[2] * g / alpha;           // the part of alpha's denominator known before delta
+			}
 		}
-		const double delta = g1[0], alpha = ab[0], beta = ab[1];
-		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
-			code = isfinite(delta) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
-			break;
+		double cta1[1];
+		block_fx_sum<1, TV>(d1, fs, cta1, H);     // its barriers also publish nx
+		if (pending) {
+			gam = nx[0];
+			rr = nx[1];
+			first = false;
+			++it;
+			if (!isfinite(gam) || !isfinite(rr)) { code = SA_ERR_NONFINITE; break; }
+			if (rr < tolSqu * bb) { code = SA_OK; break; }
+			if (it >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
 		}
-		// p, s, x, r, u of the own row; (r, u) and (r, r)
-		TV d2[2] = {(TV) 0, (TV) 0};
-		double g2[2];
-		if (own) {
-			const TV al = (TV) alpha, be = (TV) beta;
+		beta = first ? 0.0 : nx[2];
+		// (2) reducer: publish (w, u), wait for the grid, alpha.  Rows meanwhile: p and s
+		target += (unsigned int) nctas;
+		if (reducer) {
+			int ok = 1;
+			if (lane == 0) {
+				partD[lc] = cta1[0];
+				__threadfence();
+				atomicAdd(&bar->count, 1u);
+				ok = wait_grid(bar, target) ? 1 : 0;
+				__threadfence();
+			}
+			ok = __shfl_sync(0xffffffffu, ok, 0);
+			__syncwarp();                        // orders lane 0's acquire before the other lanes' loads
+			if (ok) {
+				const double delta = warp_fx_partials(partD, nctas);
+				if (lane == 0) {
+					al[0] = first ? gam / delta : gam / (delta - nx[3]);
+					al[1] = delta;
+				}
+			} else if (lane == 0) {
+				gaveUp = 1;
+			}
+		} else if (own) {
+			const TV be = (TV) beta;
 			for (int c = 0; c < B; ++c) {
 				pv[c] = uv[c] + be * pv[c];
 				sv[c] = wv[c] + be * sv[c];
-				xv[c] = xv[c] + (TX) al * (TX) pv[c];
-				rv[c] = rv[c] - al * sv[c];
 			}
+		}
+		__syncthreads();
+		if (gaveUp) { code = SA_ERR_TIMEOUT; break; }
+		alpha = al[0];
+		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
+			code = isfinite(al[1]) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
+			break;
+		}
+		// (3) rows: x, r, u and (r, u), (r, r); the reducer publishes them and waits for the grid (u complete)
+		TV d2[2] = {(TV) 0, (TV) 0};
+		const TV al_ = (TV) alpha;
+		if (own) {
+			for (int c = 0; c < B; ++c) rv[c] = rv[c] - al_ * sv[c];
 			if constexpr (kBlk) prec_block<B, TV>(bv, rv, uv);
 			else for (int c = 0; c < B; ++c) uv[c] = dv[c] * rv[c];
 			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uv[c];
 			d2[0] = row_dot<B, TV>(rv, uv);
 			d2[1] = row_dot<B, TV>(rv, rv);
 		}
-		if (!grid_reduce<2, TV>(d2, g2, part + nctas, blockIdx.x, nctas, bar, target, fs)) {
-			code = SA_ERR_TIMEOUT;
-			break;
+		double cta2[2];
+		block_fx_sum<2, TV>(d2, fs, cta2, H);
+		target += (unsigned int) nctas;
+		if (reducer && lane == 0) {
+			partG[lc] = cta2[0];
+			partG[nctas + lc] = cta2[1];
+			__threadfence();
+			atomicAdd(&bar->count, 1u);
+			if (!wait_grid(bar, target)) gaveUp = 1;
+			__threadfence();
+		} else if (own) {
+			for (int c = 0; c < B; ++c) xv[c] = xv[c] + (TX) al_ * (TX) pv[c];   // while the reducer waits
 		}
-		gamPrev = gam;
-		gam = g2[0];
-		rr = g2[1];
-		alphaPrev = alpha;
-		first = false;
-		++it;
-		if (!isfinite(gam) || !isfinite(rr)) { code = SA_ERR_NONFINITE; break; }
-		if (rr < tolSqu * bb) { code = SA_OK; break; }
-		if (it >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
+		__syncthreads();
+		if (gaveUp) { code = SA_ERR_TIMEOUT; break; }
+		pending = true;
 	}
 	if (own)
 		for (int c = 0; c < B; ++c) x[(long) i * B + c] = xv[c];
-	if (blockIdx.x == 0 && threadIdx.x == 0) {
+	if (lc == 0 && threadIdx.x == 0) {
 		sc->iters = it; sc->code = code; sc->rr = rr; sc->gam = gam; sc->done = 1;
 	}
 }
@@ -864,13 +935,13 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	if (timing && !prof->ev[0])
 		for (int k = 0; k < 4 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
 	set_scal(sc, tolSqu, itrMax, bb, s);
-	// persistent launch: one CTA per SM, one slice per warp
-	const int pwCap = std::max(1, std::min(kPersistMaxWarps, tuning().persistMaxWarps));
+	// persistent launch: one CTA per SM, one slice per row warp plus the reducer warp
+	const int pwCap = std::max(1, std::min(kPersistMaxWarps, tuning().persistMaxWarps) - 1);
 	const int pw = std::max(1, std::min(pwCap, (m.nslice + prof->smCount - 1) / prof->smCount));
 	const int nctas = (m.nslice + pw - 1) / pw;
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
 	                     (!block_prec<TV>() || prof->binv32) &&
-	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw);
+	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw + 1);
 	if (persist) {
 		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first).  FP32
 		// inner solves of mixed precision are block-Jacobi preconditioned (3x3 node blocks)
@@ -889,7 +960,7 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		                (void *) &part, (void *) &sc, (void *) &bar};
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
 		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
-		                                     dim3(32 * pw), args, 0, s));
+		                                     dim3(32 * (pw + 1)), args, 0, s));
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[1], s));
 		k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
 		prof->launches += 3;

@@ -14,6 +14,7 @@
 // K-preconditioned CG with the dense RKHS matrix of x_t.
 #include "sa_internal.cuh"
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <cmath>
 #include <string>
@@ -51,7 +52,12 @@ struct Pool {                 // device allocations of one call, freed at the en
 	cudaStream_t s;
 	size_t bytes = 0;         // device bytes allocated
 	explicit Pool(cudaStream_t st) : s(st) {}
-	~Pool() { for (void *p : ptrs) cudaFree(p); }
+	~Pool() { release(); }
+	void release()
+	{
+		for (void *p : ptrs) cudaFree(p);
+		ptrs.clear();
+	}
 	template <typename T> T *alloc(size_t n)
 	{
 		void *p = nullptr;
@@ -73,6 +79,27 @@ struct Pool {                 // device allocations of one call, freed at the en
 		T *d = alloc<T>(n);
 		SA_CHECK(cudaMemcpyAsync(d, p, sizeof(T) * n, cudaMemcpyHostToDevice, s));
 		return d;
+	}
+};
+
+// Host-side phase timing of the one-call entry points, printed to stderr when the environment variable
+// SA_TRACE is set (each mark waits for the stream, so traced calls run slightly slower).
+struct PhaseTrace {
+	bool on;
+	cudaStream_t s;
+	std::chrono::steady_clock::time_point t0;
+	explicit PhaseTrace(cudaStream_t st) : on(std::getenv("SA_TRACE") != nullptr), s(st)
+	{
+		if (on) t0 = std::chrono::steady_clock::now();
+	}
+	void mark(const char *phase)
+	{
+		if (!on) return;
+		cudaStreamSynchronize(s);
+		const auto t = std::chrono::steady_clock::now();
+		std::fprintf(stderr, "[sa_trace] %-30s %9.3f ms\n", phase,
+		             std::chrono::duration<double, std::milli>(t - t0).count());
+		t0 = t;
 	}
 };
 
@@ -125,7 +152,7 @@ __global__ void k_init_sign(int E, const int *__restrict__ elmVtx, const double 
 }
 
 static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool needGrad, bool layered, int lyrNum,
-                       Pool &P)
+                       Pool &P, PhaseTrace *tr = nullptr)
 {
 	cudaStream_t s = P.s;
 	int D = o->dim;
@@ -170,6 +197,7 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		m.elmLyr = (int *) P.dev(o->elmLyrVec, (size_t) m.E);
 	}
 
+	if (tr) tr->mark("mesh: upload");
 	// host-side validation of every index (one pass over each array)
 	std::vector<int> ev = to_host(m.elmVtx, (size_t) m.E * m.V, s);
 	for (int v : ev) SA_REQUIRE(v >= 0 && v < m.N, "elmVtxMat index out of range");
@@ -245,6 +273,7 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		std::vector<int> ly = to_host(m.elmLyr, (size_t) m.E, s);
 		for (int v : ly) SA_REQUIRE(v >= 0 && v < lyrNum, "elmLyrVec entry outside the layer tables");
 	}
+	if (tr) tr->mark("mesh: validate");
 	m.rowPtr = P.alloc<int>(m.N + 1);
 	SA_CHECK(cudaMemcpyAsync(m.rowPtr, rp.data(), sizeof(int) * (m.N + 1), cudaMemcpyHostToDevice, s));
 	{   // sliced layout: 32-row slices, slot k of row 32 s + lane at off[s] + 32 k + lane
@@ -307,6 +336,7 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		SA_CHECK(cudaMemcpyAsync(m.slDest, dest.data(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaStreamSynchronize(s));      // host vectors go out of scope
 	}
+	if (tr) tr->mark("mesh: sliced layout, transposes");
 	m.asmCols = maxAdj;
 	m.asmTab = P.alloc<int>((size_t) std::max(1, maxAdj) * m.Z);
 	int *bad = P.zeros<int>(1);
@@ -316,6 +346,7 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 	SA_CHECK(cudaStreamSynchronize(s));
 	SA_REQUIRE(hbad == 0, "femIfoMat lists an element that does not contain both nodes of the slot");
 	m.sign0 = P.alloc<signed char>(m.E);
+	if (tr) tr->mark("mesh: assembly table");
 }
 
 // ---------------------------------------------------------------------------
@@ -579,11 +610,13 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
                         double *tauMat, double *objVec, sa_solve_info *info)
 {
 	cudaStream_t s = ctx->stream;
+	PhaseTrace tr(s);
 	Pool P(s);
 	Mesh m;
 	Model md;
 	fill_model(md, D, prm, tgt, P);
-	build_mesh(m, obj, tgt != nullptr, false, !md.frame, md.lyrNum, P);
+	tr.mark("model");
+	build_mesh(m, obj, tgt != nullptr, false, !md.frame, md.lyrNum, P, &tr);
 	if (md.frame || md.ldmWgt != 0.0)
 		SA_REQUIRE((size_t) m.N * m.N * sizeof(double) <= kDenseLimitBytes && m.N <= 65535,
 		           "dense RKHS kernel matrix exceeds the device budget for this node count");
@@ -607,6 +640,7 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 	}
 	std::vector<double> objs(objNum, 0.0);
 	SolveOut last{};
+	tr.mark("inputs, work buffers");
 	VfdTargetCache vcache;                    // target-target varifold rows, shared by the columns
 	if (tgt) { vcache.rows = P.alloc<double>((size_t) tgt->tgtElmNum); vcache.capacity = tgt->tgtElmNum; }
 	SA_CHECK(cudaEventRecord(ctx->e0, s));
@@ -630,11 +664,13 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 	SA_CHECK(cudaEventSynchronize(ctx->e1));
 	float ms = 0.f;
 	cudaEventElapsedTime(&ms, ctx->e0, ctx->e1);
+	tr.mark("solve, objective");
 	long n = (long) m.N * D;
 	if (lmkStk) SA_CHECK(cudaMemcpyAsync(lmkStk, w.trajX, sizeof(double) * n * md.timeNum, cudaMemcpyDefault, s));
 	if (tauMat) SA_CHECK(cudaMemcpyAsync(tauMat, w.trajT, sizeof(double) * m.N * md.timeNum, cudaMemcpyDefault, s));
 	if (objVec) SA_CHECK(cudaMemcpyAsync(objVec, objs.data(), sizeof(double) * objNum, cudaMemcpyDefault, s));
 	SA_CHECK(cudaStreamSynchronize(s));
+	tr.mark("download");
 	if (info) {
 		info->status = last.status;
 		info->cgIterTotal = last.cgTotal;
@@ -642,6 +678,10 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 		info->cgIterMax = last.cgMax;
 		info->invertedElements = last.inverted;
 		info->elapsedMs = ms;
+	}
+	if (tr.on) {
+		P.release();
+		tr.mark("free");
 	}
 	return SA_OK;
 }
