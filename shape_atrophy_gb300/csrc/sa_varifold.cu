@@ -24,24 +24,26 @@ namespace sa {
 
 constexpr int kVfdTile = 128;
 
-template <typename T>
-__device__ __forceinline__ T cen_knl(int type, T w, T d2, T &d1)
+// Kernel values with the widths' reciprocals iw = 1/w, iw2 = 1/w^2 precomputed (no division per pair: FP64
+// divisions cost about ten FP64-pipe instructions each on GB300); derivatives d1 only when G (gradient).
+template <typename T, bool G>
+__device__ __forceinline__ T cen_knl(int type, T iw, T iw2, T d2, T &d1)
 {
-	if (type == 'G') { T k = exp(-d2 / (w * w)); d1 = (T) -2.0 * k / (w * w); return k; }
-	if (type == 'C') { T k = (T) 1.0 / ((T) 1.0 + d2 / (w * w)); d1 = (T) -2.0 * k * k / (w * w); return k; }
-	T r = sqrt(d2) / w, ex = exp(-r);           // 'M'
-	d1 = -ex / (w * w);
+	if (type == 'G') { T k = exp(-d2 * iw2); if (G) d1 = (T) -2.0 * k * iw2; return k; }
+	if (type == 'C') { T k = (T) 1.0 / ((T) 1.0 + d2 * iw2); if (G) d1 = (T) -2.0 * k * k * iw2; return k; }
+	T r = sqrt(d2) * iw, ex = exp(-r);          // 'M'
+	if (G) d1 = -ex * iw2;
 	return ((T) 1.0 + r) * ex;
 }
 
-template <typename T>
-__device__ __forceinline__ T dir_knl(int type, T w, T ang, T &d1)
+template <typename T, bool G>
+__device__ __forceinline__ T dir_knl(int type, T iw2, T ang, T &d1)
 {
-	if (type == 'B') { d1 = (T) 2.0 * ang; return ang * ang; }
-	if (type == 'L') { d1 = (T) 1.0; return ang; }
-	if (type == 'O') { T k = exp((T) 2.0 * (ang - (T) 1.0) / (w * w)); d1 = (T) 2.0 * k / (w * w); return k; }
-	T k = exp((T) 2.0 * (ang * ang - (T) 1.0) / (w * w));     // 'U'
-	d1 = (T) 4.0 * ang * k / (w * w);
+	if (type == 'B') { if (G) d1 = (T) 2.0 * ang; return ang * ang; }
+	if (type == 'L') { if (G) d1 = (T) 1.0; return ang; }
+	if (type == 'O') { T k = exp((T) 2.0 * (ang - (T) 1.0) * iw2); if (G) d1 = (T) 2.0 * k * iw2; return k; }
+	T k = exp((T) 2.0 * (ang * ang - (T) 1.0) * iw2);     // 'U'
+	if (G) d1 = (T) 4.0 * ang * k * iw2;
 	return k;
 }
 
@@ -80,10 +82,10 @@ struct VfdSet { const double *cen, *dir, *vol; int n; };
 // k_vfd_chunks.  One chunk: the reference's per-row order exactly.
 // symA != 0 (objective only, set A is the row set itself): K is symmetric, so row i takes the pairs
 // j >= i of set A with weight 2 (1 on the diagonal) -- the same total with half the pair evaluations.
-template <int D, typename T>
+template <int D, typename T, bool G>
 __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, int ck, double cw, int dk,
-                           double dw, double *__restrict__ out, int grad, double *__restrict__ dc,
-                           double *__restrict__ dt, int symA = 0)
+                           double dw, double *__restrict__ out, double *__restrict__ dc, double *__restrict__ dt,
+                           int symA = 0)
 {
 	constexpr bool kSplit = sizeof(T) < sizeof(double);     // two-float centres in FP32
 	__shared__ T sc[kVfdTile * D], su[kVfdTile * D], sv[kVfdTile], sl[kSplit ? kVfdTile * D : 1];
@@ -100,13 +102,13 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 	const T nLen = (D == 2 ? vi : (T) 2.0 * vi), half = (D == 2 ? (T) 1.0 : (T) 0.5);
 	double acc = 0.0, gc[D], gt[D];
 	for (int d = 0; d < D; ++d) { gc[d] = 0.0; gt[d] = 0.0; }
-	const T cwT = (T) cw, dwT = (T) dw;
+	const T ciw = (T) (1.0 / cw), ciw2 = (T) (1.0 / (cw * cw)), diw2 = (T) (1.0 / (dw * dw));
 	const int C = gridDim.y, cy = blockIdx.y;
 	out += (long) cy * R.n;
-	if (grad) { dc += (long) cy * D * R.n; dt += (long) cy * D * R.n; }
+	if (G) { dc += (long) cy * D * R.n; dt += (long) cy * D * R.n; }
 	for (int set = 0; set < 2; ++set) {
 		const VfdSet &S = set == 0 ? A : Bs;
-		T coef = (T) (set == 0 ? cA : cB);
+		const T coef = (T) (set == 0 ? cA : cB), cv = coef * vi;
 		const bool sym = set == 0 && symA;
 		const int lo = sym ? (int) (blockIdx.x * blockDim.x) : 0;   // columns below the CTA's rows: none
 		const int span = S.n > lo ? S.n - lo : 0;
@@ -146,11 +148,11 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 				for (int d = 1; d < D; ++d) d2 = d2 + df[d] * df[d];
 				T ang = ui[0] * su[jj * D];
 				for (int d = 1; d < D; ++d) ang = ang + ui[d] * su[jj * D + d];
-				T d1c, d1d;
-				T kc = cen_knl<T>(ck, cwT, d2, d1c);
-				T kd = dir_knl<T>(dk, dwT, ang, d1d);
+				T d1c = 0, d1d = 0;
+				T kc = cen_knl<T, G>(ck, ciw, ciw2, d2, d1c);
+				T kd = dir_knl<T, G>(dk, diw2, ang, d1d);
 				T vj = sv[jj];
-				const T term = wgt * coef * kc * kd * vi * vj;
+				const T term = wgt * cv * kc * kd * vj;
 				if (kSplit) {                  // Kahan: the FP32 tile sum keeps its lost low bits
 					T y = term - comp, t = tile + y;
 					comp = (t - tile) - y;
@@ -158,7 +160,7 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 				} else {
 					tile += term;
 				}
-				if (grad) {
+				if (G) {
 					// geometricFunction/grassmanFunction gradients and dqVfd_DD_DT accumulation
 					for (int d = 0; d < D; ++d) {
 						T dK = d1c * df[d];
@@ -169,12 +171,12 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 				}
 			}
 			acc += (double) tile;
-			if (grad) for (int d = 0; d < D; ++d) { gc[d] += (double) tgc[d]; gt[d] += (double) tgt[d]; }
+			if (G) for (int d = 0; d < D; ++d) { gc[d] += (double) tgc[d]; gt[d] += (double) tgt[d]; }
 		}
 	}
 	if (!act) return;
 	out[i] = acc;
-	if (grad)
+	if (G)
 		for (int d = 0; d < D; ++d) { dc[d * (long) R.n + i] = gc[d]; dt[d * (long) R.n + i] = gt[d]; }
 }
 
@@ -311,12 +313,14 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 		if (R.n == 0) return;
 		dim3 grid(grid_for(R.n, blk), C);
 		const int sym = g ? 0 : 1;
-		if (precision == SA_PREC_MIXED)
-			k_vfd_rows<D, float><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk, md.dirWidth, part, g,
-			                                          pdc, pdt, sym);
-		else
-			k_vfd_rows<D, double><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, md.cenWidth, dk, md.dirWidth, part, g,
-			                                           pdc, pdt, sym);
+		const double cw = md.cenWidth, dw = md.dirWidth;
+		if (precision == SA_PREC_MIXED) {
+			if (g) k_vfd_rows<D, float, true><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym);
+			else k_vfd_rows<D, float, false><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym);
+		} else {
+			if (g) k_vfd_rows<D, double, true><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym);
+			else k_vfd_rows<D, double, false><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym);
+		}
 		k_vfd_chunks<D><<<grid_for(R.n), kBlock, 0, s>>>(R.n, C, part, out, g, pdc, pdt, dc, dt);
 	};
 	if (grad || Vd >= Vt) {
@@ -408,15 +412,15 @@ static double varifold_in_scratch(double *scr, int N, const double *x, int Vd, c
 	const int blk = 128;
 	// same row/column roles as the allocating path (reference branch on Vd >= Vt)
 	if (Vd >= Vt) {
-		k_vfd_rows<D, double><<<grid_for(Vd, blk), blk, 0, s>>>(Ds, Ds, 1.0, Ts, -2.0, ck, cw, dk, dw, vfd, 0,
-		                                                        nullptr, nullptr);
-		k_vfd_rows<D, double><<<grid_for(Vt, blk), blk, 0, s>>>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, vfd + Vd, 0,
-		                                                        nullptr, nullptr);
+		k_vfd_rows<D, double, false><<<grid_for(Vd, blk), blk, 0, s>>>(Ds, Ds, 1.0, Ts, -2.0, ck, cw, dk, dw, vfd,
+		                                                               nullptr, nullptr);
+		k_vfd_rows<D, double, false><<<grid_for(Vt, blk), blk, 0, s>>>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, vfd + Vd,
+		                                                               nullptr, nullptr);
 	} else {
-		k_vfd_rows<D, double><<<grid_for(Vt, blk), blk, 0, s>>>(Ts, Ts, 1.0, Ds, -2.0, ck, cw, dk, dw, vfd, 0,
-		                                                        nullptr, nullptr);
-		k_vfd_rows<D, double><<<grid_for(Vd, blk), blk, 0, s>>>(Ds, Ds, 1.0, E0, 0.0, ck, cw, dk, dw, vfd + Vt, 0,
-		                                                        nullptr, nullptr);
+		k_vfd_rows<D, double, false><<<grid_for(Vt, blk), blk, 0, s>>>(Ts, Ts, 1.0, Ds, -2.0, ck, cw, dk, dw, vfd,
+		                                                               nullptr, nullptr);
+		k_vfd_rows<D, double, false><<<grid_for(Vd, blk), blk, 0, s>>>(Ds, Ds, 1.0, E0, 0.0, ck, cw, dk, dw, vfd + Vt,
+		                                                               nullptr, nullptr);
 	}
 	SA_CHECK(cudaGetLastError());
 	// device_sum clears the part of its buffer that accumulates before using it
