@@ -548,6 +548,21 @@ __device__ __forceinline__ bool wait_grid(GridBar *bar, unsigned int target)
 	return true;
 }
 
+// a slot whose column is already known (the persistent CG keeps its CTA's columns in shared memory)
+template <int B, typename TM, typename TV>
+__device__ __forceinline__ void spmv_slot_col(const SellOp &A, const TM *__restrict__ blk, const TV *u, long idx, int j,
+                                              TV (&acc)[B])
+{
+	TV xj[B];
+	for (int c = 0; c < B; ++c) xj[c] = __ldcg(u + (long) j * B + c);   // written during the launch
+	TM a[B * B];
+	load_block<B, TM>(blk, A.total, idx, a);
+	for (int r = 0; r < B; ++r)
+		for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
+}
+
+constexpr int kColSmemMax = 160 * 1024;    // shared memory for a CTA's column indices (else two-kernel CG)
+
 template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
 k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, const TV *__restrict__ binv, TX *x,
@@ -557,6 +572,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	__shared__ double nx[4];                     // next gamma, rr, beta, beta * gamma / alphaPrev
 	__shared__ double al[2];                     // alpha, delta of the iteration
 	__shared__ int gaveUp;
+	extern __shared__ int scol[];                // the column of every slot of the CTA's slices
 	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
 	const int nctas = gridDim.x, lc = blockIdx.x;
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
@@ -569,6 +585,13 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	const bool own = rowWarp && i < A.N;
 	const int wdt = rowWarp ? __ldg(A.width + sl) : 0;
 	const long base = rowWarp ? __ldg(A.off + sl) + lane : 0;
+	// the CTA's slices are consecutive, so their slots are one range [c0, c1) of the sliced layout; its
+	// columns do not change during the solve: one coalesced copy, then no dependent column load per slot
+	const long c0 = __ldg(A.off + lc * H);
+	const long c1 = (lc + 1) * H < nsl ? (long) __ldg(A.off + (lc + 1) * H) : A.total;
+	for (long t = threadIdx.x; t < c1 - c0; t += blockDim.x) scol[t] = __ldg(A.col + c0 + t);
+	const int lbase = (int) (base - c0);         // local slot of lane's slot 0 (row warps)
+	__syncthreads();                             // scol and gaveUp before their first use
 	const double bb = sc->bb, tolSqu = sc->tolSqu;
 	const int itrMax = sc->itrMax;
 	double gam = sc->gam, rr = sc->rr, alpha = 1.0, beta = 0.0;
@@ -601,10 +624,11 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
 			int k = 0;
 			for (; k + 2 <= wdt; k += 2) {
-				spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
-				spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), acc1);
+				const int j0 = scol[lbase + (k << 5)], j1 = scol[lbase + ((k + 1) << 5)];
+				spmv_slot_col<B, TM, TV>(A, blk, u, base + ((long) k << 5), j0, acc0);
+				spmv_slot_col<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), j1, acc1);
 			}
-			if (k < wdt) spmv_slot_cg<B, TM, TV>(A, blk, u, base + ((long) k << 5), acc0);
+			if (k < wdt) spmv_slot_col<B, TM, TV>(A, blk, u, base + ((long) k << 5), scol[lbase + (k << 5)], acc0);
 			for (int c = 0; c < B; ++c) wv[c] = acc0[c] + acc1[c];
 			if (own) d1[0] = row_dot<B, TV>(wv, uv);
 		} else if (pending) {
@@ -895,22 +919,38 @@ static void set_scal(CgScal *d, double tolSqu, int itrMax, double bb, cudaStream
 
 // CTAs of k_cg_persist with `warps` warps each that can be resident at once (0: it cannot run)
 template <int B, typename TM, typename TV, typename TX>
-static int persist_capacity(int smCount, int warps)
+static int persist_capacity(int smCount, int warps, size_t smemBytes)
 {
-	static int perSm[kPersistMaxWarps + 1] = {};
-	static bool known[kPersistMaxWarps + 1] = {};
-	if (warps < 1 || warps > kPersistMaxWarps) return 0;
-	if (!known[warps]) {
-		int v = 0;
-		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist<B, TM, TV, TX>, 32 * warps, 0) !=
-		    cudaSuccess) {
+	static bool attr = false;
+	if (warps < 1 || warps > kPersistMaxWarps || smemBytes > (size_t) kColSmemMax) return 0;
+	if (!attr) {               // allow the column cache beyond the default 48 KB of dynamic shared memory
+		if (cudaFuncSetAttribute(k_cg_persist<B, TM, TV, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         kColSmemMax) != cudaSuccess) {
 			cudaGetLastError();
-			v = 0;
+			return 0;
 		}
-		perSm[warps] = v;
-		known[warps] = true;
+		attr = true;
 	}
-	return perSm[warps] * smCount;
+	int v = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist<B, TM, TV, TX>, 32 * warps, smemBytes) !=
+	    cudaSuccess) {
+		cudaGetLastError();
+		v = 0;
+	}
+	return v * smCount;
+}
+
+// largest slot range of one CTA (pw consecutive slices), in column-index bytes
+static size_t col_span_bytes(const Mesh &m, int pw)
+{
+	long span = 0;
+	const std::vector<int> &off = m.slOffHost;
+	if ((int) off.size() != m.nslice + 1) return (size_t) -1;
+	for (int s0 = 0; s0 < m.nslice; s0 += pw) {
+		const int s1 = std::min(m.nslice, s0 + pw);
+		span = std::max(span, (long) off[s1] - off[s0]);
+	}
+	return (size_t) span * sizeof(int);
 }
 
 static CgScal read_scal(const CgScal *d, cudaStream_t s)
@@ -939,9 +979,10 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	const int pwCap = std::max(1, std::min(kPersistMaxWarps, tuning().persistMaxWarps) - 1);
 	const int pw = std::max(1, std::min(pwCap, (m.nslice + prof->smCount - 1) / prof->smCount));
 	const int nctas = (m.nslice + pw - 1) / pw;
+	const size_t colSmem = col_span_bytes(m, pw);
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
 	                     (!block_prec<TV>() || prof->binv32) &&
-	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw + 1);
+	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw + 1, colSmem);
 	if (persist) {
 		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first).  FP32
 		// inner solves of mixed precision are block-Jacobi preconditioned (3x3 node blocks)
@@ -960,7 +1001,7 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		                (void *) &part, (void *) &sc, (void *) &bar};
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
 		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
-		                                     dim3(32 * (pw + 1)), args, 0, s));
+		                                     dim3(32 * (pw + 1)), args, colSmem, s));
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[1], s));
 		k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
 		prof->launches += 3;

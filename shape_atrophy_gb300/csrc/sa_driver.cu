@@ -332,6 +332,8 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		SA_CHECK(cudaMemcpyAsync(m.asmOrder, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slWidth, wid.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slOff, off.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
+		m.slOffHost = off;
+		m.slOffHost.push_back((int) total);
 		SA_CHECK(cudaMemcpyAsync(m.slCol, col.data(), sizeof(int) * total, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaMemcpyAsync(m.slDest, dest.data(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaStreamSynchronize(s));      // host vectors go out of scope

@@ -169,6 +169,7 @@ struct Mesh {              // device copy of one element object + derived tables
 	long slTotal = 0;          // slots including padding
 	int *slWidth = nullptr;    // nslice: longest row of the slice
 	int *slOff = nullptr;      // nslice: first slot of the slice
+	std::vector<int> slOffHost;  // host copy of slOff plus slTotal at the end (per-CTA column spans)
 	int *slCol = nullptr;      // slTotal: column (node) of each slot; padding points at the row itself
 	int *slDest = nullptr;     // Z: sliced slot of each femVtxMat slot
 	int *transZ = nullptr;     // Z: femVtxMat slot of the transposed entry (j, i)
