@@ -188,6 +188,17 @@ int sa_session_create(sa_context *ctx, const sa_element_object *obj, const doubl
                       sa_session **out);
 int sa_session_step(sa_session *s, int nsteps, int *stepsDone);
 int sa_session_state(sa_session *s, double *lmkMat, double *tauVec, int *step);
+/* Streamed trajectory (no reference counterpart: deformation's lmkStk keeps
+ * every step on the device and copies it at the end).  Advances up to nsteps
+ * steps (like sa_session_step) and writes the state after every step whose
+ * session step number is a multiple of stride, at most maxSnapshots of them,
+ * in order: snapshot k to lmkOut + k * N * dim (the lmkStk column layout:
+ * dim blocks of N) and tauOut + k * N.  lmkOut and tauOut are host memory
+ * (either may be NULL); each snapshot is copied to pinned memory on a
+ * second stream while the following steps run.  *snapshotsWritten,
+ * *stepsDone: counts (may be NULL). */
+int sa_session_stream(sa_session *s, int nsteps, int stride, double *lmkOut, double *tauOut, int maxSnapshots,
+                      int *snapshotsWritten, int *stepsDone);
 int sa_session_objective(sa_session *s, double *obj);
 int sa_session_info(sa_session *s, sa_solve_info *info);
 int sa_session_profile(sa_session *s, int enable, double *kernelMs, long long *launches, double *bytes,

@@ -271,6 +271,22 @@ class Session:
                                                      tau.ctypes.data_as(_lib._dp), C.byref(t)), "sa_session_state")
         return lmk, tau, t.value
 
+    def stream(self, nsteps: int, stride: int = 1, max_snapshots: int = None, positions: bool = True,
+               concentration: bool = True):
+        """Advance up to nsteps steps, collecting the state after every step whose session step number is a
+        multiple of stride (copied to the host while the next steps run).  Returns (lmk (K, D, N) or None,
+        tau (K, N) or None, steps taken); K = snapshots written."""
+        K = nsteps // stride + 1 if max_snapshots is None else int(max_snapshots)
+        lmk = np.zeros((K, self.D, self.N)) if positions else None
+        tau = np.zeros((K, self.N)) if concentration else None
+        wr, done = C.c_int(), C.c_int()
+        self.ctx.check(self.ctx.lib.sa_session_stream(
+            self.h, int(nsteps), int(stride), lmk.ctypes.data_as(_lib._dp) if positions else None,
+            tau.ctypes.data_as(_lib._dp) if concentration else None, K, C.byref(wr), C.byref(done)),
+            "sa_session_stream")
+        k = wr.value
+        return (lmk[:k] if positions else None), (tau[:k] if concentration else None), done.value
+
     def objective(self) -> float:
         v = C.c_double()
         self.ctx.check(self.ctx.lib.sa_session_objective(self.h, C.byref(v)), "sa_session_objective")

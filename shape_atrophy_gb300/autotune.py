@@ -43,7 +43,7 @@ from . import api, problems
 
 CANDIDATES = {
     "persistMaxWarps": [8, 12, 16, 20],
-    "vfdCtasPerSm": [2, 4, 8, 16],
+    "vfdCtasPerSm": [2, 4, 8, 16, 32],
     "batchBlock": [128, 256],
     "batchSlicesPerWarp": [1, 2, 4],
 }

@@ -739,6 +739,7 @@ struct SessionBase {
 	virtual double objective() = 0;
 	virtual void info(sa_solve_info *i) = 0;
 	virtual void profile(int enable, double *ms, long long *cnt, double *bytes, double *flops) = 0;
+	virtual int stream(int nsteps, int stride, double *lmkOut, double *tauOut, int maxSnap, int *written) = 0;
 };
 
 template <int D>
@@ -832,6 +833,76 @@ struct Session : SessionBase {
 		i->invertedElements = hs.inverted;
 		i->elapsedMs = lastStepMs;             // device time of the last sa_session_step call
 		i->kernelLaunches = w.cw.launches;
+	}
+	// streamed snapshots: a ring of device and pinned host buffers; each snapshot is converted to the
+	// lmkStk layout on the compute stream, copied to pinned memory on a copy stream while the next steps
+	// run, and moved into the caller's buffer when its ring slot is needed again (or at the end)
+	struct Slot {
+		double *dev = nullptr, *host = nullptr;
+		cudaEvent_t ready = nullptr, copied = nullptr;
+		long snap = -1;                    // snapshot index held, -1: free
+	};
+	static constexpr int kRing = 3;
+	Slot ring[kRing];
+	cudaStream_t copyStream = nullptr;
+	~Session() override
+	{
+		if (copyStream) cudaStreamSynchronize(copyStream);
+		for (Slot &r : ring) {
+			if (r.host) cudaFreeHost(r.host);
+			if (r.ready) cudaEventDestroy(r.ready);
+			if (r.copied) cudaEventDestroy(r.copied);
+		}
+		if (copyStream) cudaStreamDestroy(copyStream);
+	}
+	int stream(int nsteps, int stride, double *lmkOut, double *tauOut, int maxSnap, int *written) override
+	{
+		SA_REQUIRE(nsteps >= 0 && stride >= 1 && maxSnap >= 0, "stream: nsteps >= 0, stride >= 1, maxSnapshots >= 0");
+		SA_REQUIRE(!is_device_ptr(lmkOut) && !is_device_ptr(tauOut), "stream: output buffers must be host memory");
+		cudaStream_t s = ctx->stream;
+		const size_t nx = (size_t) m.N * D, per = nx + (size_t) m.N;
+		if (!copyStream) {
+			SA_CHECK(cudaStreamCreateWithFlags(&copyStream, cudaStreamNonBlocking));
+			for (Slot &r : ring) {
+				r.dev = P.alloc<double>(per);
+				SA_CHECK(cudaHostAlloc((void **) &r.host, sizeof(double) * per, cudaHostAllocDefault));
+				SA_CHECK(cudaEventCreateWithFlags(&r.ready, cudaEventDisableTiming));
+				SA_CHECK(cudaEventCreateWithFlags(&r.copied, cudaEventDisableTiming));
+			}
+		}
+		auto drain = [&](Slot &r) {
+			if (r.snap < 0) return;
+			SA_CHECK(cudaEventSynchronize(r.copied));
+			if (lmkOut) std::memcpy(lmkOut + (size_t) r.snap * nx, r.host, sizeof(double) * nx);
+			if (tauOut) std::memcpy(tauOut + (size_t) r.snap * m.N, r.host + nx, sizeof(double) * m.N);
+			r.snap = -1;
+		};
+		int snaps = 0, done = 0;
+		SA_CHECK(cudaEventRecord(ctx->e0, s));
+		while (done < nsteps) {
+			if (st.step(1) == 0) break;
+			++done;
+			if (st.t % stride != 0 || snaps >= maxSnap) continue;
+			Slot &r = ring[snaps % kRing];
+			drain(r);                          // the snapshot kRing back, copied long since
+			launch_aos_to_soa(m.N, D, st.xn, r.dev, s);
+			SA_CHECK(cudaMemcpyAsync(r.dev + nx, st.tau_now(), sizeof(double) * m.N, cudaMemcpyDeviceToDevice, s));
+			SA_CHECK(cudaEventRecord(r.ready, s));
+			SA_CHECK(cudaStreamWaitEvent(copyStream, r.ready, 0));
+			SA_CHECK(cudaMemcpyAsync(r.host, r.dev, sizeof(double) * per, cudaMemcpyDeviceToHost, copyStream));
+			SA_CHECK(cudaEventRecord(r.copied, copyStream));
+			r.snap = snaps++;
+			w.cw.launches += 1;
+		}
+		SA_CHECK(cudaEventRecord(ctx->e1, s));
+		for (int k = std::max(0, snaps - kRing); k < snaps; ++k) drain(ring[k % kRing]);
+		SA_CHECK(cudaEventSynchronize(ctx->e1));
+		float ms = 0.f;
+		SA_CHECK(cudaEventElapsedTime(&ms, ctx->e0, ctx->e1));
+		lastStepMs = ms;
+		SA_CHECK(cudaGetLastError());
+		if (written) *written = snaps;
+		return done;
 	}
 	void profile(int enable, double *ms, long long *cnt, double *bytes, double *flops) override
 	{
@@ -1448,6 +1519,17 @@ int sa_session_step(sa_session *s, int nsteps, int *stepsDone)
 	if (!s) return SA_ERR_ARG;
 	return sa::guarded(s->impl->ctx, [&]() {
 		int k = s->impl->step(nsteps);
+		if (stepsDone) *stepsDone = k;
+		return SA_OK;
+	});
+}
+
+int sa_session_stream(sa_session *s, int nsteps, int stride, double *lmkOut, double *tauOut, int maxSnapshots,
+                      int *snapshotsWritten, int *stepsDone)
+{
+	if (!s) return SA_ERR_ARG;
+	return sa::guarded(s->impl->ctx, [&]() {
+		int k = s->impl->stream(nsteps, stride, lmkOut, tauOut, maxSnapshots, snapshotsWritten);
 		if (stepsDone) *stepsDone = k;
 		return SA_OK;
 	});

@@ -300,6 +300,7 @@ template <int D> void launch_rd_rhs(const Mesh &m, const Geom &gNow, const doubl
 template <int D> void launch_advance(int N, const double *x, const double *v, double dt, double *xn,
                                      double *trajSlot, cudaStream_t s);
 void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_t s);
+void launch_aos_to_soa(int N, int D, const double *aos, double *soa, cudaStream_t s);
 
 
 // --------------------------------------------------------------------------

@@ -549,6 +549,18 @@ void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_
 	k_soa_to_aos<<<grid_for((long) N * D), kBlock, 0, s>>>(N, D, soa, aos);
 }
 
+__global__ void k_aos_to_soa(int N, int D, const double *__restrict__ aos, double *__restrict__ soa)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k >= (long) N * D) return;
+	soa[(k % D) * N + k / D] = aos[k];
+}
+
+void launch_aos_to_soa(int N, int D, const double *aos, double *soa, cudaStream_t s)
+{
+	k_aos_to_soa<<<grid_for((long) N * D), kBlock, 0, s>>>(N, D, aos, soa);
+}
+
 // explicit instantiations
 #define SA_INST(D)                                                                                           \
 	template void launch_elem_geom<D>(const Mesh &, const Model &, const double *, Geom &, Status *, bool,     \
