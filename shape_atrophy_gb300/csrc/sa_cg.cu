@@ -1234,25 +1234,30 @@ static int batch_capacity(int smCount, int block)
 }
 
 template <int B, typename TM, typename TV, typename TX>
-void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJobs, int maxJobs, cudaStream_t s)
+int cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJobs, int maxJobs, cudaStream_t s)
 {
+	int nLaunch = 0;
 	const int block = std::max(32, std::min(kBatchBlock, tuning().batchBlock / 32 * 32));
 	const int cap = batch_capacity<B, TM, TV, TX>(smCount, block);
 	if (cap <= 0) throw CudaError{cudaErrorLaunchOutOfResources, "k_cg_batch occupancy"};
 	const int W = block / 32;
-	size_t k0 = 0;
-	while (k0 < solves.size()) {
-		// CTAs of a solve: one per kBatchSlicesPerWarp slices per warp, from its own size only (its partial
-		// sums, and so its result, do not depend on the other solves); solves [k0, k1) share one launch
+	std::vector<char> taken(solves.size(), 0);
+	size_t left = solves.size();
+	while (left > 0) {
+		// CTAs of a solve: one per batchSlicesPerWarp slices per warp, from its own size only (its partial
+		// sums, and so its result, do not depend on the other solves).  First fit in the caller's order:
+		// each launch takes every remaining solve that still fits its co-resident CTA capacity
 		std::vector<CgJob> jobs;
 		int cta = 0;
-		size_t k1 = k0;
-		for (; k1 < solves.size() && (int) jobs.size() < maxJobs; ++k1) {
+		for (size_t k1 = 0; k1 < solves.size() && (int) jobs.size() < maxJobs; ++k1) {
+			if (taken[k1]) continue;
 			const BatchSolve &b = solves[k1];
 			const Mesh &m = *b.m;
 			const int per = W * std::max(1, tuning().batchSlicesPerWarp);
 			const int want = std::max(1, std::min(cap, (m.nslice + per - 1) / per));
-			if (cta + want > cap) break;
+			if (cta + want > cap) continue;
+			taken[k1] = 1;
+			--left;
 			CgWork &w = *b.cw;
 			CgJob j;
 			j.A = sell_of(m);
@@ -1278,6 +1283,7 @@ void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *dev
 		void *args[] = {(void *) &dj, (void *) &nj};
 		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_batch<B, TM, TV, TX>, dim3(cta), dim3(block),
 		                                     args, 0, s));
+		++nLaunch;
 		// the job table is read by the kernel: wait before the host vector goes away or is rewritten
 		SA_CHECK(cudaStreamSynchronize(s));
 		for (const CgJob &j : jobs) {
@@ -1285,8 +1291,8 @@ void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *dev
 			SA_CHECK(cudaMemcpy(&gaveUp, &((GridBar *) j.bar)->abort, sizeof(unsigned int), cudaMemcpyDeviceToHost));
 			if (gaveUp) throw DeviceWaitError{"batched CG grid barrier"};
 		}
-		k0 = k1;
 	}
+	return nLaunch;
 }
 
 #define SA_BATCH_INST(B)                                                                                          \
@@ -1296,9 +1302,9 @@ void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *dev
 	template void cg_mixed_outer<B>(const Mesh &, const double *, const double *, const double *, const double *, \
 	                                double, int, CgWork &, cudaStream_t);                                         \
 	template void cg_mixed_inner<B>(const Mesh &, int, double, CgWork &, cudaStream_t);                          \
-	template void cg_batch_run<B, double, double, double>(const std::vector<BatchSolve> &, int, CgJob *, int,    \
+	template int cg_batch_run<B, double, double, double>(const std::vector<BatchSolve> &, int, CgJob *, int,    \
 	                                                      cudaStream_t);                                          \
-	template void cg_batch_run<B, float, float, float>(const std::vector<BatchSolve> &, int, CgJob *, int,       \
+	template int cg_batch_run<B, float, float, float>(const std::vector<BatchSolve> &, int, CgJob *, int,       \
 	                                                   cudaStream_t);
 SA_BATCH_INST(1)
 SA_BATCH_INST(2)

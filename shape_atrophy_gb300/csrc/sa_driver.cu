@@ -1010,7 +1010,12 @@ struct InstBase {
 	int its = 0, rits = 0;
 	double bb = -1.0, innerTol = 0.0;
 	int mixedTotal = 0, mixedDone = 0;
+	int lastVelIts = 0;                      // velocity iterations of the previous step (launch packing order)
 	virtual ~InstBase() {}
+	virtual int nodes() const = 0;
+	// expected length of the next solve, for packing batched launches: the previous step's iterations,
+	// or 1.5 sqrt(N) before the first step.  Only the order of solves in launches depends on it.
+	double vel_key() const { return lastVelIts > 0 ? lastVelIts : 1.5 * std::sqrt((double) nodes()); }
 	virtual int dim() const = 0;
 	virtual int precision() const = 0;
 	virtual bool finished() const = 0;
@@ -1097,8 +1102,10 @@ struct Inst : InstBase {
 	CgWork &cg() override { return w.cw; }
 	const Model &model() const override { return md; }
 	void set_status(int code) override { st.out.status = code; }
+	int nodes() const override { return m.N; }
 	void account(int velIts, int rdIts) override
 	{
+		lastVelIts = velIts;
 		st.out.cgTotal += velIts;
 		st.out.cgMax = std::max(st.out.cgMax, velIts);
 		st.out.rdTotal += rdIts;
@@ -1150,6 +1157,20 @@ struct Server {
 	CgJob *devJobs = nullptr;
 	int smCount = 1;
 	std::thread th;
+	// SA_TRACE: time per tick phase (element kernels, FP64 velocity, mixed velocity, reaction-diffusion,
+	// bookkeeping) and batched CG launches, printed when the server is destroyed
+	bool trace = std::getenv("SA_TRACE") != nullptr;
+	double phaseMs[5] = {0, 0, 0, 0, 0};
+	long long batchLaunches[3] = {0, 0, 0};
+	std::chrono::steady_clock::time_point tMark;
+	void mark(int phase)
+	{
+		if (!trace) return;
+		cudaStreamSynchronize(s);
+		const auto t = std::chrono::steady_clock::now();
+		if (phase >= 0) phaseMs[phase] += std::chrono::duration<double, std::milli>(t - tMark).count();
+		tMark = t;
+	}
 
 	static constexpr int kMaxJobs = 4096;
 
@@ -1170,6 +1191,13 @@ struct Server {
 		cv.notify_all();
 		if (th.joinable()) th.join();
 		active.clear();
+		if (trace)
+			std::fprintf(stderr,
+			             "[sa_trace] server: %lld ticks; ms in element kernels %.1f, FP64 velocity %.1f, mixed "
+			             "velocity %.1f, reaction-diffusion %.1f, bookkeeping %.1f; batched CG launches FP64 %lld, "
+			             "FP32 %lld, RD %lld\n",
+			             ticks, phaseMs[0], phaseMs[1], phaseMs[2], phaseMs[3], phaseMs[4], batchLaunches[0],
+			             batchLaunches[1], batchLaunches[2]);
 		cudaSetDevice(ctx->device);
 		if (devJobs) cudaFree(devJobs);
 		if (s) cudaStreamDestroy(s);
@@ -1183,12 +1211,18 @@ struct Server {
 		in.set_status(code);
 	}
 
-	// one time step of every running instance
+	// one time step of every running instance.  When the solves of a batched CG do not fit one cooperative
+	// launch they run in several (first fit), each as long as its slowest solve.  The FP32 inner solves of
+	// mixed precision are latency bound, so their length follows their iteration count: they are ordered
+	// longest first, so that long solves share launches.  The FP64 solves are FP64-pipe bound and keep
+	// arrival order (measured faster on the served stream).  Results do not depend on the order.
 	void tick()
 	{
 		std::vector<InstBase *> run;
 		for (auto &u : active) if (!u->finished()) run.push_back(u.get());
+		mark(-1);
 		for (InstBase *in : run) { in->its = 0; in->rits = 0; in->pre_velocity(); }
+		mark(0);
 		// velocity: FP64 instances, one batched launch per dimension
 		for (int D = 2; D <= 3; ++D) {
 			std::vector<InstBase *> g;
@@ -1196,8 +1230,8 @@ struct Server {
 			if (g.empty()) continue;
 			std::vector<BatchSolve> bs;
 			for (InstBase *in : g) { in->prepare_velocity_fp64(); bs.push_back(in->velocity_fp64()); }
-			if (D == 2) cg_batch_run<2, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
-			else cg_batch_run<3, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
+			batchLaunches[0] += D == 2 ? cg_batch_run<2, double, double, double>(bs, smCount, devJobs, kMaxJobs, s)
+			                           : cg_batch_run<3, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
 			for (InstBase *in : g) in->finish_velocity_fp64();
 			for (InstBase *in : g) {
 				CgState c = cg_state(in->cg(), s);
@@ -1205,11 +1239,15 @@ struct Server {
 				if (c.code != SA_OK) fail(*in, c.code);
 			}
 		}
+		mark(1);
 		// velocity: mixed precision, FP64 iterative refinement around batched FP32 solves
 		for (int D = 2; D <= 3; ++D) {
 			std::vector<InstBase *> g;
 			for (InstBase *in : run) if (in->dim() == D && in->precision() == SA_PREC_MIXED) g.push_back(in);
 			if (g.empty()) continue;
+			std::stable_sort(g.begin(), g.end(), [](const InstBase *a, const InstBase *b) {
+				return a->vel_key() > b->vel_key();
+			});
 			for (InstBase *in : g) { in->bb = -1.0; in->mixedTotal = 0; in->mixedDone = 0; }
 			for (int outer = 0; outer < 64 && !g.empty(); ++outer) {
 				for (InstBase *in : g) in->mixed_outer(outer == 0);
@@ -1229,8 +1267,8 @@ struct Server {
 				if (inner.empty()) break;
 				std::vector<BatchSolve> bs;
 				for (InstBase *in : inner) { in->mixed_inner(); bs.push_back(in->velocity_mixed()); }
-				if (D == 2) cg_batch_run<2, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
-				else cg_batch_run<3, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
+				batchLaunches[1] += D == 2 ? cg_batch_run<2, float, float, float>(bs, smCount, devJobs, kMaxJobs, s)
+				                           : cg_batch_run<3, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
 				std::vector<InstBase *> next;
 				for (InstBase *in : inner) {
 					CgState c = cg_state(in->cg(), s);
@@ -1246,13 +1284,14 @@ struct Server {
 			for (InstBase *in : run)
 				if (in->dim() == D && in->precision() == SA_PREC_MIXED) in->its = in->mixedTotal;
 		}
+		mark(2);
 		// reaction-diffusion: one batched launch for every instance still running
 		std::vector<InstBase *> rd;
 		for (InstBase *in : run) if (!in->failed) rd.push_back(in);
 		if (!rd.empty()) {
 			std::vector<BatchSolve> bs;
 			for (InstBase *in : rd) { in->prepare_rd(); bs.push_back(in->rd_solve()); }
-			cg_batch_run<1, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
+			batchLaunches[2] += cg_batch_run<1, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
 			for (InstBase *in : rd) in->finish_rd();
 			for (InstBase *in : rd) {
 				CgState c = cg_state(in->cg(), s);
@@ -1260,10 +1299,12 @@ struct Server {
 				if (c.code != SA_OK) fail(*in, c.code);
 			}
 		}
+		mark(3);
 		for (InstBase *in : run) {
 			in->account(in->its, in->rits);
 			if (!in->failed) in->end_step();
 		}
+		mark(4);
 		++ticks;
 	}
 

@@ -384,7 +384,7 @@ template <int B> void cg_mixed_inner(const Mesh &m, int itrMax, double innerTolS
 void cg_mixed_apply(long n, double *x, const CgWork &w, cudaStream_t s);
 // one launch (or several, when the CTAs do not fit at once) over all solves
 template <int B, typename TM, typename TV, typename TX>
-void cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJobs, int maxJobs,
+int cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJobs, int maxJobs,
                   cudaStream_t s);
 // x = 0 where the right-hand side was zero (after a batched FP64 solve)
 template <int B> void cg_finish_fp64(const Mesh &m, double *x, CgWork &w, cudaStream_t s);
