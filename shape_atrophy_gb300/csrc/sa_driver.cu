@@ -24,6 +24,7 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <functional>
 #include <mutex>
 #include <thread>
 
@@ -105,6 +106,96 @@ struct PhaseTrace {
 
 struct ArgError { std::string msg; };
 #define SA_REQUIRE(c, m) do { if (!(c)) throw ::sa::ArgError{m}; } while (0)
+
+// A persistent pool of host threads for the set-up loops (thread start-up would cost more than the loops).
+// run(f) calls f(t) for t = 0 .. size()-1, t = 0 on the calling thread; calls from several threads are
+// serialised.
+class HostPool {
+public:
+	static HostPool &get()
+	{
+		static HostPool pool;
+		return pool;
+	}
+	int size() const { return T; }
+	void run(const std::function<void(int)> &f)
+	{
+		std::lock_guard<std::mutex> one(callMu);
+		{
+			std::lock_guard<std::mutex> g(mu);
+			job = &f;
+			pending = T - 1;
+			++gen;
+		}
+		cv.notify_all();
+		f(0);
+		std::unique_lock<std::mutex> lk(mu);
+		doneCv.wait(lk, [this] { return pending == 0; });
+		job = nullptr;
+	}
+	~HostPool()
+	{
+		{
+			std::lock_guard<std::mutex> g(mu);
+			quit = true;
+		}
+		cv.notify_all();
+		for (std::thread &t : th) t.join();
+	}
+
+private:
+	HostPool() : T((int) std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency())))
+	{
+		for (int i = 1; i < T; ++i) th.emplace_back([this, i] { worker(i); });
+	}
+	void worker(int i)
+	{
+		long seen = 0;
+		for (;;) {
+			const std::function<void(int)> *f;
+			{
+				std::unique_lock<std::mutex> lk(mu);
+				cv.wait(lk, [&] { return quit || gen != seen; });
+				if (quit) return;
+				seen = gen;
+				f = job;
+			}
+			(*f)(i);
+			std::lock_guard<std::mutex> g(mu);
+			if (--pending == 0) doneCv.notify_one();
+		}
+	}
+	int T;
+	std::vector<std::thread> th;
+	std::mutex mu, callMu;
+	std::condition_variable cv, doneCv;
+	const std::function<void(int)> *job = nullptr;
+	long gen = 0;
+	int pending = 0;
+	bool quit = false;
+};
+
+// f(lo, hi) over [0, n) in contiguous chunks on the host pool (small n: the calling thread alone); an
+// ArgError in any chunk is rethrown after all chunks end
+template <typename F> static void parallel_chunks(long n, F &&f)
+{
+	HostPool &pool = HostPool::get();
+	const long T = pool.size();
+	if (n < 32768 || T <= 1) {
+		f(0L, n);
+		return;
+	}
+	std::vector<std::string> err((size_t) T);
+	pool.run([&](int t) {
+		try {
+			f(n * t / T, n * (t + 1) / T);
+		} catch (const ArgError &e) {
+			err[(size_t) t] = e.msg;
+		}
+	});
+	for (const std::string &e : err)
+		if (!e.empty()) throw ArgError{e};
+}
 
 template <typename T> static std::vector<T> to_host(const T *p, size_t n, cudaStream_t s)
 {
@@ -198,80 +289,118 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 	}
 
 	if (tr) tr->mark("mesh: upload");
-	// host-side validation of every index (one pass over each array)
-	std::vector<int> ev = to_host(m.elmVtx, (size_t) m.E * m.V, s);
-	for (int v : ev) SA_REQUIRE(v >= 0 && v < m.N, "elmVtxMat index out of range");
-	std::vector<int> fv = to_host(m.femVtx, (size_t) m.Z * 2, s);
-	std::vector<int> rp(m.N + 1, -1);
-	for (int z = 0; z < m.Z; ++z) {
-		int r = fv[z], c = fv[m.Z + z];
-		SA_REQUIRE(r >= 0 && r < m.N && c >= 0 && c < m.N, "femVtxMat index out of range");
-		if (z > 0) SA_REQUIRE(r > fv[z - 1] || (r == fv[z - 1] && c > fv[m.Z + z - 1]),
-		                      "femVtxMat rows must be sorted by (row, col) (generateElementObject sortrows)");
-		if (rp[r] < 0) rp[r] = z;
-	}
-	rp[m.N] = m.Z;
-	for (int i = m.N - 1; i >= 0; --i) SA_REQUIRE(rp[i] >= 0, "femVtxMat misses a node row");
-	std::vector<int> fi = to_host(m.femIfo, (size_t) m.Z * 2, s);
-	int maxAdj = 0;
-	for (int z = 0; z < m.Z; ++z) {
-		SA_REQUIRE(fi[z] >= 0 && 2 + 2 * fi[z] <= o->femIfoCols, "femIfoMat count exceeds its columns");
-		maxAdj = std::max(maxAdj, fi[z]);
-	}
-	std::vector<int> ve = to_host(m.vtxElm, (size_t) m.N * o->vtxElmCols, s);
-	for (int i = 0; i < m.N; ++i) {
-		int c = ve[i];
-		SA_REQUIRE(c >= 0 && 1 + 2 * c <= o->vtxElmCols, "vtxElmMat count exceeds its columns");
-		for (int a = 0; a < c; ++a) {
-			int e = ve[(1 + 2 * a) * (long) m.N + i], l = ve[(2 + 2 * a) * (long) m.N + i];
-			SA_REQUIRE(e >= 0 && e < m.E && l >= 0 && l < m.V && ev[(long) l * m.E + e] == i,
-			           "vtxElmMat entry does not match elmVtxMat");
+	// host-side validation of every index (one pass over each array, split over host threads); host inputs
+	// are read where they are, device inputs are downloaded once
+	auto host_ints = [&](const int *orig, const int *dev, size_t n, std::vector<int> &buf) -> const int * {
+		if (orig && !is_device_ptr(orig)) return orig;
+		buf = to_host(dev, n, s);
+		return buf.data();
+	};
+	auto in_range = [&](const int *v, size_t n, int hi, const char *msg) {
+		parallel_chunks((long) n, [&](long lo, long up) {
+			for (long k = lo; k < up; ++k) SA_REQUIRE(v[k] >= 0 && v[k] < hi, msg);
+		});
+	};
+	std::vector<int> evBuf, fvBuf, fiBuf, veBuf;
+	const int *ev = host_ints(o->elmVtxMat, m.elmVtx, (size_t) m.E * m.V, evBuf);
+	in_range(ev, (size_t) m.E * m.V, m.N, "elmVtxMat index out of range");
+	const int *fv = host_ints(o->femVtxMat, m.femVtx, (size_t) m.Z * 2, fvBuf);
+	parallel_chunks(m.Z, [&](long lo, long up) {
+		for (long z = lo; z < up; ++z) {
+			int r = fv[z], c = fv[m.Z + z];
+			SA_REQUIRE(r >= 0 && r < m.N && c >= 0 && c < m.N, "femVtxMat index out of range");
+			if (z > 0) SA_REQUIRE(r > fv[z - 1] || (r == fv[z - 1] && c > fv[m.Z + z - 1]),
+			                      "femVtxMat rows must be sorted by (row, col) (generateElementObject sortrows)");
 		}
+	});
+	std::vector<int> rp(m.N + 1, -1);
+	parallel_chunks(m.Z, [&](long lo, long up) {        // sorted: each row starts at exactly one slot
+		for (long z = lo; z < up; ++z)
+			if (z == 0 || fv[z] != fv[z - 1]) rp[fv[z]] = (int) z;
+	});
+	rp[m.N] = m.Z;
+	parallel_chunks(m.N, [&](long lo, long up) {
+		for (long i = lo; i < up; ++i) SA_REQUIRE(rp[i] >= 0, "femVtxMat misses a node row");
+	});
+	const int *fi = host_ints(o->femIfoMat, m.femIfo, (size_t) m.Z * 2, fiBuf);   // count row first
+	int maxAdj = 0;
+	{
+		std::mutex mx;
+		parallel_chunks(m.Z, [&](long lo, long up) {
+			int mloc = 0;
+			for (long z = lo; z < up; ++z) {
+				SA_REQUIRE(fi[z] >= 0 && 2 + 2 * fi[z] <= o->femIfoCols, "femIfoMat count exceeds its columns");
+				mloc = std::max(mloc, fi[z]);
+			}
+			std::lock_guard<std::mutex> g(mx);
+			maxAdj = std::max(maxAdj, mloc);
+		});
 	}
+	const int *ve = host_ints(o->vtxElmMat, m.vtxElm, (size_t) m.N * o->vtxElmCols, veBuf);
+	parallel_chunks(m.N, [&](long lo, long up) {
+		for (long i = lo; i < up; ++i) {
+			int c = ve[i];
+			SA_REQUIRE(c >= 0 && 1 + 2 * c <= o->vtxElmCols, "vtxElmMat count exceeds its columns");
+			for (int a = 0; a < c; ++a) {
+				int e = ve[(1 + 2 * a) * (long) m.N + i], l = ve[(2 + 2 * a) * (long) m.N + i];
+				SA_REQUIRE(e >= 0 && e < m.E && l >= 0 && l < m.V && ev[(long) l * m.E + e] == i,
+				           "vtxElmMat entry does not match elmVtxMat");
+			}
+		}
+	});
 	if (haveFrame) {
-		std::vector<int> fr = to_host(m.frmVtx, (size_t) m.E * frmCols, s);
-		for (int v : fr) SA_REQUIRE(v >= 0 && v < m.N, "tan/nmlVtxMat index out of range");
-		std::vector<int> ts = to_host(m.tsvVtx, (size_t) m.E * frmCols, s);
-		for (int v : ts) SA_REQUIRE(v >= 0 && v < m.N, "tsvVtxMat index out of range");
+		std::vector<int> b1, b2;
+		in_range(host_ints(o->frmVtxMat, m.frmVtx, (size_t) m.E * frmCols, b1), (size_t) m.E * frmCols, m.N,
+		         "tan/nmlVtxMat index out of range");
+		in_range(host_ints(o->tsvVtxMat, m.tsvVtx, (size_t) m.E * frmCols, b2), (size_t) m.E * frmCols, m.N,
+		         "tsvVtxMat index out of range");
 	}
 	if (m.Bt > 0) {
-		std::vector<int> bv = to_host(m.btmVtx, (size_t) m.Bt * D, s);
-		for (int v : bv) SA_REQUIRE(v >= 0 && v < m.N, "btmVtxMat index out of range");
-		std::vector<int> vb = to_host(m.vtxBtm, (size_t) m.Nb * o->vtxBtmCols, s);
-		for (int i = 0; i < m.Nb; ++i) {
-			int c = vb[i];
-			SA_REQUIRE(c >= 0 && 1 + 2 * c <= o->vtxBtmCols, "vtxBtmMat count exceeds its columns");
-			for (int a = 0; a < c; ++a) {
-				int f = vb[(1 + 2 * a) * (long) m.Nb + i], l = vb[(2 + 2 * a) * (long) m.Nb + i];
-				SA_REQUIRE(f >= 0 && f < m.Bt && l >= 0 && l < D && bv[(long) l * m.Bt + f] == i,
-				           "vtxBtmMat entry must name its own node (bottom nodes numbered first)");
+		std::vector<int> b1, b2;
+		const int *bv = host_ints(o->btmVtxMat, m.btmVtx, (size_t) m.Bt * D, b1);
+		in_range(bv, (size_t) m.Bt * D, m.N, "btmVtxMat index out of range");
+		const int *vb = host_ints(o->vtxBtmMat, m.vtxBtm, (size_t) m.Nb * o->vtxBtmCols, b2);
+		parallel_chunks(m.Nb, [&](long lo, long up) {
+			for (long i = lo; i < up; ++i) {
+				int c = vb[i];
+				SA_REQUIRE(c >= 0 && 1 + 2 * c <= o->vtxBtmCols, "vtxBtmMat count exceeds its columns");
+				for (int a = 0; a < c; ++a) {
+					int f = vb[(1 + 2 * a) * (long) m.Nb + i], l = vb[(2 + 2 * a) * (long) m.Nb + i];
+					SA_REQUIRE(f >= 0 && f < m.Bt && l >= 0 && l < D && bv[(long) l * m.Bt + f] == i,
+					           "vtxBtmMat entry must name its own node (bottom nodes numbered first)");
+				}
 			}
-		}
+		});
 	}
 	if (needVfd) {
-		std::vector<int> vv = to_host(m.vfdVtx, (size_t) m.Vd * D, s);
-		for (int v : vv) SA_REQUIRE(v >= 0 && v < m.N, "vfdVtxMat index out of range");
+		std::vector<int> b1;
+		in_range(host_ints(o->vfdVtxMat, m.vfdVtx, (size_t) m.Vd * D, b1), (size_t) m.Vd * D, m.N,
+		         "vfdVtxMat index out of range");
 	}
 	if (needGrad) {
-		std::vector<int> gi = to_host(m.vfdIfo, (size_t) m.N * o->vfdIfoCols, s);
+		std::vector<int> b1;
+		const int *gi = host_ints(o->vfdIfoMat, m.vfdIfo, (size_t) m.N * o->vfdIfoCols, b1);
 		int w = D == 2 ? 2 : 3;
-		for (int i = 0; i < m.N; ++i) {
-			int c = gi[i];
-			SA_REQUIRE(c >= 0 && 1 + w * c <= o->vfdIfoCols, "vfdIfoMat count exceeds its columns");
-			for (int a = 0; a < c; ++a) {
-				int e = gi[(1 + w * a) * (long) m.N + i];
-				SA_REQUIRE(e >= 0 && e < m.Vd, "vfdIfoMat element out of range");
-				if (D == 3)
-					for (int t = 2; t <= 3; ++t) {
-						int q = gi[(t + w * a) * (long) m.N + i];
-						SA_REQUIRE(q >= 0 && q < m.N, "vfdIfoMat node out of range");
-					}
+		parallel_chunks(m.N, [&](long lo, long up) {
+			for (long i = lo; i < up; ++i) {
+				int c = gi[i];
+				SA_REQUIRE(c >= 0 && 1 + w * c <= o->vfdIfoCols, "vfdIfoMat count exceeds its columns");
+				for (int a = 0; a < c; ++a) {
+					int e = gi[(1 + w * a) * (long) m.N + i];
+					SA_REQUIRE(e >= 0 && e < m.Vd, "vfdIfoMat element out of range");
+					if (D == 3)
+						for (int t = 2; t <= 3; ++t) {
+							int q = gi[(t + w * a) * (long) m.N + i];
+							SA_REQUIRE(q >= 0 && q < m.N, "vfdIfoMat node out of range");
+						}
+				}
 			}
-		}
+		});
 	}
 	if (layered) {
-		std::vector<int> ly = to_host(m.elmLyr, (size_t) m.E, s);
-		for (int v : ly) SA_REQUIRE(v >= 0 && v < lyrNum, "elmLyrVec entry outside the layer tables");
+		std::vector<int> b1;
+		in_range(host_ints(o->elmLyrVec, m.elmLyr, (size_t) m.E, b1), (size_t) m.E, lyrNum,
+		         "elmLyrVec entry outside the layer tables");
 	}
 	if (tr) tr->mark("mesh: validate");
 	m.rowPtr = P.alloc<int>(m.N + 1);
@@ -279,28 +408,34 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 	{   // sliced layout: 32-row slices, slot k of row 32 s + lane at off[s] + 32 k + lane
 		int nsl = (m.N + 31) / 32;
 		std::vector<int> wid(nsl), off(nsl);
+		parallel_chunks(nsl, [&](long lo, long up) {
+			for (long sl = lo; sl < up; ++sl) {
+				int w = 0;
+				for (int i = (int) sl * 32; i < std::min(m.N, (int) sl * 32 + 32); ++i) w = std::max(w, rp[i + 1] - rp[i]);
+				wid[sl] = w;
+			}
+		});
 		long total = 0;
 		for (int sl = 0; sl < nsl; ++sl) {
-			int w = 0;
-			for (int i = sl * 32; i < std::min(m.N, sl * 32 + 32); ++i) w = std::max(w, rp[i + 1] - rp[i]);
-			wid[sl] = w;
-			off[sl] = (int) total;
-			total += 32L * w;
+			off[sl] = (int) std::min(total, (long) INT32_MAX);
+			total += 32L * wid[sl];
 		}
 		SA_REQUIRE(total < (1L << 31) / 8, "operator too large for 32-bit slot offsets");
 		std::vector<int> col(total), dest(m.Z);
-		for (int sl = 0; sl < nsl; ++sl)
-			for (int lane = 0; lane < 32; ++lane) {
-				int i = sl * 32 + lane;
-				int len = i < m.N ? rp[i + 1] - rp[i] : 0;
-				for (int k = 0; k < wid[sl]; ++k) {
-					long idx = off[sl] + 32L * k + lane;
-					if (k < len) {
-						col[idx] = fv[m.Z + rp[i] + k];
-						dest[rp[i] + k] = (int) idx;
-					} else col[idx] = i < m.N ? i : 0;     // padding: zero block on the row's own node
+		parallel_chunks(nsl, [&](long lo, long up) {
+			for (long sl = lo; sl < up; ++sl)
+				for (int lane = 0; lane < 32; ++lane) {
+					int i = (int) sl * 32 + lane;
+					int len = i < m.N ? rp[i + 1] - rp[i] : 0;
+					for (int k = 0; k < wid[sl]; ++k) {
+						long idx = off[sl] + 32L * k + lane;
+						if (k < len) {
+							col[idx] = fv[m.Z + rp[i] + k];
+							dest[rp[i] + k] = (int) idx;
+						} else col[idx] = i < m.N ? i : 0;     // padding: zero block on the row's own node
+					}
 				}
-			}
+		});
 		m.nslice = nsl;
 		m.slTotal = total;
 		m.slWidth = P.alloc<int>(nsl);
@@ -310,14 +445,16 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		// slot of the transposed entry: row j of femVtxMat is sorted by column
 		// (checked above), so (j, i) is found by bisection
 		std::vector<int> tz(m.Z);
-		for (int z = 0; z < m.Z; ++z) {
-			int i = fv[z], j = fv[m.Z + z];
-			const int *b = fv.data() + m.Z + rp[j], *e = fv.data() + m.Z + rp[j + 1];
-			const int *q = std::lower_bound(b, e, i);
-			SA_REQUIRE(q != e && *q == i, "femVtxMat pattern is not symmetric");
-			tz[z] = rp[j] + (int) (q - b);
-			SA_REQUIRE(fi[z] == fi[tz[z]], "femIfoMat lists differ between (i, j) and (j, i)");
-		}
+		parallel_chunks(m.Z, [&](long lo, long up) {
+			for (long z = lo; z < up; ++z) {
+				int i = fv[z], j = fv[m.Z + z];
+				const int *b = fv + m.Z + rp[j], *e = fv + m.Z + rp[j + 1];
+				const int *q = std::lower_bound(b, e, i);
+				SA_REQUIRE(q != e && *q == i, "femVtxMat pattern is not symmetric");
+				tz[z] = rp[j] + (int) (q - b);
+				SA_REQUIRE(fi[z] == fi[tz[z]], "femIfoMat lists differ between (i, j) and (j, i)");
+			}
+		});
 		m.transZ = P.alloc<int>(m.Z);
 		SA_CHECK(cudaMemcpyAsync(m.transZ, tz.data(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
 		// assembly order: the N diagonal slots (many elements each) first, then

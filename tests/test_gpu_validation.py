@@ -1,0 +1,70 @@
+"""Index validation of the element object on the one-call path (host inputs,
+arrays large enough that the checks run split over host threads): each
+corrupted array is rejected with its own message, and the call returns an
+error instead of faulting.  The corruption is made on the host, in numpy
+copies of a valid icosphere-3 shell element object."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def spec():
+    from shape_atrophy_gb300 import problems
+    return problems.shell_layered(level=3, lyrCntNum=5, steps=2)
+
+
+def _run(spec, key, mutate):
+    from shape_atrophy_gb300 import api
+    sp = dict(spec)
+    obj = dict(sp["elmObj"])
+    arr = np.array(obj[key], copy=True)
+    mutate(arr)
+    obj[key] = arr
+    sp["elmObj"] = obj
+    return api.forward(sp, trajectory=False, objective=False)
+
+
+def test_valid_object_runs(spec):
+    from shape_atrophy_gb300 import api
+    assert api.forward(spec, trajectory=False, objective=False)["info"]["status"] == 0
+
+
+def test_unsorted_pattern_rejected(spec):
+    def m(a):
+        z = a.shape[1] // 2
+        a[:, [z, z + 1]] = a[:, [z + 1, z]]
+    with pytest.raises(RuntimeError, match="sorted"):
+        _run(spec, "femVtxMat", m)
+
+
+def test_pattern_index_out_of_range_rejected(spec):
+    def m(a):
+        a[1, -1] = 10 ** 7
+    with pytest.raises(RuntimeError, match="femVtxMat index out of range"):
+        _run(spec, "femVtxMat", m)
+
+
+def test_asymmetric_element_lists_rejected(spec):
+    def m(a):
+        fv = spec["elmObj"]["femVtxMat"]
+        z = int(np.nonzero((fv[0] != fv[1]) & (a[0] > 1))[0][10])
+        a[0, z] -= 1                                        # (i, j) lists one element fewer than (j, i)
+    with pytest.raises(RuntimeError, match="differ between"):
+        _run(spec, "femIfoMat", m)
+
+
+def test_count_beyond_columns_rejected(spec):
+    def m(a):
+        a[0, 5] = a.shape[0]
+    with pytest.raises(RuntimeError, match="femIfoMat count exceeds"):
+        _run(spec, "femIfoMat", m)
+
+
+def test_adjacency_mismatch_rejected(spec):
+    def m(a):
+        E = spec["elmObj"]["elmVtxMat"].shape[1]
+        a[1, 100] = (a[1, 100] + E // 2) % E                   # an element of another layer
+    with pytest.raises(RuntimeError, match="vtxElmMat entry does not match"):
+        _run(spec, "vtxElmMat", m)
