@@ -164,14 +164,14 @@ SERVED = ("Poisson stream of forward solves: 3D layered shells, icosphere level 
           "the same stream served in FP64 and in mixed precision")
 
 
-SERVED_FULL = ("Poisson stream of forward solves over the whole config-5 range: 3D layered shells, icosphere "
+SERVED_FULL = ("Poisson stream of forward solves over the whole served range: 3D layered shells, icosphere "
                "level 3-6 x 4-12 prism layers (up to 532k nodes, 2.95M tets), 20-100 steps each, random bump, "
                "Lame and diffusivity per layer; served in FP64 and in mixed precision")
 
 
 def served_requests(n: int, seed: int = 7, mean_gap_s: float = 0.04, full: bool = False):
     """Seeded request stream (specs + Poisson inter-arrival gaps); meshes are shared between requests.
-    full=True draws from the whole config-5 range (icosphere 3-6, 4-12 layers, 20-100 steps)."""
+    full=True draws from the whole served range (icosphere 3-6, 4-12 layers, 20-100 steps)."""
     import numpy as np
     from shape_atrophy_gb300 import problems
     rng = np.random.default_rng(seed)
@@ -239,7 +239,7 @@ def served_leg(device: int, n: int = 32, full: bool = False):
 
 
 def mixed_error_leg(args, device: int, steps: int = 100, every: int = 10):
-    """Config 3: the mixed-precision solve of the shell against the FP64 solve, both on the GPU, at every
+    """The mixed-precision solve of the shell against the FP64 solve, both on the GPU, at every
     10th step (node positions, concentration, objective).  The FP64 GPU path stands in for the FP64 oracle
     (it matches the oracle to 1e-10 in the parity tests; the oracle itself needs minutes per step here)."""
     import numpy as np
@@ -296,7 +296,7 @@ def main():
     ap.add_argument("--no-mixed-error", action="store_true", help="skip the mixed-vs-FP64 error leg")
     ap.add_argument("--served-requests", type=int, default=32)
     ap.add_argument("--served-full", action="store_true",
-                    help="served stream over the whole config-5 range (levels 3-6, 20-100 steps; minutes)")
+                    help="served stream over the whole served range (levels 3-6, 20-100 steps; minutes)")
     args = ap.parse_args()
     rank, local, ws, dist = dist_init()
     if args.impl == "reference":

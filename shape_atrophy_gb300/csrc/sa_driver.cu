@@ -27,6 +27,7 @@
 #include <functional>
 #include <mutex>
 #include <thread>
+#include <unistd.h>
 
 struct sa_context {
 	int device = 0;
@@ -109,13 +110,17 @@ struct ArgError { std::string msg; };
 
 // A persistent pool of host threads for the set-up loops (thread start-up would cost more than the loops).
 // run(f) calls f(t) for t = 0 .. size()-1, t = 0 on the calling thread; calls from several threads are
-// serialised.
+// serialised.  The pool lives for the process (never destroyed: its workers end with the process); a
+// child made by fork() has none of the parent's threads, so it gets a pool of its own.
 class HostPool {
 public:
 	static HostPool &get()
 	{
-		static HostPool pool;
-		return pool;
+		static std::mutex m;
+		static HostPool *pool = nullptr;
+		std::lock_guard<std::mutex> g(m);
+		if (!pool || pool->pid != getpid()) pool = new HostPool();
+		return *pool;
 	}
 	int size() const { return T; }
 	void run(const std::function<void(int)> &f)
@@ -133,18 +138,9 @@ public:
 		doneCv.wait(lk, [this] { return pending == 0; });
 		job = nullptr;
 	}
-	~HostPool()
-	{
-		{
-			std::lock_guard<std::mutex> g(mu);
-			quit = true;
-		}
-		cv.notify_all();
-		for (std::thread &t : th) t.join();
-	}
 
 private:
-	HostPool() : T((int) std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency())))
+	HostPool() : T((int) std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()))), pid(getpid())
 	{
 		for (int i = 1; i < T; ++i) th.emplace_back([this, i] { worker(i); });
 	}
@@ -155,8 +151,7 @@ private:
 			const std::function<void(int)> *f;
 			{
 				std::unique_lock<std::mutex> lk(mu);
-				cv.wait(lk, [&] { return quit || gen != seen; });
-				if (quit) return;
+				cv.wait(lk, [&] { return gen != seen; });
 				seen = gen;
 				f = job;
 			}
@@ -166,13 +161,13 @@ private:
 		}
 	}
 	int T;
+	pid_t pid;
 	std::vector<std::thread> th;
 	std::mutex mu, callMu;
 	std::condition_variable cv, doneCv;
 	const std::function<void(int)> *job = nullptr;
 	long gen = 0;
 	int pending = 0;
-	bool quit = false;
 };
 
 // f(lo, hi) over [0, n) in contiguous chunks on the host pool (small n: the calling thread alone); an

@@ -18,8 +18,7 @@ dirKnlType, dirKnlWidth).
   Jacobi-PCG 1e-8, Matern-3/2 varifold (width 0.08) on the 20480 outer
   triangles.
 
-Choices the layered workloads leave open are fixed here and stated in
-DESIGN.md: bottom penalty weight ``btmWgt`` (anchors the inner boundary;
+Choices the layered workloads leave open are fixed here: bottom penalty weight ``btmWgt`` (anchors the inner boundary;
 pure elasticity has rigid-body null modes), the direction kernel ('B',
 Binet), the bump centre (outer surface, angle 0 / +z pole) and the
 target (seeded smooth displacement of the initial boundary).
