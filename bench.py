@@ -289,7 +289,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="shell", choices=["shell", "annulus"])
-    ap.add_argument("--cg-kernel", default="auto", choices=["auto", "persistent", "two-kernel"])
+    ap.add_argument("--cg-kernel", default="auto", choices=["auto", "persistent", "two-kernel", "persistent-global"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")

@@ -52,9 +52,11 @@ extern "C" {
 #define SA_PREC_FP64          0   /* all arithmetic in FP64 */
 #define SA_PREC_MIXED         1   /* FP32 operators, FP64 dots/residuals + refinement */
 
-#define SA_CG_AUTO            0   /* persistent CG kernel when the grid fits on the GPU, else two kernels */
-#define SA_CG_PERSISTENT      1   /* same as AUTO (falls back when the grid does not fit) */
+#define SA_CG_AUTO            0   /* persistent CG kernel (row state in registers when the grid fits one CTA
+                                     per SM, else vectors in global memory), two kernels when neither fits */
+#define SA_CG_PERSISTENT      1   /* same as AUTO */
 #define SA_CG_TWO_KERNEL      2   /* matvec + vector kernel per iteration */
+#define SA_CG_PERSISTENT_GLOBAL 3 /* the persistent kernel with vectors in global memory at any size */
 
 typedef struct sa_context sa_context;
 
@@ -98,7 +100,7 @@ typedef struct sa_params {
 	double cgTolSqu;
 	int rdItrMax;                       /* isotropic reaction-diffusion PCG (frame: same as cgItrMax) */
 	double rdTolSqu;                    /* isotropic RD PCG tolerance squared (frame: 1e-28) */
-	int cgKernel;                       /* SA_CG_AUTO (0), SA_CG_PERSISTENT or SA_CG_TWO_KERNEL */
+	int cgKernel;                       /* SA_CG_AUTO (0), SA_CG_PERSISTENT, SA_CG_TWO_KERNEL, SA_CG_PERSISTENT_GLOBAL */
 } sa_params;
 
 /* Varifold target and kernels (computeObjfcn prhs[13..20]). */

@@ -162,7 +162,8 @@ def _params(spec: dict, K: _Keep, precision: str) -> _lib.Params:
     p.rdItrMax = int(spec.get("rdItrMax", 0))
     p.rdTolSqu = float(spec.get("rdTolSqu", 0.0))
     p.cgKernel = {"auto": _lib.SA_CG_AUTO, "persistent": _lib.SA_CG_PERSISTENT,
-                  "two-kernel": _lib.SA_CG_TWO_KERNEL}[spec.get("cgKernel", "auto")]
+                  "two-kernel": _lib.SA_CG_TWO_KERNEL,
+                  "persistent-global": _lib.SA_CG_PERSISTENT_GLOBAL}[spec.get("cgKernel", "auto")]
     return p
 
 

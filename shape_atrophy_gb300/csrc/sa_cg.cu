@@ -726,6 +726,190 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 }
 
 // ---------------------------------------------------------------------------
+// Persistent CG for operators too large for row state in registers (more than
+// one slice per row warp at one CTA per SM): the same iteration, reducer warp
+// and fixed-point grid sums as k_cg_persist, but x, r, u, w, p, s live in
+// global memory (mostly L2) and CTA c owns the contiguous slices
+// [c nsl / nctas, (c + 1) nsl / nctas), which its row warps stride over.  The
+// CTA's column indices are cached in shared memory when they fit.
+// ---------------------------------------------------------------------------
+template <int B, typename TM, typename TV, typename TX>
+__global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
+k_cg_persist_g(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, const TV *__restrict__ binv, TX *x,
+               TV *r, TV *u, TV *w, TV *p, TV *sv, int colsCached, double *part, CgScal *sc, GridBar *bar)
+{
+	__shared__ FxScratch fs;
+	__shared__ double nx[4];                     // next gamma, rr, beta, beta * gamma / alphaPrev
+	__shared__ double al[2];                     // alpha, delta of the iteration
+	__shared__ int gaveUp;
+	extern __shared__ int scol[];
+	if (sc->done) return;
+	const int nctas = gridDim.x, lc = blockIdx.x;
+	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+	const int H = (blockDim.x >> 5) - 1;         // reducer warp; row warps 0 .. H-1
+	const bool reducer = wp == H;
+	const int nsl = (A.N + 31) >> 5;
+	const int s0 = (int) ((long) lc * nsl / nctas), s1 = (int) ((long) (lc + 1) * nsl / nctas);
+	const long c0 = s0 < nsl ? (long) __ldg(A.off + s0) : A.total;
+	const long c1 = s1 < nsl ? (long) __ldg(A.off + s1) : A.total;
+	if (colsCached)
+		for (long t = threadIdx.x; t < c1 - c0; t += blockDim.x) scol[t] = __ldg(A.col + c0 + t);
+	if (threadIdx.x == 0) gaveUp = 0;
+	__syncthreads();
+	const double bb = sc->bb, tolSqu = sc->tolSqu;
+	const int itrMax = sc->itrMax;
+	double gam = sc->gam, rr = sc->rr, alpha = 1.0, beta = 0.0;
+	double *partD = part, *partG = part + nctas;
+	unsigned int target = 0;
+	constexpr bool kBlk = block_prec<TV>();
+	int it = 0, code = SA_OK;
+	bool first = true, pending = false;
+	for (;;) {
+		// (1) rows: w = A u and (w, u) over the warp's slices.  Reducer: sums of the last update
+		double d1[1] = {0.0};
+		if (!reducer) {
+			for (int sl = s0 + wp; sl < s1; sl += H) {
+				const int i = sl * 32 + lane, wdt = __ldg(A.width + sl);
+				const long base = __ldg(A.off + sl) + lane;
+				TV acc0[B], acc1[B];
+				for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
+				int k = 0;
+				for (; k + 2 <= wdt; k += 2) {
+					const long i0 = base + ((long) k << 5), i1 = i0 + 32;
+					const int j0 = colsCached ? scol[i0 - c0] : __ldg(A.col + i0);
+					const int j1 = colsCached ? scol[i1 - c0] : __ldg(A.col + i1);
+					spmv_slot_col<B, TM, TV>(A, blk, u, i0, j0, acc0);
+					spmv_slot_col<B, TM, TV>(A, blk, u, i1, j1, acc1);
+				}
+				if (k < wdt) {
+					const long i0 = base + ((long) k << 5);
+					spmv_slot_col<B, TM, TV>(A, blk, u, i0, colsCached ? scol[i0 - c0] : __ldg(A.col + i0), acc0);
+				}
+				if (i < A.N) {
+					TV wv[B], uv[B];
+					for (int c = 0; c < B; ++c) {
+						wv[c] = acc0[c] + acc1[c];
+						w[(long) i * B + c] = wv[c];
+						uv[c] = __ldcg(u + (long) i * B + c);
+					}
+					d1[0] += (double) row_dot<B, TV>(wv, uv);
+				}
+			}
+		} else if (pending) {
+			const double g = warp_fx_partials(partG, nctas);
+			const double q = warp_fx_partials(partG + nctas, nctas);
+			if (lane == 0) {
+				nx[0] = g;
+				nx[1] = q;
+				nx[2] = g / gam;
+				nx[3] = nx[2] * g / alpha;
+			}
+		}
+		double cta1[1];
+		block_fx_sum<1, double>(d1, fs, cta1, H);
+		if (pending) {
+			gam = nx[0];
+			rr = nx[1];
+			first = false;
+			++it;
+			if (!isfinite(gam) || !isfinite(rr)) { code = SA_ERR_NONFINITE; break; }
+			if (rr < tolSqu * bb) { code = SA_OK; break; }
+			if (it >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
+		}
+		beta = first ? 0.0 : nx[2];
+		// (2) reducer: publish (w, u), wait, alpha.  Rows: p and s
+		target += (unsigned int) nctas;
+		if (reducer) {
+			int ok = 1;
+			if (lane == 0) {
+				partD[lc] = cta1[0];
+				__threadfence();
+				atomicAdd(&bar->count, 1u);
+				ok = wait_grid(bar, target) ? 1 : 0;
+				__threadfence();
+			}
+			ok = __shfl_sync(0xffffffffu, ok, 0);
+			__syncwarp();
+			if (ok) {
+				const double delta = warp_fx_partials(partD, nctas);
+				if (lane == 0) {
+					al[0] = first ? gam / delta : gam / (delta - nx[3]);
+					al[1] = delta;
+				}
+			} else if (lane == 0) {
+				gaveUp = 1;
+			}
+		} else {
+			const TV be = (TV) beta;
+			for (int sl = s0 + wp; sl < s1; sl += H) {
+				const int i = sl * 32 + lane;
+				if (i >= A.N) continue;
+				for (int c = 0; c < B; ++c) {
+					const long k = (long) i * B + c;
+					p[k] = __ldcg(u + k) + be * p[k];
+					sv[k] = w[k] + be * sv[k];
+				}
+			}
+		}
+		__syncthreads();
+		if (gaveUp) { code = SA_ERR_TIMEOUT; break; }
+		alpha = al[0];
+		if (!(alpha > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
+			code = isfinite(al[1]) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE;
+			break;
+		}
+		// (3) rows: r, u and (r, u), (r, r); x while the reducer waits for the grid (u complete)
+		double d2[2] = {0.0, 0.0};
+		const TV al_ = (TV) alpha;
+		if (!reducer) {
+			for (int sl = s0 + wp; sl < s1; sl += H) {
+				const int i = sl * 32 + lane;
+				if (i >= A.N) continue;
+				TV rk[B], uk[B];
+				for (int c = 0; c < B; ++c) {
+					const long k = (long) i * B + c;
+					rk[c] = r[k] - al_ * sv[k];
+					r[k] = rk[c];
+				}
+				if constexpr (kBlk) prec_block<B, TV>(binv + (long) i * B * B, rk, uk);
+				else for (int c = 0; c < B; ++c) uk[c] = dinv[(long) i * B + c] * rk[c];
+				for (int c = 0; c < B; ++c) u[(long) i * B + c] = uk[c];
+				d2[0] += (double) row_dot<B, TV>(rk, uk);
+				d2[1] += (double) row_dot<B, TV>(rk, rk);
+			}
+		}
+		double cta2[2];
+		block_fx_sum<2, double>(d2, fs, cta2, H);
+		target += (unsigned int) nctas;
+		if (reducer) {
+			if (lane == 0) {
+				partG[lc] = cta2[0];
+				partG[nctas + lc] = cta2[1];
+				__threadfence();
+				atomicAdd(&bar->count, 1u);
+				if (!wait_grid(bar, target)) gaveUp = 1;
+				__threadfence();
+			}
+		} else {
+			for (int sl = s0 + wp; sl < s1; sl += H) {
+				const int i = sl * 32 + lane;
+				if (i >= A.N) continue;
+				for (int c = 0; c < B; ++c) {
+					const long k = (long) i * B + c;
+					x[k] = x[k] + (TX) al_ * (TX) p[k];
+				}
+			}
+		}
+		__syncthreads();
+		if (gaveUp) { code = SA_ERR_TIMEOUT; break; }
+		pending = true;
+	}
+	if (lc == 0 && threadIdx.x == 0) {
+		sc->iters = it; sc->code = code; sc->rr = rr; sc->gam = gam; sc->done = 1;
+	}
+}
+
+// ---------------------------------------------------------------------------
 // Batched persistent CG: one cooperative launch advances many independent
 // solves (the instances of a serving batch).  Job j owns the CTAs
 // [cta0, cta0 + nctas) of the launch; its warps stride over its slices, its
@@ -940,6 +1124,42 @@ static int persist_capacity(int smCount, int warps, size_t smemBytes)
 	return v * smCount;
 }
 
+// CTAs of k_cg_persist_g (warps per CTA, dynamic shared memory) that can be resident at once
+template <int B, typename TM, typename TV, typename TX>
+static int persist_g_capacity(int smCount, int warps, size_t smemBytes)
+{
+	static bool attr = false;
+	if (warps < 2 || warps > kPersistMaxWarps || smemBytes > (size_t) kColSmemMax) return 0;
+	if (!attr) {
+		if (cudaFuncSetAttribute(k_cg_persist_g<B, TM, TV, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         kColSmemMax) != cudaSuccess) {
+			cudaGetLastError();
+			return 0;
+		}
+		attr = true;
+	}
+	int v = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist_g<B, TM, TV, TX>, 32 * warps, smemBytes) !=
+	    cudaSuccess) {
+		cudaGetLastError();
+		v = 0;
+	}
+	return v * smCount;
+}
+
+// largest slot range of the nctas contiguous CTA ranges [c nsl / nctas, (c + 1) nsl / nctas), in bytes
+static size_t col_span_bytes_even(const Mesh &m, int nctas)
+{
+	const std::vector<int> &off = m.slOffHost;
+	if ((int) off.size() != m.nslice + 1 || nctas < 1) return (size_t) -1;
+	long span = 0;
+	for (int c = 0; c < nctas; ++c) {
+		const int s0 = (int) ((long) c * m.nslice / nctas), s1 = (int) ((long) (c + 1) * m.nslice / nctas);
+		span = std::max(span, (long) off[s1] - off[s0]);
+	}
+	return (size_t) span * sizeof(int);
+}
+
 // largest slot range of one CTA (pw consecutive slices), in column-index bytes
 static size_t col_span_bytes(const Mesh &m, int pw)
 {
@@ -980,7 +1200,7 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	const int pw = std::max(1, std::min(pwCap, (m.nslice + prof->smCount - 1) / prof->smCount));
 	const int nctas = (m.nslice + pw - 1) / pw;
 	const size_t colSmem = col_span_bytes(m, pw);
-	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar &&
+	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->cgKernel != SA_CG_PERSISTENT_GLOBAL && prof->bar &&
 	                     (!block_prec<TV>() || prof->binv32) &&
 	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw + 1, colSmem);
 	if (persist) {
@@ -1023,6 +1243,53 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		// any CTA that gave up leaves the abort flag set, whatever CTA 0 reported
 		if (gaveUp || h.code == SA_ERR_TIMEOUT) throw DeviceWaitError{"persistent CG grid barrier"};
 		return h;
+	}
+	// too large for row state in registers: the global-state persistent kernel, one CTA per SM
+	if (prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar && (!block_prec<TV>() || prof->binv32)) {
+		const int warpsG = pwCap + 1;
+		const int nctasG = std::min(prof->smCount, m.nslice);
+		const size_t span = col_span_bytes_even(m, nctasG);
+		const int cached = span <= (size_t) kColSmemMax ? 1 : 0;
+		const size_t smemG = cached ? span : 0;
+		if (nctasG >= 1 && nctasG <= persist_g_capacity<B, TM, TV, TX>(prof->smCount, warpsG, smemG)) {
+			const TV *binv = nullptr;
+			if constexpr (block_prec<TV>()) {
+				binv = prof->binv32;
+				k_cg_init_blk<B><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
+			} else {
+				k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
+			}
+			SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
+			SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
+			GridBar *bar = (GridBar *) prof->bar;
+			SA_CHECK(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
+			SellOp A = sell_of(m);
+			void *args[] = {&A, (void *) &blk, (void *) &dinv, (void *) &binv, (void *) &x, (void *) &r, (void *) &u,
+			                (void *) &w, (void *) &p, (void *) &sv, (void *) &cached, (void *) &part, (void *) &sc,
+			                (void *) &bar};
+			if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
+			SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist_g<B, TM, TV, TX>, dim3(nctasG),
+			                                     dim3(32 * warpsG), args, smemG, s));
+			if (timing) SA_CHECK(cudaEventRecord(prof->ev[1], s));
+			k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
+			prof->launches += 3;
+			unsigned int gaveUp = 0;
+			SA_CHECK(cudaMemcpyAsync(&gaveUp, &bar->abort, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+			CgScal h = read_scal(sc, s);
+			if (timing && h.iters > 0) {
+				float ms = 0.f;
+				SA_CHECK(cudaEventElapsedTime(&ms, prof->ev[0], prof->ev[1]));
+				prof->spmvMs += ms;
+				prof->spmvCount += 1;
+				// per iteration: operator values (+ columns unless cached), slice table, u gathered, and the
+				// vectors w, p, s, r, x read and written, u read twice and written
+				prof->profBytes += (double) h.iters * ((double) m.slTotal * (B * B * sizeof(TM) + (cached ? 0.0 : 4.0)) +
+				                                       8.0 * m.nslice + 14.0 * sizeof(TV) * n);
+				prof->profFlops += (double) h.iters * 2.0 * ((double) B * B * m.slTotal + 8.0 * n);
+			}
+			if (gaveUp || h.code == SA_ERR_TIMEOUT) throw DeviceWaitError{"persistent CG grid barrier"};
+			return h;
+		}
 	}
 	SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
 	SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));

@@ -725,7 +725,7 @@ static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *
 	SA_REQUIRE(md.timeNum >= 1, "timeNum must be >= 1");
 	md.rdItrMax = p->rdItrMax > 0 ? p->rdItrMax : std::max(p->cgItrMax, 1000);
 	md.rdTolSqu = p->rdTolSqu > 0.0 ? p->rdTolSqu : (md.frame ? 1e-26 : p->cgTolSqu);
-	SA_REQUIRE(p->cgKernel >= SA_CG_AUTO && p->cgKernel <= SA_CG_TWO_KERNEL, "cgKernel must be 0, 1 or 2");
+	SA_REQUIRE(p->cgKernel >= SA_CG_AUTO && p->cgKernel <= SA_CG_PERSISTENT_GLOBAL, "cgKernel must be 0, 1, 2 or 3");
 	md.cgKernel = p->cgKernel;
 	if (tgt) {
 		md.cenKnl = tgt->cenKnlType; md.dirKnl = tgt->dirKnlType;

@@ -1,7 +1,7 @@
 """Largest meshes of the workload family: an icosphere level-6 shell with 12
 prism layers (532 494 nodes, 2.95 M tets, the top of the served range).  Its
-persistent-CG grid does not fit on the GPU, so this is the two-kernel CG path
-at scale.  One time step is compared with the CPU oracle (1e-9 at the
+row state does not fit in registers at one CTA per SM, so this is the
+persistent CG with vectors in global memory at scale.  One time step is compared with the CPU oracle (1e-9 at the
 workload's CG tolerance 1e-8), and mixed precision with FP64 (1e-6)."""
 import numpy as np
 import pytest

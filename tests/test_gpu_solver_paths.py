@@ -1,8 +1,9 @@
 """Solver variants on the GPU against the oracle.
 
-- persistent CG kernel (one cooperative launch per solve) and the two-kernel
-  CG (matvec + vector kernel per iteration) both match the FP64 oracle to
-  1e-10 relative, and each other to 1e-12;
+- persistent CG kernel (one cooperative launch per solve; row state in
+  registers, or vectors in global memory for operators too large for that),
+  and the two-kernel CG (matvec + vector kernel per iteration) all match the
+  FP64 oracle to 1e-10 relative, and each other to 1e-12;
 - mixed precision (FP32 operators and vectors, FP64 dots and iterative
   refinement) stays within 1e-6 relative of the FP64 oracle in node
   positions, concentration and objective;
@@ -43,7 +44,7 @@ def test_cg_paths_match_oracle_and_each_other(name, oracle_runs):
     from shape_atrophy_gb300 import api
     want = oracle_runs[name]
     runs = {}
-    for path in ("persistent", "two-kernel"):
+    for path in ("persistent", "two-kernel", "persistent-global"):
         spec = _case(name)
         spec["cgKernel"] = path
         got = api.forward(spec, trajectory=True, objective=True)
@@ -52,14 +53,16 @@ def test_cg_paths_match_oracle_and_each_other(name, oracle_runs):
         assert rel(got["tauMat"], want["tauMat"]) < TOL, path
         assert abs(got["obj"][0] - want["obj"]) <= TOL * abs(want["obj"]), path
         runs[path] = got
-    a, b = runs["persistent"], runs["two-kernel"]
-    assert rel(a["lmkStk"], b["lmkStk"]) < 1e-12
-    assert rel(a["tauMat"], b["tauMat"]) < 1e-12
-    assert a["info"]["cgIterTotal"] == pytest.approx(b["info"]["cgIterTotal"], abs=2 * 4)
+    a = runs["persistent"]
+    for other in ("two-kernel", "persistent-global"):
+        b = runs[other]
+        assert rel(a["lmkStk"], b["lmkStk"]) < 1e-12, other
+        assert rel(a["tauMat"], b["tauMat"]) < 1e-12, other
+        assert a["info"]["cgIterTotal"] == pytest.approx(b["info"]["cgIterTotal"], abs=2 * 4), other
 
 
 @pytest.mark.parametrize("name", ["annulus", "shell"])
-@pytest.mark.parametrize("path", ["persistent", "two-kernel"])
+@pytest.mark.parametrize("path", ["persistent", "two-kernel", "persistent-global"])
 def test_mixed_precision_error_against_fp64_oracle(name, path, oracle_runs):
     from shape_atrophy_gb300 import api
     want = oracle_runs[name]
