@@ -148,6 +148,22 @@ int sa_forward(sa_context *ctx, const sa_element_object *obj, const double *lmkI
 int sa_varifold(sa_context *ctx, const sa_element_object *obj, const double *lmkMat,
                 const sa_target *tgt, int precision, double *obj_out, double *gradMat);
 
+/* Objective and its gradient with respect to the bump parameters (no
+ * reference counterpart; the reference's computeObjfcn returns objectives
+ * only).  Layered model (elaType isotropic, ldmWgt 0), FP64, one parameter
+ * vector tauVarVec = [c (dim values), h, sigma]: runs the forward solve with
+ * the tangent-linear model of every time step for each of the dim + 2
+ * parameters (one extra velocity and reaction-diffusion solve per parameter
+ * and step, on the operators of the forward step) and returns
+ * objOut = J(x_T) and gradOut[k] = dJ/dp_k, k = 0 .. dim + 1.  The gradient
+ * is that of the discrete model (exact up to the CG tolerances).  A failed
+ * solve gives objOut = DBL_MAX, NaN gradient and its status in info;
+ * info->cgIterMax holds the iterations of all tangent solves.  Needs the
+ * element object's vfdIfoMat (varifold gradient). */
+int sa_objective_gradient(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat,
+                          const sa_params *prm, const sa_target *tgt, const double *tauVarVec, int tauVarNum,
+                          double *objOut, double *gradOut, sa_solve_info *info);
+
 /* Varifold objective without any device allocation (no counterpart in the
  * reference).  For callers that must not allocate while they evaluate the
  * objective: an optimiser's line search that calls it hundreds of times on

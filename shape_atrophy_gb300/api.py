@@ -216,6 +216,34 @@ def forward(spec: dict, tauVarMat=None, precision: str = "fp64", trajectory: boo
                           elapsedMs=info.elapsedMs))
 
 
+def gradient(spec: dict, tauVarVec=None, device: int = 0) -> dict:
+    """Objective and its gradient with respect to the bump parameters [c (dim), h, sigma] of one parameter
+    vector (layered model, FP64): the forward solve with the tangent-linear model of every step
+    (sa_objective_gradient).  Returns dict(obj, grad (dim + 2,), info)."""
+    ctx = context(device)
+    D = int(spec["dim"])
+    lmk = np.ascontiguousarray(np.asarray(spec["lmkIniMat"], dtype=np.float64))
+    N = lmk.shape[1]
+    tv = np.ascontiguousarray(np.asarray(spec["tauVarVec"] if tauVarVec is None else tauVarVec,
+                                         dtype=np.float64).reshape(-1))
+    K = _Keep()
+    o = _element_object(spec["elmObj"], D, N, K, with_vfd=True, with_grad=True)
+    if "elmLyrVec" in spec:
+        o.elmLyrVec = K.i32(spec["elmLyrVec"])
+    p = _params(spec, K, "fp64")
+    t = _target(spec, K)
+    obj = np.zeros(1)
+    grad = np.zeros(D + 2)
+    info = _lib.SolveInfo()
+    rc = ctx.lib.sa_objective_gradient(ctx.h, C.byref(o), lmk.ctypes.data_as(_lib._dp), C.byref(p), C.byref(t),
+                                       tv.ctypes.data_as(_lib._dp), tv.size, obj.ctypes.data_as(_lib._dp),
+                                       grad.ctypes.data_as(_lib._dp), C.byref(info))
+    ctx.check(rc, "sa_objective_gradient")
+    return dict(obj=float(obj[0]), grad=grad,
+                info=dict(status=info.status, cgIterTotal=info.cgIterTotal, rdIterTotal=info.rdIterTotal,
+                          tangentIters=info.cgIterMax, elapsedMs=info.elapsedMs))
+
+
 def varifold(spec: dict, lmk, grad: bool = False, precision: str = "fp64", device: int = 0):
     """Varifold objective of the shape ``lmk`` (D, N) against spec['tgt'];
     with grad=True also its gradient with respect to the nodes, (D, N)."""

@@ -27,6 +27,7 @@
 #include <functional>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 #include <unistd.h>
 
 struct sa_context {
@@ -855,6 +856,144 @@ static int varifold_impl(sa_context *ctx, const sa_element_object *obj, const do
 			for (int d = 0; d < D; ++d) o[(size_t) d * m.N + i] = h[(size_t) i * D + d];
 		SA_CHECK(cudaMemcpyAsync(grad, o.data(), sizeof(double) * o.size(), cudaMemcpyDefault, s));
 		SA_CHECK(cudaStreamSynchronize(s));
+	}
+	return SA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// objective gradient with respect to the bump parameters [c, h, sigma]
+// (layered model): the forward steps with the tangent-linear model of every
+// step carried along for each of the dim + 2 parameters (sa_tangent.cu), then
+// dJ/dp_k = grad_x J(x_T) . dx_T,k.  One extra velocity and one extra
+// reaction-diffusion solve per parameter and step, on the operators the
+// forward step assembled; no trajectory is stored.
+// ---------------------------------------------------------------------------
+template <int D>
+static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const double *lmkIni, const sa_params *prm,
+                         const sa_target *tgt, const double *tauVar, int tauVarNum, double *objOut, double *gradOut,
+                         sa_solve_info *info)
+{
+	cudaStream_t s = ctx->stream;
+	PhaseTrace tr(s);
+	Pool P(s);
+	Mesh m;
+	Model md;
+	fill_model(md, D, prm, tgt, P);
+	SA_REQUIRE(!md.frame && md.ldmWgt == 0.0, "gradients: layered model (elaType isotropic, ldmWgt 0) only");
+	SA_REQUIRE(md.precision == SA_PREC_FP64, "gradients: FP64 only");
+	SA_REQUIRE(tgt && tgt->tgtElmNum > 0 && tgt->cenPosMat && tgt->uniDirMat && tgt->elmVolVec, "gradients need a target");
+	const int K = D + 2;
+	SA_REQUIRE(tauVar && tauVarNum >= K, "tauVarVec needs [c (dim), h, sigma]");
+	build_mesh(m, obj, true, true, true, md.lyrNum, P, &tr);
+	const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
+	std::vector<double> tv = to_host(tauVar, (size_t) tauVarNum, s);
+	const double *tc = P.dev(tgt->cenPosMat, (size_t) tgt->tgtElmNum * D);
+	const double *tu = P.dev(tgt->uniDirMat, (size_t) tgt->tgtElmNum * D);
+	const double *tvl = P.dev(tgt->elmVolVec, (size_t) tgt->tgtElmNum);
+	Work w;
+	alloc_work<D>(w, m, md, false, P);
+	{
+		double *xa = P.alloc<double>((size_t) m.N * D);
+		launch_soa_to_aos(m.N, D, x0, xa, s);
+		k_init_sign<D><<<grid_for(m.E), kBlock, 0, s>>>(m.E, m.elmVtx, xa, m.sign0);
+	}
+	const long n = (long) m.N * D, N = m.N;
+	// tangent state per parameter: positions (two copies: t, t+1), concentration (t, t+1), velocity
+	std::vector<double *> dx[2], dtau[2], dv;
+	for (int k = 0; k < K; ++k) {
+		for (int c = 0; c < 2; ++c) { dx[c].push_back(P.zeros<double>(n)); dtau[c].push_back(P.zeros<double>(N)); }
+		dv.push_back(P.zeros<double>(n));
+	}
+	double *drecA = P.alloc<double>((size_t) rec_len<D>() * m.E), *drecB = P.alloc<double>((size_t) rec_len<D>() * m.E);
+	double *rhsV = P.alloc<double>(n), *rhsT = P.alloc<double>(N), *dpd = P.zeros<double>(N), *dfy = P.alloc<double>(N);
+	double *gx = P.alloc<double>(n);
+	Stepper<D> st(m, md, w, s);
+	st.start(x0, tv.data());
+	for (int k = 0; k < K; ++k) launch_tau0_tan<D>(m, st.xn, st.tau_now(), tv.data(), k, dtau[0][k], s);
+	tr.mark("inputs, work buffers");
+	SA_CHECK(cudaEventRecord(ctx->e0, s));
+	int cur = 0, status = SA_OK, tanIts = 0;
+	const int T = md.timeNum;
+	const double dt = md.timeStp, y0 = md.ynk[0];
+	auto solve = [&](auto B_, const double *A, const double *dinvA, const double *rhs, double *xs, int itrMax,
+	                 double tolSqu) {
+		constexpr int B = decltype(B_)::value;
+		int its = 0;
+		int code = cg_jacobi<B>(m, A, dinvA, rhs, xs, itrMax, tolSqu, w.cw, st.st, &its, s, SA_PREC_FP64);
+		tanIts += its;
+		return code;
+	};
+	while (st.t < T - 1 && status == SA_OK) {
+		st.pre_velocity();
+		int its = 0;
+		int code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st.st, &its, s,
+		                        SA_PREC_FP64);
+		st.out.cgTotal += its;
+		st.out.cgMax = std::max(st.out.cgMax, its);
+		if (code != SA_OK) { status = code; break; }
+		// velocity tangents: K dv = db - dK v - btmWgt dpd v at x_t
+		for (int k = 0; k < K && status == SA_OK; ++k) {
+			launch_geom_tan<D>(m, st.gn->rec, dx[cur][k], drecA, s);
+			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_tan<D>(m, st.xn, dx[cur][k], dpd, s);
+			launch_axpy64(N, dtau[cur][k], y0 - 1.0, dtau[cur][k], dfy, s);     // dfy = y0 dtau
+			launch_vel_tan_rhs<D>(m, md, st.gn->rec, drecA, w.fy, dfy, w.v, dpd, rhsV, s);
+			code = solve(std::integral_constant<int, D>(), w.blk, w.dinv, rhsV, dv[k], md.cgItrMax, md.cgTolSqu);
+			if (code != SA_OK) { status = code; break; }
+			launch_axpy64(n, dx[cur][k], dt, dv[k], dx[1 - cur][k], s);
+		}
+		if (status != SA_OK) break;
+		st.post_velocity();
+		int rits = 0;
+		code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, st.tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, st.st, &rits, s,
+		                    SA_PREC_FP64);
+		st.out.rdTotal += rits;
+		if (code != SA_OK) { status = code; break; }
+		// concentration tangents: L dtau' = dM_t (tau + dt R) + M_t (dtau + dt R' dtau) - (dM' + dt dG') tau'
+		for (int k = 0; k < K && status == SA_OK; ++k) {
+			launch_geom_tan<D>(m, st.gn->rec, dx[cur][k], drecA, s);
+			launch_geom_tan<D>(m, st.gx->rec, dx[1 - cur][k], drecB, s);
+			launch_rd_tan_rhs<D>(m, md, w.Mnow, st.gn->rec, drecA, st.gx->rec, drecB, st.tau_now(), w.fr,
+			                     dtau[cur][k], st.tau_next(), rhsT, s);
+			SA_CHECK(cudaMemcpyAsync(dtau[1 - cur][k], dtau[cur][k], sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+			code = solve(std::integral_constant<int, 1>(), w.L, w.dinvRd, rhsT, dtau[1 - cur][k], md.rdItrMax,
+			             md.rdTolSqu);
+			if (code != SA_OK) { status = code; break; }
+		}
+		if (status != SA_OK) break;
+		st.end_step();
+		cur = 1 - cur;
+	}
+	st.finish();
+	double J = DBL_MAX;
+	std::vector<double> grad((size_t) K, std::nan(""));
+	if (status == SA_OK) {
+		int err = SA_OK;
+		J = varifold<D>(m, md, w.xa, tc, tu, tvl, tgt->tgtElmNum, gx, s, SA_PREC_FP64, &err, nullptr);
+		SA_REQUIRE(err == SA_OK, "varifold gradient needs vfdIfoMat");
+		std::vector<double> hg = to_host(gx, (size_t) n, s);
+		for (int k = 0; k < K; ++k) {
+			std::vector<double> hd = to_host(dx[cur][k], (size_t) n, s);
+			double acc = 0.0;
+			for (long q = 0; q < n; ++q) acc += hg[q] * hd[q];
+			grad[k] = acc;
+		}
+	}
+	SA_CHECK(cudaEventRecord(ctx->e1, s));
+	SA_CHECK(cudaEventSynchronize(ctx->e1));
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, ctx->e0, ctx->e1);
+	tr.mark("forward + tangent steps, objective, gradient");
+	if (objOut) SA_CHECK(cudaMemcpyAsync(objOut, &J, sizeof(double), cudaMemcpyDefault, s));
+	if (gradOut) SA_CHECK(cudaMemcpyAsync(gradOut, grad.data(), sizeof(double) * K, cudaMemcpyDefault, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	if (info) {
+		info->status = status;
+		info->cgIterTotal = st.out.cgTotal;
+		info->rdIterTotal = st.out.rdTotal;
+		info->cgIterMax = tanIts;            // iterations of all tangent solves
+		info->invertedElements = st.out.inverted;
+		info->elapsedMs = ms;
+		info->kernelLaunches = w.cw.launches;
 	}
 	return SA_OK;
 }
@@ -1694,6 +1833,19 @@ int sa_session_step(sa_session *s, int nsteps, int *stepsDone)
 		int k = s->impl->step(nsteps);
 		if (stepsDone) *stepsDone = k;
 		return SA_OK;
+	});
+}
+
+int sa_objective_gradient(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat,
+                          const sa_params *prm, const sa_target *tgt, const double *tauVarVec, int tauVarNum,
+                          double *objOut, double *gradOut, sa_solve_info *info)
+{
+	if (!ctx || !obj || !prm) return SA_ERR_ARG;
+	return sa::guarded(ctx, [&]() {
+		if (obj->dim == 2)
+			return sa::gradient_impl<2>(ctx, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum, objOut, gradOut, info);
+		SA_REQUIRE(obj->dim == 3, "dim must be 2 or 3");
+		return sa::gradient_impl<3>(ctx, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum, objOut, gradOut, info);
 	});
 }
 

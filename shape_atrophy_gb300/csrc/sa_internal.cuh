@@ -300,6 +300,19 @@ template <int D> void launch_rd_rhs(const Mesh &m, const Geom &gNow, const doubl
 template <int D> void launch_advance(int N, const double *x, const double *v, double dt, double *xn,
                                      double *trajSlot, cudaStream_t s);
 void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_t s);
+// tangent-linear kernels of the layered model (sa_tangent.cu)
+void launch_axpy64(long n, const double *x, double a, const double *y, double *out, cudaStream_t s);
+template <int D> void launch_geom_tan(const Mesh &m, const double *rec, const double *dx, double *drec, cudaStream_t s);
+template <int D> void launch_penalty_tan(const Mesh &m, const double *x, const double *dx, double *dpd, cudaStream_t s);
+template <int D> void launch_vel_tan_rhs(const Mesh &m, const Model &md, const double *rec, const double *drec,
+                                         const double *fy, const double *dfy, const double *v, const double *dpd,
+                                         double *out, cudaStream_t s);
+template <int D> void launch_rd_tan_rhs(const Mesh &m, const Model &md, const double *Mnow, const double *recNow,
+                                        const double *drecNow, const double *recNext, const double *drecNext,
+                                        const double *tau, const double *fr, const double *dtau,
+                                        const double *tauNext, double *out, cudaStream_t s);
+template <int D> void launch_tau0_tan(const Mesh &m, const double *x, const double *tau0, const double *tv, int k,
+                                      double *dtau, cudaStream_t s);
 void launch_aos_to_soa(int N, int D, const double *aos, double *soa, cudaStream_t s);
 
 
