@@ -294,6 +294,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
     ap.add_argument("--no-mixed-error", action="store_true", help="skip the mixed-vs-FP64 error leg")
+    ap.add_argument("--no-gradient", action="store_true", help="skip the objective-gradient leg")
     ap.add_argument("--served-requests", type=int, default=32)
     ap.add_argument("--served-full", action="store_true",
                     help="served stream over the whole served range (levels 3-6, 20-100 steps; minutes)")
@@ -401,6 +402,23 @@ def main():
     if not args.no_mixed_error and rank == 0 and args.workload == "shell":
         mixed_error = mixed_error_leg(args, local)
 
+    gradient = None
+    if not args.no_gradient and rank == 0 and args.precision == "fp64":
+        # objective + gradient with respect to the bump parameters (tangent-linear model) against one forward
+        # solve with objective, same K steps, host buffers, both synchronous calls timed on the host clock
+        spec_g = spec_for(args, K)
+        api.forward(spec_g, trajectory=False, objective=True, device=local)        # warm-up
+        t0 = time.perf_counter()
+        api.forward(spec_g, trajectory=False, objective=True, device=local)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        gr = api.gradient(spec_g, device=local)
+        t_grad = time.perf_counter() - t0
+        gradient = {"what": f"sa_objective_gradient ({K} steps, objective and d obj / d [c, h, sigma], "
+                            "tangent-linear model of every step) beside one sa_forward of the same steps",
+                    "params": int(gr["grad"].size), "s": t_grad, "forward_s": t_fwd, "vs_forward": t_grad / t_fwd,
+                    "status": gr["info"]["status"]}
+
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:
         v, cores, sample = cpu_sample(spec_for(args, 4))
@@ -415,7 +433,7 @@ def main():
                            "elements": spec["elmObj"]["elmVtxMat"].shape[1], "cg_iters_per_step": cg_iters / K,
                            "l2": "per-step working set (~0.3 GB) larger than the 129 MB L2",
                            "parallelism": f"replicas x{ws}"},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "objective": objective,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "objective": objective, "gradient": gradient,
                 "mixed_error": mixed_error, "served": served,
                 "clocks": clocks,
                 "gpu_launches": launches}
