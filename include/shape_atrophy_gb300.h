@@ -150,13 +150,16 @@ int sa_varifold(sa_context *ctx, const sa_element_object *obj, const double *lmk
 
 /* Objective and its gradient with respect to the bump parameters (no
  * reference counterpart; the reference's computeObjfcn returns objectives
- * only).  Layered model (elaType isotropic, ldmWgt 0), FP64, one parameter
+ * only).  Layered model (elaType isotropic, ldmWgt 0), one parameter
  * vector tauVarVec = [c (dim values), h, sigma]: runs the forward solve with
  * the tangent-linear model of every time step for each of the dim + 2
  * parameters (one extra velocity and reaction-diffusion solve per parameter
  * and step, on the operators of the forward step) and returns
  * objOut = J(x_T) and gradOut[k] = dJ/dp_k, k = 0 .. dim + 1.  The gradient
- * is that of the discrete model (exact up to the CG tolerances).  A failed
+ * is that of the discrete model (exact up to the CG tolerances).  With
+ * prm->precision SA_PREC_MIXED the velocity solves (forward and tangent) run
+ * as FP32 inner CG with FP64 refinement and the objective in FP32 pair sums
+ * (the reaction-diffusion solves stay FP64, as in the forward model).  A failed
  * solve gives objOut = DBL_MAX, NaN gradient and its status in info;
  * info->cgIterMax holds the iterations of all tangent solves.  Needs the
  * element object's vfdIfoMat (varifold gradient). */

@@ -216,10 +216,11 @@ def forward(spec: dict, tauVarMat=None, precision: str = "fp64", trajectory: boo
                           elapsedMs=info.elapsedMs))
 
 
-def gradient(spec: dict, tauVarVec=None, device: int = 0) -> dict:
+def gradient(spec: dict, tauVarVec=None, precision: str = "fp64", device: int = 0) -> dict:
     """Objective and its gradient with respect to the bump parameters [c (dim), h, sigma] of one parameter
-    vector (layered model, FP64): the forward solve with the tangent-linear model of every step
-    (sa_objective_gradient).  Returns dict(obj, grad (dim + 2,), info)."""
+    vector (layered model): the forward solve with the tangent-linear model of every step
+    (sa_objective_gradient).  precision="mixed" runs the velocity solves (forward and tangent) as FP32 inner
+    CG with FP64 refinement and the objective in FP32 pair sums.  Returns dict(obj, grad (dim + 2,), info)."""
     ctx = context(device)
     D = int(spec["dim"])
     lmk = np.ascontiguousarray(np.asarray(spec["lmkIniMat"], dtype=np.float64))
@@ -230,7 +231,7 @@ def gradient(spec: dict, tauVarVec=None, device: int = 0) -> dict:
     o = _element_object(spec["elmObj"], D, N, K, with_vfd=True, with_grad=True)
     if "elmLyrVec" in spec:
         o.elmLyrVec = K.i32(spec["elmLyrVec"])
-    p = _params(spec, K, "fp64")
+    p = _params(spec, K, precision)
     t = _target(spec, K)
     obj = np.zeros(1)
     grad = np.zeros(D + 2)

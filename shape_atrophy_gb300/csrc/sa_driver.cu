@@ -880,7 +880,6 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 	Model md;
 	fill_model(md, D, prm, tgt, P);
 	SA_REQUIRE(!md.frame && md.ldmWgt == 0.0, "gradients: layered model (elaType isotropic, ldmWgt 0) only");
-	SA_REQUIRE(md.precision == SA_PREC_FP64, "gradients: FP64 only");
 	SA_REQUIRE(tgt && tgt->tgtElmNum > 0 && tgt->cenPosMat && tgt->uniDirMat && tgt->elmVolVec, "gradients need a target");
 	const int K = D + 2;
 	SA_REQUIRE(tauVar && tauVarNum >= K, "tauVarVec needs [c (dim), h, sigma]");
@@ -915,11 +914,14 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 	int cur = 0, status = SA_OK, tanIts = 0;
 	const int T = md.timeNum;
 	const double dt = md.timeStp, y0 = md.ynk[0];
+	// velocity solves in the model's precision (mixed: FP32 inner CG with FP64 refinement, as the forward
+	// step); reaction-diffusion solves in FP64, as the forward step
 	auto solve = [&](auto B_, const double *A, const double *dinvA, const double *rhs, double *xs, int itrMax,
 	                 double tolSqu) {
 		constexpr int B = decltype(B_)::value;
 		int its = 0;
-		int code = cg_jacobi<B>(m, A, dinvA, rhs, xs, itrMax, tolSqu, w.cw, st.st, &its, s, SA_PREC_FP64);
+		int code = cg_jacobi<B>(m, A, dinvA, rhs, xs, itrMax, tolSqu, w.cw, st.st, &its, s,
+		                        B == D ? md.precision : SA_PREC_FP64);
 		tanIts += its;
 		return code;
 	};
@@ -927,7 +929,7 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 		st.pre_velocity();
 		int its = 0;
 		int code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st.st, &its, s,
-		                        SA_PREC_FP64);
+		                        md.precision);
 		st.out.cgTotal += its;
 		st.out.cgMax = std::max(st.out.cgMax, its);
 		if (code != SA_OK) { status = code; break; }
@@ -968,7 +970,7 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 	std::vector<double> grad((size_t) K, std::nan(""));
 	if (status == SA_OK) {
 		int err = SA_OK;
-		J = varifold<D>(m, md, w.xa, tc, tu, tvl, tgt->tgtElmNum, gx, s, SA_PREC_FP64, &err, nullptr);
+		J = varifold<D>(m, md, w.xa, tc, tu, tvl, tgt->tgtElmNum, gx, s, md.precision, &err, nullptr);
 		SA_REQUIRE(err == SA_OK, "varifold gradient needs vfdIfoMat");
 		std::vector<double> hg = to_host(gx, (size_t) n, s);
 		for (int k = 0; k < K; ++k) {

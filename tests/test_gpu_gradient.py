@@ -9,6 +9,8 @@ differences are not limited by the solves).
   3e-8 on the shell and 2e-9 on the annulus);
 - the objective returned with the gradient is the one-call forward
   objective of the same parameters (1e-12);
+- mixed precision (FP32 inner velocity solves, FP32 pair sums) gives the
+  FP64 gradient to 1e-5 of its largest component;
 - the frame model is refused with an error.
 """
 import numpy as np
@@ -45,6 +47,16 @@ def test_gradient_matches_central_differences(name):
     scale = np.abs(fd).max()
     assert scale > 0
     np.testing.assert_allclose(g["grad"], fd, rtol=0, atol=1e-6 * scale)
+
+
+@pytest.mark.parametrize("name", ["shell", "annulus"])
+def test_mixed_precision_gradient_close_to_fp64(name):
+    from shape_atrophy_gb300 import api
+    spec = _cases()[name]
+    spec["cgTolSqu"] = 1e-16                    # the workload tolerance, 1e-8 relative residual
+    g64 = api.gradient(spec)["grad"]
+    g32 = api.gradient(spec, precision="mixed")["grad"]
+    np.testing.assert_allclose(g32, g64, rtol=0, atol=1e-5 * np.abs(g64).max())
 
 
 def test_gradient_refuses_frame_model():
