@@ -1,6 +1,6 @@
 """Launch-shape autotuner.
 
-Measures the four launch shapes of the CUDA library on the current device and
+Measures the launch shapes (and the mixed-precision inner floor) of the CUDA library on the current device and
 writes them to ``tuning.json`` beside this file, keyed by device name and SM
 count; ``api.context()`` applies the entry for its device the first time a
 context is made (``SA_TUNING=off`` keeps the compiled defaults).
@@ -16,6 +16,9 @@ far):
 * ``vfdCtasPerSm`` -- CTAs per SM of the varifold pair sums (sets the number of
   column chunks).  Workload: the varifold objective of the same shell, FP64 and
   mixed.
+* ``mixedInnerFloor`` -- the lowest squared relative residual (10^-k) the FP32
+  inner solves of mixed precision aim for before the FP64 refinement takes
+  over.  Workload: mixed-precision steps of the same shell.
 * ``batchBlock`` x ``batchSlicesPerWarp`` -- CTA size of the batched serving CG
   and the rows per warp that size each solve's share of CTAs.  Workload: a
   seeded batch of shell requests (icosphere 3-5, 4-12 layers, 20 steps)
@@ -44,6 +47,7 @@ from . import api, problems
 CANDIDATES = {
     "persistMaxWarps": [8, 12, 16, 20],
     "vfdCtasPerSm": [2, 4, 8, 16, 32],
+    "mixedInnerFloor": [8, 9, 10, 11, 12],
     "batchBlock": [128, 256],
     "batchSlicesPerWarp": [1, 2, 4],
 }
@@ -132,6 +136,8 @@ def tune(reps=3, device=0, log=print):
     log("varifold pair sums (icosphere-5 shell, ms per objective, FP64 + mixed)")
     sweep("vfdCtasPerSm", lambda: time_objective(shell, "fp64", device=device) +
           time_objective(shell, "mixed", device=device))
+    log("mixed-precision inner floor (icosphere-5 shell, ms per mixed step)")
+    sweep("mixedInnerFloor", lambda: time_steps(shell, "mixed", device=device))
     log("batched CG (16 shell requests at once, ms to drain, FP64 + mixed)")
     time_served(reqs[:2], "fp64", device=device)     # warm the server path
     for name in ("batchBlock", "batchSlicesPerWarp"):
@@ -140,6 +146,7 @@ def tune(reps=3, device=0, log=print):
     return {"name": name, "smCount": sms, "values": best, "ms": meas, "reps": reps,
             "workloads": {"persistMaxWarps": "icosphere-5 shell, 8 prism layers, 10 steps after 3, FP64 + mixed",
                           "vfdCtasPerSm": "varifold objective of the same shell, 5 calls, FP64 + mixed",
+                          "mixedInnerFloor": "mixed-precision steps of the same shell, 10 steps after 3",
                           "batchBlock": "16 seeded shell requests (icosphere 3-5, 4-12 layers, 20 steps) "
                                         "drained by the server, FP64 + mixed",
                           "batchSlicesPerWarp": "as batchBlock"}}

@@ -1394,9 +1394,10 @@ int cg_jacobi(const Mesh &m, const double *blk, const double *dinv, const double
 		if (h0.zero) { SA_CHECK(cudaMemsetAsync(x, 0, sizeof(double) * n, s)); code = SA_OK; break; }
 		if (h0.rr < tolSqu * bb) { code = SA_OK; break; }
 		if (total >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
-		// inner tolerance: 1e-5 relative, or just below what the outer test still needs
+		// inner tolerance: just below what the outer test still needs, not below the FP32 floor
 		double need = 0.01 * tolSqu * bb / h0.rr;
-		double innerTol = need > 1e-10 ? need : 1e-10;
+		const double floorSqu = std::pow(10.0, -(double) tuning().mixedInnerFloor);
+		double innerTol = need > floorSqu ? need : floorSqu;
 		SA_CHECK(cudaMemsetAsync(d32, 0, sizeof(float) * n, s));
 		CgScal h = run_cg<B, float, float, float>(m, wk.blk32, dinv32, rin, d32, zero, r32, u32, w32, p32, s32,
 		                                           wk.part, sc, itrMax - total, innerTol, -1.0, s, &wk);

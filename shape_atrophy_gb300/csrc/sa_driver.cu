@@ -1534,7 +1534,8 @@ struct Server {
 					if (c.rr < md.cgTolSqu * in->bb) continue;
 					if (in->mixedTotal >= md.cgItrMax) { fail(*in, SA_ERR_NOT_CONVERGED); continue; }
 					double need = 0.01 * md.cgTolSqu * in->bb / c.rr;
-					in->innerTol = need > 1e-10 ? need : 1e-10;
+					const double floorSqu = std::pow(10.0, -(double) tuning().mixedInnerFloor);
+					in->innerTol = need > floorSqu ? need : floorSqu;
 					inner.push_back(in);
 				}
 				if (inner.empty()) break;
@@ -2121,6 +2122,7 @@ int sa_set_tuning(const char *name, int value)
 	else if (n == "batchBlock" && (value == 128 || value == 256)) t.batchBlock = value;
 	else if (n == "batchSlicesPerWarp" && value >= 1 && value <= 16) t.batchSlicesPerWarp = value;
 	else if (n == "vfdCtasPerSm" && value >= 1 && value <= 32) t.vfdCtasPerSm = value;
+	else if (n == "mixedInnerFloor" && value >= 4 && value <= 16) t.mixedInnerFloor = value;
 	else return SA_ERR_ARG;
 	return SA_OK;
 }
@@ -2147,6 +2149,7 @@ int sa_get_tuning(const char *name, int *value)
 	else if (n == "batchBlock") *value = t.batchBlock;
 	else if (n == "batchSlicesPerWarp") *value = t.batchSlicesPerWarp;
 	else if (n == "vfdCtasPerSm") *value = t.vfdCtasPerSm;
+	else if (n == "mixedInnerFloor") *value = t.mixedInnerFloor;
 	else return SA_ERR_ARG;
 	return SA_OK;
 }

@@ -330,6 +330,7 @@ struct Tuning {
 	int batchBlock = 256;          // threads per CTA of the batched (serving) CG: 128 or 256
 	int batchSlicesPerWarp = 2;    // 32-row slices per warp when a batched solve's CTAs are sized
 	int vfdCtasPerSm = 8;          // CTAs per SM of the varifold pair sums (column chunks)
+	int mixedInnerFloor = 10;      // mixed precision: inner FP32 solves stop at 10^-k squared relative residual
 };
 Tuning &tuning();
 
