@@ -5,19 +5,31 @@
 // layered model and for the reaction-diffusion solve (which the reference
 // does by dense Cholesky, 2D_frame/deform.cu:99-104).
 //
-// Chronopoulos-Gear form: per iteration one matvec kernel (w = A u, fused
-// with the dot (w, u)) and one vector kernel (p, s, x, r, u updates fused
-// with the dots (r, u) and (r, r)).  All scalars stay on the device; the
-// last block of each kernel finishes its reduction in a fixed order, so
-// results do not depend on block scheduling.  Iterations are queued in
-// chunks of 16, one chunk ahead of the host's check of the status word (a
-// kernel returns at once when the solve has stopped), so the device does
-// not wait for the host.  Stopping rule as the reference: |r|^2 < tol^2 |b|^2, b = 0
-// gives x = 0.
+// Chronopoulos-Gear form: per iteration one matvec w = A u with the dot
+// (w, u), and one update of p, s, x, r, u with the dots (r, u) and (r, r).
+// Stopping rule as the reference: |r|^2 < tol^2 |b|^2; b = 0 gives x = 0.
+// Four implementations of the same recurrences:
+//   k_cg_persist   one cooperative launch per solve, one CTA per SM, one
+//                  32-row slice per row warp with the row state in
+//                  registers, a reducer warp per CTA, the CTA's column
+//                  indices in shared memory, grid reductions in exact
+//                  128-bit fixed point (sa_fixsum.cuh) behind bounded
+//                  arrival-count barriers;
+//   k_cg_persist_g the same for operators too large for row state in
+//                  registers: vectors in global memory, contiguous slice
+//                  ranges per CTA;
+//   k_cg_spmv + k_cg_update  two kernels per iteration (fallback), scalars
+//                  on the device, the last block of each kernel finishes
+//                  its reduction in a fixed order; iterations queued in
+//                  chunks of 16 one chunk ahead of the host's status check;
+//   k_cg_batch     many independent solves (the server's instances) in one
+//                  cooperative launch, each on its own CTA range.
+// All results are deterministic (fixed grouping or order-free sums).
 //
 // Mixed precision (SA_PREC_MIXED): FP32 operator values and FP32 vectors in
-// an inner CG with FP64 dot products, inside an FP64 iterative-refinement
-// loop whose residual b - A x is recomputed with the FP64 operator.
+// an inner CG (3x3 block-Jacobi) with FP64 dot products, inside an FP64
+// iterative-refinement loop whose residual b - A x is recomputed with the
+// FP64 operator.
 #include "sa_internal.cuh"
 #include "sa_fixsum.cuh"
 #include <algorithm>
@@ -34,10 +46,11 @@ struct CgScal {
 
 // FP64 throughput on GB300 is 2 thread-DFMA per clock per SM (a warp
 // instruction occupies the SM's FP64 pipe for 16 cycles), so the kernels
-// below avoid FP64 work that is not the algorithm's own: block sums of the
-// dot products go through shared memory and are added by one warp, and the
-// vector kernels run on a grid of kVecCtasPerSm CTAs per SM, every SM taking
-// the same share of entries.
+// below avoid FP64 work that is not the algorithm's own: in the two-kernel
+// path block sums of the dot products go through shared memory and are added
+// by one warp, and the vector kernels run on a grid of kVecCtasPerSm CTAs per
+// SM, every SM taking the same share of entries; the persistent kernels sum
+// on the integer pipes.
 constexpr int kCgBlock = 256;      // vector kernels
 constexpr int kVecCtasPerSm = 4;   // vector kernels: CTAs per SM (grid-stride loops)
 constexpr int kSlicesPerCta = 4;   // matvec: one warp per 32-row slice, one thread per row
