@@ -58,6 +58,11 @@ extern "C" {
 #define SA_CG_TWO_KERNEL      2   /* matvec + vector kernel per iteration */
 #define SA_CG_PERSISTENT_GLOBAL 3 /* the persistent kernel with vectors in global memory at any size */
 
+/* sa_params.velocityGuess: where each step's velocity CG starts (layered model) */
+#define SA_GUESS_PREVIOUS     0   /* the previous step's velocity (the reference's warm start) */
+#define SA_GUESS_EXTRAPOLATE  1   /* 2 v_t-1 - v_t-2 from the third step on: same answer to the CG tolerance,
+                                     about a third fewer iterations on the layered shell */
+
 typedef struct sa_context sa_context;
 
 /* Element object: the fields of the reference's elmObj struct
@@ -101,6 +106,8 @@ typedef struct sa_params {
 	int rdItrMax;                       /* isotropic reaction-diffusion PCG (frame: same as cgItrMax) */
 	double rdTolSqu;                    /* isotropic RD PCG tolerance squared (frame: 1e-28) */
 	int cgKernel;                       /* SA_CG_AUTO (0), SA_CG_PERSISTENT, SA_CG_TWO_KERNEL, SA_CG_PERSISTENT_GLOBAL */
+	int velocityGuess;                  /* layered model's velocity CG start: SA_GUESS_PREVIOUS (0, the reference's
+	                                       warm start) or SA_GUESS_EXTRAPOLATE; the frame model always uses 0 */
 } sa_params;
 
 /* Varifold target and kernels (computeObjfcn prhs[13..20]). */

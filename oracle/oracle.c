@@ -1377,6 +1377,7 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 	double *exY = malloc(sizeof(double) * nd), *exYElm = malloc(sizeof(double) * (size_t) E * DIM * VTX);
 	double *rpdElm = malloc(sizeof(double) * (size_t) E * VTX), *rpd = malloc(sizeof(double) * N);
 	double *vlc = calloc((size_t) nd, sizeof(double));
+	double *vlcPrev = calloc((size_t) nd, sizeof(double));
 	vstate S; memset(&S, 0, sizeof(S));
 	S.P = P;
 	S.elYElm = malloc(sizeof(double) * (size_t) E * DIM * VTX);
@@ -1430,6 +1431,14 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 		yank_apply(P, edgNow, ynk, exYElm, exY);
 
 		int itr = 0, st;
+		if (!useK && !frame && P->velocityGuess == 1) {
+			/* layered model option: start from 2 v_t-1 - v_t-2 (from the third step on) instead of v_t-1 */
+			for (long i = 0; i < nd; ++i) {
+				double a = vlc[i];
+				if (t >= 2) vlc[i] = 2.0 * a - vlcPrev[i];
+				vlcPrev[i] = a;
+			}
+		}
 		if (useK) st = ipcg(&S, vlc, exY, &itr);
 		else {
 			elastic_diag_state(P, lmkNow, edgNow, S.diag);
@@ -1497,7 +1506,7 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 
 	free(edgNow); free(edgNxt); free(frmNow); free(frmNxt); free(tsvNow); free(tsvNxt);
 	free(ppdElm); free(ggdElm); free(ynk); free(rea); free(exY); free(exYElm);
-	free(rpdElm); free(rpd); free(vlc); free(S.elYElm); free(S.elY); free(S.pnl);
+	free(rpdElm); free(rpd); free(vlc); free(vlcPrev); free(S.elYElm); free(S.elY); free(S.pnl);
 	free(ppdNow); free(ppdNxt); free(ggdNxt); free(femLft);
 	free(ppdValNow); free(ppdValNxt); free(ggdValNxt); free(lftVal); free(S.diag);
 	free(S.knlMat); free(S.knLMat);

@@ -36,6 +36,7 @@ class OrcProblem(C.Structure):
         ("tauPrmVec", _dp), ("ldmWgt", C.c_double), ("knlOrder", C.c_int), ("knlWidth", C.c_double),
         ("knlEps", C.c_double), ("btmWgt", C.c_double), ("timeStp", C.c_double), ("timeNum", C.c_int),
         ("cgItrMax", C.c_int), ("cgTolSqu", C.c_double), ("rdItrMax", C.c_int), ("rdTolSqu", C.c_double),
+        ("velocityGuess", C.c_int),
     ]
 
 
@@ -121,6 +122,7 @@ class Problem:
         p.btmWgt, p.timeStp, p.timeNum = float(spec["btmWgt"]), float(spec["timeStp"]), int(spec["timeNum"])
         p.cgItrMax, p.cgTolSqu = int(spec["cgItrMax"]), float(spec["cgTolSqu"])
         p.rdItrMax, p.rdTolSqu = int(spec.get("rdItrMax", 10000)), float(spec.get("rdTolSqu", 1e-26))
+        p.velocityGuess = {"previous": 0, "extrapolate": 1}[spec.get("velocityGuess", "extrapolate")]
         self.p = p
         self.keep = keep
         self.dim, self.N = D, N

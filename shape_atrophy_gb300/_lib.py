@@ -19,6 +19,7 @@ _dp = C.POINTER(C.c_double)
 SA_OK, SA_ERR_ARG, SA_ERR_CUDA, SA_ERR_UNSUPPORTED = 0, 1, 2, 3
 SA_ERR_NOT_CONVERGED, SA_ERR_BREAKDOWN, SA_ERR_NONFINITE, SA_ERR_TIMEOUT = 4, 5, 6, 7
 SA_CG_AUTO, SA_CG_PERSISTENT, SA_CG_TWO_KERNEL, SA_CG_PERSISTENT_GLOBAL = 0, 1, 2, 3
+SA_GUESS_PREVIOUS, SA_GUESS_EXTRAPOLATE = 0, 1
 SA_ELA_FRAME, SA_ELA_ISOTROPIC = 0, 1
 SA_PREC_FP64, SA_PREC_MIXED = 0, 1
 
@@ -44,6 +45,7 @@ class Params(C.Structure):
         ("spdLyrVec", _dp), ("lyrNum", C.c_int), ("ynkActPrmVec", _dp), ("reaActPrmVec", _dp),
         ("btmWgt", C.c_double), ("timeStp", C.c_double), ("timeNum", C.c_int), ("cgItrMax", C.c_int),
         ("cgTolSqu", C.c_double), ("rdItrMax", C.c_int), ("rdTolSqu", C.c_double), ("cgKernel", C.c_int),
+        ("velocityGuess", C.c_int),
     ]
 
 

@@ -490,6 +490,7 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 struct Work {
 	double *xa, *xb;            // node positions t, t+1 (interleaved)
 	double *v, *b, *pd, *blk, *dinv, *fy, *fr;
+	double *vPrev = nullptr;    // velocity of the step before (extrapolated CG start)
 	double *Mnow, *Mnxt, *L, *dinvRd, *rhs;
 	Geom g0, g1;
 	CgWork cw;
@@ -504,6 +505,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	long N = m.N, E = m.E, Z = m.Z, n = N * D;
 	w.xa = P.alloc<double>(n); w.xb = P.alloc<double>(n);
 	w.v = P.alloc<double>(n); w.b = P.alloc<double>(n); w.pd = P.zeros<double>(N);
+	w.vPrev = P.zeros<double>(n);
 	long T = m.slTotal;                    // sliced slots, padding included (padding stays zero)
 	w.blk = P.zeros<double>((size_t) T * sell_vals<D>()); w.dinv = P.alloc<double>(n);
 	w.fy = P.alloc<double>(N); w.fr = P.alloc<double>(N);
@@ -599,6 +601,13 @@ struct Stepper {
 	// step part 1: loads and the velocity operator at the current shape
 	void pre_velocity()
 	{
+		// CG start: the previous velocity (the reference's choice), or (layered model, velocityGuess
+		// SA_GUESS_EXTRAPOLATE) its linear extrapolation 2 v_t-1 - v_t-2 from the third step on: the same
+		// converged answer to the CG tolerance, about a third fewer iterations when the motion is smooth
+		if (md.velocityGuess == SA_GUESS_EXTRAPOLATE && !useK) {
+			if (t >= 2) launch_extrapolate(m.N * (long) D, w.v, w.vPrev, s);
+			else SA_CHECK(cudaMemcpyAsync(w.vPrev, w.v, sizeof(double) * m.N * D, cudaMemcpyDeviceToDevice, s));
+		}
 		launch_activity<D>(m, md, tau_now(), w.fy, w.fr, s);
 		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
 		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, w.cw.binv32, s);
@@ -728,6 +737,9 @@ static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *
 	md.rdTolSqu = p->rdTolSqu > 0.0 ? p->rdTolSqu : (md.frame ? 1e-26 : p->cgTolSqu);
 	SA_REQUIRE(p->cgKernel >= SA_CG_AUTO && p->cgKernel <= SA_CG_PERSISTENT_GLOBAL, "cgKernel must be 0, 1, 2 or 3");
 	md.cgKernel = p->cgKernel;
+	SA_REQUIRE(p->velocityGuess == SA_GUESS_PREVIOUS || p->velocityGuess == SA_GUESS_EXTRAPOLATE,
+	           "velocityGuess must be 0 or 1");
+	md.velocityGuess = md.frame ? SA_GUESS_PREVIOUS : p->velocityGuess;
 	if (tgt) {
 		md.cenKnl = tgt->cenKnlType; md.dirKnl = tgt->dirKnlType;
 		md.cenWidth = tgt->cenKnlWidth; md.dirWidth = tgt->dirKnlWidth;

@@ -211,6 +211,7 @@ struct Model {
 	char cenKnl, dirKnl; double cenWidth, dirWidth;
 	int precision;             // SA_PREC_FP64 or SA_PREC_MIXED
 	int cgKernel = 0;          // SA_CG_AUTO / SA_CG_PERSISTENT / SA_CG_TWO_KERNEL
+	int velocityGuess = 0;     // layered model: SA_GUESS_PREVIOUS or SA_GUESS_EXTRAPOLATE
 };
 
 // --------------------------------------------------------------------------
@@ -302,6 +303,7 @@ template <int D> void launch_advance(int N, const double *x, const double *v, do
 void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_t s);
 // tangent-linear kernels of the layered model (sa_tangent.cu)
 void launch_axpy64(long n, const double *x, double a, const double *y, double *out, cudaStream_t s);
+void launch_extrapolate(long n, double *v, double *vPrev, cudaStream_t s);
 template <int D> void launch_geom_tan(const Mesh &m, const double *rec, const double *dx, double *drec, cudaStream_t s);
 template <int D> void launch_penalty_tan(const Mesh &m, const double *x, const double *dx, double *dpd, cudaStream_t s);
 template <int D> void launch_vel_tan_rhs(const Mesh &m, const Model &md, const double *rec, const double *drec,

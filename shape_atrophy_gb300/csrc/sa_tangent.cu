@@ -226,6 +226,21 @@ __global__ void k_tau0_tan(int N, const double *__restrict__ x, const double *__
 	dtau[i] = v;
 }
 
+// v <- 2 v - vPrev, vPrev <- old v (linear extrapolation of the velocity as the next CG start)
+__global__ void k_extrapolate(long n, double *__restrict__ v, double *__restrict__ vPrev)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k >= n) return;
+	const double a = v[k];
+	v[k] = 2.0 * a - vPrev[k];
+	vPrev[k] = a;
+}
+
+void launch_extrapolate(long n, double *v, double *vPrev, cudaStream_t s)
+{
+	k_extrapolate<<<grid_for(n), kBlock, 0, s>>>(n, v, vPrev);
+}
+
 __global__ void k_axpy64(long n, const double *__restrict__ x, double a, const double *__restrict__ y,
                          double *__restrict__ out)
 {
