@@ -910,10 +910,11 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 	}
 	const long n = (long) m.N * D, N = m.N;
 	// tangent state per parameter: positions (two copies: t, t+1), concentration (t, t+1), velocity
-	std::vector<double *> dx[2], dtau[2], dv;
+	std::vector<double *> dx[2], dtau[2], dv, dvPrev;
 	for (int k = 0; k < K; ++k) {
 		for (int c = 0; c < 2; ++c) { dx[c].push_back(P.zeros<double>(n)); dtau[c].push_back(P.zeros<double>(N)); }
 		dv.push_back(P.zeros<double>(n));
+		dvPrev.push_back(P.zeros<double>(n));
 	}
 	double *drecA = P.alloc<double>((size_t) rec_len<D>() * m.E), *drecB = P.alloc<double>((size_t) rec_len<D>() * m.E);
 	double *rhsV = P.alloc<double>(n), *rhsT = P.alloc<double>(N), *dpd = P.zeros<double>(N), *dfy = P.alloc<double>(N);
@@ -951,6 +952,11 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_tan<D>(m, st.xn, dx[cur][k], dpd, s);
 			launch_axpy64(N, dtau[cur][k], y0 - 1.0, dtau[cur][k], dfy, s);     // dfy = y0 dtau
 			launch_vel_tan_rhs<D>(m, md, st.gn->rec, drecA, w.fy, dfy, w.v, dpd, rhsV, s);
+			// start as the forward solve does: previous tangent velocity, or its extrapolation
+			if (md.velocityGuess == SA_GUESS_EXTRAPOLATE) {
+				if (st.t >= 2) launch_extrapolate(n, dv[k], dvPrev[k], s);
+				else SA_CHECK(cudaMemcpyAsync(dvPrev[k], dv[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+			}
 			code = solve(std::integral_constant<int, D>(), w.blk, w.dinv, rhsV, dv[k], md.cgItrMax, md.cgTolSqu);
 			if (code != SA_OK) { status = code; break; }
 			launch_axpy64(n, dx[cur][k], dt, dv[k], dx[1 - cur][k], s);
