@@ -62,6 +62,8 @@ extern "C" {
 #define SA_GUESS_PREVIOUS     0   /* the previous step's velocity (the reference's warm start) */
 #define SA_GUESS_EXTRAPOLATE  1   /* 2 v_t-1 - v_t-2 from the third step on: same answer to the CG tolerance,
                                      about a third fewer iterations on the layered shell */
+#define SA_GUESS_QUADRATIC    2   /* 3 v_t-1 - 3 v_t-2 + v_t-3 from the fourth step on (linear at the third):
+                                     half the iterations of SA_GUESS_PREVIOUS on the layered shell */
 
 typedef struct sa_context sa_context;
 
@@ -107,7 +109,8 @@ typedef struct sa_params {
 	double rdTolSqu;                    /* isotropic RD PCG tolerance squared (frame: 1e-28) */
 	int cgKernel;                       /* SA_CG_AUTO (0), SA_CG_PERSISTENT, SA_CG_TWO_KERNEL, SA_CG_PERSISTENT_GLOBAL */
 	int velocityGuess;                  /* layered model's velocity CG start: SA_GUESS_PREVIOUS (0, the reference's
-	                                       warm start) or SA_GUESS_EXTRAPOLATE; the frame model always uses 0 */
+	                                       warm start), SA_GUESS_EXTRAPOLATE or SA_GUESS_QUADRATIC; the frame
+	                                       model always uses 0 */
 } sa_params;
 
 /* Varifold target and kernels (computeObjfcn prhs[13..20]). */

@@ -1377,7 +1377,7 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 	double *exY = malloc(sizeof(double) * nd), *exYElm = malloc(sizeof(double) * (size_t) E * DIM * VTX);
 	double *rpdElm = malloc(sizeof(double) * (size_t) E * VTX), *rpd = malloc(sizeof(double) * N);
 	double *vlc = calloc((size_t) nd, sizeof(double));
-	double *vlcPrev = calloc((size_t) nd, sizeof(double));
+	double *vlcPrev = calloc((size_t) nd, sizeof(double)), *vlcPrev2 = calloc((size_t) nd, sizeof(double));
 	vstate S; memset(&S, 0, sizeof(S));
 	S.P = P;
 	S.elYElm = malloc(sizeof(double) * (size_t) E * DIM * VTX);
@@ -1436,6 +1436,15 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 			for (long i = 0; i < nd; ++i) {
 				double a = vlc[i];
 				if (t >= 2) vlc[i] = 2.0 * a - vlcPrev[i];
+				vlcPrev[i] = a;
+			}
+		} else if (!useK && !frame && P->velocityGuess == 2) {
+			/* quadratic: 3 v_t-1 - 3 v_t-2 + v_t-3 from the fourth step on, linear at the third */
+			for (long i = 0; i < nd; ++i) {
+				double a = vlc[i], b = vlcPrev[i], c = vlcPrev2[i];
+				if (t >= 3) vlc[i] = 3.0 * a - 3.0 * b + c;
+				else if (t == 2) vlc[i] = 2.0 * a - b;
+				vlcPrev2[i] = b;
 				vlcPrev[i] = a;
 			}
 		}
@@ -1506,7 +1515,7 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 
 	free(edgNow); free(edgNxt); free(frmNow); free(frmNxt); free(tsvNow); free(tsvNxt);
 	free(ppdElm); free(ggdElm); free(ynk); free(rea); free(exY); free(exYElm);
-	free(rpdElm); free(rpd); free(vlc); free(vlcPrev); free(S.elYElm); free(S.elY); free(S.pnl);
+	free(rpdElm); free(rpd); free(vlc); free(vlcPrev); free(vlcPrev2); free(S.elYElm); free(S.elY); free(S.pnl);
 	free(ppdNow); free(ppdNxt); free(ggdNxt); free(femLft);
 	free(ppdValNow); free(ppdValNxt); free(ggdValNxt); free(lftVal); free(S.diag);
 	free(S.knlMat); free(S.knLMat);

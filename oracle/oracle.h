@@ -75,7 +75,8 @@ typedef struct orc_problem {
 	double cgTolSqu;
 	int rdItrMax;            /* isotropic reaction-diffusion Jacobi-PCG */
 	double rdTolSqu;
-	int velocityGuess;       /* isotropic: velocity PCG start, 0 previous velocity, 1 2 v_t-1 - v_t-2 */
+	int velocityGuess;       /* isotropic: velocity PCG start, 0 previous velocity, 1 2 v_t-1 - v_t-2,
+	                            2 3 v_t-1 - 3 v_t-2 + v_t-3 */
 } orc_problem;
 
 /* Full forward model (reference deform(), 2D/deform.cu:22-119) and, when

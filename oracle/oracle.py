@@ -122,7 +122,7 @@ class Problem:
         p.btmWgt, p.timeStp, p.timeNum = float(spec["btmWgt"]), float(spec["timeStp"]), int(spec["timeNum"])
         p.cgItrMax, p.cgTolSqu = int(spec["cgItrMax"]), float(spec["cgTolSqu"])
         p.rdItrMax, p.rdTolSqu = int(spec.get("rdItrMax", 10000)), float(spec.get("rdTolSqu", 1e-26))
-        p.velocityGuess = {"previous": 0, "extrapolate": 1}[spec.get("velocityGuess", "extrapolate")]
+        p.velocityGuess = {"previous": 0, "extrapolate": 1, "quadratic": 2}[spec.get("velocityGuess", "quadratic")]
         self.p = p
         self.keep = keep
         self.dim, self.N = D, N

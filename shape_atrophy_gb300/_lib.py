@@ -19,7 +19,7 @@ _dp = C.POINTER(C.c_double)
 SA_OK, SA_ERR_ARG, SA_ERR_CUDA, SA_ERR_UNSUPPORTED = 0, 1, 2, 3
 SA_ERR_NOT_CONVERGED, SA_ERR_BREAKDOWN, SA_ERR_NONFINITE, SA_ERR_TIMEOUT = 4, 5, 6, 7
 SA_CG_AUTO, SA_CG_PERSISTENT, SA_CG_TWO_KERNEL, SA_CG_PERSISTENT_GLOBAL = 0, 1, 2, 3
-SA_GUESS_PREVIOUS, SA_GUESS_EXTRAPOLATE = 0, 1
+SA_GUESS_PREVIOUS, SA_GUESS_EXTRAPOLATE, SA_GUESS_QUADRATIC = 0, 1, 2
 SA_ELA_FRAME, SA_ELA_ISOTROPIC = 0, 1
 SA_PREC_FP64, SA_PREC_MIXED = 0, 1
 

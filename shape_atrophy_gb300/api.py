@@ -164,9 +164,10 @@ def _params(spec: dict, K: _Keep, precision: str) -> _lib.Params:
     p.cgKernel = {"auto": _lib.SA_CG_AUTO, "persistent": _lib.SA_CG_PERSISTENT,
                   "two-kernel": _lib.SA_CG_TWO_KERNEL,
                   "persistent-global": _lib.SA_CG_PERSISTENT_GLOBAL}[spec.get("cgKernel", "auto")]
-    # layered model: velocity CG start, "extrapolate" (default) or "previous" (the reference's warm start)
-    p.velocityGuess = {"previous": _lib.SA_GUESS_PREVIOUS,
-                       "extrapolate": _lib.SA_GUESS_EXTRAPOLATE}[spec.get("velocityGuess", "extrapolate")]
+    # layered model: velocity CG start, "quadratic" (default), "extrapolate" (linear) or "previous" (the
+    # reference's warm start)
+    p.velocityGuess = {"previous": _lib.SA_GUESS_PREVIOUS, "extrapolate": _lib.SA_GUESS_EXTRAPOLATE,
+                       "quadratic": _lib.SA_GUESS_QUADRATIC}[spec.get("velocityGuess", "quadratic")]
     return p
 
 

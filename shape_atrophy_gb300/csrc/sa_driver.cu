@@ -491,6 +491,7 @@ struct Work {
 	double *xa, *xb;            // node positions t, t+1 (interleaved)
 	double *v, *b, *pd, *blk, *dinv, *fy, *fr;
 	double *vPrev = nullptr;    // velocity of the step before (extrapolated CG start)
+	double *vPrev2 = nullptr;   // and of the step before that (quadratic extrapolation)
 	double *Mnow, *Mnxt, *L, *dinvRd, *rhs;
 	Geom g0, g1;
 	CgWork cw;
@@ -506,6 +507,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	w.xa = P.alloc<double>(n); w.xb = P.alloc<double>(n);
 	w.v = P.alloc<double>(n); w.b = P.alloc<double>(n); w.pd = P.zeros<double>(N);
 	w.vPrev = P.zeros<double>(n);
+	w.vPrev2 = md.velocityGuess == SA_GUESS_QUADRATIC ? P.zeros<double>(n) : nullptr;
 	long T = m.slTotal;                    // sliced slots, padding included (padding stays zero)
 	w.blk = P.zeros<double>((size_t) T * sell_vals<D>()); w.dinv = P.alloc<double>(n);
 	w.fy = P.alloc<double>(N); w.fr = P.alloc<double>(N);
@@ -607,6 +609,8 @@ struct Stepper {
 		if (md.velocityGuess == SA_GUESS_EXTRAPOLATE && !useK) {
 			if (t >= 2) launch_extrapolate(m.N * (long) D, w.v, w.vPrev, s);
 			else SA_CHECK(cudaMemcpyAsync(w.vPrev, w.v, sizeof(double) * m.N * D, cudaMemcpyDeviceToDevice, s));
+		} else if (md.velocityGuess == SA_GUESS_QUADRATIC && !useK) {
+			launch_extrapolate2(m.N * (long) D, t, w.v, w.vPrev, w.vPrev2, s);
 		}
 		launch_activity<D>(m, md, tau_now(), w.fy, w.fr, s);
 		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
@@ -737,8 +741,8 @@ static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *
 	md.rdTolSqu = p->rdTolSqu > 0.0 ? p->rdTolSqu : (md.frame ? 1e-26 : p->cgTolSqu);
 	SA_REQUIRE(p->cgKernel >= SA_CG_AUTO && p->cgKernel <= SA_CG_PERSISTENT_GLOBAL, "cgKernel must be 0, 1, 2 or 3");
 	md.cgKernel = p->cgKernel;
-	SA_REQUIRE(p->velocityGuess == SA_GUESS_PREVIOUS || p->velocityGuess == SA_GUESS_EXTRAPOLATE,
-	           "velocityGuess must be 0 or 1");
+	SA_REQUIRE(p->velocityGuess >= SA_GUESS_PREVIOUS && p->velocityGuess <= SA_GUESS_QUADRATIC,
+	           "velocityGuess must be 0, 1 or 2");
 	md.velocityGuess = md.frame ? SA_GUESS_PREVIOUS : p->velocityGuess;
 	if (tgt) {
 		md.cenKnl = tgt->cenKnlType; md.dirKnl = tgt->dirKnlType;
@@ -910,11 +914,12 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 	}
 	const long n = (long) m.N * D, N = m.N;
 	// tangent state per parameter: positions (two copies: t, t+1), concentration (t, t+1), velocity
-	std::vector<double *> dx[2], dtau[2], dv, dvPrev;
+	std::vector<double *> dx[2], dtau[2], dv, dvPrev, dvPrev2;
 	for (int k = 0; k < K; ++k) {
 		for (int c = 0; c < 2; ++c) { dx[c].push_back(P.zeros<double>(n)); dtau[c].push_back(P.zeros<double>(N)); }
 		dv.push_back(P.zeros<double>(n));
 		dvPrev.push_back(P.zeros<double>(n));
+		dvPrev2.push_back(md.velocityGuess == SA_GUESS_QUADRATIC ? P.zeros<double>(n) : nullptr);
 	}
 	double *drecA = P.alloc<double>((size_t) rec_len<D>() * m.E), *drecB = P.alloc<double>((size_t) rec_len<D>() * m.E);
 	double *rhsV = P.alloc<double>(n), *rhsT = P.alloc<double>(N), *dpd = P.zeros<double>(N), *dfy = P.alloc<double>(N);
@@ -956,6 +961,8 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 			if (md.velocityGuess == SA_GUESS_EXTRAPOLATE) {
 				if (st.t >= 2) launch_extrapolate(n, dv[k], dvPrev[k], s);
 				else SA_CHECK(cudaMemcpyAsync(dvPrev[k], dv[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+			} else if (md.velocityGuess == SA_GUESS_QUADRATIC) {
+				launch_extrapolate2(n, st.t, dv[k], dvPrev[k], dvPrev2[k], s);
 			}
 			code = solve(std::integral_constant<int, D>(), w.blk, w.dinv, rhsV, dv[k], md.cgItrMax, md.cgTolSqu);
 			if (code != SA_OK) { status = code; break; }

@@ -241,6 +241,24 @@ void launch_extrapolate(long n, double *v, double *vPrev, cudaStream_t s)
 	k_extrapolate<<<grid_for(n), kBlock, 0, s>>>(n, v, vPrev);
 }
 
+// quadratic extrapolation from three previous velocities (linear at step 2, none before): v holds v_t-1,
+// p1 v_t-2, p2 v_t-3; afterwards p1, p2 hold v_t-1, v_t-2
+__global__ void k_extrapolate2(long n, int t, double *__restrict__ v, double *__restrict__ p1, double *__restrict__ p2)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k >= n) return;
+	const double a = v[k], b = p1[k], c = p2[k];
+	if (t >= 3) v[k] = 3.0 * a - 3.0 * b + c;
+	else if (t == 2) v[k] = 2.0 * a - b;
+	p2[k] = b;
+	p1[k] = a;
+}
+
+void launch_extrapolate2(long n, int t, double *v, double *p1, double *p2, cudaStream_t s)
+{
+	k_extrapolate2<<<grid_for(n), kBlock, 0, s>>>(n, t, v, p1, p2);
+}
+
 __global__ void k_axpy64(long n, const double *__restrict__ x, double a, const double *__restrict__ y,
                          double *__restrict__ out)
 {
