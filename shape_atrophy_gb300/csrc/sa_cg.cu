@@ -34,6 +34,7 @@
 #include "sa_fixsum.cuh"
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 namespace sa {
 
@@ -1118,8 +1119,10 @@ static void set_scal(CgScal *d, double tolSqu, int itrMax, double bb, cudaStream
 template <int B, typename TM, typename TV, typename TX>
 static int persist_capacity(int smCount, int warps, size_t smemBytes)
 {
+	static std::mutex mu;                    // sessions and servers may size launches from several threads
 	static bool attr = false;
 	if (warps < 1 || warps > kPersistMaxWarps || smemBytes > (size_t) kColSmemMax) return 0;
+	std::lock_guard<std::mutex> lock(mu);
 	if (!attr) {               // allow the column cache beyond the default 48 KB of dynamic shared memory
 		if (cudaFuncSetAttribute(k_cg_persist<B, TM, TV, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                         kColSmemMax) != cudaSuccess) {
@@ -1141,8 +1144,10 @@ static int persist_capacity(int smCount, int warps, size_t smemBytes)
 template <int B, typename TM, typename TV, typename TX>
 static int persist_g_capacity(int smCount, int warps, size_t smemBytes)
 {
+	static std::mutex mu;
 	static bool attr = false;
 	if (warps < 2 || warps > kPersistMaxWarps || smemBytes > (size_t) kColSmemMax) return 0;
+	std::lock_guard<std::mutex> lock(mu);
 	if (!attr) {
 		if (cudaFuncSetAttribute(k_cg_persist_g<B, TM, TV, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                         kColSmemMax) != cudaSuccess) {
@@ -1498,10 +1503,12 @@ CgState cg_state(const CgWork &w, cudaStream_t s)
 template <int B, typename TM, typename TV, typename TX>
 static int batch_capacity(int smCount, int block)
 {
+	static std::mutex mu;
 	static int perSm[kBatchBlock / 32 + 1];
 	static bool known[kBatchBlock / 32 + 1] = {};
 	const int w = block / 32;
 	if (w < 1 || w > kBatchBlock / 32 || block % 32) return 0;
+	std::lock_guard<std::mutex> lock(mu);
 	if (!known[w]) {
 		int v = 0;
 		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_batch<B, TM, TV, TX>, block, 0) != cudaSuccess) {
