@@ -1492,7 +1492,10 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 			free(Mt);
 			double *dinv = malloc(sizeof(double) * N);
 			for (int z = 0; z < Z; ++z) if (fv[z] == fv[Z + z]) dinv[fv[z]] = 1.0 / lftVal[z];
-			memcpy(tauNxt, tauNow, sizeof(double) * N);   /* warm start */
+			if (P->velocityGuess != 0 && t >= 1)       /* extrapolated start: 2 tau_t - tau_t-1 */
+				for (int i = 0; i < N; ++i) tauNxt[i] = 2.0 * tauNow[i] - tauNow[i - N];
+			else
+				memcpy(tauNxt, tauNow, sizeof(double) * N);   /* warm start */
 			csrctx C1 = { P, lftVal };
 			int rdItr = 0;
 			if (jpcg(csr_apply, &C1, dinv, N, tauNxt, rpd, P->rdItrMax, P->rdTolSqu, &rdItr) != 0) {

@@ -633,7 +633,12 @@ struct Stepper {
 		launch_elem_geom<D>(m, md, xx, *gx, st, true, s);
 		launch_assemble_rd<D>(m, md, *gx, dt, w.Mnxt, w.L, w.dinvRd, s);
 		launch_rd_rhs<D>(m, *gn, w.Mnow, tau_now(), w.fr, dt, w.rhs, s);
-		SA_CHECK(cudaMemcpyAsync(tau_next(), tau_now(), sizeof(double) * m.N, cudaMemcpyDeviceToDevice, s));
+		// reaction-diffusion CG start: tau_t, or its linear extrapolation 2 tau_t - tau_t-1 when the velocity
+		// starts are extrapolated (layered model; the trajectory holds tau_t-1)
+		if (md.velocityGuess != SA_GUESS_PREVIOUS && !md.frame && t >= 1)
+			launch_lin_extrap(m.N, tau_now(), tau_now() - m.N, tau_next(), s);
+		else
+			SA_CHECK(cudaMemcpyAsync(tau_next(), tau_now(), sizeof(double) * m.N, cudaMemcpyDeviceToDevice, s));
 		w.cw.launches += 4;                 // advance, geometry, rd assembly, rd rhs
 	}
 
@@ -981,7 +986,11 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 			launch_geom_tan<D>(m, st.gx->rec, dx[1 - cur][k], drecB, s);
 			launch_rd_tan_rhs<D>(m, md, w.Mnow, st.gn->rec, drecA, st.gx->rec, drecB, st.tau_now(), w.fr,
 			                     dtau[cur][k], st.tau_next(), rhsT, s);
-			SA_CHECK(cudaMemcpyAsync(dtau[1 - cur][k], dtau[cur][k], sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+			// start as the forward concentration solve does (dtau[1 - cur] still holds the step before)
+			if (md.velocityGuess != SA_GUESS_PREVIOUS && st.t >= 1)
+				launch_lin_extrap(N, dtau[cur][k], dtau[1 - cur][k], dtau[1 - cur][k], s);
+			else
+				SA_CHECK(cudaMemcpyAsync(dtau[1 - cur][k], dtau[cur][k], sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
 			code = solve(std::integral_constant<int, 1>(), w.L, w.dinvRd, rhsT, dtau[1 - cur][k], md.rdItrMax,
 			             md.rdTolSqu);
 			if (code != SA_OK) { status = code; break; }

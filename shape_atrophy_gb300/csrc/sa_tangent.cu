@@ -259,6 +259,18 @@ void launch_extrapolate2(long n, int t, double *v, double *p1, double *p2, cudaS
 	k_extrapolate2<<<grid_for(n), kBlock, 0, s>>>(n, t, v, p1, p2);
 }
 
+// out = 2 a - b (out may alias b)
+__global__ void k_lin_extrap(long n, const double *__restrict__ a, const double *b, double *out)
+{
+	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
+	if (k < n) out[k] = 2.0 * a[k] - b[k];
+}
+
+void launch_lin_extrap(long n, const double *a, const double *b, double *out, cudaStream_t s)
+{
+	k_lin_extrap<<<grid_for(n), kBlock, 0, s>>>(n, a, b, out);
+}
+
 __global__ void k_axpy64(long n, const double *__restrict__ x, double a, const double *__restrict__ y,
                          double *__restrict__ out)
 {
