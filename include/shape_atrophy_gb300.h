@@ -62,8 +62,9 @@ extern "C" {
 #define SA_GUESS_PREVIOUS     0   /* the previous step's velocity (the reference's warm start) */
 #define SA_GUESS_EXTRAPOLATE  1   /* 2 v_t-1 - v_t-2 from the third step on: same answer to the CG tolerance,
                                      about a third fewer iterations on the layered shell */
-#define SA_GUESS_QUADRATIC    2   /* 3 v_t-1 - 3 v_t-2 + v_t-3 from the fourth step on (linear at the third):
-                                     half the iterations of SA_GUESS_PREVIOUS on the layered shell */
+#define SA_GUESS_QUADRATIC    2   /* 3 v_t-1 - 3 v_t-2 + v_t-3 from the fourth step on (linear at the third) */
+#define SA_GUESS_MAX_ORDER    5   /* velocityGuess k = 1 .. 5: the degree-k polynomial through the last k + 1
+                                     velocities, evaluated one step ahead (lower degrees in the first steps) */
 
 typedef struct sa_context sa_context;
 

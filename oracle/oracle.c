@@ -1377,7 +1377,7 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 	double *exY = malloc(sizeof(double) * nd), *exYElm = malloc(sizeof(double) * (size_t) E * DIM * VTX);
 	double *rpdElm = malloc(sizeof(double) * (size_t) E * VTX), *rpd = malloc(sizeof(double) * N);
 	double *vlc = calloc((size_t) nd, sizeof(double));
-	double *vlcPrev = calloc((size_t) nd, sizeof(double)), *vlcPrev2 = calloc((size_t) nd, sizeof(double));
+	double *vlcHist = calloc((size_t) nd * 5, sizeof(double));     /* up to 5 earlier velocities */
 	vstate S; memset(&S, 0, sizeof(S));
 	S.P = P;
 	S.elYElm = malloc(sizeof(double) * (size_t) E * DIM * VTX);
@@ -1431,21 +1431,25 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 		yank_apply(P, edgNow, ynk, exYElm, exY);
 
 		int itr = 0, st;
-		if (!useK && !frame && P->velocityGuess == 1) {
-			/* layered model option: start from 2 v_t-1 - v_t-2 (from the third step on) instead of v_t-1 */
+		if (!useK && !frame && P->velocityGuess > 0) {
+			/* layered model: start from the degree-q polynomial through the last q + 1 velocities,
+			 * evaluated one step ahead, q = min(velocityGuess, t - 1); then shift the history */
+			static const double cb[6][6] = {{1, 0, 0, 0, 0, 0}, {2, -1, 0, 0, 0, 0}, {3, -3, 1, 0, 0, 0},
+			                                {4, -6, 4, -1, 0, 0}, {5, -10, 10, -5, 1, 0}, {6, -15, 20, -15, 6, -1}};
+			const int depth = P->velocityGuess < 5 ? P->velocityGuess : 5;
+			int q = t - 1 < depth ? t - 1 : depth;
+			if (q < 0) q = 0;
 			for (long i = 0; i < nd; ++i) {
-				double a = vlc[i];
-				if (t >= 2) vlc[i] = 2.0 * a - vlcPrev[i];
-				vlcPrev[i] = a;
-			}
-		} else if (!useK && !frame && P->velocityGuess == 2) {
-			/* quadratic: 3 v_t-1 - 3 v_t-2 + v_t-3 from the fourth step on, linear at the third */
-			for (long i = 0; i < nd; ++i) {
-				double a = vlc[i], b = vlcPrev[i], c = vlcPrev2[i];
-				if (t >= 3) vlc[i] = 3.0 * a - 3.0 * b + c;
-				else if (t == 2) vlc[i] = 2.0 * a - b;
-				vlcPrev2[i] = b;
-				vlcPrev[i] = a;
+				double h[6];
+				h[0] = vlc[i];
+				for (int j = 1; j <= depth; ++j) h[j] = vlcHist[(size_t) (j - 1) * nd + i];
+				if (q > 0) {
+					double s = 0.0;
+					for (int j = 0; j <= q; ++j) s += cb[q][j] * h[j];
+					vlc[i] = s;
+				}
+				for (int j = depth - 1; j >= 1; --j) vlcHist[(size_t) j * nd + i] = h[j];
+				vlcHist[i] = h[0];
 			}
 		}
 		if (useK) st = ipcg(&S, vlc, exY, &itr);
@@ -1518,7 +1522,7 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 
 	free(edgNow); free(edgNxt); free(frmNow); free(frmNxt); free(tsvNow); free(tsvNxt);
 	free(ppdElm); free(ggdElm); free(ynk); free(rea); free(exY); free(exYElm);
-	free(rpdElm); free(rpd); free(vlc); free(vlcPrev); free(vlcPrev2); free(S.elYElm); free(S.elY); free(S.pnl);
+	free(rpdElm); free(rpd); free(vlc); free(vlcHist); free(S.elYElm); free(S.elY); free(S.pnl);
 	free(ppdNow); free(ppdNxt); free(ggdNxt); free(femLft);
 	free(ppdValNow); free(ppdValNxt); free(ggdValNxt); free(lftVal); free(S.diag);
 	free(S.knlMat); free(S.knLMat);

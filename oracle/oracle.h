@@ -75,8 +75,8 @@ typedef struct orc_problem {
 	double cgTolSqu;
 	int rdItrMax;            /* isotropic reaction-diffusion Jacobi-PCG */
 	double rdTolSqu;
-	int velocityGuess;       /* isotropic: velocity PCG start, 0 previous velocity, 1 2 v_t-1 - v_t-2,
-	                            2 3 v_t-1 - 3 v_t-2 + v_t-3 */
+	int velocityGuess;       /* isotropic: velocity PCG start, the degree-k polynomial through the last k + 1
+	                            velocities (k = 0 .. 5; 0: the previous velocity) */
 } orc_problem;
 
 /* Full forward model (reference deform(), 2D/deform.cu:22-119) and, when

@@ -122,7 +122,11 @@ class Problem:
         p.btmWgt, p.timeStp, p.timeNum = float(spec["btmWgt"]), float(spec["timeStp"]), int(spec["timeNum"])
         p.cgItrMax, p.cgTolSqu = int(spec["cgItrMax"]), float(spec["cgTolSqu"])
         p.rdItrMax, p.rdTolSqu = int(spec.get("rdItrMax", 10000)), float(spec.get("rdTolSqu", 1e-26))
-        p.velocityGuess = {"previous": 0, "extrapolate": 1, "quadratic": 2}[spec.get("velocityGuess", "quadratic")]
+        g = spec.get("velocityGuess", "cubic")     # the layered model's default start (polynomial order 3)
+        p.velocityGuess = {"previous": 0, "extrapolate": 1, "linear": 1, "quadratic": 2, "cubic": 3, "quartic": 4,
+                           "quintic": 5}[g] if isinstance(g, str) else int(g)
+        if not 0 <= p.velocityGuess <= 5:
+            raise ValueError("velocityGuess order outside 0 .. 5")
         self.p = p
         self.keep = keep
         self.dim, self.N = D, N

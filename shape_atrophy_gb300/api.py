@@ -89,6 +89,19 @@ def apply_tuning(device: int = 0, path: str = TUNING_FILE):
     return e
 
 
+# Layered model: where each step's velocity CG starts -- the polynomial through the last k + 1 velocities,
+# evaluated one step ahead (k = 0: the previous velocity, the reference's warm start).  Names or orders.
+GUESS_ORDERS = {"previous": 0, "extrapolate": 1, "linear": 1, "quadratic": 2, "cubic": 3, "quartic": 4, "quintic": 5}
+DEFAULT_GUESS = "cubic"
+
+
+def guess_order(g) -> int:
+    k = GUESS_ORDERS[g] if isinstance(g, str) else int(g)
+    if not 0 <= k <= 5:
+        raise ValueError(f"velocityGuess order {k} outside 0 .. 5")
+    return k
+
+
 def context(device: int = 0) -> _lib.Context:
     if device not in _CTX:
         _CTX[device] = _lib.Context(device)
@@ -164,10 +177,7 @@ def _params(spec: dict, K: _Keep, precision: str) -> _lib.Params:
     p.cgKernel = {"auto": _lib.SA_CG_AUTO, "persistent": _lib.SA_CG_PERSISTENT,
                   "two-kernel": _lib.SA_CG_TWO_KERNEL,
                   "persistent-global": _lib.SA_CG_PERSISTENT_GLOBAL}[spec.get("cgKernel", "auto")]
-    # layered model: velocity CG start, "quadratic" (default), "extrapolate" (linear) or "previous" (the
-    # reference's warm start)
-    p.velocityGuess = {"previous": _lib.SA_GUESS_PREVIOUS, "extrapolate": _lib.SA_GUESS_EXTRAPOLATE,
-                       "quadratic": _lib.SA_GUESS_QUADRATIC}[spec.get("velocityGuess", "quadratic")]
+    p.velocityGuess = guess_order(spec.get("velocityGuess", DEFAULT_GUESS))
     return p
 
 

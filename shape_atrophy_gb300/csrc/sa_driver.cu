@@ -490,8 +490,7 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 struct Work {
 	double *xa, *xb;            // node positions t, t+1 (interleaved)
 	double *v, *b, *pd, *blk, *dinv, *fy, *fr;
-	double *vPrev = nullptr;    // velocity of the step before (extrapolated CG start)
-	double *vPrev2 = nullptr;   // and of the step before that (quadratic extrapolation)
+	double *vHist = nullptr;    // velocities of earlier steps (extrapolated CG start), velocityGuess x n
 	double *Mnow, *Mnxt, *L, *dinvRd, *rhs;
 	Geom g0, g1;
 	CgWork cw;
@@ -506,8 +505,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	long N = m.N, E = m.E, Z = m.Z, n = N * D;
 	w.xa = P.alloc<double>(n); w.xb = P.alloc<double>(n);
 	w.v = P.alloc<double>(n); w.b = P.alloc<double>(n); w.pd = P.zeros<double>(N);
-	w.vPrev = P.zeros<double>(n);
-	w.vPrev2 = md.velocityGuess == SA_GUESS_QUADRATIC ? P.zeros<double>(n) : nullptr;
+	if (md.velocityGuess > 0) w.vHist = P.zeros<double>((size_t) md.velocityGuess * n);
 	long T = m.slTotal;                    // sliced slots, padding included (padding stays zero)
 	w.blk = P.zeros<double>((size_t) T * sell_vals<D>()); w.dinv = P.alloc<double>(n);
 	w.fy = P.alloc<double>(N); w.fr = P.alloc<double>(N);
@@ -606,12 +604,7 @@ struct Stepper {
 		// CG start: the previous velocity (the reference's choice), or (layered model, velocityGuess
 		// SA_GUESS_EXTRAPOLATE) its linear extrapolation 2 v_t-1 - v_t-2 from the third step on: the same
 		// converged answer to the CG tolerance, about a third fewer iterations when the motion is smooth
-		if (md.velocityGuess == SA_GUESS_EXTRAPOLATE && !useK) {
-			if (t >= 2) launch_extrapolate(m.N * (long) D, w.v, w.vPrev, s);
-			else SA_CHECK(cudaMemcpyAsync(w.vPrev, w.v, sizeof(double) * m.N * D, cudaMemcpyDeviceToDevice, s));
-		} else if (md.velocityGuess == SA_GUESS_QUADRATIC && !useK) {
-			launch_extrapolate2(m.N * (long) D, t, w.v, w.vPrev, w.vPrev2, s);
-		}
+		if (md.velocityGuess > 0 && !useK) launch_extrap_poly(m.N * (long) D, md.velocityGuess, t, w.v, w.vHist, s);
 		launch_activity<D>(m, md, tau_now(), w.fy, w.fr, s);
 		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
 		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, w.cw.binv32, s);
@@ -746,8 +739,8 @@ static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *
 	md.rdTolSqu = p->rdTolSqu > 0.0 ? p->rdTolSqu : (md.frame ? 1e-26 : p->cgTolSqu);
 	SA_REQUIRE(p->cgKernel >= SA_CG_AUTO && p->cgKernel <= SA_CG_PERSISTENT_GLOBAL, "cgKernel must be 0, 1, 2 or 3");
 	md.cgKernel = p->cgKernel;
-	SA_REQUIRE(p->velocityGuess >= SA_GUESS_PREVIOUS && p->velocityGuess <= SA_GUESS_QUADRATIC,
-	           "velocityGuess must be 0, 1 or 2");
+	SA_REQUIRE(p->velocityGuess >= 0 && p->velocityGuess <= SA_GUESS_MAX_ORDER,
+	           "velocityGuess must be a polynomial order 0 .. 5");
 	md.velocityGuess = md.frame ? SA_GUESS_PREVIOUS : p->velocityGuess;
 	if (tgt) {
 		md.cenKnl = tgt->cenKnlType; md.dirKnl = tgt->dirKnlType;
@@ -919,12 +912,11 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 	}
 	const long n = (long) m.N * D, N = m.N;
 	// tangent state per parameter: positions (two copies: t, t+1), concentration (t, t+1), velocity
-	std::vector<double *> dx[2], dtau[2], dv, dvPrev, dvPrev2;
+	std::vector<double *> dx[2], dtau[2], dv, dvHist;
 	for (int k = 0; k < K; ++k) {
 		for (int c = 0; c < 2; ++c) { dx[c].push_back(P.zeros<double>(n)); dtau[c].push_back(P.zeros<double>(N)); }
 		dv.push_back(P.zeros<double>(n));
-		dvPrev.push_back(P.zeros<double>(n));
-		dvPrev2.push_back(md.velocityGuess == SA_GUESS_QUADRATIC ? P.zeros<double>(n) : nullptr);
+		dvHist.push_back(md.velocityGuess > 0 ? P.zeros<double>((size_t) md.velocityGuess * n) : nullptr);
 	}
 	double *drecA = P.alloc<double>((size_t) rec_len<D>() * m.E), *drecB = P.alloc<double>((size_t) rec_len<D>() * m.E);
 	double *rhsV = P.alloc<double>(n), *rhsT = P.alloc<double>(N), *dpd = P.zeros<double>(N), *dfy = P.alloc<double>(N);
@@ -963,12 +955,7 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 			launch_axpy64(N, dtau[cur][k], y0 - 1.0, dtau[cur][k], dfy, s);     // dfy = y0 dtau
 			launch_vel_tan_rhs<D>(m, md, st.gn->rec, drecA, w.fy, dfy, w.v, dpd, rhsV, s);
 			// start as the forward solve does: previous tangent velocity, or its extrapolation
-			if (md.velocityGuess == SA_GUESS_EXTRAPOLATE) {
-				if (st.t >= 2) launch_extrapolate(n, dv[k], dvPrev[k], s);
-				else SA_CHECK(cudaMemcpyAsync(dvPrev[k], dv[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-			} else if (md.velocityGuess == SA_GUESS_QUADRATIC) {
-				launch_extrapolate2(n, st.t, dv[k], dvPrev[k], dvPrev2[k], s);
-			}
+			if (md.velocityGuess > 0) launch_extrap_poly(n, md.velocityGuess, st.t, dv[k], dvHist[k], s);
 			code = solve(std::integral_constant<int, D>(), w.blk, w.dinv, rhsV, dv[k], md.cgItrMax, md.cgTolSqu);
 			if (code != SA_OK) { status = code; break; }
 			launch_axpy64(n, dx[cur][k], dt, dv[k], dx[1 - cur][k], s);

@@ -303,9 +303,8 @@ template <int D> void launch_advance(int N, const double *x, const double *v, do
 void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_t s);
 // tangent-linear kernels of the layered model (sa_tangent.cu)
 void launch_axpy64(long n, const double *x, double a, const double *y, double *out, cudaStream_t s);
-void launch_extrapolate(long n, double *v, double *vPrev, cudaStream_t s);
+void launch_extrap_poly(long n, int order, int t, double *v, double *hist, cudaStream_t s);
 void launch_lin_extrap(long n, const double *a, const double *b, double *out, cudaStream_t s);
-void launch_extrapolate2(long n, int t, double *v, double *p1, double *p2, cudaStream_t s);
 template <int D> void launch_geom_tan(const Mesh &m, const double *rec, const double *dx, double *drec, cudaStream_t s);
 template <int D> void launch_penalty_tan(const Mesh &m, const double *x, const double *dx, double *dpd, cudaStream_t s);
 template <int D> void launch_vel_tan_rhs(const Mesh &m, const Model &md, const double *rec, const double *drec,

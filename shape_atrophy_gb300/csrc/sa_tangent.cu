@@ -226,37 +226,42 @@ __global__ void k_tau0_tan(int N, const double *__restrict__ x, const double *__
 	dtau[i] = v;
 }
 
-// v <- 2 v - vPrev, vPrev <- old v (linear extrapolation of the velocity as the next CG start)
-__global__ void k_extrapolate(long n, double *__restrict__ v, double *__restrict__ vPrev)
+// Polynomial extrapolation of the next CG start from the previous solutions: v holds x_t-1, hist[j n ..]
+// holds x_t-2-j (j < depth).  With q of them usable, v <- sum_{j=0..q} (-1)^j C(q+1, j+1) x_t-1-j (the
+// degree-q polynomial through the last q+1 solutions, evaluated one step ahead); then the history shifts.
+constexpr int kMaxGuessOrder = 5;
+__constant__ double c_binom[kMaxGuessOrder + 1][kMaxGuessOrder + 1] = {
+	{1, 0, 0, 0, 0, 0},
+	{2, -1, 0, 0, 0, 0},
+	{3, -3, 1, 0, 0, 0},
+	{4, -6, 4, -1, 0, 0},
+	{5, -10, 10, -5, 1, 0},
+	{6, -15, 20, -15, 6, -1},
+};
+
+__global__ void k_extrap_poly(long n, int q, int depth, double *__restrict__ v, double *__restrict__ hist)
 {
 	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
 	if (k >= n) return;
-	const double a = v[k];
-	v[k] = 2.0 * a - vPrev[k];
-	vPrev[k] = a;
+	double h[kMaxGuessOrder + 1];
+	h[0] = v[k];
+	for (int j = 1; j <= depth; ++j) h[j] = hist[(long) (j - 1) * n + k];
+	if (q > 0) {
+		double s = 0.0;
+		for (int j = 0; j <= q; ++j) s += c_binom[q][j] * h[j];
+		v[k] = s;
+	}
+	for (int j = depth - 1; j >= 1; --j) hist[(long) j * n + k] = h[j];
+	if (depth > 0) hist[k] = h[0];
 }
 
-void launch_extrapolate(long n, double *v, double *vPrev, cudaStream_t s)
+void launch_extrap_poly(long n, int order, int t, double *v, double *hist, cudaStream_t s)
 {
-	k_extrapolate<<<grid_for(n), kBlock, 0, s>>>(n, v, vPrev);
-}
-
-// quadratic extrapolation from three previous velocities (linear at step 2, none before): v holds v_t-1,
-// p1 v_t-2, p2 v_t-3; afterwards p1, p2 hold v_t-1, v_t-2
-__global__ void k_extrapolate2(long n, int t, double *__restrict__ v, double *__restrict__ p1, double *__restrict__ p2)
-{
-	long k = blockIdx.x * (long) blockDim.x + threadIdx.x;
-	if (k >= n) return;
-	const double a = v[k], b = p1[k], c = p2[k];
-	if (t >= 3) v[k] = 3.0 * a - 3.0 * b + c;
-	else if (t == 2) v[k] = 2.0 * a - b;
-	p2[k] = b;
-	p1[k] = a;
-}
-
-void launch_extrapolate2(long n, int t, double *v, double *p1, double *p2, cudaStream_t s)
-{
-	k_extrapolate2<<<grid_for(n), kBlock, 0, s>>>(n, t, v, p1, p2);
+	const int depth = order < kMaxGuessOrder ? order : kMaxGuessOrder;
+	int q = t - 1;                       // previous solutions x_0 .. x_t-1: degree at most t - 1
+	if (q > depth) q = depth;
+	if (q < 0) q = 0;
+	if (depth > 0) k_extrap_poly<<<grid_for(n), kBlock, 0, s>>>(n, q, depth, v, hist);
 }
 
 // out = 2 a - b (out may alias b)
