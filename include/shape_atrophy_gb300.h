@@ -328,6 +328,13 @@ int sa_device_name(int device, char *buf, int len, int *smCount);
  * *ctasGaveUp = CTAs that gave up (2 when the mechanism works). */
 int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs);
 
+/* Accuracy check of the FP64 exponential (fn = 0: table-driven) and square
+ * root (fn = 1: Newton iteration from the FP32 reciprocal square root) that
+ * the varifold pair sums use (no reference counterpart): for n host values
+ * x, y[k] = that function of x[k] and yref[k] = CUDA's exp(x[k]) or
+ * sqrt(x[k]), both evaluated on the device. */
+int sa_selftest_math(sa_context *ctx, int fn, long n, const double *x, double *y, double *yref);
+
 /* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and
  * deformation_3D_frame (dim 3): arguments in prhs order
  * (CUDA/2D_frame/deformation.cu:24-50), outputs plhs[0..2]

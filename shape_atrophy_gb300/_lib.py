@@ -124,6 +124,7 @@ def load():
     lib.sa_set_tuning.argtypes = [C.c_char_p, C.c_int]
     lib.sa_get_tuning.argtypes = [C.c_char_p, _ip]
     lib.sa_device_name.argtypes = [C.c_int, C.c_char_p, C.c_int, _ip]
+    lib.sa_selftest_math.argtypes = [vp, C.c_int, C.c_long, _dp, _dp, _dp]
     _LIB = lib
     return lib
 

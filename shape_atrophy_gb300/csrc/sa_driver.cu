@@ -2133,6 +2133,24 @@ int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs
 	});
 }
 
+int sa_selftest_math(sa_context *ctx, int fn, long n, const double *x, double *y, double *yref)
+{
+	if (fn < 0 || fn > 1 || n < 0 || (n > 0 && (!x || !y || !yref))) return SA_ERR_ARG;
+	return sa::guarded(ctx, [&]() {
+		if (n == 0) return SA_OK;
+		double *d = nullptr;
+		cudaStream_t s = ctx->stream;
+		SA_CHECK(cudaMallocAsync(&d, sizeof(double) * 3 * n, s));
+		SA_CHECK(cudaMemcpyAsync(d, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+		sa::math_check(fn, n, d, d + n, d + 2 * n, s);
+		SA_CHECK(cudaMemcpyAsync(y, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+		SA_CHECK(cudaMemcpyAsync(yref, d + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+		SA_CHECK(cudaFreeAsync(d, s));
+		SA_CHECK(cudaStreamSynchronize(s));
+		return SA_OK;
+	});
+}
+
 
 int sa_set_tuning(const char *name, int value)
 {

@@ -303,6 +303,9 @@ template <int D> void launch_advance(int N, const double *x, const double *v, do
 void launch_soa_to_aos(int N, int D, const double *soa, double *aos, cudaStream_t s);
 // tangent-linear kernels of the layered model (sa_tangent.cu)
 void launch_axpy64(long n, const double *x, double a, const double *y, double *out, cudaStream_t s);
+// accuracy check of the varifold's FP64 exponential and square root (sa_varifold.cu): fn 0: y = exp_tab(x),
+// yref = exp(x); fn 1: y = sqrt_nr(x), yref = sqrt(x)
+void math_check(int fn, long n, const double *x, double *y, double *yref, cudaStream_t s);
 void launch_extrap_poly(long n, int order, int t, double *v, double *hist, cudaStream_t s);
 void launch_lin_extrap(long n, const double *a, const double *b, double *out, cudaStream_t s);
 template <int D> void launch_geom_tan(const Mesh &m, const double *rec, const double *dx, double *drec, cudaStream_t s);

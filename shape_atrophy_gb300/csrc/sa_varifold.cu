@@ -24,27 +24,116 @@ namespace sa {
 
 constexpr int kVfdTile = 128;
 
+// 2^(j/64), j = 0 .. 63, each rounded to the nearest double (computed with 60-digit decimal arithmetic)
+__constant__ double c_exp2_64[64] = {
+	0x1.0000000000000p+0, 0x1.02c9a3e778061p+0, 0x1.059b0d3158574p+0, 0x1.0874518759bc8p+0,
+	0x1.0b5586cf9890fp+0, 0x1.0e3ec32d3d1a2p+0, 0x1.11301d0125b51p+0, 0x1.1429aaea92de0p+0,
+	0x1.172b83c7d517bp+0, 0x1.1a35beb6fcb75p+0, 0x1.1d4873168b9aap+0, 0x1.2063b88628cd6p+0,
+	0x1.2387a6e756238p+0, 0x1.26b4565e27cddp+0, 0x1.29e9df51fdee1p+0, 0x1.2d285a6e4030bp+0,
+	0x1.306fe0a31b715p+0, 0x1.33c08b26416ffp+0, 0x1.371a7373aa9cbp+0, 0x1.3a7db34e59ff7p+0,
+	0x1.3dea64c123422p+0, 0x1.4160a21f72e2ap+0, 0x1.44e086061892dp+0, 0x1.486a2b5c13cd0p+0,
+	0x1.4bfdad5362a27p+0, 0x1.4f9b2769d2ca7p+0, 0x1.5342b569d4f82p+0, 0x1.56f4736b527dap+0,
+	0x1.5ab07dd485429p+0, 0x1.5e76f15ad2148p+0, 0x1.6247eb03a5585p+0, 0x1.6623882552225p+0,
+	0x1.6a09e667f3bcdp+0, 0x1.6dfb23c651a2fp+0, 0x1.71f75e8ec5f74p+0, 0x1.75feb564267c9p+0,
+	0x1.7a11473eb0187p+0, 0x1.7e2f336cf4e62p+0, 0x1.82589994cce13p+0, 0x1.868d99b4492edp+0,
+	0x1.8ace5422aa0dbp+0, 0x1.8f1ae99157736p+0, 0x1.93737b0cdc5e5p+0, 0x1.97d829fde4e50p+0,
+	0x1.9c49182a3f090p+0, 0x1.a0c667b5de565p+0, 0x1.a5503b23e255dp+0, 0x1.a9e6b5579fdbfp+0,
+	0x1.ae89f995ad3adp+0, 0x1.b33a2b84f15fbp+0, 0x1.b7f76f2fb5e47p+0, 0x1.bcc1e904bc1d2p+0,
+	0x1.c199bdd85529cp+0, 0x1.c67f12e57d14bp+0, 0x1.cb720dcef9069p+0, 0x1.d072d4a07897cp+0,
+	0x1.d5818dcfba487p+0, 0x1.da9e603db3285p+0, 0x1.dfc97337b9b5fp+0, 0x1.e502ee78b3ff6p+0,
+	0x1.ea4afa2a490dap+0, 0x1.efa1bee615a27p+0, 0x1.f50765b6e4540p+0, 0x1.fa7c1819e90d8p+0,
+};
+
+// e^x in FP64 by Tang's table-driven method (P. T. P. Tang, "Table-driven implementation of the
+// exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2), 1989): with
+// N = rint(64 x / ln 2) = 64 m + j, r = x - N ln2/64 (|r| <= ln2/128, formed exactly enough by two fused
+// multiply-adds with ln2/64 split in a leading and a trailing part),
+//     e^x = 2^m * 2^(j/64) * (1 + p(r)),   p(r) = r + r^2/2 + r^3/6 + r^4/24 + r^5/120,
+// the Taylor remainder r^6/720 staying below 2^-54.  2^(j/64) comes from a 64-entry table in shared
+// memory (tab), 2^m is added to the exponent field.  Ten FP64-pipe instructions; |x| >= 700, infinities
+// and NaN are passed to exp().  Error about 1 ulp (tests/test_gpu_pair_math.py checks it against exp()).
+__device__ __forceinline__ double exp_tab(double x, const double *__restrict__ tab)
+{
+	const int hx = __double2hiint(x) & 0x7fffffff;
+	if (hx >= 0x4085E000) return exp(x);                      // |x| >= 700 (0x4085E000... = 700.0), Inf, NaN
+	const double t = fma(x, 0x1.71547652b82fep+6, 0x1.8p52);  // 64/ln2; 1.5 * 2^52 rounds to an integer
+	const int N = __double2loint(t);
+	const double Nd = t - 0x1.8p52;
+	double r = fma(-Nd, 0x1.62e42fefa39efp-7, x);             // ln2/64, leading part
+	r = fma(-Nd, 0x1.abc9e3b39803fp-62, r);                   // trailing part
+	double p = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+	p = fma(p, r, 1.0 / 6.0);
+	p = fma(p, r, 0.5);
+	p = fma(p, r, 1.0);
+	p = p * r;
+	const double S = tab[N & 63];
+	const double y = fma(S, p, S);
+	return __hiloint2double(__double2hiint(y) + (int) ((unsigned) (N >> 6) << 20), __double2loint(y));
+}
+
+// sqrt(a) in FP64 by Newton's (Heron's) iteration s <- s + (a - s^2) h with h = y / 2 fixed, where y is the
+// FP32 reciprocal square root of a (relative error d of a few 1e-8): from s = a y each step multiplies the
+// relative error by about d (1.5 d^2 after the first, below 1e-20 after the second), so the result is
+// within about 1 ulp of the root.  Six FP64-pipe instructions.  Arguments outside [2^-95, 2^96) (zero
+// included) go to sqrt(); tests/test_gpu_pair_math.py checks the result against sqrt().
+__device__ __forceinline__ double sqrt_nr(double a)
+{
+	const unsigned e = (unsigned) __double2hiint(a) >> 20;   // sign and biased exponent
+	if (e < 1023u - 95u || e >= 1023u + 96u) return sqrt(a);
+	const double y = (double) rsqrtf(__double2float_rn(a));
+	const double h = 0.5 * y;
+	double s = a * y;
+	s = fma(fma(-s, s, a), h, s);
+	s = fma(fma(-s, s, a), h, s);
+	return s;
+}
+
+__device__ __forceinline__ double exp_k(double x, const double *tab) { return exp_tab(x, tab); }
+__device__ __forceinline__ float exp_k(float x, const double *) { return exp(x); }
+__device__ __forceinline__ double sqrt_k(double x) { return sqrt_nr(x); }
+__device__ __forceinline__ float sqrt_k(float x) { return sqrt(x); }
+
 // Kernel values with the widths' reciprocals iw = 1/w, iw2 = 1/w^2 precomputed (no division per pair: FP64
 // divisions cost about ten FP64-pipe instructions each on GB300); derivatives d1 only when G (gradient).
+// tab: the 2^(j/64) table in shared memory (FP64 exponentials).
 template <typename T, bool G>
-__device__ __forceinline__ T cen_knl(int type, T iw, T iw2, T d2, T &d1)
+__device__ __forceinline__ T cen_knl(int type, T iw, T iw2, T d2, T &d1, const double *tab)
 {
-	if (type == 'G') { T k = exp(-d2 * iw2); if (G) d1 = (T) -2.0 * k * iw2; return k; }
+	if (type == 'G') { T k = exp_k(-d2 * iw2, tab); if (G) d1 = (T) -2.0 * k * iw2; return k; }
 	if (type == 'C') { T k = (T) 1.0 / ((T) 1.0 + d2 * iw2); if (G) d1 = (T) -2.0 * k * k * iw2; return k; }
-	T r = sqrt(d2) * iw, ex = exp(-r);          // 'M'
+	T r = sqrt_k(d2) * iw, ex = exp_k(-r, tab);   // 'M'
 	if (G) d1 = -ex * iw2;
-	return ((T) 1.0 + r) * ex;
+	return fma(r, ex, ex);                          // (1 + r) e^-r
 }
 
 template <typename T, bool G>
-__device__ __forceinline__ T dir_knl(int type, T iw2, T ang, T &d1)
+__device__ __forceinline__ T dir_knl(int type, T iw2, T ang, T &d1, const double *tab)
 {
 	if (type == 'B') { if (G) d1 = (T) 2.0 * ang; return ang * ang; }
 	if (type == 'L') { if (G) d1 = (T) 1.0; return ang; }
-	if (type == 'O') { T k = exp((T) 2.0 * (ang - (T) 1.0) * iw2); if (G) d1 = (T) 2.0 * k * iw2; return k; }
-	T k = exp((T) 2.0 * (ang * ang - (T) 1.0) * iw2);     // 'U'
+	if (type == 'O') { T k = exp_k((T) 2.0 * (ang - (T) 1.0) * iw2, tab); if (G) d1 = (T) 2.0 * k * iw2; return k; }
+	T k = exp_k((T) 2.0 * (ang * ang - (T) 1.0) * iw2, tab);     // 'U'
 	if (G) d1 = (T) 4.0 * ang * k * iw2;
 	return k;
+}
+
+// exp_tab and exp() (fn 0) or sqrt_nr and sqrt() (fn 1) side by side: accuracy check
+__global__ void k_math_check(int fn, long n, const double *__restrict__ x, double *__restrict__ y,
+                             double *__restrict__ yref)
+{
+	__shared__ double tab[64];
+	if (threadIdx.x < 64) tab[threadIdx.x] = c_exp2_64[threadIdx.x];
+	__syncthreads();
+	for (long k = blockIdx.x * (long) blockDim.x + threadIdx.x; k < n; k += (long) gridDim.x * blockDim.x) {
+		if (fn == 0) { y[k] = exp_tab(x[k], tab); yref[k] = exp(x[k]); }
+		else { y[k] = sqrt_nr(x[k]); yref[k] = sqrt(x[k]); }
+	}
+}
+
+void math_check(int fn, long n, const double *x, double *y, double *yref, cudaStream_t s)
+{
+	k_math_check<<<4 * 152, 128, 0, s>>>(fn, n, x, y, yref);
+	SA_CHECK(cudaGetLastError());
 }
 
 template <int D>
@@ -89,6 +178,8 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 {
 	constexpr bool kSplit = sizeof(T) < sizeof(double);     // two-float centres in FP32
 	__shared__ T sc[kVfdTile * D], su[kVfdTile * D], sv[kVfdTile], sl[kSplit ? kVfdTile * D : 1];
+	__shared__ double sExp[kSplit ? 1 : 64];
+	if (!kSplit && threadIdx.x < 64) sExp[threadIdx.x] = c_exp2_64[threadIdx.x];   // read after the tile barrier
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	bool act = i < R.n;
 	T ci[D], cl[D], ui[D], vi = 0;
@@ -130,14 +221,17 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 			}
 			__syncthreads();
 			if (!act) continue;
-			T tile = 0, comp = 0, tgc[D], tgt[D];
+			// tile = sum of K_c K_d vol_j over the tile's columns; the row factor coef * vol_i and, for the
+			// symmetric half, the weights (2 off the diagonal, 1 on it: 2 tile - diagonal term) are applied
+			// once per tile
+			T tile = 0, comp = 0, diag = 0, tgc[D], tgt[D];
 			for (int d = 0; d < D; ++d) { tgc[d] = 0; tgt[d] = 0; }
 			for (int jj = 0; jj < nt; ++jj) {
-				T wgt = (T) 1;
+				bool onDiag = false;
 				if (sym) {
 					const int j = j0 + jj;
 					if (j < i) continue;
-					if (j > i) wgt = (T) 2;
+					onDiag = j == i;
 				}
 				T df[D];
 				for (int d = 0; d < D; ++d) {
@@ -149,16 +243,17 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 				T ang = ui[0] * su[jj * D];
 				for (int d = 1; d < D; ++d) ang = ang + ui[d] * su[jj * D + d];
 				T d1c = 0, d1d = 0;
-				T kc = cen_knl<T, G>(ck, ciw, ciw2, d2, d1c);
-				T kd = dir_knl<T, G>(dk, diw2, ang, d1d);
+				T kc = cen_knl<T, G>(ck, ciw, ciw2, d2, d1c, sExp);
+				T kd = dir_knl<T, G>(dk, diw2, ang, d1d, sExp);
 				T vj = sv[jj];
-				const T term = wgt * cv * kc * kd * vj;
+				const T kv = kd * vj;
+				if (onDiag) diag = kc * kv;
 				if (kSplit) {                  // Kahan: the FP32 tile sum keeps its lost low bits
-					T y = term - comp, t = tile + y;
+					T y = kc * kv - comp, t = tile + y;
 					comp = (t - tile) - y;
 					tile = t;
 				} else {
-					tile += term;
+					tile = fma(kc, kv, tile);
 				}
 				if (G) {
 					// geometricFunction/grassmanFunction gradients and dqVfd_DD_DT accumulation
@@ -170,7 +265,7 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 					}
 				}
 			}
-			acc += (double) tile;
+			acc += (double) cv * (sym ? 2.0 * (double) tile - (double) diag : (double) tile);
 			if (G) for (int d = 0; d < D; ++d) { gc[d] += (double) tgc[d]; gt[d] += (double) tgt[d]; }
 		}
 	}
