@@ -33,7 +33,9 @@
 struct sa_context {
 	int device = 0;
 	cudaStream_t stream = nullptr;
+	cudaStream_t side = nullptr;                    // work that overlaps the host's set-up (target varifold rows)
 	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	cudaEvent_t sideIn = nullptr, sideOut = nullptr;
 	std::string err;
 };
 
@@ -54,17 +56,25 @@ struct Pool {                 // device allocations of one call, freed at the en
 	std::vector<void *> ptrs;
 	cudaStream_t s;
 	size_t bytes = 0;         // device bytes allocated
-	explicit Pool(cudaStream_t st) : s(st) {}
+	// stream-ordered (cudaMallocAsync on s, freed on s): for a call whose side stream runs while the host
+	// allocates -- a plain cudaMalloc between two streams' launches keeps them from running concurrently.
+	// Only for pools whose memory no other stream uses after the pool's stream has moved on.
+	bool ordered = false;
+	explicit Pool(cudaStream_t st, bool streamOrdered = false) : s(st), ordered(streamOrdered) {}
 	~Pool() { release(); }
 	void release()
 	{
-		for (void *p : ptrs) cudaFree(p);
+		for (void *p : ptrs) {
+			if (ordered) cudaFreeAsync(p, s);
+			else cudaFree(p);
+		}
 		ptrs.clear();
 	}
 	template <typename T> T *alloc(size_t n)
 	{
 		void *p = nullptr;
-		SA_CHECK(cudaMalloc(&p, sizeof(T) * (n ? n : 1)));
+		if (ordered) SA_CHECK(cudaMallocAsync(&p, sizeof(T) * (n ? n : 1), s));
+		else SA_CHECK(cudaMalloc(&p, sizeof(T) * (n ? n : 1)));
 		ptrs.push_back(p);
 		bytes += sizeof(T) * (n ? n : 1);
 		return (T *) p;
@@ -104,6 +114,13 @@ struct PhaseTrace {
 		             std::chrono::duration<double, std::milli>(t - t0).count());
 		t0 = t;
 	}
+};
+
+// waits for the context's side stream when a call that launched work on it leaves (normally or by an error)
+struct SideJoin {
+	cudaStream_t side;
+	bool on = false;
+	~SideJoin() { if (on) cudaStreamSynchronize(side); }
 };
 
 struct ArgError { std::string msg; };
@@ -760,11 +777,34 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 {
 	cudaStream_t s = ctx->stream;
 	PhaseTrace tr(s);
-	Pool P(s);
+	Pool P(s, true);                          // stream-ordered: the host's set-up overlaps the side stream
+	SideJoin join{ctx->side};                 // before P's destructor frees what the side stream reads
 	Mesh m;
 	Model md;
 	fill_model(md, D, prm, tgt, P);
 	tr.mark("model");
+	const double *tc = nullptr, *tu = nullptr, *tvl = nullptr;
+	VfdTargetCache vcache;                    // target-target varifold rows, shared by the columns
+	if (tgt) {
+		SA_REQUIRE(tgt->tgtElmNum > 0 && tgt->cenPosMat && tgt->uniDirMat && tgt->elmVolVec, "empty target");
+		SA_REQUIRE(obj && obj->vfdElmNum >= 0, "vfdElmNum");
+		const int Vt = tgt->tgtElmNum, Vd = obj->vfdElmNum;
+		tc = P.dev(tgt->cenPosMat, (size_t) Vt * D);
+		tu = P.dev(tgt->uniDirMat, (size_t) Vt * D);
+		tvl = P.dev(tgt->elmVolVec, (size_t) Vt);
+		vcache.rows = P.alloc<double>((size_t) Vt);
+		vcache.capacity = Vt;
+		if (Vd >= Vt) {
+			// the objective's target-target rows depend on the target only: the side stream computes them
+			// while the host validates and lays out the mesh (the objective finds them in the cache)
+			double *part = P.alloc<double>((size_t) vfd_chunk_count(Vd, Vt) * Vt);
+			SA_CHECK(cudaEventRecord(ctx->sideIn, s));
+			SA_CHECK(cudaStreamWaitEvent(ctx->side, ctx->sideIn, 0));
+			join.on = true;
+			varifold_target_rows<D>(md, Vd, tc, tu, tvl, Vt, md.precision, part, vcache, ctx->side);
+			SA_CHECK(cudaEventRecord(ctx->sideOut, ctx->side));
+		}
+	}
 	build_mesh(m, obj, tgt != nullptr, false, !md.frame, md.lyrNum, P, &tr);
 	if (md.frame || md.ldmWgt != 0.0)
 		SA_REQUIRE((size_t) m.N * m.N * sizeof(double) <= kDenseLimitBytes && m.N <= 65535,
@@ -773,13 +813,6 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 	           "tauVarMat too small");
 	const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
 	std::vector<double> tv = to_host(tauVarMat, (size_t) tauVarNum * objNum, s);
-	const double *tc = nullptr, *tu = nullptr, *tvl = nullptr;
-	if (tgt) {
-		SA_REQUIRE(tgt->tgtElmNum > 0 && tgt->cenPosMat && tgt->uniDirMat && tgt->elmVolVec, "empty target");
-		tc = P.dev(tgt->cenPosMat, (size_t) tgt->tgtElmNum * D);
-		tu = P.dev(tgt->uniDirMat, (size_t) tgt->tgtElmNum * D);
-		tvl = P.dev(tgt->elmVolVec, (size_t) tgt->tgtElmNum);
-	}
 	Work w;
 	alloc_work<D>(w, m, md, lmkStk != nullptr, P);
 	{   // initial element orientation for the Jacobian sign check
@@ -790,8 +823,7 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 	std::vector<double> objs(objNum, 0.0);
 	SolveOut last{};
 	tr.mark("inputs, work buffers");
-	VfdTargetCache vcache;                    // target-target varifold rows, shared by the columns
-	if (tgt) { vcache.rows = P.alloc<double>((size_t) tgt->tgtElmNum); vcache.capacity = tgt->tgtElmNum; }
+	if (join.on) SA_CHECK(cudaStreamWaitEvent(s, ctx->sideOut, 0));
 	SA_CHECK(cudaEventRecord(ctx->e0, s));
 	for (int k = 0; k < objNum; ++k) {
 		const double *tvk = tv.data() + (size_t) k * tauVarNum;
@@ -1779,7 +1811,10 @@ int sa_create(sa_context **out, int device)
 	sa_context *c = new sa_context();
 	c->device = device;
 	if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-	    cudaEventCreate(&c->e0) != cudaSuccess || cudaEventCreate(&c->e1) != cudaSuccess) {
+	    cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+	    cudaEventCreate(&c->e0) != cudaSuccess || cudaEventCreate(&c->e1) != cudaSuccess ||
+	    cudaEventCreateWithFlags(&c->sideIn, cudaEventDisableTiming) != cudaSuccess ||
+	    cudaEventCreateWithFlags(&c->sideOut, cudaEventDisableTiming) != cudaSuccess) {
 		cudaGetLastError();
 		delete c;
 		return SA_ERR_CUDA;
@@ -1793,9 +1828,13 @@ int sa_destroy(sa_context *c)
 	if (!c) return SA_OK;
 	cudaSetDevice(c->device);
 	if (c->stream) cudaStreamSynchronize(c->stream);
+	if (c->side) cudaStreamSynchronize(c->side);
 	if (c->e0) cudaEventDestroy(c->e0);
 	if (c->e1) cudaEventDestroy(c->e1);
+	if (c->sideIn) cudaEventDestroy(c->sideIn);
+	if (c->sideOut) cudaEventDestroy(c->sideOut);
 	if (c->stream) cudaStreamDestroy(c->stream);
+	if (c->side) cudaStreamDestroy(c->side);
 	delete c;
 	return SA_OK;
 }

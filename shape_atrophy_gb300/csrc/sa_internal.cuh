@@ -437,6 +437,14 @@ template <int D> double varifold(const Mesh &m, const Model &md, const double *x
                                  const double *tgtDir, const double *tgtVol, int Vt, double *grad,
                                  cudaStream_t s, int precision, int *err, VfdTargetCache *cache = nullptr);
 
+// column chunks of the varifold pair sums of a Vd x Vt objective
+int vfd_chunk_count(int Vd, int Vt);
+// the target-target rows of a Vd x Vt objective into cache.rows on stream s (the objective's own launches);
+// part: vfd_chunk_count(Vd, Vt) * Vt doubles
+template <int D> void varifold_target_rows(const Model &md, int Vd, const double *tgtCen, const double *tgtDir,
+                                           const double *tgtVol, int Vt, int precision, double *part,
+                                           VfdTargetCache &cache, cudaStream_t s);
+
 // deterministic sum of n doubles on the device (returned via host)
 double device_sum(const double *v, long n, double *scratch, cudaStream_t s);
 

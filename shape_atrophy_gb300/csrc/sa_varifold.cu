@@ -372,6 +372,53 @@ double device_sum(const double *v, long n, double *scratch, cudaStream_t s)
 	return h;
 }
 
+constexpr int kVfdBlock = 128;
+
+// column chunks of the pair sums of a Vd x Vt objective: enough CTAs to fill the GPU (the pair sums are latency
+// bound at one CTA per SM), each chunk at least two tiles wide
+int vfd_chunk_count(int Vd, int Vt)
+{
+	int dev = 0, sms = 1;
+	SA_CHECK(cudaGetDevice(&dev));
+	SA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	const int rowMax = std::max(Vd, Vt), colMin = std::min(Vd, Vt);
+	const int perSm = std::max(1, tuning().vfdCtasPerSm);
+	const int rowCtas = std::max(1, grid_for(rowMax, kVfdBlock));
+	int C = std::max(1, (perSm * sms + rowCtas - 1) / rowCtas);
+	C = std::min(C, std::max(1, colMin / (2 * kVfdTile)));
+	return std::min(C, 32);
+}
+
+// the target-target rows (vfd_TT) of a Vd x Vt objective into cache.rows, launched on stream s: the same
+// launches as inside varifold(), so the objective gives the same value whether it finds these rows in the
+// cache or computes them itself.  part: vfd_chunk_count(Vd, Vt) * Vt doubles of scratch.
+template <int D>
+void varifold_target_rows(const Model &md, int Vd, const double *tgtCen, const double *tgtDir, const double *tgtVol,
+                          int Vt, int precision, double *part, VfdTargetCache &cache, cudaStream_t s)
+{
+	if (!cache.rows || cache.capacity < Vt || Vt <= 0) return;     // not cached: the objective computes them
+	const int C = vfd_chunk_count(Vd, Vt);
+	VfdSet Ts{tgtCen, tgtDir, tgtVol, Vt}, E0{nullptr, nullptr, nullptr, 0};
+	dim3 grid(grid_for(Vt, kVfdBlock), C);
+	const int ck = md.cenKnl, dk = md.dirKnl;
+	const double cw = md.cenWidth, dw = md.dirWidth;
+	if (precision == SA_PREC_MIXED)
+		k_vfd_rows<D, float, false><<<grid, kVfdBlock, 0, s>>>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, part, nullptr,
+		                                                         nullptr, 1);
+	else
+		k_vfd_rows<D, double, false><<<grid, kVfdBlock, 0, s>>>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, part, nullptr,
+		                                                          nullptr, 1);
+	k_vfd_chunks<D><<<grid_for(Vt), kBlock, 0, s>>>(Vt, C, part, cache.rows, 0, nullptr, nullptr, nullptr, nullptr);
+	SA_CHECK(cudaGetLastError());
+	cache.valid = true; cache.Vt = Vt; cache.precision = precision;
+	cache.ck = ck; cache.dk = dk; cache.cw = cw; cache.dw = dw;
+}
+
+template void varifold_target_rows<2>(const Model &, int, const double *, const double *, const double *, int, int,
+                                      double *, VfdTargetCache &, cudaStream_t);
+template void varifold_target_rows<3>(const Model &, int, const double *, const double *, const double *, int, int,
+                                      double *, VfdTargetCache &, cudaStream_t);
+
 template <int D>
 double varifold(const Mesh &m, const Model &md, const double *x, const double *tgtCen, const double *tgtDir,
                 const double *tgtVol, int Vt, double *grad, cudaStream_t s, int precision, int *err,
@@ -380,16 +427,9 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 	int Vd = m.Vd;
 	*err = SA_OK;
 	if (grad && !m.vfdIfo) { *err = SA_ERR_ARG; return 0.0; }
-	// column chunks: enough CTAs to fill the GPU (the pair sums are latency bound at one CTA per SM)
-	int dev = 0, sms = 1;
-	SA_CHECK(cudaGetDevice(&dev));
-	SA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-	const int blk = 128;
-	const int rowMax = std::max(Vd, Vt), colMin = std::min(Vd, Vt);
-	const int perSm = std::max(1, tuning().vfdCtasPerSm);
-	int C = std::max(1, (perSm * sms + grid_for(rowMax, blk) - 1) / std::max(1, grid_for(rowMax, blk)));
-	C = std::min(C, std::max(1, colMin / (2 * kVfdTile)));
-	C = std::min(C, 32);
+	const int blk = kVfdBlock;
+	const int rowMax = std::max(Vd, Vt);
+	const int C = vfd_chunk_count(Vd, Vt);
 	double *buf = nullptr;
 	const size_t rows = (size_t) (Vd + Vt);
 	size_t need = (size_t) Vd * (2 * D + 1) + rows + kSum + 1 + (grad ? (size_t) 2 * D * Vd : 0) +
