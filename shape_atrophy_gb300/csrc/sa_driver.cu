@@ -797,7 +797,7 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 		if (Vd >= Vt) {
 			// the objective's target-target rows depend on the target only: the side stream computes them
 			// while the host validates and lays out the mesh (the objective finds them in the cache)
-			double *part = P.alloc<double>((size_t) vfd_chunk_count(Vd, Vt) * Vt);
+			double *part = P.alloc<double>(varifold_target_rows_scratch(D, Vd, Vt, md.precision));
 			SA_CHECK(cudaEventRecord(ctx->sideIn, s));
 			SA_CHECK(cudaStreamWaitEvent(ctx->side, ctx->sideIn, 0));
 			join.on = true;

@@ -440,7 +440,8 @@ template <int D> double varifold(const Mesh &m, const Model &md, const double *x
 // column chunks of the varifold pair sums of a Vd x Vt objective
 int vfd_chunk_count(int Vd, int Vt);
 // the target-target rows of a Vd x Vt objective into cache.rows on stream s (the objective's own launches);
-// part: vfd_chunk_count(Vd, Vt) * Vt doubles
+// part: varifold_target_rows_scratch(D, Vd, Vt, precision) doubles
+size_t varifold_target_rows_scratch(int D, int Vd, int Vt, int precision);
 template <int D> void varifold_target_rows(const Model &md, int Vd, const double *tgtCen, const double *tgtDir,
                                            const double *tgtVol, int Vt, int precision, double *part,
                                            VfdTargetCache &cache, cudaStream_t s);

@@ -23,6 +23,7 @@
 namespace sa {
 
 constexpr int kVfdTile = 128;
+constexpr float kNearField = 0.01f;     // mixed-precision objective: K_c K_d above this is evaluated in FP64
 
 // 2^(j/64), j = 0 .. 63, each rounded to the nearest double (computed with 60-digit decimal arithmetic)
 __constant__ double c_exp2_64[64] = {
@@ -177,18 +178,30 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
                            int symA = 0)
 {
 	constexpr bool kSplit = sizeof(T) < sizeof(double);     // two-float centres in FP32
+	// mixed-precision objective: pairs whose FP32 kernel product K_c K_d exceeds kNearField (the near field,
+	// about 6 % of the pairs on the shell workload: Matern r < ~6) are evaluated again in FP64 and summed in
+	// FP64; only the far field keeps FP32 terms.  The near field carries most of the objective and of the
+	// FP32 rounding (the column volumes' FP32 rounding in particular is systematic and survives the
+	// cancellation DD - 2 DT + TT).
+	constexpr bool kNear = kSplit && !G;
+	constexpr int kN = kNear ? 1 : 0;
 	__shared__ T sc[kVfdTile * D], su[kVfdTile * D], sv[kVfdTile], sl[kSplit ? kVfdTile * D : 1];
-	__shared__ double sExp[kSplit ? 1 : 64];
-	if (!kSplit && threadIdx.x < 64) sExp[threadIdx.x] = c_exp2_64[threadIdx.x];   // read after the tile barrier
+	__shared__ double sc64[kN * kVfdTile * D + 1], su64[kN * kVfdTile * D + 1], sv64[kN * kVfdTile + 1];
+	__shared__ double sExp[(kSplit && !kNear) ? 1 : 64];
+	if ((!kSplit || kNear) && threadIdx.x < 64) sExp[threadIdx.x] = c_exp2_64[threadIdx.x];   // read after the tile barrier
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	bool act = i < R.n;
 	T ci[D], cl[D], ui[D], vi = 0;
+	double ci64[D], ui64[D];
 	for (int d = 0; d < D; ++d) {
 		double c = act ? R.cen[d * (long) R.n + i] : 0.0;
 		ci[d] = (T) c;
 		cl[d] = kSplit ? (T) (c - (double) ci[d]) : (T) 0;
-		ui[d] = act ? (T) R.dir[d * (long) R.n + i] : (T) 0;
+		ci64[d] = c;
+		ui64[d] = act ? R.dir[d * (long) R.n + i] : 0.0;
+		ui[d] = (T) ui64[d];
 	}
+	const double ciw64 = 1.0 / cw, ciw2_64 = 1.0 / (cw * cw), diw2_64 = 1.0 / (dw * dw);
 	if (act) vi = (T) R.vol[i];
 	const T nLen = (D == 2 ? vi : (T) 2.0 * vi), half = (D == 2 ? (T) 1.0 : (T) 0.5);
 	double acc = 0.0, gc[D], gt[D];
@@ -199,7 +212,8 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 	if (G) { dc += (long) cy * D * R.n; dt += (long) cy * D * R.n; }
 	for (int set = 0; set < 2; ++set) {
 		const VfdSet &S = set == 0 ? A : Bs;
-		const T coef = (T) (set == 0 ? cA : cB), cv = coef * vi;
+		// row factor coef * vol_i in FP64 from the FP64 volume (applied to each tile's FP32 or FP64 sum)
+		const double cv = (set == 0 ? cA : cB) * (act ? R.vol[i] : 0.0);
 		const bool sym = set == 0 && symA;
 		const int lo = sym ? (int) (blockIdx.x * blockDim.x) : 0;   // columns below the CTA's rows: none
 		const int span = S.n > lo ? S.n - lo : 0;
@@ -212,12 +226,15 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 			__syncthreads();
 			for (int t = threadIdx.x; t < nt; t += blockDim.x) {
 				for (int d = 0; d < D; ++d) {
-					double c = S.cen[d * (long) S.n + j0 + t];
+					double c = S.cen[d * (long) S.n + j0 + t], u = S.dir[d * (long) S.n + j0 + t];
 					sc[t * D + d] = (T) c;
 					if (kSplit) sl[t * D + d] = (T) (c - (double) sc[t * D + d]);
-					su[t * D + d] = (T) S.dir[d * (long) S.n + j0 + t];
+					su[t * D + d] = (T) u;
+					if (kNear) { sc64[t * D + d] = c; su64[t * D + d] = u; }
 				}
-				sv[t] = (T) S.vol[j0 + t];
+				const double v = S.vol[j0 + t];
+				sv[t] = (T) v;
+				if (kNear) sv64[t] = v;
 			}
 			__syncthreads();
 			if (!act) continue;
@@ -225,6 +242,7 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 			// symmetric half, the weights (2 off the diagonal, 1 on it: 2 tile - diagonal term) are applied
 			// once per tile
 			T tile = 0, comp = 0, diag = 0, tgc[D], tgt[D];
+			double nearSum = 0.0, diag64 = 0.0;                       // FP64 near-field terms (kNear)
 			for (int d = 0; d < D; ++d) { tgc[d] = 0; tgt[d] = 0; }
 			for (int jj = 0; jj < nt; ++jj) {
 				bool onDiag = false;
@@ -247,12 +265,24 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 				T kd = dir_knl<T, G>(dk, diw2, ang, d1d, sExp);
 				T vj = sv[jj];
 				const T kv = kd * vj;
-				if (onDiag) diag = kc * kv;
-				if (kSplit) {                  // Kahan: the FP32 tile sum keeps its lost low bits
+				if (kNear && kc * kd > (T) kNearField) {
+					double e2 = 0.0, a64 = 0.0, u1 = 0.0, u2 = 0.0;
+					for (int d = 0; d < D; ++d) {
+						const double df = ci64[d] - sc64[jj * D + d];
+						e2 = fma(df, df, e2);
+						a64 = fma(ui64[d], su64[jj * D + d], a64);
+					}
+					const double t64 = cen_knl<double, false>(ck, ciw64, ciw2_64, e2, u1, sExp) *
+					                   (dir_knl<double, false>(dk, diw2_64, a64, u2, sExp) * sv64[jj]);
+					nearSum += t64;
+					if (onDiag) diag64 = t64;
+				} else if (kSplit) {           // Kahan: the FP32 tile sum keeps its lost low bits
+					if (onDiag) diag = kc * kv;
 					T y = kc * kv - comp, t = tile + y;
 					comp = (t - tile) - y;
 					tile = t;
 				} else {
+					if (onDiag) diag = kc * kv;
 					tile = fma(kc, kv, tile);
 				}
 				if (G) {
@@ -265,7 +295,9 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 					}
 				}
 			}
-			acc += (double) cv * (sym ? 2.0 * (double) tile - (double) diag : (double) tile);
+			// Kahan: the FP32 sum with its lost low part, plus the FP64 near-field terms
+			const double tsum = ((double) tile - (double) comp) + nearSum;
+			acc += cv * (sym ? 2.0 * tsum - ((double) diag + diag64) : tsum);
 			if (G) for (int d = 0; d < D; ++d) { gc[d] += (double) tgc[d]; gt[d] += (double) tgt[d]; }
 		}
 	}
@@ -273,6 +305,151 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 	out[i] = acc;
 	if (G)
 		for (int d = 0; d < D; ++d) { dc[d * (long) R.n + i] = gc[d]; dt[d * (long) R.n + i] = gt[d]; }
+}
+
+// ---------------------------------------------------------------------------
+// Spatial order of a set of boundary elements (mixed-precision objective).
+// The FP64 near-field branch of the FP32 pair sums is taken by a warp when
+// any of its 32 rows is near the column; in mesh order a warp's rows lie all
+// over the surface, so nearly every warp would take it.  Sorted by the Morton
+// code of their centres (10 bits per axis in 3D, 15 in 2D, inside the set's
+// bounding box; ties broken by index, so the 64-bit keys are distinct and the
+// order is deterministic) a warp's rows are neighbours.  The objective is a
+// double sum over the sets, so its value does not depend on the order.
+// ---------------------------------------------------------------------------
+constexpr int kSortBlock = 2048;        // keys per CTA in the shared-memory bitonic stages
+
+template <int D>
+__global__ void k_set_bbox(int n, const double *__restrict__ cen, double *__restrict__ box)
+{
+	__shared__ double lo[256][D], hi[256][D];
+	const int t = threadIdx.x;
+	for (int d = 0; d < D; ++d) { lo[t][d] = 1e300; hi[t][d] = -1e300; }
+	for (int e = t; e < n; e += blockDim.x)
+		for (int d = 0; d < D; ++d) {
+			const double c = cen[d * (long) n + e];
+			lo[t][d] = fmin(lo[t][d], c);
+			hi[t][d] = fmax(hi[t][d], c);
+		}
+	__syncthreads();
+	for (int h = 128; h > 0; h >>= 1) {
+		if (t < h)
+			for (int d = 0; d < D; ++d) {
+				lo[t][d] = fmin(lo[t][d], lo[t + h][d]);
+				hi[t][d] = fmax(hi[t][d], hi[t + h][d]);
+			}
+		__syncthreads();
+	}
+	if (t < D) { box[t] = lo[0][t]; box[D + t] = hi[0][t]; }
+}
+
+__device__ __forceinline__ unsigned spread_bits(unsigned v, int D)
+{
+	unsigned r = 0;
+	const int bits = D == 3 ? 10 : 15;
+	for (int b = 0; b < bits; ++b) r |= ((v >> b) & 1u) << (b * D);
+	return r;
+}
+
+template <int D>
+__global__ void k_set_keys(int n, int npad, const double *__restrict__ cen, const double *__restrict__ box,
+                           unsigned long long *__restrict__ keys)
+{
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= npad) return;
+	if (k >= n) { keys[k] = ~0ULL; return; }                 // padding sorts last
+	const unsigned cells = D == 3 ? 1024u : 32768u;
+	unsigned code = 0;
+	for (int d = 0; d < D; ++d) {
+		const double ext = box[D + d] - box[d];
+		const double f = ext > 0.0 ? (cen[d * (long) n + k] - box[d]) / ext : 0.0;
+		unsigned q = (unsigned) fmin(fmax(f * (double) cells, 0.0), (double) (cells - 1));
+		code |= spread_bits(q, D) << d;
+	}
+	keys[k] = ((unsigned long long) code << 32) | (unsigned) k;
+}
+
+__device__ __forceinline__ void cmp_swap(unsigned long long &a, unsigned long long &b, bool up)
+{
+	if ((a > b) == up) { const unsigned long long t = a; a = b; b = t; }
+}
+
+// bitonic stages with j < kSortBlock inside one CTA's 2048 keys: all sizes k <= kSortBlock when k == 0,
+// else the stages j = kSortBlock/2 .. 1 of size k
+__global__ void __launch_bounds__(kSortBlock / 2) k_bitonic_local(unsigned long long *__restrict__ keys, int k)
+{
+	__shared__ unsigned long long s[kSortBlock];
+	const int base = blockIdx.x * kSortBlock, t = threadIdx.x;
+	s[t] = keys[base + t];
+	s[t + kSortBlock / 2] = keys[base + t + kSortBlock / 2];
+	__syncthreads();
+	const int kLo = k == 0 ? 2 : k, kHi = k == 0 ? kSortBlock : k;
+	for (int kk = kLo; kk <= kHi; kk <<= 1)
+		for (int j = min(kk, kSortBlock) >> 1; j > 0; j >>= 1) {
+			// thread t handles the pair (i, i + j) with i the t-th index whose bit j is clear
+			const int i = 2 * t - (t & (j - 1));
+			const bool up = ((base + i) & kk) == 0;
+			cmp_swap(s[i], s[i + j], up);
+			__syncthreads();
+		}
+	keys[base + t] = s[t];
+	keys[base + t + kSortBlock / 2] = s[t + kSortBlock / 2];
+}
+
+// one bitonic stage (size k, distance j >= kSortBlock) over all npad keys
+__global__ void k_bitonic_global(unsigned long long *__restrict__ keys, int npad, int j, int k)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= npad) return;
+	const int l = i ^ j;
+	if (l <= i) return;
+	unsigned long long a = keys[i], b = keys[l];
+	const bool up = (i & k) == 0;
+	if ((a > b) == up) { keys[i] = b; keys[l] = a; }
+}
+
+template <int D>
+__global__ void k_set_gather(int n, const unsigned long long *__restrict__ keys, VfdSet S, double *__restrict__ cen,
+                             double *__restrict__ dir, double *__restrict__ vol)
+{
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= n) return;
+	const int e = (int) (keys[k] & 0xffffffffu);
+	for (int d = 0; d < D; ++d) {
+		cen[d * (long) n + k] = S.cen[d * (long) n + e];
+		dir[d * (long) n + k] = S.dir[d * (long) n + e];
+	}
+	vol[k] = S.vol[e];
+}
+
+static int sort_pad(int n)
+{
+	int p = kSortBlock;
+	while (p < n) p <<= 1;
+	return p;
+}
+
+// doubles of scratch spatial_order needs for a set of n elements
+static size_t spatial_order_doubles(int D, int n) { return (size_t) (2 * D + 1) * n + sort_pad(n) + 2 * D + 8; }
+
+// the set S in spatial order, written into scr (spatial_order_doubles(D, S.n) doubles)
+template <int D>
+static VfdSet spatial_order(const VfdSet &S, double *scr, cudaStream_t s)
+{
+	if (S.n <= 0) return S;
+	const int n = S.n, npad = sort_pad(n);
+	double *cen = scr, *dir = cen + (long) D * n, *vol = dir + (long) D * n, *box = vol + n;
+	unsigned long long *keys = reinterpret_cast<unsigned long long *>(box + 2 * D + 8);
+	k_set_bbox<D><<<1, 256, 0, s>>>(n, S.cen, box);
+	k_set_keys<D><<<(npad + 255) / 256, 256, 0, s>>>(n, npad, S.cen, box, keys);
+	k_bitonic_local<<<npad / kSortBlock, kSortBlock / 2, 0, s>>>(keys, 0);
+	for (int k = 2 * kSortBlock; k <= npad; k <<= 1) {
+		for (int j = k >> 1; j >= kSortBlock; j >>= 1)
+			k_bitonic_global<<<(npad + 255) / 256, 256, 0, s>>>(keys, npad, j, k);
+		k_bitonic_local<<<npad / kSortBlock, kSortBlock / 2, 0, s>>>(keys, k);
+	}
+	k_set_gather<D><<<grid_for(n), kBlock, 0, s>>>(n, keys, S, cen, dir, vol);
+	return VfdSet{cen, dir, vol, n};
 }
 
 // row sums of the column chunks of k_vfd_rows, chunk order fixed (K values per row: 1, or 1 + 2D with the
@@ -391,7 +568,12 @@ int vfd_chunk_count(int Vd, int Vt)
 
 // the target-target rows (vfd_TT) of a Vd x Vt objective into cache.rows, launched on stream s: the same
 // launches as inside varifold(), so the objective gives the same value whether it finds these rows in the
-// cache or computes them itself.  part: vfd_chunk_count(Vd, Vt) * Vt doubles of scratch.
+// cache or computes them itself.  part: varifold_target_rows_scratch(D, Vd, Vt, precision) doubles.
+size_t varifold_target_rows_scratch(int D, int Vd, int Vt, int precision)
+{
+	return (size_t) vfd_chunk_count(Vd, Vt) * Vt + (precision == SA_PREC_MIXED ? spatial_order_doubles(D, Vt) : 0);
+}
+
 template <int D>
 void varifold_target_rows(const Model &md, int Vd, const double *tgtCen, const double *tgtDir, const double *tgtVol,
                           int Vt, int precision, double *part, VfdTargetCache &cache, cudaStream_t s)
@@ -399,6 +581,7 @@ void varifold_target_rows(const Model &md, int Vd, const double *tgtCen, const d
 	if (!cache.rows || cache.capacity < Vt || Vt <= 0) return;     // not cached: the objective computes them
 	const int C = vfd_chunk_count(Vd, Vt);
 	VfdSet Ts{tgtCen, tgtDir, tgtVol, Vt}, E0{nullptr, nullptr, nullptr, 0};
+	if (precision == SA_PREC_MIXED) Ts = spatial_order<D>(Ts, part + (size_t) C * Vt, s);
 	dim3 grid(grid_for(Vt, kVfdBlock), C);
 	const int ck = md.cenKnl, dk = md.dirKnl;
 	const double cw = md.cenWidth, dw = md.dirWidth;
@@ -432,15 +615,23 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 	const int C = vfd_chunk_count(Vd, Vt);
 	double *buf = nullptr;
 	const size_t rows = (size_t) (Vd + Vt);
-	size_t need = (size_t) Vd * (2 * D + 1) + rows + kSum + 1 + (grad ? (size_t) 2 * D * Vd : 0) +
-	              (size_t) C * rowMax * (1 + (grad ? 2 * D : 0));
+	// mixed-precision objective: both sets in spatial order (coherent near-field branch, see spatial_order)
+	const bool ordered = precision == SA_PREC_MIXED && !grad;
+	const size_t partLen = (size_t) C * rowMax * (1 + (grad ? 2 * D : 0));
+	size_t need = (size_t) Vd * (2 * D + 1) + rows + kSum + 1 + (grad ? (size_t) 2 * D * Vd : 0) + partLen +
+	              (ordered ? spatial_order_doubles(D, Vd) + spatial_order_doubles(D, Vt) : 0);
 	SA_CHECK(cudaMallocAsync(&buf, sizeof(double) * need, s));
 	double *cen = buf, *dir = cen + (long) D * Vd, *vol = dir + (long) D * Vd, *vfd = vol + Vd;
 	double *scr = vfd + Vd + Vt, *dc = scr + kSum + 1, *dt = dc + (long) D * Vd;
 	double *part = grad ? dt + (long) D * Vd : dc;
 	double *pdc = part + (long) C * rowMax, *pdt = pdc + (long) C * D * rowMax;
+	double *ordD = part + partLen, *ordT = ordD + (ordered ? spatial_order_doubles(D, Vd) : 0);
 	k_vfd_elems<D><<<grid_for(Vd), kBlock, 0, s>>>(m.N, Vd, m.vfdVtx, x, cen, dir, vol);
 	VfdSet Ds{cen, dir, vol, Vd}, Ts{tgtCen, tgtDir, tgtVol, Vt}, E0{nullptr, nullptr, nullptr, 0};
+	// row sets: the deformed set (spatially ordered in the mixed objective); the target set as rows (TT) is
+	// ordered when it is needed
+	const VfdSet Dr = ordered ? spatial_order<D>(Ds, ordD, s) : Ds;
+	auto target_rows = [&]() { return ordered ? spatial_order<D>(Ts, ordT, s) : Ts; };
 	int ck = md.cenKnl, dk = md.dirKnl;
 	// rows_of: per-row sums of R against A (coefficient cA) and B (cB); the self term R = A uses the
 	// symmetric half when no gradient rows are wanted
@@ -459,7 +650,7 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 		k_vfd_chunks<D><<<grid_for(R.n), kBlock, 0, s>>>(R.n, C, part, out, g, pdc, pdt, dc, dt);
 	};
 	if (grad || Vd >= Vt) {
-		rows_of(Ds, Ds, 1.0, Ts, -2.0, vfd, grad ? 1 : 0);      // vfd_DD_DT / dqVfd_DD_DT
+		rows_of(Dr, Dr, 1.0, Ts, -2.0, vfd, grad ? 1 : 0);      // vfd_DD_DT / dqVfd_DD_DT
 		// vfd_TT depends on the target only: a cache (same target, same kernels, same precision) keeps
 		// its rows between calls
 		bool hit = cache && cache->rows && cache->valid && cache->Vt == Vt && cache->precision == precision &&
@@ -467,7 +658,8 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 		if (hit) {
 			SA_CHECK(cudaMemcpyAsync(vfd + Vd, cache->rows, sizeof(double) * Vt, cudaMemcpyDeviceToDevice, s));
 		} else {
-			rows_of(Ts, Ts, 1.0, E0, 0.0, vfd + Vd, 0);
+			const VfdSet Tr = target_rows();
+			rows_of(Tr, Tr, 1.0, E0, 0.0, vfd + Vd, 0);
 			if (cache && cache->rows && cache->capacity >= Vt) {
 				SA_CHECK(cudaMemcpyAsync(cache->rows, vfd + Vd, sizeof(double) * Vt, cudaMemcpyDeviceToDevice, s));
 				cache->valid = true; cache->Vt = Vt; cache->precision = precision;
@@ -475,8 +667,9 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 			}
 		}
 	} else {
-		rows_of(Ts, Ts, 1.0, Ds, -2.0, vfd, 0);                 // vfd_TT_TD
-		rows_of(Ds, Ds, 1.0, E0, 0.0, vfd + Vt, 0);             // vfd_DD
+		const VfdSet Tr = target_rows();
+		rows_of(Tr, Tr, 1.0, Dr, -2.0, vfd, 0);                 // vfd_TT_TD
+		rows_of(Dr, Dr, 1.0, E0, 0.0, vfd + Vt, 0);             // vfd_DD
 	}
 	SA_CHECK(cudaGetLastError());
 	double obj = device_sum(vfd, Vd + Vt, scr, s);
