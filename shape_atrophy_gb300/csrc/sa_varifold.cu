@@ -175,7 +175,7 @@ struct VfdSet { const double *cen, *dir, *vol; int n; };
 template <int D, typename T, bool G>
 __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, int ck, double cw, int dk,
                            double dw, double *__restrict__ out, double *__restrict__ dc, double *__restrict__ dt,
-                           int symA = 0)
+                           int symA = 0, int C = 0, int *__restrict__ queue = nullptr)
 {
 	constexpr bool kSplit = sizeof(T) < sizeof(double);     // two-float centres in FP32
 	// mixed-precision objective: pairs whose FP32 kernel product K_c K_d exceeds kNearField (the near field,
@@ -189,7 +189,28 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 	__shared__ double sc64[kN * kVfdTile * D + 1], su64[kN * kVfdTile * D + 1], sv64[kN * kVfdTile + 1];
 	__shared__ double sExp[(kSplit && !kNear) ? 1 : 64];
 	if ((!kSplit || kNear) && threadIdx.x < 64) sExp[threadIdx.x] = c_exp2_64[threadIdx.x];   // read after the tile barrier
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	// work items (row block bx, column chunk cy), item = bx C + cy: with a queue, a persistent grid takes items
+	// in that order (largest first: a row block's span shrinks with bx in the symmetric half), each item writing
+	// its own partial-sum slot, so results do not depend on which CTA ran it; without a queue, the 2D grid
+	// (bx, cy) = (blockIdx.x, blockIdx.y) runs one item per CTA
+	if (!queue) C = gridDim.y;
+	const int rowBlocks = (R.n + blockDim.x - 1) / blockDim.x, nItems = rowBlocks * C;
+	__shared__ int sItem;
+	double *const out0 = out, *const dc0 = dc, *const dt0 = dt;
+	for (int pass = 0;; ++pass) {
+	int item;
+	if (queue) {
+		__syncthreads();                      // the previous item's tile reads are done
+		if (threadIdx.x == 0) sItem = atomicAdd(queue, 1);
+		__syncthreads();
+		item = sItem;
+	} else {
+		if (pass > 0) break;
+		item = blockIdx.x * C + blockIdx.y;
+	}
+	if (item >= nItems) break;
+	const int bx = item / C, cy = item % C;
+	int i = bx * blockDim.x + threadIdx.x;
 	bool act = i < R.n;
 	T ci[D], cl[D], ui[D], vi = 0;
 	double ci64[D], ui64[D];
@@ -207,15 +228,14 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 	double acc = 0.0, gc[D], gt[D];
 	for (int d = 0; d < D; ++d) { gc[d] = 0.0; gt[d] = 0.0; }
 	const T ciw = (T) (1.0 / cw), ciw2 = (T) (1.0 / (cw * cw)), diw2 = (T) (1.0 / (dw * dw));
-	const int C = gridDim.y, cy = blockIdx.y;
-	out += (long) cy * R.n;
-	if (G) { dc += (long) cy * D * R.n; dt += (long) cy * D * R.n; }
+	out = out0 + (long) cy * R.n;
+	if (G) { dc = dc0 + (long) cy * D * R.n; dt = dt0 + (long) cy * D * R.n; }
 	for (int set = 0; set < 2; ++set) {
 		const VfdSet &S = set == 0 ? A : Bs;
 		// row factor coef * vol_i in FP64 from the FP64 volume (applied to each tile's FP32 or FP64 sum)
 		const double cv = (set == 0 ? cA : cB) * (act ? R.vol[i] : 0.0);
 		const bool sym = set == 0 && symA;
-		const int lo = sym ? (int) (blockIdx.x * blockDim.x) : 0;   // columns below the CTA's rows: none
+		const int lo = sym ? (int) (bx * blockDim.x) : 0;           // columns below the item's rows: none
 		const int span = S.n > lo ? S.n - lo : 0;
 		const int jBeg = lo + (int) ((long) span * cy / C), jEnd = lo + (int) ((long) span * (cy + 1) / C);
 		// gradient weights of dqVfd_DD_DT: +2 for the deformed-deformed term (both ends move), -2 for
@@ -301,10 +321,12 @@ __global__ void k_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet Bs, double cB, 
 			if (G) for (int d = 0; d < D; ++d) { gc[d] += (double) tgc[d]; gt[d] += (double) tgt[d]; }
 		}
 	}
-	if (!act) return;
-	out[i] = acc;
-	if (G)
-		for (int d = 0; d < D; ++d) { dc[d * (long) R.n + i] = gc[d]; dt[d * (long) R.n + i] = gt[d]; }
+	if (act) {
+		out[i] = acc;
+		if (G)
+			for (int d = 0; d < D; ++d) { dc[d * (long) R.n + i] = gc[d]; dt[d * (long) R.n + i] = gt[d]; }
+	}
+	}   // items
 }
 
 // ---------------------------------------------------------------------------
@@ -551,6 +573,29 @@ double device_sum(const double *v, long n, double *scratch, cudaStream_t s)
 
 constexpr int kVfdBlock = 128;
 
+// persistent grid of k_vfd_rows: as many CTAs as fit on the GPU at once, at most one per work item
+template <int D, typename T, bool G>
+static int vfd_grid(int items)
+{
+	int dev = 0, sms = 1, per = 1;
+	SA_CHECK(cudaGetDevice(&dev));
+	SA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	SA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vfd_rows<D, T, G>, kVfdBlock, 0));
+	return std::max(1, std::min(items, std::max(1, per) * sms));
+}
+
+// one k_vfd_rows launch over all (row block, column chunk) items of R, taken from the queue counter (zeroed
+// here on the stream)
+template <int D, typename T, bool G>
+static void launch_vfd_rows(VfdSet R, VfdSet A, double cA, VfdSet B, double cB, int ck, double cw, int dk, double dw,
+                            double *out, double *dc, double *dt, int sym, int C, int *queue, cudaStream_t s)
+{
+	const int items = grid_for(R.n, kVfdBlock) * C;
+	SA_CHECK(cudaMemsetAsync(queue, 0, sizeof(int), s));
+	k_vfd_rows<D, T, G><<<vfd_grid<D, T, G>(items), kVfdBlock, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, out, dc, dt,
+	                                                                     sym, C, queue);
+}
+
 // column chunks of the pair sums of a Vd x Vt objective: enough CTAs to fill the GPU (the pair sums are latency
 // bound at one CTA per SM), each chunk at least two tiles wide
 int vfd_chunk_count(int Vd, int Vt)
@@ -571,7 +616,8 @@ int vfd_chunk_count(int Vd, int Vt)
 // cache or computes them itself.  part: varifold_target_rows_scratch(D, Vd, Vt, precision) doubles.
 size_t varifold_target_rows_scratch(int D, int Vd, int Vt, int precision)
 {
-	return (size_t) vfd_chunk_count(Vd, Vt) * Vt + (precision == SA_PREC_MIXED ? spatial_order_doubles(D, Vt) : 0);
+	return (size_t) vfd_chunk_count(Vd, Vt) * Vt + (precision == SA_PREC_MIXED ? spatial_order_doubles(D, Vt) : 0) +
+	       1;                                                      // + the work-item counter
 }
 
 template <int D>
@@ -581,16 +627,14 @@ void varifold_target_rows(const Model &md, int Vd, const double *tgtCen, const d
 	if (!cache.rows || cache.capacity < Vt || Vt <= 0) return;     // not cached: the objective computes them
 	const int C = vfd_chunk_count(Vd, Vt);
 	VfdSet Ts{tgtCen, tgtDir, tgtVol, Vt}, E0{nullptr, nullptr, nullptr, 0};
+	int *queue = reinterpret_cast<int *>(part + varifold_target_rows_scratch(D, Vd, Vt, precision) - 1);
 	if (precision == SA_PREC_MIXED) Ts = spatial_order<D>(Ts, part + (size_t) C * Vt, s);
-	dim3 grid(grid_for(Vt, kVfdBlock), C);
 	const int ck = md.cenKnl, dk = md.dirKnl;
 	const double cw = md.cenWidth, dw = md.dirWidth;
 	if (precision == SA_PREC_MIXED)
-		k_vfd_rows<D, float, false><<<grid, kVfdBlock, 0, s>>>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, part, nullptr,
-		                                                         nullptr, 1);
+		launch_vfd_rows<D, float, false>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, part, nullptr, nullptr, 1, C, queue, s);
 	else
-		k_vfd_rows<D, double, false><<<grid, kVfdBlock, 0, s>>>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, part, nullptr,
-		                                                          nullptr, 1);
+		launch_vfd_rows<D, double, false>(Ts, Ts, 1.0, E0, 0.0, ck, cw, dk, dw, part, nullptr, nullptr, 1, C, queue, s);
 	k_vfd_chunks<D><<<grid_for(Vt), kBlock, 0, s>>>(Vt, C, part, cache.rows, 0, nullptr, nullptr, nullptr, nullptr);
 	SA_CHECK(cudaGetLastError());
 	cache.valid = true; cache.Vt = Vt; cache.precision = precision;
@@ -610,7 +654,6 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 	int Vd = m.Vd;
 	*err = SA_OK;
 	if (grad && !m.vfdIfo) { *err = SA_ERR_ARG; return 0.0; }
-	const int blk = kVfdBlock;
 	const int rowMax = std::max(Vd, Vt);
 	const int C = vfd_chunk_count(Vd, Vt);
 	double *buf = nullptr;
@@ -619,13 +662,14 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 	const bool ordered = precision == SA_PREC_MIXED && !grad;
 	const size_t partLen = (size_t) C * rowMax * (1 + (grad ? 2 * D : 0));
 	size_t need = (size_t) Vd * (2 * D + 1) + rows + kSum + 1 + (grad ? (size_t) 2 * D * Vd : 0) + partLen +
-	              (ordered ? spatial_order_doubles(D, Vd) + spatial_order_doubles(D, Vt) : 0);
+	              (ordered ? spatial_order_doubles(D, Vd) + spatial_order_doubles(D, Vt) : 0) + 1;
 	SA_CHECK(cudaMallocAsync(&buf, sizeof(double) * need, s));
 	double *cen = buf, *dir = cen + (long) D * Vd, *vol = dir + (long) D * Vd, *vfd = vol + Vd;
 	double *scr = vfd + Vd + Vt, *dc = scr + kSum + 1, *dt = dc + (long) D * Vd;
 	double *part = grad ? dt + (long) D * Vd : dc;
 	double *pdc = part + (long) C * rowMax, *pdt = pdc + (long) C * D * rowMax;
 	double *ordD = part + partLen, *ordT = ordD + (ordered ? spatial_order_doubles(D, Vd) : 0);
+	int *queue = reinterpret_cast<int *>(buf + need - 1);          // work-item counter of the pair-sum launches
 	k_vfd_elems<D><<<grid_for(Vd), kBlock, 0, s>>>(m.N, Vd, m.vfdVtx, x, cen, dir, vol);
 	VfdSet Ds{cen, dir, vol, Vd}, Ts{tgtCen, tgtDir, tgtVol, Vt}, E0{nullptr, nullptr, nullptr, 0};
 	// row sets: the deformed set (spatially ordered in the mixed objective); the target set as rows (TT) is
@@ -637,15 +681,14 @@ double varifold(const Mesh &m, const Model &md, const double *x, const double *t
 	// symmetric half when no gradient rows are wanted
 	auto rows_of = [&](VfdSet R, VfdSet A, double cA, VfdSet B, double cB, double *out, int g) {
 		if (R.n == 0) return;
-		dim3 grid(grid_for(R.n, blk), C);
 		const int sym = g ? 0 : 1;
 		const double cw = md.cenWidth, dw = md.dirWidth;
 		if (precision == SA_PREC_MIXED) {
-			if (g) k_vfd_rows<D, float, true><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym);
-			else k_vfd_rows<D, float, false><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym);
+			if (g) launch_vfd_rows<D, float, true>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym, C, queue, s);
+			else launch_vfd_rows<D, float, false>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym, C, queue, s);
 		} else {
-			if (g) k_vfd_rows<D, double, true><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym);
-			else k_vfd_rows<D, double, false><<<grid, blk, 0, s>>>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym);
+			if (g) launch_vfd_rows<D, double, true>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym, C, queue, s);
+			else launch_vfd_rows<D, double, false>(R, A, cA, B, cB, ck, cw, dk, dw, part, pdc, pdt, sym, C, queue, s);
 		}
 		k_vfd_chunks<D><<<grid_for(R.n), kBlock, 0, s>>>(R.n, C, part, out, g, pdc, pdt, dc, dt);
 	};
