@@ -384,6 +384,9 @@ def main():
     e2e = None
     if not args.no_e2e and rank == 0:
         spec_e = spec_for(args, K)
+        # one untimed call of the same entry point first (a single step): loads the objective's kernels, which
+        # the timed step leg above does not launch, so the timed call measures a user's repeated calls
+        api.forward(dict(spec_e, timeNum=2), trajectory=True, objective=True, precision=args.precision, device=local)
         t0 = time.perf_counter()
         r = api.forward(spec_e, trajectory=True, objective=True, precision=args.precision, device=local)
         wall = time.perf_counter() - t0
@@ -393,7 +396,7 @@ def main():
         d2h = r["lmkStk"].nbytes + r["tauMat"].nbytes + r["obj"].nbytes
         e2e = {"value": K / wall, "unit": "steps/s", "h2d_bytes_per_step": h2d // K, "d2h_bytes_per_step": d2h // K,
                "what": f"one sa_forward call ({K} steps + objective) with host buffers: mesh upload and set-up, "
-                       "solve, trajectory download"}
+                       "solve, trajectory download; after one untimed one-step call"}
 
     served = None
     if not args.no_served and rank == 0 and args.workload == "shell":
