@@ -239,6 +239,78 @@ def served_leg(device: int, n: int = 32, full: bool = False):
             "mixed_vs_fp64_max_rel_err": {"positions": ep, "objective": eo}}
 
 
+BATCHED = ("Batched solves: 256 seeded instances submitted at once to the continuous-batching server (batched "
+           "persistent CG launches per tick); half 2D layered annuli (node counts log-uniform in 2k-40k, radial:angular "
+           "nodes 1:16, 2-6 material layers), half 3D layered shells (icosphere level 3-4 x 4-8 prism layers, 3 "
+           "material layers); Lame (lambda, mu = lambda/2) log-uniform in [0.5, 10] and diffusivity in [0.005, 0.1] "
+           "per material layer, random bump on the outer boundary, 50 steps each, varifold objective; the same batch "
+           "in FP64 and in mixed precision")
+
+
+def batched_requests(n: int = 256, seed: int = 13, steps: int = 50):
+    """Seeded batch of 2D annuli and 3D shells (meshes shared between requests of the same size)."""
+    import numpy as np
+    from shape_atrophy_gb300 import problems
+    rng = np.random.default_rng(seed)
+    cache, out = {}, []
+    for _ in range(n):
+        if rng.random() < 0.5:
+            nodes = 10.0 ** rng.uniform(np.log10(2000.0), np.log10(40000.0))
+            L = int(rng.integers(2, 7))
+            rad = max(L + 1, int(round(np.sqrt(nodes / 16.0))))
+            ang = max(16, int(round(nodes / rad / 16.0)) * 16)
+            key = ("a", ang, rad, L)
+            if key not in cache:
+                cache[key] = problems.annulus_layered(angNum=ang, radNum=rad, steps=steps, layers=L, native=True)
+            sp = dict(cache[key])
+            th = rng.uniform(0.0, 2.0 * np.pi)
+            sp["tauVarVec"] = np.array([np.cos(th), np.sin(th), 1.0, 0.1])
+        else:
+            level, layers, L = int(rng.integers(3, 5)), int(rng.integers(4, 9)), 3
+            key = ("s", level, layers)
+            if key not in cache:
+                cache[key] = problems.shell_layered(level=level, lyrCntNum=layers + 1, steps=steps, native=True)
+            sp = dict(cache[key])
+            c = rng.normal(size=3)
+            c /= np.linalg.norm(c)
+            sp["tauVarVec"] = np.array([c[0], c[1], c[2], 1.0, 0.15])
+        lam = 10.0 ** rng.uniform(np.log10(0.5), 1.0, L)
+        sp["modVec"] = np.column_stack([lam, lam / 2]).reshape(-1)
+        sp["spdLyrVec"] = 10.0 ** rng.uniform(np.log10(0.005), np.log10(0.1), L)
+        out.append(sp)
+    return out
+
+
+def batched_leg(device: int, n: int = 256):
+    """The batch through the server in FP64 and in mixed precision: solves/s, latency, error of mixed vs FP64."""
+    import numpy as np
+    from shape_atrophy_gb300 import api
+    reqs = batched_requests(n)
+    runs = {}
+    for prec in ("fp64", "mixed"):
+        sv = api.Server(hbm_budget=200e9, max_instances=n, device=device)
+        t0 = time.perf_counter()
+        ids = [sv.submit(sp, precision=prec) for sp in reqs]
+        res = [sv.result(i) for i in ids]
+        wall = time.perf_counter() - t0
+        st = sv.stats()
+        sv.close()
+        lat = np.array([r["latency_ms"] for r in res])
+        runs[prec] = dict(res=res, line={
+            "solves_per_s": len(res) / wall, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "wall_s": wall,
+            "steps_per_s": sum(sp["timeNum"] - 1 for sp in reqs) / wall,
+            "ok": int(sum(r["info"]["status"] == 0 for r in res)), "peak_device_gb": st["peakBytes"] / 1e9,
+            "ticks": st["ticks"]})
+    ep = eo = 0.0
+    for a, b in zip(runs["mixed"]["res"], runs["fp64"]["res"]):
+        ep = max(ep, float(np.abs(a["lmk"] - b["lmk"]).max() / np.abs(b["lmk"]).max()))
+        eo = max(eo, abs(a["obj"] - b["obj"]) / abs(b["obj"]))
+    return {"workload": BATCHED, "requests": n, "fp64": runs["fp64"]["line"], "mixed": runs["mixed"]["line"],
+            "mixed_over_fp64_solves": runs["mixed"]["line"]["solves_per_s"] / runs["fp64"]["line"]["solves_per_s"],
+            "mixed_vs_fp64_max_rel_err": {"positions": ep, "objective": eo}}
+
+
 def mixed_error_leg(args, device: int, steps: int = 100, every: int = 10):
     """The mixed-precision solve of the shell against the FP64 solve, both on the GPU, at every
     10th step (node positions, concentration, objective).  The FP64 GPU path stands in for the FP64 oracle
@@ -294,6 +366,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances leg")
+    ap.add_argument("--batched-requests", type=int, default=256)
     ap.add_argument("--no-mixed-error", action="store_true", help="skip the mixed-vs-FP64 error leg")
     ap.add_argument("--no-gradient", action="store_true", help="skip the objective-gradient leg")
     ap.add_argument("--served-requests", type=int, default=32)
@@ -401,6 +475,9 @@ def main():
     served = None
     if not args.no_served and rank == 0 and args.workload == "shell":
         served = served_leg(local, args.served_requests, full=args.served_full)
+    batched = None
+    if not args.no_batched and rank == 0 and args.workload == "shell":
+        batched = batched_leg(local, args.batched_requests)
 
     mixed_error = None
     if not args.no_mixed_error and rank == 0 and args.workload == "shell":
@@ -438,7 +515,7 @@ def main():
                            "l2": "per-step working set (~0.3 GB) larger than the 129 MB L2",
                            "parallelism": f"replicas x{ws}"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "objective": objective, "gradient": gradient,
-                "mixed_error": mixed_error, "served": served,
+                "mixed_error": mixed_error, "served": served, "batched": batched,
                 "clocks": clocks,
                 "gpu_launches": launches}
         print(json.dumps(line), flush=True)

@@ -76,20 +76,29 @@ def frame_shell(level: int = 2, lyrCntNum: int = 4, timeEnd: float = 0.1, timeSt
 
 
 def annulus_layered(angNum: int = 256, radNum: int = 16, steps: int = 50, timeStp: float = 0.02,
-                    cgTolVal: float = 1e-8, btmWgt: float = 10.0, target_seed: int = 1) -> dict:
-    """Layered 2D annulus, radii 0.6-1.0 (periodic in angle)."""
-    obj = mesh.generate_element_object_2d(angNum, radNum, [1, radNum], periodic=True)
+                    cgTolVal: float = 1e-8, btmWgt: float = 10.0, target_seed: int = 1, layers: int = 4,
+                    native: bool = False) -> dict:
+    """Layered 2D annulus, radii 0.6-1.0 (periodic in angle); ``layers`` equal radial material layers with
+    (lambda, mu) = (2^k, 2^k / 2) and D = 0.01 * 2^k, k = 0 .. layers-1 (the default 4 layers: (1, 0.5) ..
+    (8, 4), D = 0.01 .. 0.08).  native=True builds the element object with the C library (identical arrays)."""
+    if native:
+        from . import api
+        obj = api.build_element_object_2d(angNum, radNum, [1, radNum], periodic=True)
+    else:
+        obj = mesh.generate_element_object_2d(angNum, radNum, [1, radNum], periodic=True)
     lmk = mesh.annulus_nodes(angNum, radNum, 0.6, 1.0)
     E = obj["elmVtxMat"].shape[1]
     rings = radNum - 1
-    ring_layer = np.minimum((4 * np.arange(rings)) // rings, 3)
+    L = int(layers)
+    ring_layer = np.minimum((L * np.arange(rings)) // rings, L - 1)
     obj["elmLyrVec"] = mesh.element_layers(E, obj["elmPerLayer"], ring_layer)
+    lam = 2.0 ** np.arange(L)
     spec = dict(
         dim=2, elaType="isotropic", lmkIniMat=lmk, elmObj=obj, elmLyrVec=obj["elmLyrVec"],
         tauVarVec=np.array([1.0, 0.0, 1.0, 0.1]),          # centre (r=1, angle 0), height 1, sigma 0.1
         tauPrmVec=np.array([0.0]),
-        modVec=np.array([1.0, 0.5, 2.0, 1.0, 4.0, 2.0, 8.0, 4.0]),
-        spdLyrVec=np.array([0.01, 0.02, 0.04, 0.08]),
+        modVec=np.column_stack([lam, lam / 2]).reshape(-1),
+        spdLyrVec=0.01 * lam,
         ynkActPrmVec=np.array([0.5]), reaActPrmVec=np.array([2.0]),
         ldmWgt=0.0, knlOrder=1, knlWidth=0.1, knlEps=0.0, btmWgt=btmWgt,
         timeStp=timeStp, timeNum=steps + 1, cgItrMax=20000, cgTolSqu=cgTolVal ** 2,
