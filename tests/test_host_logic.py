@@ -54,6 +54,42 @@ def test_served_request_stream_is_seeded():
         assert sa["timeNum"] == sb["timeNum"] and 21 <= sa["timeNum"] <= 61
 
 
+@pytest.mark.parametrize("layers", [2, 3, 5, 6])
+def test_annulus_material_layers(layers):
+    from shape_atrophy_gb300 import problems
+    sp = problems.annulus_layered(angNum=32, radNum=8, steps=2, layers=layers)
+    lyr = np.asarray(sp["elmLyrVec"])
+    assert sorted(set(lyr.tolist())) == list(range(layers))          # every material layer has elements
+    assert len(sp["spdLyrVec"]) == layers and len(sp["modVec"]) == 2 * layers
+    np.testing.assert_array_equal(sp["modVec"][1::2], sp["modVec"][0::2] / 2)   # mu = lambda / 2
+    # material layers follow the radial rings outward: element layer ids never decrease with the ring
+    per = sp["elmObj"]["elmPerLayer"]
+    ring = np.arange(lyr.size) // per
+    assert np.all(np.diff([lyr[ring == k].max() for k in range(ring.max() + 1)]) >= 0)
+
+
+def test_batched_instance_batch_is_seeded_and_in_range():
+    import bench
+    a, b = bench.batched_requests(24, seed=5, steps=3), bench.batched_requests(24, seed=5, steps=3)
+    dims = [sp["dim"] for sp in a]
+    assert 2 in dims and 3 in dims
+    for sa, sb in zip(a, b):
+        np.testing.assert_array_equal(sa["tauVarVec"], sb["tauVarVec"])
+        np.testing.assert_array_equal(sa["modVec"], sb["modVec"])
+        assert sa["timeNum"] == 4
+        N = sa["lmkIniMat"].shape[1]
+        L = len(sa["spdLyrVec"])
+        assert len(sa["modVec"]) == 2 * L
+        assert np.all((sa["modVec"][0::2] >= 0.5) & (sa["modVec"][0::2] <= 10.0))
+        assert np.all((sa["spdLyrVec"] >= 0.005) & (sa["spdLyrVec"] <= 0.1))
+        if sa["dim"] == 2:
+            assert 1500 <= N <= 45000 and 2 <= L <= 6
+            assert np.hypot(*sa["tauVarVec"][:2]) == pytest.approx(1.0)     # bump on the outer circle
+        else:
+            assert N in {642 * k for k in range(5, 10)} | {2562 * k for k in range(5, 10)} and L == 3
+            assert np.linalg.norm(sa["tauVarVec"][:3]) == pytest.approx(1.0)
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
