@@ -10,12 +10,19 @@
 //   dsum (2D_frame/dsum.cu:6-73)                     -> device_sum (same 512-wide tree order)
 // The Matern-3/2 centre kernel 'M' (1 + r/w) exp(-r/w) is the layered model's addition.
 //
+// FP64 pair term: e^x by a table-driven method and the Matern distance by a
+// Newton square root (exp_tab, sqrt_nr below), both within about 1 ulp;
+// work items (row block, column chunk) taken largest first by a persistent
+// grid.
+//
 // Mixed precision: pair terms in FP32 with compensated (Kahan) FP32 sums
 // inside each column tile, tile sums accumulated in FP64 per row, FP64 final
 // reduction.  Centres are carried as two floats (value and remainder), so a
 // centre difference keeps FP32 precision relative to the difference itself
 // rather than to the coordinates (the kernel widths are small against the
-// shape's extent).
+// shape's extent).  The near field (kernel product above kNearField) is
+// evaluated again in FP64, with both element sets in Morton order so that a
+// warp's rows take that branch together (spatial_order).
 #include "sa_internal.cuh"
 #include <cmath>
 #include <algorithm>
@@ -166,10 +173,11 @@ __global__ void k_vfd_elems(int N, int Vd, const int *__restrict__ vfdVtx, const
 struct VfdSet { const double *cen, *dir, *vol; int n; };
 
 // out[i] = sum_j c1 K(i, j) over set A  +  sum_j c2 K(i, j) over set B (B may be empty);
-// gradient rows (dc, dt) when grad != 0 (rows must be the deformed set).  blockIdx.y splits the
-// columns of each set into gridDim.y contiguous chunks (more CTAs than rows alone give); chunk c
+// gradient rows (dc, dt) when G (rows must be the deformed set).  The columns of each set are split
+// into C contiguous chunks (more work items than row blocks alone give); the item (row block, chunk c)
 // writes its partial row sums at out + c * R.n (dc, dt at + c * D * R.n), summed in chunk order by
-// k_vfd_chunks.  One chunk: the reference's per-row order exactly.
+// k_vfd_chunks.  With a queue, a persistent grid takes the items from it (see the loop below); without
+// one, the grid is (row blocks, C) with one item per CTA.  One chunk: the reference's per-row order.
 // symA != 0 (objective only, set A is the row set itself): K is symmetric, so row i takes the pairs
 // j >= i of set A with weight 2 (1 on the diagonal) -- the same total with half the pair evaluations.
 template <int D, typename T, bool G>
