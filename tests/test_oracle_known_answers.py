@@ -6,7 +6,8 @@ the golden vectors:
 
 * the assembled P1 mass matrix sums to the mesh's area / volume;
 * the diffusion (stiffness) matrix annihilates constants (zero row sums);
-* the elasticity operator annihilates rigid translations and is symmetric
+* the elasticity operator annihilates rigid translations and infinitesimal
+  rotations and is symmetric
   (x . E y = y . E x), frame and layered models, 2D and 3D; the bottom
   penalty is symmetric;
 * the RKHS kernel matrix equals the closed forms of the half-integer Matern
@@ -64,7 +65,7 @@ def test_mass_sums_to_volume_and_stiffness_annihilates_constants(name):
 
 
 @pytest.mark.parametrize("name", list(CASES))
-def test_elasticity_annihilates_translations_and_is_symmetric(name):
+def test_elasticity_annihilates_rigid_motions_and_is_symmetric(name):
     spec = CASES[name]()
     P = Problem(spec)
     lmk = spec["lmkIniMat"]
@@ -77,6 +78,11 @@ def test_elasticity_annihilates_translations_and_is_symmetric(name):
         t = np.zeros((D, N))
         t[d] = 1.7
         assert np.abs(P.elastic(lmk, t)).max() <= 1e-12 * scale
+    # infinitesimal rigid rotations v = W x (W skew) have zero linear strain
+    w = rng.normal(size=3)
+    W = (np.array([[0.0, -1.0], [1.0, 0.0]]) if D == 2 else
+         np.array([[0.0, -w[2], w[1]], [w[2], 0.0, -w[0]], [-w[1], w[0], 0.0]]))
+    assert np.abs(P.elastic(lmk, W @ lmk)).max() <= 1e-12 * scale
     assert np.vdot(x, Ey) == pytest.approx(np.vdot(y, Ex), rel=1e-12)
     if spec["btmWgt"] != 0.0 or spec["elmObj"]["btmVtxMat"].shape[1] > 0:
         Px, Py = P.penalty(lmk, x), P.penalty(lmk, y)
