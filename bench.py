@@ -136,8 +136,10 @@ def spec_for(args, steps: int):
     return spec
 
 
-def cpu_sample(spec_full, seconds: float = 25.0, max_steps: int = 3):
-    """Time the CPU oracle (all host cores, OpenMP) on the first steps of the same workload."""
+def cpu_sample(spec_full, seconds: float = 25.0, max_steps: int = 3, warm: int = 3):
+    """Time the CPU oracle (all host cores, OpenMP) on time steps warm+1 .. warm+k of the same workload, as the
+    GPU steps are timed after warm-up steps: the oracle is deterministic, so those steps take the difference
+    between a (warm + k)-step and a warm-step run.  k fits the time budget (at most max_steps)."""
     from oracle.oracle import Problem
 
     def run(k):
@@ -151,12 +153,16 @@ def cpu_sample(spec_full, seconds: float = 25.0, max_steps: int = 3):
             raise RuntimeError("oracle solve failed")
         return dt
 
-    t_total, steps = run(1), 1                 # one step first, then as many as fit the time budget
-    k = int(min(max_steps, max(1, seconds // max(t_total, 1e-3))))
-    if k > 1:
-        t_total, steps = run(k), k
+    t_warm = run(warm) if warm > 0 else 0.0
+    per = t_warm / warm if warm > 0 else run(1)
+    k = int(min(max_steps, max(1, (seconds - t_warm) // max(per, 1e-3))))
+    t_all = run(warm + k)
+    dt = t_all - t_warm
+    if not dt > 0.0:                           # timing noise on a tiny sample: count every step instead
+        dt, k, warm = t_all, warm + k, 0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return steps / t_total, cores, f"first {steps} time step(s) of the same shell workload, {t_total:.1f} s"
+    return k / dt, cores, (f"time steps {warm + 1}-{warm + k} of the same workload (after {warm} warm-up "
+                           f"steps, as the GPU steps), {dt:.1f} s; {t_warm + t_all:.1f} s of CPU runs in all")
 
 
 SERVED = ("Poisson stream of forward solves: 3D layered shells, icosphere level 3-5 x 4/8/12 prism layers "
