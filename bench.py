@@ -161,8 +161,9 @@ def cpu_sample(spec_full, seconds: float = 25.0, max_steps: int = 3, warm: int =
     if not dt > 0.0:                           # timing noise on a tiny sample: count every step instead
         dt, k, warm = t_all, warm + k, 0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return k / dt, cores, (f"time steps {warm + 1}-{warm + k} of the same workload (after {warm} warm-up "
-                           f"steps, as the GPU steps), {dt:.1f} s; {t_warm + t_all:.1f} s of CPU runs in all")
+    steps = f"time step {warm + 1}" if k == 1 else f"time steps {warm + 1}-{warm + k}"
+    return k / dt, cores, (f"{steps} of the same workload (after {warm} warm-up steps, as the GPU steps), "
+                           f"{dt:.1f} s; {t_warm + t_all:.1f} s of CPU runs in all")
 
 
 SERVED = ("Poisson stream of forward solves: 3D layered shells, icosphere level 3-5 x 4/8/12 prism layers "
