@@ -63,8 +63,11 @@ extern "C" {
 #define SA_GUESS_EXTRAPOLATE  1   /* 2 v_t-1 - v_t-2 from the third step on: same answer to the CG tolerance,
                                      about a third fewer iterations on the layered shell */
 #define SA_GUESS_QUADRATIC    2   /* 3 v_t-1 - 3 v_t-2 + v_t-3 from the fourth step on (linear at the third) */
+#define SA_GUESS_CUBIC        3   /* 4 v_t-1 - 6 v_t-2 + 4 v_t-3 - v_t-4 (lower degrees in the first steps) */
 #define SA_GUESS_MAX_ORDER    5   /* velocityGuess k = 1 .. 5: the degree-k polynomial through the last k + 1
                                      velocities, evaluated one step ahead (lower degrees in the first steps) */
+#define SA_GUESS_DEFAULT      SA_GUESS_CUBIC   /* fewest iterations on the layered workloads; the positional
+                                                  isotropic entry points use it */
 
 typedef struct sa_context sa_context;
 
@@ -109,9 +112,9 @@ typedef struct sa_params {
 	int rdItrMax;                       /* isotropic reaction-diffusion PCG (frame: same as cgItrMax) */
 	double rdTolSqu;                    /* isotropic RD PCG tolerance squared (frame: 1e-28) */
 	int cgKernel;                       /* SA_CG_AUTO (0), SA_CG_PERSISTENT, SA_CG_TWO_KERNEL, SA_CG_PERSISTENT_GLOBAL */
-	int velocityGuess;                  /* layered model's velocity CG start: SA_GUESS_PREVIOUS (0, the reference's
-	                                       warm start), SA_GUESS_EXTRAPOLATE or SA_GUESS_QUADRATIC; the frame
-	                                       model always uses 0 */
+	int velocityGuess;                  /* layered model's velocity CG start: a polynomial order 0 .. 5
+	                                       (SA_GUESS_PREVIOUS = 0 is the reference's warm start, SA_GUESS_DEFAULT
+	                                       the cubic); the frame model always uses 0 */
 } sa_params;
 
 /* Varifold target and kernels (computeObjfcn prhs[13..20]). */
@@ -184,18 +187,27 @@ int sa_objective_gradient(sa_context *ctx, const sa_element_object *obj, const d
  * a GPU whose memory is managed by someone else (MATLAB's gpuArray pool, a
  * serving process with a fixed budget), where cudaMalloc can fail and
  * cudaFree synchronises the whole device.  Same value as sa_varifold.
- *   - All inputs must already be device memory (nodes: N x dim
- *     column-major; vfdVtxMat: Vd x dim int32; target Vt x dim, Vt);
- *     host pointers are rejected with SA_ERR_ARG (nothing is copied).
+ *   - All inputs must already be memory of the current device (nodes:
+ *     N x dim column-major; vfdVtxMat: Vd x dim int32; target Vt x dim,
+ *     Vt); host pointers and other GPUs' memory are rejected with
+ *     SA_ERR_ARG (nothing is copied).
  *   - Limit: vfdElmNum and tgtElmNum at most 32768 each; larger sizes
  *     return SA_ERR_ARG.  The scratch is a fixed ~2.4 MB device array that
  *     every GPU loading the library holds until the process exits.
+ *   - A vfdVtxMat entry outside [0, lmkNum) is found on the device (the
+ *     element is skipped, nothing outside the arrays is read) and the call
+ *     returns SA_ERR_ARG.  cenKnlWidth, and dirKnlWidth for the 'O' and
+ *     'U' direction kernels, must be finite and > 0.
  *   - The first call on a device looks the array's device address up
- *     (cudaGetSymbolAddress); make that first call before any stream
- *     capture.  Runs on the given stream (NULL: the legacy default stream)
- *     of the current device and waits for it before returning.
- *   - All calls share the one array: calls that overlap on the GPU (other
- *     threads, other streams) race; serialise them.
+ *     (cudaGetSymbolAddress) and keeps it for later calls; make that first
+ *     call before any stream capture.  cudaDeviceReset invalidates the
+ *     kept address: do not call this function after resetting the device.
+ *   - Runs on the given stream (NULL: the legacy default stream) of the
+ *     current device and returns only when the objective has been written
+ *     to objOut: it waits for that stream.
+ *   - All calls share the one array and each leaves its contents behind:
+ *     calls that overlap on the GPU (other threads, other streams) race;
+ *     serialise them.
  *   - objOut may be host or device memory. */
 int sa_varifold_noalloc(int dim, int lmkNum, const double *lmkMat, int vfdElmNum, const int *vfdVtxMat,
                         int tgtElmNum, const double *tgtCenPosMat, const double *tgtUniDirMat,
@@ -335,6 +347,12 @@ int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs
  * sqrt(x[k]), both evaluated on the device. */
 int sa_selftest_math(sa_context *ctx, int fn, long n, const double *x, double *y, double *yref);
 
+/* FMA throughput of the device's FP64 (fp64 = 1) or FP32 (fp64 = 0) pipe in
+ * TFLOP/s (no reference counterpart): eight independent FMA chains per
+ * thread, 8 CTAs of 256 threads per SM, best of three timed launches after a
+ * warm-up.  The denominator of the pipe fractions the benchmark reports. */
+int sa_selftest_fma_peak(sa_context *ctx, int fp64, double *tflops);
+
 /* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and
  * deformation_3D_frame (dim 3): arguments in prhs order
  * (CUDA/2D_frame/deformation.cu:24-50), outputs plhs[0..2]
@@ -385,6 +403,73 @@ int sa_computeObjfcn_frame(sa_context *ctx, int dim,
 	double ldmWgt, int knlOrder, double knlWidth, double knlEps,   /* prhs[21..24]               */
 	const double *modVec,                                   /* prhs[25]                           */
 	double spdTanVal, double spdTsvVal,                     /* prhs[26..27]                       */
+	const double *ynkActPrmVec, const double *reaActPrmVec, /* prhs[28..29]                       */
+	double btmWgt, double timeStp, int timeNum,             /* prhs[30..32]                       */
+	int cgItrMax, double cgTolSqu,                          /* prhs[33..34]                       */
+	double *objVec);                                        /* plhs[0]                            */
+
+/* The layered (isotropic) model through the positional surface of the
+ * frame entry points: the branch that CUDA/deformation.m:12-13,22-24 and
+ * CUDA/computeObjfcn.m:12-13,22-24 parse (d_modMat = reshape(h_modVec, 2,
+ * [])') and leave empty.  Arguments are those of sa_deformation_frame with
+ * three changes: elmLyrVec (E int32, the 0-based material layer of each
+ * element) follows femIfoMat; modMat (lyrNum x 2 column-major: lambda in
+ * column 0, mu in column 1; host or device memory) replaces modVec; and
+ * spdLyrVec (lyrNum per-layer diffusivities, the wrapper's spdTanVal)
+ * replaces spdTanVal, spdTsvVal.  ynkActPrmVec = [c] (load -c u I),
+ * reaActPrmVec = [rate] (Fisher-KPP rate u (1 - u)), tauVarMat columns are
+ * the bump [centre (dim), height, sigma].  tanVtxMat/nmlVtxMat and
+ * tsvVtxMat are not used by this model and may be NULL.  FP64, velocity CG
+ * started from SA_GUESS_DEFAULT; outputs as sa_deformation_frame. */
+int sa_deformation_isotropic(sa_context *ctx, int dim,
+	const double *tauVarMat, int tauVarNum, int objTotNum,  /* prhs[0]                            */
+	const double *tauPrmVec, int tauPrmNum,                 /* prhs[1]                            */
+	const double *lmkIniMat, int lmkNum,                    /* prhs[2]  N x dim                   */
+	const int *elmVtxMat, int elmNum,                       /* prhs[3]                            */
+	const int *vtxElmMat, int vtxElmCols,                   /* prhs[4]                            */
+	const int *frmVtxMat,                                   /* prhs[5]  unused here (may be NULL) */
+	const int *tsvVtxMat,                                   /* prhs[6]  unused here (may be NULL) */
+	const int *bdrVtxMat, int bdrElmNum,                    /* prhs[7]                            */
+	const int *vtxBdrMat, int vtxBdrCols,                   /* prhs[8]                            */
+	const int *btmVtxMat, int btmElmNum,                    /* prhs[9]                            */
+	const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols,    /* prhs[10]                           */
+	const int *femVtxMat, int nzrNum,                       /* prhs[11]                           */
+	const int *femIfoMat, int femIfoCols,                   /* prhs[12]                           */
+	const int *elmLyrVec,                                   /* prhs[13] E                         */
+	double ldmWgt, int knlOrder, double knlWidth, double knlEps,   /* prhs[14..17]               */
+	const double *modMat, int lyrNum,                       /* prhs[18] lyrNum x 2 (lambda, mu)   */
+	const double *spdLyrVec,                                /* prhs[19] lyrNum                    */
+	const double *ynkActPrmVec, const double *reaActPrmVec, /* prhs[20..21] 1 value each          */
+	double btmWgt, double timeStp, int timeNum,             /* prhs[22..24]                       */
+	int cgItrMax, double cgTolSqu,                          /* prhs[25..26]                       */
+	double *lmkStk, double *tauMat, double *objVec);        /* plhs[0..2]                         */
+
+/* computeObjfcn for the layered model: the arguments of
+ * sa_computeObjfcn_frame with the three changes of sa_deformation_isotropic
+ * (elmLyrVec after femIfoMat, modMat, spdLyrVec). */
+int sa_computeObjfcn_isotropic(sa_context *ctx, int dim,
+	const double *tauVarMat, int tauVarNum, int objTotNum,  /* prhs[0]                            */
+	const double *tauPrmVec, int tauPrmNum,                 /* prhs[1]                            */
+	const double *lmkIniMat, int lmkNum,                    /* prhs[2]                            */
+	const int *elmVtxMat, int elmNum,                       /* prhs[3]                            */
+	const int *vtxElmMat, int vtxElmCols,                   /* prhs[4]                            */
+	const int *frmVtxMat,                                   /* prhs[5]  unused here (may be NULL) */
+	const int *tsvVtxMat,                                   /* prhs[6]  unused here (may be NULL) */
+	const int *bdrVtxMat, int bdrElmNum,                    /* prhs[7]                            */
+	const int *vtxBdrMat, int vtxBdrCols,                   /* prhs[8]                            */
+	const int *btmVtxMat, int btmElmNum,                    /* prhs[9]                            */
+	const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols,    /* prhs[10]                           */
+	const int *femVtxMat, int nzrNum,                       /* prhs[11]                           */
+	const int *femIfoMat, int femIfoCols,                   /* prhs[12]                           */
+	const int *elmLyrVec,                                   /* prhs[13] E                         */
+	const int *vfdVtxMat, int vfdElmNum,                    /* prhs[14] Vd x dim                  */
+	const double *tgtCenPosMat, const double *tgtUniDirMat, /* prhs[15..16] Vt x dim              */
+	const double *tgtElmVolVec, int tgtElmNum,              /* prhs[17] Vt                        */
+	double cenKnlType, double cenKnlWidth,                  /* prhs[18..19] (char code as double) */
+	double dirKnlType, double dirKnlWidth,                  /* prhs[20..21]                       */
+	double ldmWgt, int knlOrder, double knlWidth, double knlEps,   /* prhs[22..25]               */
+	const double *modMat, int lyrNum,                       /* prhs[26] lyrNum x 2                */
+	const double *spdLyrVec,                                /* prhs[27] lyrNum                    */
 	const double *ynkActPrmVec, const double *reaActPrmVec, /* prhs[28..29]                       */
 	double btmWgt, double timeStp, int timeNum,             /* prhs[30..32]                       */
 	int cgItrMax, double cgTolSqu,                          /* prhs[33..34]                       */

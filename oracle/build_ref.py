@@ -1,7 +1,9 @@
 """Compile the reference's own CUDA sources for the CPU (checker only).
 
-TEST INFRASTRUCTURE ONLY.  This recipe reads the reference tree (default
-/root/reference, override with SA_REFERENCE_ROOT), takes the four MEX
+TEST INFRASTRUCTURE ONLY.  This recipe reads the reference tree (the
+directory SA_REFERENCE_ROOT names or, when that is unset, a checkout named
+``reference`` beside this repository's root, recognised by its
+CUDA/compile.m), takes the four MEX
 source lists from its CUDA/compile.m (parsed as text, the build script is
 not run), and builds each list with g++ into oracle/_ref/:
 
@@ -36,7 +38,12 @@ SHIM = os.path.join(HERE, "ref_shim")
 
 
 def reference_root() -> str:
-    return os.environ.get("SA_REFERENCE_ROOT", "/root/reference")
+    """The reference checkout, or "" when none is found (then nothing here is built)."""
+    env = os.environ.get("SA_REFERENCE_ROOT")
+    if env:
+        return env
+    beside = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return beside if os.path.isfile(os.path.join(beside, "CUDA", "compile.m")) else ""
 
 
 def parse_compile_m(path: str):

@@ -16,6 +16,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <stdio.h>
+#include <omp.h>
 #include "oracle.h"
 
 #ifndef DIM
@@ -1359,6 +1360,12 @@ double orc_varifold(const orc_problem *P, const double *lmk, double *grad)
 int orc_forward(const orc_problem *P, const double *tauVarVec,
                 double *lmkStk, double *tauMat, double *objPtr, int *cgItr)
 {
+	return orc_forward_timed(P, tauVarVec, lmkStk, tauMat, objPtr, cgItr, NULL);
+}
+
+int orc_forward_timed(const orc_problem *P, const double *tauVarVec, double *lmkStk, double *tauMat,
+                      double *objPtr, int *cgItr, double *stepSec)
+{
 	int N = P->lmkNum, E = P->elmNum, Z = P->nzrNum, T = P->timeNum;
 	long nd = (long) N * DIM;
 	double dt = P->timeStp;
@@ -1416,6 +1423,7 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 	}
 
 	for (int t = 0; t < T - 1; ++t) {
+		double tStep = omp_get_wtime();
 		double *lmkNow = lmkStk + (size_t) t * nd, *lmkNxt = lmkStk + (size_t) (t + 1) * nd;
 		double *tauNow = tauMat + (size_t) t * N, *tauNxt = tauMat + (size_t) (t + 1) * N;
 		S.lmk = lmkNow; S.edg = edgNow; S.frmA = frmNow; S.tsv = tsvNow;
@@ -1513,6 +1521,7 @@ int orc_forward(const orc_problem *P, const double *tauVarVec,
 		sw = edgNow; edgNow = edgNxt; edgNxt = sw;
 		sw = frmNow; frmNow = frmNxt; frmNxt = sw;
 		sw = tsvNow; tsvNow = tsvNxt; tsvNxt = sw;
+		if (stepSec) stepSec[t] = omp_get_wtime() - tStep;
 	}
 
 	if (objPtr) {

@@ -88,6 +88,12 @@ typedef struct orc_problem {
 int orc_forward(const orc_problem *P, const double *tauVarVec,
                 double *lmkStk, double *tauMat, double *objPtr, int *cgItr);
 
+/* orc_forward that also records, in stepSec (timeNum-1 doubles, optional),
+ * the wall time of every time step (omp_get_wtime), for the CPU timing of
+ * a sample of steps after warm-up steps. */
+int orc_forward_timed(const orc_problem *P, const double *tauVarVec, double *lmkStk, double *tauMat,
+                      double *objPtr, int *cgItr, double *stepSec);
+
 /* Single operators, for operator-level parity tests. */
 void orc_initial_tau(const orc_problem *P, const double *tauVarVec, double *tau);
 void orc_frame(const orc_problem *P, const double *lmk, double *frmA, double *tsv);

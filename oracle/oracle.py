@@ -40,15 +40,20 @@ class OrcProblem(C.Structure):
     ]
 
 
-def lib(dim: int):
-    if dim not in _LIBS:
+def lib(dim: int, fast: bool = False):
+    """The parity build of the oracle, or with fast=True the -O3 -march=native timing build (same results)."""
+    key = (dim, fast)
+    if key not in _LIBS:
         paths = build_oracle.build()
+        if fast:
+            paths = build_oracle.fast_paths()
         l = C.CDLL(paths[0 if dim == 2 else 1])
         l.orc_forward.restype = C.c_int
+        l.orc_forward_timed.restype = C.c_int
         l.orc_varifold.restype = C.c_double
         l.orc_dsum.restype = C.c_double
-        _LIBS[dim] = l
-    return _LIBS[dim]
+        _LIBS[key] = l
+    return _LIBS[key]
 
 
 def _d(a):
@@ -62,7 +67,7 @@ def _i(a):
 class Problem:
     """Holds the numpy arrays alive and the packed struct."""
 
-    def __init__(self, spec: dict):
+    def __init__(self, spec: dict, fast: bool = False):
         self.spec = spec
         obj = spec["elmObj"]
         D = spec["dim"]
@@ -130,19 +135,23 @@ class Problem:
         self.p = p
         self.keep = keep
         self.dim, self.N = D, N
-        self.lib = lib(D)
+        self.lib = lib(D, fast)
 
     # -- full model ------------------------------------------------------
     def forward(self, tauVarVec, with_obj: bool = False):
+        """Whole trajectory: dict(status, lmkStk (T, D, N), tauMat (T, N), obj, cgItr (T-1,), stepSec (T-1,))
+        -- stepSec is the wall time of each time step."""
         N, D, T = self.N, self.dim, self.p.timeNum
         lmk = np.zeros((T, D, N))
         tau = np.zeros((T, N))
         obj = C.c_double(0.0)
         itr = np.zeros(max(T - 1, 1), dtype=np.int32)
+        sec = np.zeros(max(T - 1, 1))
         tv = np.ascontiguousarray(np.asarray(tauVarVec, dtype=np.float64))
-        st = self.lib.orc_forward(C.byref(self.p), _d(tv), _d(lmk), _d(tau),
-                                  C.byref(obj) if with_obj else None, _i(itr))
-        return dict(status=st, lmkStk=lmk, tauMat=tau, obj=obj.value if with_obj else None, cgItr=itr)
+        st = self.lib.orc_forward_timed(C.byref(self.p), _d(tv), _d(lmk), _d(tau),
+                                        C.byref(obj) if with_obj else None, _i(itr), _d(sec))
+        return dict(status=st, lmkStk=lmk, tauMat=tau, obj=obj.value if with_obj else None, cgItr=itr,
+                    stepSec=sec)
 
     # -- operators -------------------------------------------------------
     def _vec(self, name, lmk, x, out_shape):

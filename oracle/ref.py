@@ -21,7 +21,8 @@ _LIBS = {}
 
 
 def available() -> bool:
-    return os.path.isdir(os.path.join(build_ref.reference_root(), "CUDA"))
+    root = build_ref.reference_root()
+    return bool(root) and os.path.isdir(os.path.join(root, "CUDA"))
 
 
 def _lib(name: str):

@@ -89,6 +89,14 @@ def apply_tuning(device: int = 0, path: str = TUNING_FILE):
     return e
 
 
+def fma_peak(fp64: bool = True, device: int = 0) -> float:
+    """Measured FMA throughput (TFLOP/s) of the device's FP64 or FP32 pipe (sa_selftest_fma_peak)."""
+    ctx = context(device)
+    v = C.c_double()
+    ctx.check(ctx.lib.sa_selftest_fma_peak(ctx.h, 1 if fp64 else 0, C.byref(v)), "sa_selftest_fma_peak")
+    return v.value
+
+
 # Layered model: where each step's velocity CG starts -- the polynomial through the last k + 1 velocities,
 # evaluated one step ahead (k = 0: the previous velocity, the reference's warm start).  Names or orders.
 GUESS_ORDERS = {"previous": 0, "extrapolate": 1, "linear": 1, "quadratic": 2, "cubic": 3, "quartic": 4, "quintic": 5}

@@ -2,14 +2,17 @@
 
 Plain nvcc, one -gencode (compute_103a -> sm_103a), translation units
 compiled in parallel, output in shape_atrophy_gb300/_build/.  No torch,
-no cmake.  Used by __graft_entry__.build() on every host (the GPU host
-rebuilds from source: binaries built elsewhere are not portable across
-host architectures).
+no cmake.  Used by __graft_entry__.build() on every host.  A library is
+reused only when a key file written beside it names this host's machine
+architecture, this nvcc's version and the same flags, and no source is
+newer: a binary built on another host (x86_64 vs aarch64) or by another
+toolkit is rebuilt, whatever its modification time.
 """
 from __future__ import annotations
 
 import glob
 import os
+import platform
 import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
@@ -35,16 +38,32 @@ def sources():
     return sorted(glob.glob(os.path.join(SRC, "*.cu")))
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+KEY = os.path.join(OUT, "build_key.txt")
+
+
+def build_key(extra=()) -> str:
+    """Host architecture, nvcc version and flags the library is built with."""
+    try:
+        ver = subprocess.run([nvcc(), "--version"], capture_output=True, text=True).stdout.strip().splitlines()
+        ver = ver[-1] if ver else "unknown"
+    except OSError:
+        ver = "unknown"
+    return "\n".join([platform.machine(), ver, " ".join(ARCH + FLAGS + list(extra))]) + "\n"
+
+
+def up_to_date(extra=()) -> bool:
+    if not os.path.exists(LIB) or not os.path.exists(KEY):
         return False
+    with open(KEY) as f:
+        if f.read() != build_key(extra):
+            return False
     t = os.path.getmtime(LIB)
     deps = sources() + glob.glob(os.path.join(SRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
     return all(os.path.getmtime(d) <= t for d in deps)
 
 
 def build(force: bool = False, verbose: bool = False, extra=()) -> str:
-    if not force and up_to_date():
+    if not force and up_to_date(extra):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     objs = []
@@ -69,6 +88,8 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     if run(link) != 0:
         raise RuntimeError("link failed")
     os.replace(tmp, LIB)
+    with open(KEY, "w") as f:
+        f.write(build_key(extra))
     return LIB
 
 

@@ -1096,6 +1096,56 @@ int barrier_selftest(cudaStream_t s, int *ctasGaveUp, int *abortFlag)
 }
 
 // ---------------------------------------------------------------------------
+// FMA throughput of the FP64 or FP32 pipe: 8 independent FMA chains per
+// thread, 8 CTAs of 256 threads per SM.  The denominators of the pipe
+// fractions the benchmark reports (measured on the same GPU in the same run).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_peak(int iters, T a, T b, T *sink)
+{
+	T x[8];
+	for (int k = 0; k < 8; ++k) x[k] = (T) (threadIdx.x + k) * (T) 1e-3;
+	for (int i = 0; i < iters; ++i) {
+#pragma unroll
+		for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+	}
+	T t = x[0] + x[1] + x[2] + x[3] + x[4] + x[5] + x[6] + x[7];
+	if (t == (T) -1) sink[blockIdx.x] = t;        // never true (x stays in (0, 1]); keeps the chains live
+}
+
+int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops)
+{
+	int dev = 0, sms = 0;
+	SA_CHECK(cudaGetDevice(&dev));
+	SA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	const int nt = 256, nb = 8 * sms;
+	const int iters = fp64 ? 12000 : 600000;              // ~50 ms per launch on GB300
+	void *sink = nullptr;
+	SA_CHECK(cudaMallocAsync(&sink, sizeof(double) * nb, s));
+	cudaEvent_t e0, e1;
+	SA_CHECK(cudaEventCreate(&e0));
+	SA_CHECK(cudaEventCreate(&e1));
+	double best = 0.0;
+	for (int rep = 0; rep < 4; ++rep) {                   // first launch is a warm-up
+		SA_CHECK(cudaEventRecord(e0, s));
+		if (fp64) k_fma_peak<double><<<nb, nt, 0, s>>>(iters, 0.9999999, 1e-7, (double *) sink);
+		else k_fma_peak<float><<<nb, nt, 0, s>>>(iters, 0.9999f, 1e-4f, (float *) sink);
+		SA_CHECK(cudaEventRecord(e1, s));
+		SA_CHECK(cudaEventSynchronize(e1));
+		float ms = 0.f;
+		SA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+		double fl = 2.0 * 8.0 * (double) iters * (double) nt * nb;
+		if (rep > 0) best = std::max(best, fl / (ms * 1e-3) / 1e12);
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	SA_CHECK(cudaFreeAsync(sink, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	*tflops = best;
+	return SA_OK;
+}
+
+// ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
 // CTAs of the vector kernels: kVecCtasPerSm per SM, fewer for short vectors

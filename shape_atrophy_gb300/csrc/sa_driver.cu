@@ -765,6 +765,8 @@ static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *
 		SA_REQUIRE(md.cenKnl == 'G' || md.cenKnl == 'C' || md.cenKnl == 'M', "cenKnlType must be G, C or M");
 		SA_REQUIRE(md.dirKnl == 'B' || md.dirKnl == 'L' || md.dirKnl == 'O' || md.dirKnl == 'U',
 		           "dirKnlType must be B, L, O or U");
+		SA_REQUIRE(kernel_widths_ok(md.cenWidth, md.dirKnl, md.dirWidth),
+		           "cenKnlWidth (and dirKnlWidth for 'O'/'U') must be finite and > 0");
 	}
 }
 
@@ -883,6 +885,8 @@ static int varifold_impl(sa_context *ctx, const sa_element_object *obj, const do
 	SA_REQUIRE(md.cenKnl == 'G' || md.cenKnl == 'C' || md.cenKnl == 'M', "cenKnlType must be G, C or M");
 	SA_REQUIRE(md.dirKnl == 'B' || md.dirKnl == 'L' || md.dirKnl == 'O' || md.dirKnl == 'U',
 	           "dirKnlType must be B, L, O or U");
+	SA_REQUIRE(kernel_widths_ok(md.cenWidth, md.dirKnl, md.dirWidth),
+	           "cenKnlWidth (and dirKnlWidth for 'O'/'U') must be finite and > 0");
 	build_mesh(m, obj, true, grad != nullptr, false, 0, P);
 	const double *x = P.dev(lmk, (size_t) m.N * D);
 	double *xa = P.alloc<double>((size_t) m.N * D);
@@ -2044,6 +2048,98 @@ int sa_computeObjfcn_frame(sa_context *ctx, int dim, const double *tauVarMat, in
 }
 
 
+// The layered (isotropic) model behind the positional surface of the frame entry points: the branch
+// CUDA/deformation.m:12-13,22-24 and CUDA/computeObjfcn.m:12-13,22-24 leave empty.  modMat is the wrapper's
+// d_modMat = reshape(h_modVec, 2, [])' (lyrNum x 2, column-major: lambda in column 0, mu in column 1, host or
+// device memory); the library's parameter table interleaves (lambda, mu) per layer.
+static int isotropic_params(sa_params &p, std::vector<double> &mod, const double *tauPrmVec, int tauPrmNum,
+                            double ldmWgt, int knlOrder, double knlWidth, double knlEps, const double *modMat,
+                            int lyrNum, const double *spdLyrVec, const double *ynk, const double *rea,
+                            double btmWgt, double timeStp, int timeNum, int cgItrMax, double cgTolSqu)
+{
+	if (lyrNum <= 0 || !modMat || !spdLyrVec) return SA_ERR_ARG;
+	std::vector<double> cm((size_t) 2 * lyrNum);
+	if (cudaMemcpy(cm.data(), modMat, sizeof(double) * cm.size(), cudaMemcpyDefault) != cudaSuccess) {
+		cudaGetLastError();
+		return SA_ERR_ARG;
+	}
+	mod.resize(cm.size());
+	for (int l = 0; l < lyrNum; ++l) { mod[2 * l] = cm[l]; mod[2 * l + 1] = cm[lyrNum + l]; }
+	memset(&p, 0, sizeof(p));
+	p.elaType = SA_ELA_ISOTROPIC; p.precision = SA_PREC_FP64;
+	p.tauPrmVec = tauPrmVec; p.tauPrmNum = tauPrmNum;
+	p.ldmWgt = ldmWgt; p.knlOrder = knlOrder; p.knlWidth = knlWidth; p.knlEps = knlEps;
+	p.modVec = mod.data(); p.modNum = 2 * lyrNum;
+	p.spdLyrVec = spdLyrVec; p.lyrNum = lyrNum;
+	p.ynkActPrmVec = ynk; p.reaActPrmVec = rea;
+	p.btmWgt = btmWgt; p.timeStp = timeStp; p.timeNum = timeNum; p.cgItrMax = cgItrMax; p.cgTolSqu = cgTolSqu;
+	p.cgKernel = SA_CG_AUTO;
+	p.velocityGuess = SA_GUESS_DEFAULT;
+	return SA_OK;
+}
+
+int sa_deformation_isotropic(sa_context *ctx, int dim, const double *tauVarMat, int tauVarNum, int objTotNum,
+                             const double *tauPrmVec, int tauPrmNum, const double *lmkIniMat, int lmkNum,
+                             const int *elmVtxMat, int elmNum, const int *vtxElmMat, int vtxElmCols,
+                             const int *frmVtxMat, const int *tsvVtxMat, const int *bdrVtxMat, int bdrElmNum,
+                             const int *vtxBdrMat, int vtxBdrCols, const int *btmVtxMat, int btmElmNum,
+                             const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols, const int *femVtxMat,
+                             int nzrNum, const int *femIfoMat, int femIfoCols, const int *elmLyrVec,
+                             double ldmWgt, int knlOrder, double knlWidth, double knlEps, const double *modMat,
+                             int lyrNum, const double *spdLyrVec, const double *ynkActPrmVec,
+                             const double *reaActPrmVec, double btmWgt, double timeStp, int timeNum, int cgItrMax,
+                             double cgTolSqu, double *lmkStk, double *tauMat, double *objVec)
+{
+	sa_element_object o;
+	frame_object(o, dim, lmkNum, elmVtxMat, elmNum, vtxElmMat, vtxElmCols, frmVtxMat, tsvVtxMat, bdrVtxMat,
+	             bdrElmNum, vtxBdrMat, vtxBdrCols, btmVtxMat, btmElmNum, vtxBtmMat, btmLmkNum, vtxBtmCols,
+	             femVtxMat, nzrNum, femIfoMat, femIfoCols);
+	o.elmLyrVec = elmLyrVec;
+	sa_params p;
+	std::vector<double> mod;
+	int rc = isotropic_params(p, mod, tauPrmVec, tauPrmNum, ldmWgt, knlOrder, knlWidth, knlEps, modMat, lyrNum,
+	                          spdLyrVec, ynkActPrmVec, reaActPrmVec, btmWgt, timeStp, timeNum, cgItrMax, cgTolSqu);
+	if (rc != SA_OK) return rc;
+	return sa_forward(ctx, &o, lmkIniMat, &p, nullptr, tauVarMat, tauVarNum, objTotNum, lmkStk, tauMat, objVec,
+	                  nullptr);
+}
+
+int sa_computeObjfcn_isotropic(sa_context *ctx, int dim, const double *tauVarMat, int tauVarNum, int objTotNum,
+                               const double *tauPrmVec, int tauPrmNum, const double *lmkIniMat, int lmkNum,
+                               const int *elmVtxMat, int elmNum, const int *vtxElmMat, int vtxElmCols,
+                               const int *frmVtxMat, const int *tsvVtxMat, const int *bdrVtxMat, int bdrElmNum,
+                               const int *vtxBdrMat, int vtxBdrCols, const int *btmVtxMat, int btmElmNum,
+                               const int *vtxBtmMat, int btmLmkNum, int vtxBtmCols, const int *femVtxMat,
+                               int nzrNum, const int *femIfoMat, int femIfoCols, const int *elmLyrVec,
+                               const int *vfdVtxMat, int vfdElmNum, const double *tgtCenPosMat,
+                               const double *tgtUniDirMat, const double *tgtElmVolVec, int tgtElmNum,
+                               double cenKnlType, double cenKnlWidth, double dirKnlType, double dirKnlWidth,
+                               double ldmWgt, int knlOrder, double knlWidth, double knlEps, const double *modMat,
+                               int lyrNum, const double *spdLyrVec, const double *ynkActPrmVec,
+                               const double *reaActPrmVec, double btmWgt, double timeStp, int timeNum,
+                               int cgItrMax, double cgTolSqu, double *objVec)
+{
+	sa_element_object o;
+	frame_object(o, dim, lmkNum, elmVtxMat, elmNum, vtxElmMat, vtxElmCols, frmVtxMat, tsvVtxMat, bdrVtxMat,
+	             bdrElmNum, vtxBdrMat, vtxBdrCols, btmVtxMat, btmElmNum, vtxBtmMat, btmLmkNum, vtxBtmCols,
+	             femVtxMat, nzrNum, femIfoMat, femIfoCols);
+	o.elmLyrVec = elmLyrVec;
+	o.vfdVtxMat = vfdVtxMat;
+	o.vfdElmNum = vfdElmNum;
+	sa_params p;
+	std::vector<double> mod;
+	int rc = isotropic_params(p, mod, tauPrmVec, tauPrmNum, ldmWgt, knlOrder, knlWidth, knlEps, modMat, lyrNum,
+	                          spdLyrVec, ynkActPrmVec, reaActPrmVec, btmWgt, timeStp, timeNum, cgItrMax, cgTolSqu);
+	if (rc != SA_OK) return rc;
+	sa_target t;
+	memset(&t, 0, sizeof(t));
+	t.cenPosMat = tgtCenPosMat; t.uniDirMat = tgtUniDirMat; t.elmVolVec = tgtElmVolVec; t.tgtElmNum = tgtElmNum;
+	t.cenKnlType = (char) cenKnlType; t.cenKnlWidth = cenKnlWidth;
+	t.dirKnlType = (char) dirKnlType; t.dirKnlWidth = dirKnlWidth;
+	return sa_forward(ctx, &o, lmkIniMat, &p, &t, tauVarMat, tauVarNum, objTotNum, nullptr, nullptr, objVec,
+	                  nullptr);
+}
+
 // ---------------------------------------------------------------------------
 // serving
 // ---------------------------------------------------------------------------
@@ -2170,6 +2266,12 @@ int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs
 		SA_REQUIRE(abortFlag == 1, "the poisoned barrier did not record an abort");
 		return SA_OK;
 	});
+}
+
+int sa_selftest_fma_peak(sa_context *ctx, int fp64, double *tflops)
+{
+	if (!tflops) return SA_ERR_ARG;
+	return sa::guarded(ctx, [&]() { return sa::fma_peak_selftest(ctx->stream, fp64 ? 1 : 0, tflops); });
 }
 
 int sa_selftest_math(sa_context *ctx, int fn, long n, const double *x, double *y, double *yref)

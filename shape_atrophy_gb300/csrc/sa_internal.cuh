@@ -24,6 +24,14 @@ constexpr int kBlock = 256;
 
 inline int grid_for(long n, int block = kBlock) { return (int) ((n + block - 1) / block); }
 
+// varifold kernel widths: the centre width always divides, the direction width only for the 'O' and 'U'
+// direction kernels (2D_frame/varifold.cu:105-120); a width that divides must be finite and > 0
+inline bool kernel_widths_ok(double cenWidth, char dirType, double dirWidth)
+{
+	auto pos = [](double w) { return w > 0.0 && w < DBL_MAX; };     // false for NaN and Inf
+	return pos(cenWidth) && ((dirType != 'O' && dirType != 'U') || pos(dirWidth));
+}
+
 // --------------------------------------------------------------------------
 // small fixed-size vector math (mirrors inc/matvec.h operation order)
 // --------------------------------------------------------------------------
@@ -412,6 +420,7 @@ template <int B> void cg_finish_fp64(const Mesh &m, double *x, CgWork &w, cudaSt
 CgState cg_state(const CgWork &w, cudaStream_t s);
 // bounded grid wait self-test: CTAs that gave up, and the abort flag they left
 int barrier_selftest(cudaStream_t s, int *ctasGaveUp, int *abortFlag);
+int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops);
 
 // frame mode K-preconditioned CG (2D/ipcg.cu:11-100) with dense K
 struct KpcgWork {

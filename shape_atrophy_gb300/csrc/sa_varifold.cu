@@ -747,19 +747,38 @@ template double varifold<3>(const Mesh &, const Model &, const double *, const d
 // that address is what the kernels receive.
 // ---------------------------------------------------------------------------
 constexpr int kNoAllocMaxElm = 32768;                       // max Vd and max Vt
+struct BadIndex {};                                         // a vfdVtxMat entry outside [0, N)
 constexpr long kNoAllocDoubles = 9L * kNoAllocMaxElm + 1024;
 __device__ __align__(256) double g_noallocScratch[kNoAllocDoubles];
 
-// boundary elements from nodes in the reference's N x D column-major layout
+// the last double of the scratch array: set (as an int) when an element names a node outside [0, N)
+constexpr long kNoAllocFlagSlot = kNoAllocDoubles - 1;
+
+// boundary elements from nodes in the reference's N x D column-major layout.  The caller's indices are not
+// checked on the host (they are device memory): an element with a node index outside [0, N) is written as
+// zeros and raises *badIndex, and the host turns that into SA_ERR_ARG -- no out-of-range read is made.
 template <int D>
 __global__ void k_vfd_elems_soa(int N, int Vd, const int *__restrict__ vfdVtx, const double *__restrict__ x,
-                                double *__restrict__ cen, double *__restrict__ dir, double *__restrict__ vol)
+                                double *__restrict__ cen, double *__restrict__ dir, double *__restrict__ vol,
+                                int *__restrict__ badIndex)
 {
 	int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if (e >= Vd) return;
+	int idx[D];
+	bool ok = true;
+	for (int k = 0; k < D; ++k) {
+		idx[k] = vfdVtx[(long) k * Vd + e];
+		ok = ok && idx[k] >= 0 && idx[k] < N;
+	}
+	if (!ok) {
+		*badIndex = 1;
+		for (int d = 0; d < D; ++d) { cen[d * (long) Vd + e] = 0.0; dir[d * (long) Vd + e] = 0.0; }
+		vol[e] = 0.0;
+		return;
+	}
 	Vec<D> q[D];
 	for (int k = 0; k < D; ++k)
-		for (int d = 0; d < D; ++d) q[k].c[d] = x[(long) d * N + vfdVtx[(long) k * Vd + e]];
+		for (int d = 0; d < D; ++d) q[k].c[d] = x[(long) d * N + idx[k]];
 	Vec<D> c, u;
 	double v;
 	if (D == 2) {
@@ -786,7 +805,9 @@ static double varifold_in_scratch(double *scr, int N, const double *x, int Vd, c
 {
 	double *cen = scr, *dir = cen + (long) D * Vd, *vol = dir + (long) D * Vd, *vfd = vol + Vd;
 	double *sumScr = vfd + Vd + Vt;
-	k_vfd_elems_soa<D><<<grid_for(Vd), kBlock, 0, s>>>(N, Vd, vfdVtx, x, cen, dir, vol);
+	int *badIndex = (int *) (scr + kNoAllocFlagSlot);
+	SA_CHECK(cudaMemsetAsync(badIndex, 0, sizeof(int), s));
+	k_vfd_elems_soa<D><<<grid_for(Vd), kBlock, 0, s>>>(N, Vd, vfdVtx, x, cen, dir, vol, badIndex);
 	VfdSet Ds{cen, dir, vol, Vd}, Ts{tc, tu, tv, Vt}, E0{nullptr, nullptr, nullptr, 0};
 	const int blk = 128;
 	// same row/column roles as the allocating path (reference branch on Vd >= Vt)
@@ -802,8 +823,12 @@ static double varifold_in_scratch(double *scr, int N, const double *x, int Vd, c
 		                                                               nullptr, nullptr);
 	}
 	SA_CHECK(cudaGetLastError());
-	// device_sum clears the part of its buffer that accumulates before using it
-	return device_sum(vfd, Vd + Vt, sumScr, s);
+	// device_sum clears the part of its buffer that accumulates before using it (and waits for the stream)
+	double v = device_sum(vfd, Vd + Vt, sumScr, s);
+	int bad = 0;
+	SA_CHECK(cudaMemcpy(&bad, badIndex, sizeof(int), cudaMemcpyDeviceToHost));
+	if (bad) throw BadIndex{};
+	return v;
 }
 
 }  // namespace sa
@@ -829,11 +854,13 @@ int noalloc_scratch(int dev, double **out)
 	return SA_OK;
 }
 
-bool on_device(const void *p)
+// device memory of GPU dev (or managed memory): memory of another GPU is refused, a kernel on this one would
+// read it only through peer access
+bool on_device(const void *p, int dev)
 {
 	cudaPointerAttributes a;
 	if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+	return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev);
 }
 }  // namespace
 
@@ -847,11 +874,12 @@ extern "C" int sa_varifold_noalloc(int dim, int lmkNum, const double *lmkMat, in
 	if (vfdElmNum > sa::kNoAllocMaxElm || tgtElmNum > sa::kNoAllocMaxElm) return SA_ERR_ARG;   // scratch limit
 	if (cenKnlType != 'G' && cenKnlType != 'C' && cenKnlType != 'M') return SA_ERR_ARG;
 	if (dirKnlType != 'B' && dirKnlType != 'L' && dirKnlType != 'O' && dirKnlType != 'U') return SA_ERR_ARG;
-	if (!on_device(lmkMat) || !on_device(vfdVtxMat) || !on_device(tgtCenPosMat) || !on_device(tgtUniDirMat) ||
-	    !on_device(tgtElmVolVec))
-		return SA_ERR_ARG;                     // inputs must already be in device memory: nothing is copied
+	if (!sa::kernel_widths_ok(cenKnlWidth, dirKnlType, dirKnlWidth)) return SA_ERR_ARG;
 	int dev = 0;
 	if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SA_ERR_CUDA; }
+	if (!on_device(lmkMat, dev) || !on_device(vfdVtxMat, dev) || !on_device(tgtCenPosMat, dev) ||
+	    !on_device(tgtUniDirMat, dev) || !on_device(tgtElmVolVec, dev))
+		return SA_ERR_ARG;                     // inputs must already be in this device's memory: nothing is copied
 	double *scr = nullptr;
 	int rc = noalloc_scratch(dev, &scr);
 	if (rc != SA_OK) return rc;
@@ -868,6 +896,8 @@ extern "C" int sa_varifold_noalloc(int dim, int lmkNum, const double *lmkMat, in
 			cudaGetLastError();
 			return SA_ERR_CUDA;
 		}
+	} catch (const sa::BadIndex &) {
+		return SA_ERR_ARG;                     // a node index outside [0, lmkNum): no objective
 	} catch (const sa::CudaError &) {
 		cudaGetLastError();
 		return SA_ERR_CUDA;

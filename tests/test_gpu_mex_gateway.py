@@ -1,9 +1,12 @@
 """The drop-in boundary end to end: the MEX gateways of shape_atrophy_gb300/mex/
 (the files a maintainer compiles with `mex` to replace deformation_{2D,3D}_frame
-and computeObjfcn_{2D,3D}_frame) are compiled against a stand-in of the MEX API
-and called with the reference's 27 / 35 right-hand sides, gpuArray arguments in
-device memory (zero-copy, as MATLAB passes them).  Outputs are compared with the
-reference's own outputs (golden vectors) at 1e-10."""
+and computeObjfcn_{2D,3D}_frame, and to fill the empty isotropic branch with
+deformation_{2D,3D}_isotropic and computeObjfcn_{2D,3D}_isotropic) are compiled
+against a stand-in of the MEX API and called with 27 / 35 right-hand sides,
+gpuArray arguments in device memory (zero-copy, as MATLAB passes them).  Frame
+outputs are compared with the reference's own outputs (golden vectors) at
+1e-10; isotropic outputs with sa_forward bit for bit and with the oracle at
+1e-10."""
 import ctypes as C
 
 import numpy as np
@@ -139,3 +142,105 @@ def test_gateways_reproduce_the_reference(gateways, name):
             assert obj[k] == DBL_MAX
         else:
             assert abs(obj[k] - ref["objfcn"][k]) <= 1e-10 * abs(ref["objfcn"][k])
+
+
+# ---------------------------------------------------------------------------
+# the layered (isotropic) model: deformation_{2D,3D}_isotropic, computeObjfcn_{2D,3D}_isotropic
+# ---------------------------------------------------------------------------
+def _layered_case(dim):
+    from shape_atrophy_gb300 import problems
+    if dim == 2:
+        spec = problems.annulus_layered(angNum=48, radNum=7, steps=6, cgTolVal=1e-12)
+        tv = np.array([[1.0, 0.0, 1.0, 0.1], [0.0, 1.0, 0.8, 0.15]])
+    else:
+        spec = problems.shell_layered(level=2, lyrCntNum=4, steps=4, cgTolVal=1e-12)
+        tv = np.array([[0.0, 0.0, 1.0, 1.0, 0.15], [1.0, 0.0, 0.0, 0.7, 0.2]])
+    return spec, tv
+
+
+def _isotropic_middle(R, spec):
+    """prhs[13]: elmObj.elmLyrVec, gpuArray int32."""
+    R.gpu(spec["elmLyrVec"], np.int32)
+
+
+def _isotropic_tail(R, spec):
+    for k in ["ldmWgt", "knlOrder", "knlWidth", "knlEps"]:
+        R.scalar(spec[k])
+    mv = np.asarray(spec["modVec"], dtype=np.float64)
+    R.gpu(np.stack([mv[0::2], mv[1::2]]), np.float64)       # d_modMat = reshape(h_modVec, 2, [])': L x 2
+    R.host(spec["spdLyrVec"])                                # per-layer diffusivities
+    R.host(spec["ynkActPrmVec"]); R.host(spec["reaActPrmVec"])
+    for k in ["btmWgt", "timeStp", "timeNum", "cgItrMax", "cgTolSqu"]:
+        R.scalar(spec[k])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_isotropic_gateways_match_forward(gateways, dim):
+    """The isotropic gateways give sa_forward's results bit for bit (same solves), and the oracle's to 1e-10."""
+    torch = pytest.importorskip("torch")
+    from oracle.oracle import Problem
+    from shape_atrophy_gb300 import api
+    spec, tv = _layered_case(dim)
+    N, T = spec["lmkIniMat"].shape[1], int(spec["timeNum"])
+    want = api.forward(spec, tv, trajectory=True, objective=True)
+    assert want["info"]["status"] == 0
+
+    lib = gateways[("deformation", dim, "isotropic")]
+    R = _Rhs(lib, torch)
+    _common_head(R, spec, tv)                                # prhs[0..12]
+    _isotropic_middle(R, spec)                               # prhs[13]
+    _isotropic_tail(R, spec)                                 # prhs[14..26]
+    assert len(R.ptrs) == 27
+    p = _call(lib, R, 3)
+    lmk = _take(lib, p[0], N * dim * T).reshape(T, dim, N)
+    tau = _take(lib, p[1], N * T).reshape(T, N)
+    obj = _take(lib, p[2], tv.shape[0])
+    np.testing.assert_array_equal(lmk, want["lmkStk"])
+    np.testing.assert_array_equal(tau, want["tauMat"])
+    assert np.all(obj == 0.0)
+
+    lib = gateways[("computeObjfcn", dim, "isotropic")]
+    R = _Rhs(lib, torch)
+    _common_head(R, spec, tv)                                # prhs[0..12]
+    _isotropic_middle(R, spec)                               # prhs[13]
+    R.gpu(spec["elmObj"]["vfdVtxMat"], np.int32)             # prhs[14]
+    cen, udir, vol = spec["tgt"]
+    R.gpu(cen, np.float64); R.gpu(udir, np.float64); R.gpu(vol, np.float64)   # prhs[15..17]
+    ck, cw, dk, dw = spec["vfd"]
+    R.scalar(ord(ck)); R.scalar(cw); R.scalar(ord(dk)); R.scalar(dw)          # prhs[18..21]
+    _isotropic_tail(R, spec)                                 # prhs[22..34]
+    assert len(R.ptrs) == 35
+    p = _call(lib, R, 1)
+    obj = _take(lib, p[0], tv.shape[0])
+    np.testing.assert_array_equal(obj, want["obj"])
+    P = Problem(spec)
+    for k in range(tv.shape[0]):
+        r = P.forward(tv[k], with_obj=True)
+        assert abs(obj[k] - r["obj"]) <= 1e-10 * abs(r["obj"])
+    assert np.abs(lmk - r["lmkStk"]).max() <= 1e-10 * np.abs(r["lmkStk"]).max()
+
+
+def test_isotropic_gateway_rejects_bad_layer_table(gateways):
+    """modMat must be lyrNum x 2 with lyrNum diffusivities: a mismatch is a MEX error, not a fault."""
+    torch = pytest.importorskip("torch")
+    spec, tv = _layered_case(2)
+    lib = gateways[("deformation", 2, "isotropic")]
+    R = _Rhs(lib, torch)
+    _common_head(R, spec, tv)
+    _isotropic_middle(R, spec)
+    for k in ["ldmWgt", "knlOrder", "knlWidth", "knlEps"]:
+        R.scalar(spec[k])
+    mv = np.asarray(spec["modVec"], dtype=np.float64)
+    R.gpu(np.stack([mv[0::2], mv[1::2]]), np.float64)
+    R.host(spec["spdLyrVec"][:-1])                           # one diffusivity short
+    R.host(spec["ynkActPrmVec"]); R.host(spec["reaActPrmVec"])
+    for k in ["btmWgt", "timeStp", "timeNum", "cgItrMax", "cgTolSqu"]:
+        R.scalar(spec[k])
+    torch.cuda.synchronize()
+    plhs = (C.c_void_p * 3)()
+    prhs = (C.c_void_p * len(R.ptrs))(*R.ptrs)
+    err = C.create_string_buffer(1024)
+    rc = lib.stub_call(3, plhs, len(R.ptrs), prhs, err, 1024)
+    for p in R.ptrs:
+        lib.stub_free(p)
+    assert rc != 0 and b"lyrNum" in err.value

@@ -68,3 +68,22 @@ def test_adjacency_mismatch_rejected(spec):
         a[1, 100] = (a[1, 100] + E // 2) % E                   # an element of another layer
     with pytest.raises(RuntimeError, match="vtxElmMat entry does not match"):
         _run(spec, "vtxElmMat", m)
+
+
+@pytest.mark.parametrize("vfd", [("M", 0.0, "B", 1.0), ("G", float("nan"), "B", 1.0), ("G", 0.1, "O", 0.0),
+                                 ("G", 0.1, "U", -1.0)])
+def test_bad_kernel_width_rejected(spec, vfd):
+    """A varifold width that divides must be finite and > 0 (the forward objective and sa_varifold)."""
+    from shape_atrophy_gb300 import api
+    sp = dict(spec, vfd=vfd)
+    with pytest.raises(RuntimeError, match="must be finite and > 0"):
+        api.forward(sp, trajectory=False, objective=True)
+    with pytest.raises(RuntimeError, match="must be finite and > 0"):
+        api.varifold(sp, sp["lmkIniMat"])
+
+
+def test_unused_direction_width_accepted(spec):
+    """The Binet kernel does not use dirKnlWidth (2D_frame/varifold.cu:91-120): any value passes."""
+    from shape_atrophy_gb300 import api
+    sp = dict(spec, vfd=("M", 0.08, "B", 0.0))
+    assert np.isfinite(api.varifold(sp, sp["lmkIniMat"]))

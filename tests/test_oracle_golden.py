@@ -49,3 +49,24 @@ def test_reference_runs_here_when_available():
     lmk, tau, _ = refmod.deformation(spec, ref["tauVarMat"])
     np.testing.assert_array_equal(lmk, ref["lmkStk"])
     np.testing.assert_array_equal(tau, ref["tauMat"])
+
+
+@pytest.mark.parametrize("name", ["frame2d_matern2", "frame3d_matern3", "annulus", "shell"])
+def test_timing_build_equals_parity_build(name):
+    """The -O3 -march=native build (CPU baseline timing, large parity cases) gives the parity build's results
+    bit for bit: both compile with -ffp-contract=off and gcc reorders no FP64 operation at -O3."""
+    from shape_atrophy_gb300 import problems
+    if name == "annulus":
+        spec, tv = problems.annulus_layered(angNum=48, radNum=7, steps=6), None
+    elif name == "shell":
+        spec, tv = problems.shell_layered(level=2, lyrCntNum=4, steps=4), None
+    else:
+        spec, ref = load(name)
+        tv = ref["tauVarMat"][-1]
+    tv = spec["tauVarVec"] if tv is None else tv
+    a = Problem(spec).forward(tv, with_obj=True)
+    b = Problem(spec, fast=True).forward(tv, with_obj=True)
+    np.testing.assert_array_equal(a["lmkStk"], b["lmkStk"])
+    np.testing.assert_array_equal(a["tauMat"], b["tauMat"])
+    assert a["obj"] == b["obj"]
+    assert a["stepSec"].shape == (spec["timeNum"] - 1,) and np.all(a["stepSec"] > 0)

@@ -65,3 +65,20 @@ def test_noalloc_matches_allocating_entry(dim):
     rc = fn(dim, N, h.ctypes.data, Vd, v_d.data_ptr(), Vt, c_d.data_ptr(), u_d.data_ptr(), w_d.data_ptr(),
             b"G", 0.4, b"B", 1.0, None, C.byref(out))
     assert rc == SA_ERR_ARG
+    # a zero centre width: rejected before any launch
+    rc = fn(dim, N, x_d.data_ptr(), Vd, v_d.data_ptr(), Vt, c_d.data_ptr(), u_d.data_ptr(), w_d.data_ptr(),
+            b"G", 0.0, b"B", 1.0, None, C.byref(out))
+    assert rc == SA_ERR_ARG
+    # a node index equal to N (one past the end, e.g. a 1-based index): found on the device, no read made
+    bad = np.array(spec["elmObj"]["vfdVtxMat"], dtype=np.int32, copy=True)
+    bad[0, Vd // 2] = N
+    b_d = _device(torch, bad, torch.int32)
+    torch.cuda.synchronize()
+    rc = fn(dim, N, x_d.data_ptr(), Vd, b_d.data_ptr(), Vt, c_d.data_ptr(), u_d.data_ptr(), w_d.data_ptr(),
+            b"G", 0.4, b"B", 1.0, None, C.byref(out))
+    assert rc == SA_ERR_ARG
+    # the next valid call is unaffected by the rejected one
+    out = C.c_double(0.0)
+    rc = fn(dim, N, x_d.data_ptr(), Vd, v_d.data_ptr(), Vt, c_d.data_ptr(), u_d.data_ptr(), w_d.data_ptr(),
+            b"G", 0.4, b"B", 1.0, None, C.byref(out))
+    assert rc == SA_OK and abs(out.value - want) <= 1e-12 * abs(want)
