@@ -537,10 +537,17 @@ def main():
         fl = k_flops / k_cnt / avg_launch_s / 1e12
         fp64 = args.precision == "fp64"
         pk = api.fma_peak(fp64=fp64, device=local)
+        sms = api.device_name(local)[1]
+        # the pipe's rate per SM clock (clock64 in the FMA loop) at the SM clock sampled during the timed steps
+        mhz = (clocks or {}).get("sm_mhz") or pk["sm_mhz"]
+        peak_at_clock = pk["flops_per_clock_sm"] * sms * mhz * 1e6 / 1e12
         roofline["fp64_pipe" if fp64 else "fp32_pipe"] = {
-            "achieved_tflops": fl, "peak_tflops": pk, "frac": fl / pk,
+            "achieved_tflops": fl, "peak_tflops": peak_at_clock, "frac": fl / peak_at_clock,
+            "peak_flops_per_clock_sm": pk["flops_per_clock_sm"], "peak_clock_mhz": mhz,
+            "fma_loop_tflops": pk["tflops"], "fma_loop_sm_mhz": pk["sm_mhz"],
             "peak_source": "measured in this run: sa_selftest_fma_peak (8 independent FMA chains per thread, "
-                           "8 x 256-thread CTAs per SM, best of 3 CUDA-event-timed launches)",
+                           "8 x 256-thread CTAs per SM, best of 3 launches), flops per SM clock (clock64) x SMs x "
+                           "the SM clock sampled during the timed steps",
             "flops_model": "2 x (9 x operator slots + 8 x rows) per CG iteration (assembled 3x3 blocks)"}
 
     e2e = None

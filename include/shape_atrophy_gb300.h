@@ -347,11 +347,14 @@ int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs
  * sqrt(x[k]), both evaluated on the device. */
 int sa_selftest_math(sa_context *ctx, int fn, long n, const double *x, double *y, double *yref);
 
-/* FMA throughput of the device's FP64 (fp64 = 1) or FP32 (fp64 = 0) pipe in
- * TFLOP/s (no reference counterpart): eight independent FMA chains per
- * thread, 8 CTAs of 256 threads per SM, best of three timed launches after a
- * warm-up.  The denominator of the pipe fractions the benchmark reports. */
-int sa_selftest_fma_peak(sa_context *ctx, int fp64, double *tflops);
+/* FMA throughput of the device's FP64 (fp64 = 1) or FP32 (fp64 = 0) pipe
+ * (no reference counterpart): eight independent FMA chains per thread, 8
+ * CTAs of 256 threads per SM, best of three timed launches after a warm-up.
+ * *tflops: TFLOP/s by CUDA events; *flopsPerClockSm (optional): flops per SM
+ * clock cycle (clock64 inside the kernel), independent of the clock the
+ * launch ran at; *smMhz (optional): that clock.  The denominator of the
+ * pipe fractions the benchmark reports. */
+int sa_selftest_fma_peak(sa_context *ctx, int fp64, double *tflops, double *flopsPerClockSm, double *smMhz);
 
 /* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and
  * deformation_3D_frame (dim 3): arguments in prhs order

@@ -167,5 +167,19 @@ def build(force: bool = False, jobs: int = 8) -> list:
     return libs
 
 
+def build_ops(force: bool = False) -> str:
+    """oracle/_ref/libref_ops_2D.so: oracle/ref_ops.cpp (single-operator entry points) linked against the
+    reference's 2D library built above."""
+    build()
+    lib = os.path.join(OUT, "libref_ops_2D.so")
+    src = os.path.join(HERE, "ref_ops.cpp")
+    if os.path.exists(lib) and not force and os.path.getmtime(lib) >= os.path.getmtime(src):
+        return lib
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", src,
+                           "-L", OUT, "-lref_deformation_2D_frame", f"-Wl,-rpath,{OUT}", "-o", lib + ".tmp"])
+    os.replace(lib + ".tmp", lib)
+    return lib
+
+
 if __name__ == "__main__":
     print("\n".join(build(force="--force" in sys.argv)))

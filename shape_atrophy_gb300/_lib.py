@@ -125,7 +125,7 @@ def load():
     lib.sa_get_tuning.argtypes = [C.c_char_p, _ip]
     lib.sa_device_name.argtypes = [C.c_int, C.c_char_p, C.c_int, _ip]
     lib.sa_selftest_math.argtypes = [vp, C.c_int, C.c_long, _dp, _dp, _dp]
-    lib.sa_selftest_fma_peak.argtypes = [vp, C.c_int, _dp]
+    lib.sa_selftest_fma_peak.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     _LIB = lib
     return lib
 

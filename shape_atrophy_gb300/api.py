@@ -89,12 +89,14 @@ def apply_tuning(device: int = 0, path: str = TUNING_FILE):
     return e
 
 
-def fma_peak(fp64: bool = True, device: int = 0) -> float:
-    """Measured FMA throughput (TFLOP/s) of the device's FP64 or FP32 pipe (sa_selftest_fma_peak)."""
+def fma_peak(fp64: bool = True, device: int = 0) -> dict:
+    """Measured FMA throughput of the device's FP64 or FP32 pipe (sa_selftest_fma_peak):
+    dict(tflops, flops_per_clock_sm, sm_mhz)."""
     ctx = context(device)
-    v = C.c_double()
-    ctx.check(ctx.lib.sa_selftest_fma_peak(ctx.h, 1 if fp64 else 0, C.byref(v)), "sa_selftest_fma_peak")
-    return v.value
+    v, pc, mhz = C.c_double(), C.c_double(), C.c_double()
+    ctx.check(ctx.lib.sa_selftest_fma_peak(ctx.h, 1 if fp64 else 0, C.byref(v), C.byref(pc), C.byref(mhz)),
+              "sa_selftest_fma_peak")
+    return {"tflops": v.value, "flops_per_clock_sm": pc.value, "sm_mhz": mhz.value}
 
 
 # Layered model: where each step's velocity CG starts -- the polynomial through the last k + 1 velocities,

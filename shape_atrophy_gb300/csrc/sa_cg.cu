@@ -1099,10 +1099,15 @@ int barrier_selftest(cudaStream_t s, int *ctasGaveUp, int *abortFlag)
 // FMA throughput of the FP64 or FP32 pipe: 8 independent FMA chains per
 // thread, 8 CTAs of 256 threads per SM.  The denominators of the pipe
 // fractions the benchmark reports (measured on the same GPU in the same run).
+// Each CTA also records its SM clock cycles and nanoseconds, so the rate is
+// reported per SM clock as well (independent of the clock it ran at).
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_fma_peak(int iters, T a, T b, T *sink)
+__global__ void __launch_bounds__(256) k_fma_peak(int iters, T a, T b, long long *stamps)
 {
+	__syncthreads();
+	const long long c0 = clock64();
+	const unsigned long long t0 = global_ns();
 	T x[8];
 	for (int k = 0; k < 8; ++k) x[k] = (T) (threadIdx.x + k) * (T) 1e-3;
 	for (int i = 0; i < iters; ++i) {
@@ -1110,38 +1115,57 @@ __global__ void __launch_bounds__(256) k_fma_peak(int iters, T a, T b, T *sink)
 		for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
 	}
 	T t = x[0] + x[1] + x[2] + x[3] + x[4] + x[5] + x[6] + x[7];
-	if (t == (T) -1) sink[blockIdx.x] = t;        // never true (x stays in (0, 1]); keeps the chains live
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		stamps[2 * blockIdx.x] = clock64() - c0;
+		stamps[2 * blockIdx.x + 1] = (long long) (global_ns() - t0);
+	}
+	if (t == (T) -1) stamps[0] = 0;              // never true (x stays in (0, 1]); keeps the chains live
 }
 
-int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops)
+int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops, double *flopsPerClockSm, double *mhz)
 {
 	int dev = 0, sms = 0;
 	SA_CHECK(cudaGetDevice(&dev));
 	SA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 	const int nt = 256, nb = 8 * sms;
 	const int iters = fp64 ? 12000 : 600000;              // ~50 ms per launch on GB300
-	void *sink = nullptr;
-	SA_CHECK(cudaMallocAsync(&sink, sizeof(double) * nb, s));
+	long long *stamps = nullptr;
+	SA_CHECK(cudaMallocAsync(&stamps, sizeof(long long) * 2 * nb, s));
+	std::vector<long long> h((size_t) 2 * nb);
 	cudaEvent_t e0, e1;
 	SA_CHECK(cudaEventCreate(&e0));
 	SA_CHECK(cudaEventCreate(&e1));
-	double best = 0.0;
+	double best = 0.0, bestClk = 0.0, bestMhz = 0.0;
 	for (int rep = 0; rep < 4; ++rep) {                   // first launch is a warm-up
 		SA_CHECK(cudaEventRecord(e0, s));
-		if (fp64) k_fma_peak<double><<<nb, nt, 0, s>>>(iters, 0.9999999, 1e-7, (double *) sink);
-		else k_fma_peak<float><<<nb, nt, 0, s>>>(iters, 0.9999f, 1e-4f, (float *) sink);
+		if (fp64) k_fma_peak<double><<<nb, nt, 0, s>>>(iters, 0.9999999, 1e-7, stamps);
+		else k_fma_peak<float><<<nb, nt, 0, s>>>(iters, 0.9999f, 1e-4f, stamps);
 		SA_CHECK(cudaEventRecord(e1, s));
 		SA_CHECK(cudaEventSynchronize(e1));
 		float ms = 0.f;
 		SA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
-		double fl = 2.0 * 8.0 * (double) iters * (double) nt * nb;
-		if (rep > 0) best = std::max(best, fl / (ms * 1e-3) / 1e12);
+		SA_CHECK(cudaMemcpy(h.data(), stamps, sizeof(long long) * 2 * nb, cudaMemcpyDeviceToHost));
+		double cyc = 0.0, ns = 0.0;
+		for (int b = 0; b < nb; ++b) { cyc += (double) h[2 * b]; ns += (double) h[2 * b + 1]; }
+		cyc /= nb;
+		ns /= nb;
+		const double fl = 2.0 * 8.0 * (double) iters * (double) nt * nb;
+		// 8 resident CTAs per SM run side by side: per SM, 8 CTAs' flops in one CTA's cycles
+		const double perClk = fl / sms / cyc;
+		if (rep > 0 && fl / (ms * 1e-3) / 1e12 > best) {
+			best = fl / (ms * 1e-3) / 1e12;
+			bestClk = perClk;
+			bestMhz = ns > 0.0 ? cyc / ns * 1e3 : 0.0;
+		}
 	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
-	SA_CHECK(cudaFreeAsync(sink, s));
+	SA_CHECK(cudaFreeAsync(stamps, s));
 	SA_CHECK(cudaStreamSynchronize(s));
 	*tflops = best;
+	if (flopsPerClockSm) *flopsPerClockSm = bestClk;
+	if (mhz) *mhz = bestMhz;
 	return SA_OK;
 }
 

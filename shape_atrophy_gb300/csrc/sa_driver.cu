@@ -2268,10 +2268,12 @@ int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs
 	});
 }
 
-int sa_selftest_fma_peak(sa_context *ctx, int fp64, double *tflops)
+int sa_selftest_fma_peak(sa_context *ctx, int fp64, double *tflops, double *flopsPerClockSm, double *smMhz)
 {
 	if (!tflops) return SA_ERR_ARG;
-	return sa::guarded(ctx, [&]() { return sa::fma_peak_selftest(ctx->stream, fp64 ? 1 : 0, tflops); });
+	return sa::guarded(ctx, [&]() {
+		return sa::fma_peak_selftest(ctx->stream, fp64 ? 1 : 0, tflops, flopsPerClockSm, smMhz);
+	});
 }
 
 int sa_selftest_math(sa_context *ctx, int fn, long n, const double *x, double *y, double *yref)

@@ -420,7 +420,7 @@ template <int B> void cg_finish_fp64(const Mesh &m, double *x, CgWork &w, cudaSt
 CgState cg_state(const CgWork &w, cudaStream_t s);
 // bounded grid wait self-test: CTAs that gave up, and the abort flag they left
 int barrier_selftest(cudaStream_t s, int *ctasGaveUp, int *abortFlag);
-int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops);
+int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops, double *flopsPerClockSm, double *mhz);
 
 // frame mode K-preconditioned CG (2D/ipcg.cu:11-100) with dense K
 struct KpcgWork {
