@@ -10,7 +10,8 @@ SCALARS = ["dim", "ldmWgt", "knlOrder", "knlWidth", "knlEps", "spdTanVal", "spdT
 
 
 def names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """The whole-model frame cases (frame2d_*, frame3d_*); other fixtures have their own layout."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "frame*.npz")))
 
 
 def load(name: str):
