@@ -438,9 +438,10 @@ def main():
     ap.add_argument("--no-gradient", action="store_true", help="skip the objective-gradient leg")
     ap.add_argument("--oracle-steps", type=int, default=20,
                     help="steps of the CPU oracle run (mixed-error reference and CPU baseline)")
-    ap.add_argument("--served-requests", type=int, default=32)
-    ap.add_argument("--served-full", action="store_true",
-                    help="served stream over the whole served range (levels 3-6, 20-100 steps; minutes)")
+    ap.add_argument("--served-requests", type=int, default=None,
+                    help="length of the served stream (default 24 over the whole range, 32 with --served-short)")
+    ap.add_argument("--served-short", action="store_true",
+                    help="served stream over icosphere levels 3-5 and 20-60 steps instead of the whole served range")
     args = ap.parse_args()
     rank, local, ws, dist = dist_init()
     if args.impl == "reference":
@@ -569,7 +570,8 @@ def main():
 
     served = None
     if not args.no_served and rank == 0 and args.workload == "shell":
-        served = served_leg(local, args.served_requests, full=args.served_full)
+        n_req = args.served_requests or (32 if args.served_short else 24)
+        served = served_leg(local, n_req, full=not args.served_short)
     batched = None
     if not args.no_batched and rank == 0 and args.workload == "shell":
         batched = batched_leg(local, args.batched_requests)

@@ -509,6 +509,7 @@ struct Work {
 	double *v, *b, *pd, *blk, *dinv, *fy, *fr;
 	double *vHist = nullptr;    // velocities of earlier steps (extrapolated CG start), velocityGuess x n
 	double *Mnow, *Mnxt, *L, *dinvRd, *rhs;
+	float *L32 = nullptr, *rdInv32 = nullptr;   // mixed precision: FP32 copy of L and of its inverse diagonal
 	Geom g0, g1;
 	CgWork cw;
 	KpcgWork kw;
@@ -551,6 +552,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 		c.blk32 = P.alloc<float>((size_t) T * sell_vals<D>());
 		c.binv32 = P.alloc<float>((size_t) N * D * D);
 		c.f32 = P.alloc<float>((size_t) 7 * n);
+		if (!md.frame) { w.L32 = P.zeros<float>(T); w.rdInv32 = P.alloc<float>(N); }
 	}
 	bool useK = md.frame || md.ldmWgt != 0.0;
 	if (useK) {
@@ -661,6 +663,32 @@ struct Stepper {
 		++t;
 	}
 
+	// Mixed precision (layered model): the reaction-diffusion solve as the velocity solve, FP32 operator and
+	// FP32 inner CG with FP64 dot products inside FP64 iterative refinement whose residual b - L tau uses the
+	// FP64 operator.  The FP32 copies of L and of its inverse diagonal (the 1 x 1 block inverses of the inner
+	// solve) replace the velocity's FP32 operator in the CG work for this solve only.
+	int rd_mixed(int *rits)
+	{
+		k_to_f32<<<grid_for(m.slTotal), kBlock, 0, s>>>(m.slTotal, w.L, w.L32);
+		k_to_f32<<<grid_for(m.N), kBlock, 0, s>>>(m.N, w.dinvRd, w.rdInv32);
+		w.cw.launches += 2;
+		float *blk32 = w.cw.blk32, *binv32 = w.cw.binv32;
+		w.cw.blk32 = w.L32;
+		w.cw.binv32 = w.rdInv32;
+		int code;
+		try {
+			code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, st, rits, s,
+			                    SA_PREC_MIXED);
+		} catch (...) {
+			w.cw.blk32 = blk32;
+			w.cw.binv32 = binv32;
+			throw;
+		}
+		w.cw.blk32 = blk32;
+		w.cw.binv32 = binv32;
+		return code;
+	}
+
 	// returns the number of steps taken; stops early at timeNum - 1 or on a failed solve
 	int step(int nsteps)
 	{
@@ -681,8 +709,9 @@ struct Stepper {
 			if (code != SA_OK) { out.status = code; break; }
 			post_velocity();
 			int rits = 0;
-			code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, st, &rits, s,
-			                    SA_PREC_FP64);
+			code = w.L32 ? rd_mixed(&rits)
+			             : cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, st,
+			                            &rits, s, SA_PREC_FP64);
 			out.rdTotal += rits;
 			if (code != SA_OK) { out.status = code; break; }
 			end_step();
@@ -1333,6 +1362,8 @@ static size_t estimate_bytes(const Request &r)
 	return 4 * ints + 8 * dbl + (1 << 20);
 }
 
+enum { kMixedVelocity = 0, kMixedRd = 1 };
+
 struct InstBase {
 	Request *req = nullptr;
 	size_t bytes = 0;
@@ -1353,11 +1384,14 @@ struct InstBase {
 	virtual void prepare_velocity_fp64() = 0;
 	virtual void finish_velocity_fp64() = 0;
 	virtual BatchSolve velocity_fp64() = 0;
-	virtual void mixed_outer(int first) = 0;
-	virtual void mixed_inner() = 0;
-	virtual BatchSolve velocity_mixed() = 0;
-	virtual void mixed_apply() = 0;
-	virtual void zero_velocity() = 0;
+	// mixed precision, for the solve `kind` of the step (kMixedVelocity: B = dim, kMixedRd: B = 1): FP64
+	// residual and outer test, FP32 inner solve (batched), FP64 update
+	virtual void mixed_outer(int kind, int first) = 0;
+	virtual void mixed_inner(int kind) = 0;
+	virtual BatchSolve mixed_solve(int kind) = 0;
+	virtual void mixed_apply(int kind) = 0;
+	virtual void mixed_zero(int kind) = 0;
+	virtual void post_velocity() = 0;
 	virtual void prepare_rd() = 0;
 	virtual BatchSolve rd_solve() = 0;
 	virtual void finish_rd() = 0;
@@ -1412,18 +1446,57 @@ struct Inst : InstBase {
 	}
 	void finish_velocity_fp64() override { cg_finish_fp64<D>(m, w.v, w.cw, s); }
 	BatchSolve velocity_fp64() override { return BatchSolve{&m, &w.cw, w.blk, w.dinv, w.v, nullptr}; }
-	void mixed_outer(int first) override { cg_mixed_outer<D>(m, w.blk, w.dinv, w.b, w.v, bb, first, w.cw, s); }
-	void mixed_inner() override { cg_mixed_inner<D>(m, md.cgItrMax - mixedTotal, innerTol, w.cw, s); }
-	BatchSolve velocity_mixed() override
+	void mixed_outer(int kind, int first) override
 	{
-		long n = (long) m.N * D;
-		return BatchSolve{&m, &w.cw, w.cw.blk32, w.cw.f32 + 5 * n, w.cw.f32 + 6 * n, w.cw.binv32};
+		if (kind == kMixedVelocity) {
+			cg_mixed_outer<D>(m, w.blk, w.dinv, w.b, w.v, bb, first, w.cw, s);
+			return;
+		}
+		if (first) {                         // FP32 copies of L and of its inverse diagonal
+			k_to_f32<<<grid_for(m.slTotal), kBlock, 0, s>>>(m.slTotal, w.L, w.L32);
+			k_to_f32<<<grid_for(m.N), kBlock, 0, s>>>(m.N, w.dinvRd, w.rdInv32);
+			w.cw.launches += 2;
+		}
+		cg_mixed_outer<1>(m, w.L, w.dinvRd, w.rhs, st.tau_next(), bb, first, w.cw, s);
 	}
-	void mixed_apply() override { cg_mixed_apply((long) m.N * D, w.v, w.cw, s); }
-	void zero_velocity() override { SA_CHECK(cudaMemsetAsync(w.v, 0, sizeof(double) * m.N * D, s)); }
+	void mixed_inner(int kind) override
+	{
+		if (kind == kMixedVelocity) {
+			cg_mixed_inner<D>(m, md.cgItrMax - mixedTotal, innerTol, w.cw, s);
+			return;
+		}
+		float *binv32 = w.cw.binv32;          // the inner solve's 1 x 1 block inverses: L's inverse diagonal
+		w.cw.binv32 = w.rdInv32;
+		try {
+			cg_mixed_inner<1>(m, md.rdItrMax - mixedTotal, innerTol, w.cw, s);
+		} catch (...) {
+			w.cw.binv32 = binv32;
+			throw;
+		}
+		w.cw.binv32 = binv32;
+	}
+	BatchSolve mixed_solve(int kind) override
+	{
+		if (kind == kMixedVelocity) {
+			long n = (long) m.N * D;
+			return BatchSolve{&m, &w.cw, w.cw.blk32, w.cw.f32 + 5 * n, w.cw.f32 + 6 * n, w.cw.binv32};
+		}
+		long n = m.N;
+		return BatchSolve{&m, &w.cw, w.L32, w.cw.f32 + 5 * n, w.cw.f32 + 6 * n, w.rdInv32};
+	}
+	void mixed_apply(int kind) override
+	{
+		if (kind == kMixedVelocity) cg_mixed_apply((long) m.N * D, w.v, w.cw, s);
+		else cg_mixed_apply((long) m.N, st.tau_next(), w.cw, s);
+	}
+	void mixed_zero(int kind) override
+	{
+		if (kind == kMixedVelocity) SA_CHECK(cudaMemsetAsync(w.v, 0, sizeof(double) * m.N * D, s));
+		else SA_CHECK(cudaMemsetAsync(st.tau_next(), 0, sizeof(double) * m.N, s));
+	}
+	void post_velocity() override { st.post_velocity(); }
 	void prepare_rd() override
 	{
-		st.post_velocity();
 		cg_prepare_fp64<1>(m, w.L, w.dinvRd, w.rhs, st.tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, s);
 	}
 	BatchSolve rd_solve() override { return BatchSolve{&m, &w.cw, w.L, w.dinvRd, st.tau_next(), nullptr}; }
@@ -1491,7 +1564,7 @@ struct Server {
 	// bookkeeping) and batched CG launches, printed when the server is destroyed
 	bool trace = std::getenv("SA_TRACE") != nullptr;
 	double phaseMs[5] = {0, 0, 0, 0, 0};
-	long long batchLaunches[3] = {0, 0, 0};
+	long long batchLaunches[4] = {0, 0, 0, 0};   // FP64 velocity, FP32 velocity, FP64 RD, FP32 RD
 	std::chrono::steady_clock::time_point tMark;
 	void mark(int phase)
 	{
@@ -1525,9 +1598,9 @@ struct Server {
 			std::fprintf(stderr,
 			             "[sa_trace] server: %lld ticks; ms in element kernels %.1f, FP64 velocity %.1f, mixed "
 			             "velocity %.1f, reaction-diffusion %.1f, bookkeeping %.1f; batched CG launches FP64 %lld, "
-			             "FP32 %lld, RD %lld\n",
+			             "FP32 %lld, RD FP64 %lld, RD FP32 %lld\n",
 			             ticks, phaseMs[0], phaseMs[1], phaseMs[2], phaseMs[3], phaseMs[4], batchLaunches[0],
-			             batchLaunches[1], batchLaunches[2]);
+			             batchLaunches[1], batchLaunches[2], batchLaunches[3]);
 		cudaSetDevice(ctx->device);
 		if (devJobs) cudaFree(devJobs);
 		if (s) cudaStreamDestroy(s);
@@ -1546,6 +1619,51 @@ struct Server {
 	// mixed precision are latency bound, so their length follows their iteration count: they are ordered
 	// longest first, so that long solves share launches.  The FP64 solves are FP64-pipe bound and keep
 	// arrival order (measured faster on the served stream).  Results do not depend on the order.
+	// Mixed precision: FP64 iterative refinement of one solve of every instance in g (all of dimension B's
+	// kind), each refinement round one batched FP32 launch over the instances still refining.  Leaves each
+	// instance's FP32 iterations in mixedTotal; failed instances are marked.
+	void refine_mixed(std::vector<InstBase *> g, int kind, int B)
+	{
+		for (InstBase *in : g) { in->bb = -1.0; in->mixedTotal = 0; in->mixedDone = 0; }
+		for (int outer = 0; outer < 64 && !g.empty(); ++outer) {
+			for (InstBase *in : g) in->mixed_outer(kind, outer == 0);
+			std::vector<InstBase *> inner;
+			for (InstBase *in : g) {
+				CgState c = cg_state(in->cg(), s);
+				const Model &md = in->model();
+				const double tolSqu = kind == kMixedVelocity ? md.cgTolSqu : md.rdTolSqu;
+				const int itrMax = kind == kMixedVelocity ? md.cgItrMax : md.rdItrMax;
+				if (in->bb < 0.0) in->bb = c.bb;
+				if (c.code == SA_ERR_NONFINITE) { fail(*in, SA_ERR_NONFINITE); continue; }
+				if (c.zero) { in->mixed_zero(kind); continue; }
+				if (c.rr < tolSqu * in->bb) continue;
+				if (in->mixedTotal >= itrMax) { fail(*in, SA_ERR_NOT_CONVERGED); continue; }
+				double need = 0.01 * tolSqu * in->bb / c.rr;
+				const double floorSqu = std::pow(10.0, -(double) tuning().mixedInnerFloor);
+				in->innerTol = need > floorSqu ? need : floorSqu;
+				inner.push_back(in);
+			}
+			if (inner.empty()) break;
+			std::vector<BatchSolve> bs;
+			for (InstBase *in : inner) { in->mixed_inner(kind); bs.push_back(in->mixed_solve(kind)); }
+			const int li = kind == kMixedVelocity ? 1 : 3;
+			batchLaunches[li] += B == 1 ? cg_batch_run<1, float, float, float>(bs, smCount, devJobs, kMaxJobs, s)
+			                   : B == 2 ? cg_batch_run<2, float, float, float>(bs, smCount, devJobs, kMaxJobs, s)
+			                            : cg_batch_run<3, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
+			std::vector<InstBase *> next;
+			for (InstBase *in : inner) {
+				CgState c = cg_state(in->cg(), s);
+				in->mixedTotal += c.iters;
+				if (c.code == SA_ERR_NONFINITE) { fail(*in, SA_ERR_NONFINITE); continue; }
+				in->mixed_apply(kind);
+				next.push_back(in);
+			}
+			g.swap(next);
+			if (outer == 63)
+				for (InstBase *in : g) fail(*in, SA_ERR_NOT_CONVERGED);
+		}
+	}
+
 	void tick()
 	{
 		std::vector<InstBase *> run;
@@ -1578,47 +1696,16 @@ struct Server {
 			std::stable_sort(g.begin(), g.end(), [](const InstBase *a, const InstBase *b) {
 				return a->vel_key() > b->vel_key();
 			});
-			for (InstBase *in : g) { in->bb = -1.0; in->mixedTotal = 0; in->mixedDone = 0; }
-			for (int outer = 0; outer < 64 && !g.empty(); ++outer) {
-				for (InstBase *in : g) in->mixed_outer(outer == 0);
-				std::vector<InstBase *> inner;
-				for (InstBase *in : g) {
-					CgState c = cg_state(in->cg(), s);
-					const Model &md = in->model();
-					if (in->bb < 0.0) in->bb = c.bb;
-					if (c.code == SA_ERR_NONFINITE) { fail(*in, SA_ERR_NONFINITE); continue; }
-					if (c.zero) { in->zero_velocity(); continue; }
-					if (c.rr < md.cgTolSqu * in->bb) continue;
-					if (in->mixedTotal >= md.cgItrMax) { fail(*in, SA_ERR_NOT_CONVERGED); continue; }
-					double need = 0.01 * md.cgTolSqu * in->bb / c.rr;
-					const double floorSqu = std::pow(10.0, -(double) tuning().mixedInnerFloor);
-					in->innerTol = need > floorSqu ? need : floorSqu;
-					inner.push_back(in);
-				}
-				if (inner.empty()) break;
-				std::vector<BatchSolve> bs;
-				for (InstBase *in : inner) { in->mixed_inner(); bs.push_back(in->velocity_mixed()); }
-				batchLaunches[1] += D == 2 ? cg_batch_run<2, float, float, float>(bs, smCount, devJobs, kMaxJobs, s)
-				                           : cg_batch_run<3, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
-				std::vector<InstBase *> next;
-				for (InstBase *in : inner) {
-					CgState c = cg_state(in->cg(), s);
-					in->mixedTotal += c.iters;
-					if (c.code == SA_ERR_NONFINITE) { fail(*in, SA_ERR_NONFINITE); continue; }
-					in->mixed_apply();
-					next.push_back(in);
-				}
-				g.swap(next);
-				if (outer == 63)
-					for (InstBase *in : g) fail(*in, SA_ERR_NOT_CONVERGED);
-			}
-			for (InstBase *in : run)
-				if (in->dim() == D && in->precision() == SA_PREC_MIXED) in->its = in->mixedTotal;
+			refine_mixed(g, kMixedVelocity, D);
+			for (InstBase *in : g) in->its = in->mixedTotal;
 		}
 		mark(2);
-		// reaction-diffusion: one batched launch for every instance still running
-		std::vector<InstBase *> rd;
-		for (InstBase *in : run) if (!in->failed) rd.push_back(in);
+		for (InstBase *in : run) if (!in->failed) in->post_velocity();
+		// reaction-diffusion: one batched launch for the FP64 instances still running, the same FP64
+		// refinement around batched FP32 solves for the mixed-precision ones
+		std::vector<InstBase *> rd, rdMixed;
+		for (InstBase *in : run)
+			if (!in->failed) (in->precision() == SA_PREC_MIXED ? rdMixed : rd).push_back(in);
 		if (!rd.empty()) {
 			std::vector<BatchSolve> bs;
 			for (InstBase *in : rd) { in->prepare_rd(); bs.push_back(in->rd_solve()); }
@@ -1629,6 +1716,10 @@ struct Server {
 				in->rits = c.iters;
 				if (c.code != SA_OK) fail(*in, c.code);
 			}
+		}
+		if (!rdMixed.empty()) {
+			refine_mixed(rdMixed, kMixedRd, 1);
+			for (InstBase *in : rdMixed) in->rits = in->mixedTotal;
 		}
 		mark(3);
 		for (InstBase *in : run) {
