@@ -597,10 +597,24 @@ def main():
         t0 = time.perf_counter()
         gr = api.gradient(spec_g, device=local)
         t_grad = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ad = api.adjoint(spec_g, device=local)
+        t_adj = time.perf_counter() - t0
+        D_, N_ = int(spec_g["dim"]), spec_g["lmkIniMat"].shape[1]
+        n_bump, n_all = D_ + 2, D_ + 2 + ad["grad_layer"].size + N_ + D_ * N_
+        per_param = (t_grad - t_fwd) / n_bump            # the tangent model's cost per parameter
         gradient = {"what": f"sa_objective_gradient ({K} steps, objective and d obj / d [c, h, sigma], "
-                            "tangent-linear model of every step) beside one sa_forward of the same steps",
+                            "tangent-linear model of every step) and sa_objective_adjoint (discrete adjoint: the "
+                            "same and per-layer lambda, mu, D, every node's initial concentration and position) "
+                            "beside one sa_forward of the same steps",
                     "params": int(gr["grad"].size), "s": t_grad, "forward_s": t_fwd, "vs_forward": t_grad / t_fwd,
-                    "status": gr["info"]["status"]}
+                    "status": gr["info"]["status"],
+                    "adjoint": {"s": t_adj, "vs_forward": t_adj / t_fwd, "params": int(n_all),
+                                "status": ad["info"]["status"],
+                                "bump_grad_vs_tangent_max_rel": float(np.abs(ad["grad"] - gr["grad"]).max() /
+                                                                      np.abs(gr["grad"]).max())},
+                    "tangent_at_20_params_s_extrapolated": t_fwd + 20 * per_param,
+                    "tangent_at_all_adjoint_params_s_extrapolated": t_fwd + n_all * per_param}
 
     cpu = None
     if not args.no_cpu and rank == 0 and ws == 1:

@@ -181,6 +181,29 @@ int sa_objective_gradient(sa_context *ctx, const sa_element_object *obj, const d
                           const sa_params *prm, const sa_target *tgt, const double *tauVarVec, int tauVarNum,
                           double *objOut, double *gradOut, sa_solve_info *info);
 
+/* Objective and its gradient by the discrete adjoint (no reference
+ * counterpart).  Layered model, one parameter vector [c (dim), h, sigma]:
+ * the forward solve keeps the trajectory and the velocities on the device
+ * (N x dim x timeNum doubles twice), then one backward sweep solves two
+ * adjoint systems per step (the forward operators are symmetric: the same
+ * Jacobi-PCG, FP64) and accumulates the gradient with respect to every
+ * parameter at once, at about twice the cost of a forward solve whatever the
+ * parameter count:
+ *   gradBump  (dim + 2, optional): dJ/d[c, h, sigma], as sa_objective_gradient;
+ *   gradLayer (3 x lyrNum, optional): dJ/d(lambda_l, mu_l, D_l) per material
+ *             layer, in that order per layer;
+ *   gradTau0  (N, optional): dJ/dtau_0 at every node (the initial
+ *             concentration as free parameters);
+ *   gradX0    (N x dim column-major, optional): dJ/d(initial node positions),
+ *             including the bump's dependence on them.
+ * prm->precision is ignored (FP64 throughout).  A failed solve gives objOut
+ * = DBL_MAX, NaN gradients and its status in info; info->cgIterMax holds the
+ * iterations of all adjoint solves.  Needs vfdIfoMat. */
+int sa_objective_adjoint(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat,
+                         const sa_params *prm, const sa_target *tgt, const double *tauVarVec, int tauVarNum,
+                         double *objOut, double *gradBump, double *gradLayer, double *gradTau0, double *gradX0,
+                         sa_solve_info *info);
+
 /* Varifold objective without any device allocation (no counterpart in the
  * reference).  For callers that must not allocate while they evaluate the
  * objective: an optimiser's line search that calls it hundreds of times on
@@ -348,12 +371,13 @@ int sa_selftest_wait_timeout(sa_context *ctx, int *ctasGaveUp, double *elapsedMs
 int sa_selftest_math(sa_context *ctx, int fn, long n, const double *x, double *y, double *yref);
 
 /* FMA throughput of the device's FP64 (fp64 = 1) or FP32 (fp64 = 0) pipe
- * (no reference counterpart): eight independent FMA chains per thread, 8
- * CTAs of 256 threads per SM, best of three timed launches after a warm-up.
- * *tflops: TFLOP/s by CUDA events; *flopsPerClockSm (optional): flops per SM
- * clock cycle (clock64 inside the kernel), independent of the clock the
- * launch ran at; *smMhz (optional): that clock.  The denominator of the
- * pipe fractions the benchmark reports. */
+ * (no reference counterpart): independent FMA chains per thread (4 or 8 in
+ * FP64, 8 or 16 in FP32), 256-thread CTAs, 2, 4 or 8 CTAs per SM, the best
+ * of two timed launches of each after a warm-up.  *tflops: TFLOP/s by CUDA
+ * events; *smMhz (optional): the SM clock during that launch (clock64 over
+ * %globaltimer in the kernel); *flopsPerClockSm (optional): the rate per SM
+ * per clock cycle, independent of the clock.  The denominator of the pipe
+ * fractions the benchmark reports. */
 int sa_selftest_fma_peak(sa_context *ctx, int fp64, double *tflops, double *flopsPerClockSm, double *smMhz);
 
 /* Drop-in for the MEX binaries deformation_2D_frame (dim 2) and

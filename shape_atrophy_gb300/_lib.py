@@ -103,6 +103,8 @@ def load():
     lib.sa_session_stream.argtypes = [vp, C.c_int, C.c_int, _dp, _dp, C.c_int, _ip, _ip]
     lib.sa_objective_gradient.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Params), C.POINTER(Target),
                                           _dp, C.c_int, _dp, _dp, C.POINTER(SolveInfo)]
+    lib.sa_objective_adjoint.argtypes = [vp, C.POINTER(ElementObject), _dp, C.POINTER(Params), C.POINTER(Target),
+                                         _dp, C.c_int, _dp, _dp, _dp, _dp, _dp, C.POINTER(SolveInfo)]
     lib.sa_session_objective.argtypes = [vp, _dp]
     lib.sa_session_info.argtypes = [vp, C.POINTER(SolveInfo)]
     lib.sa_session_profile.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]

@@ -277,6 +277,39 @@ def gradient(spec: dict, tauVarVec=None, precision: str = "fp64", device: int = 
                           tangentIters=info.cgIterMax, elapsedMs=info.elapsedMs))
 
 
+def adjoint(spec: dict, tauVarVec=None, layers: bool = True, tau0: bool = True, x0: bool = True,
+            device: int = 0) -> dict:
+    """Objective and its gradient by the discrete adjoint (sa_objective_adjoint), layered model, FP64:
+    dict(obj, grad (dim + 2: d/d[c, h, sigma]), grad_layer (lyrNum, 3: d/d(lambda, mu, D)), grad_tau0 (N,),
+    grad_x0 (D, N), info).  About twice the cost of one forward solve for all of them together."""
+    ctx = context(device)
+    D = int(spec["dim"])
+    lmk = np.ascontiguousarray(np.asarray(spec["lmkIniMat"], dtype=np.float64))
+    N = lmk.shape[1]
+    tv = np.ascontiguousarray(np.asarray(spec["tauVarVec"] if tauVarVec is None else tauVarVec,
+                                         dtype=np.float64).reshape(-1))
+    K = _Keep()
+    o = _element_object(spec["elmObj"], D, N, K, with_vfd=True, with_grad=True)
+    if "elmLyrVec" in spec:
+        o.elmLyrVec = K.i32(spec["elmLyrVec"])
+    p = _params(spec, K, "fp64")
+    t = _target(spec, K)
+    L = int(np.asarray(spec["spdLyrVec"]).size)
+    obj, gb = np.zeros(1), np.zeros(D + 2)
+    gl = np.zeros((L, 3)) if layers else None
+    gt = np.zeros(N) if tau0 else None
+    gx = np.zeros((D, N)) if x0 else None
+    info = _lib.SolveInfo()
+    ptr = lambda a: a.ctypes.data_as(_lib._dp) if a is not None else None
+    rc = ctx.lib.sa_objective_adjoint(ctx.h, C.byref(o), lmk.ctypes.data_as(_lib._dp), C.byref(p), C.byref(t),
+                                      tv.ctypes.data_as(_lib._dp), tv.size, ptr(obj), ptr(gb), ptr(gl), ptr(gt),
+                                      ptr(gx), C.byref(info))
+    ctx.check(rc, "sa_objective_adjoint")
+    return dict(obj=float(obj[0]), grad=gb, grad_layer=gl, grad_tau0=gt, grad_x0=gx,
+                info=dict(status=info.status, cgIterTotal=info.cgIterTotal, rdIterTotal=info.rdIterTotal,
+                          adjointIters=info.cgIterMax, elapsedMs=info.elapsedMs))
+
+
 def varifold(spec: dict, lmk, grad: bool = False, precision: str = "fp64", device: int = 0):
     """Varifold objective of the shape ``lmk`` (D, N) against spec['tgt'];
     with grad=True also its gradient with respect to the nodes, (D, N)."""

@@ -1096,26 +1096,26 @@ int barrier_selftest(cudaStream_t s, int *ctasGaveUp, int *abortFlag)
 }
 
 // ---------------------------------------------------------------------------
-// FMA throughput of the FP64 or FP32 pipe: 8 independent FMA chains per
-// thread, 8 CTAs of 256 threads per SM.  The denominators of the pipe
-// fractions the benchmark reports (measured on the same GPU in the same run).
-// Each CTA also records its SM clock cycles and nanoseconds, so the rate is
-// reported per SM clock as well (independent of the clock it ran at).
+// FMA throughput of the FP64 or FP32 pipe: CH independent FMA chains per
+// thread, 256-thread CTAs, a few chain counts and CTAs per SM (the best is
+// kept).  The denominators of the pipe fractions the benchmark reports
+// (measured on the same GPU in the same run).  Each CTA also records its SM
+// clock cycles and nanoseconds, which give the SM clock of the launch; the
+// rate per SM clock is the event-timed rate over SMs x that clock.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int CH>
 __global__ void __launch_bounds__(256) k_fma_peak(int iters, T a, T b, long long *stamps)
 {
-	__syncthreads();
 	const long long c0 = clock64();
 	const unsigned long long t0 = global_ns();
-	T x[8];
-	for (int k = 0; k < 8; ++k) x[k] = (T) (threadIdx.x + k) * (T) 1e-3;
+	T x[CH];
+	for (int k = 0; k < CH; ++k) x[k] = (T) (threadIdx.x + k) * (T) 1e-3;
 	for (int i = 0; i < iters; ++i) {
 #pragma unroll
-		for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+		for (int k = 0; k < CH; ++k) x[k] = fma(x[k], a, b);
 	}
-	T t = x[0] + x[1] + x[2] + x[3] + x[4] + x[5] + x[6] + x[7];
-	__syncthreads();
+	T t = x[0];
+	for (int k = 1; k < CH; ++k) t += x[k];
 	if (threadIdx.x == 0) {
 		stamps[2 * blockIdx.x] = clock64() - c0;
 		stamps[2 * blockIdx.x + 1] = (long long) (global_ns() - t0);
@@ -1123,40 +1123,51 @@ __global__ void __launch_bounds__(256) k_fma_peak(int iters, T a, T b, long long
 	if (t == (T) -1) stamps[0] = 0;              // never true (x stays in (0, 1]); keeps the chains live
 }
 
+template <typename T, int CH>
+static void fma_peak_variant(cudaStream_t s, int sms, int ctasPerSm, long long *stamps, cudaEvent_t e0,
+                             cudaEvent_t e1, double &best, double &bestMhz)
+{
+	const int nt = 256, nb = ctasPerSm * sms;
+	// ~50 ms per launch on GB300 (FP64 ~1.1 TFLOP/s, FP32 ~70 TFLOP/s)
+	const double target = sizeof(T) == 8 ? 5.5e10 : 3.5e12;
+	const int iters = (int) std::max(1.0, target / (2.0 * CH * nt * (double) nb));
+	const T a = sizeof(T) == 8 ? (T) 0.9999999 : (T) 0.9999f, b = sizeof(T) == 8 ? (T) 1e-7 : (T) 1e-4f;
+	for (int rep = 0; rep < 3; ++rep) {                   // first launch is a warm-up
+		SA_CHECK(cudaEventRecord(e0, s));
+		k_fma_peak<T, CH><<<nb, nt, 0, s>>>(iters, a, b, stamps);
+		SA_CHECK(cudaEventRecord(e1, s));
+		SA_CHECK(cudaEventSynchronize(e1));
+		float ms = 0.f;
+		SA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+		long long h[2];
+		SA_CHECK(cudaMemcpy(h, stamps, sizeof(h), cudaMemcpyDeviceToHost));
+		const double fl = 2.0 * CH * (double) iters * (double) nt * nb;
+		const double tf = fl / (ms * 1e-3) / 1e12;
+		if (rep > 0 && tf > best) {
+			best = tf;
+			bestMhz = h[1] > 0 ? (double) h[0] / (double) h[1] * 1e3 : 0.0;
+		}
+	}
+}
+
 int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops, double *flopsPerClockSm, double *mhz)
 {
 	int dev = 0, sms = 0;
 	SA_CHECK(cudaGetDevice(&dev));
 	SA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-	const int nt = 256, nb = 8 * sms;
-	const int iters = fp64 ? 12000 : 600000;              // ~50 ms per launch on GB300
 	long long *stamps = nullptr;
-	SA_CHECK(cudaMallocAsync(&stamps, sizeof(long long) * 2 * nb, s));
-	std::vector<long long> h((size_t) 2 * nb);
+	SA_CHECK(cudaMallocAsync(&stamps, sizeof(long long) * 2 * 8 * sms, s));
 	cudaEvent_t e0, e1;
 	SA_CHECK(cudaEventCreate(&e0));
 	SA_CHECK(cudaEventCreate(&e1));
-	double best = 0.0, bestClk = 0.0, bestMhz = 0.0;
-	for (int rep = 0; rep < 4; ++rep) {                   // first launch is a warm-up
-		SA_CHECK(cudaEventRecord(e0, s));
-		if (fp64) k_fma_peak<double><<<nb, nt, 0, s>>>(iters, 0.9999999, 1e-7, stamps);
-		else k_fma_peak<float><<<nb, nt, 0, s>>>(iters, 0.9999f, 1e-4f, stamps);
-		SA_CHECK(cudaEventRecord(e1, s));
-		SA_CHECK(cudaEventSynchronize(e1));
-		float ms = 0.f;
-		SA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
-		SA_CHECK(cudaMemcpy(h.data(), stamps, sizeof(long long) * 2 * nb, cudaMemcpyDeviceToHost));
-		double cyc = 0.0, ns = 0.0;
-		for (int b = 0; b < nb; ++b) { cyc += (double) h[2 * b]; ns += (double) h[2 * b + 1]; }
-		cyc /= nb;
-		ns /= nb;
-		const double fl = 2.0 * 8.0 * (double) iters * (double) nt * nb;
-		// 8 resident CTAs per SM run side by side: per SM, 8 CTAs' flops in one CTA's cycles
-		const double perClk = fl / sms / cyc;
-		if (rep > 0 && fl / (ms * 1e-3) / 1e12 > best) {
-			best = fl / (ms * 1e-3) / 1e12;
-			bestClk = perClk;
-			bestMhz = ns > 0.0 ? cyc / ns * 1e3 : 0.0;
+	double best = 0.0, bestMhz = 0.0;
+	for (int cps : {2, 4, 8}) {
+		if (fp64) {
+			fma_peak_variant<double, 4>(s, sms, cps, stamps, e0, e1, best, bestMhz);
+			fma_peak_variant<double, 8>(s, sms, cps, stamps, e0, e1, best, bestMhz);
+		} else {
+			fma_peak_variant<float, 8>(s, sms, cps, stamps, e0, e1, best, bestMhz);
+			fma_peak_variant<float, 16>(s, sms, cps, stamps, e0, e1, best, bestMhz);
 		}
 	}
 	cudaEventDestroy(e0);
@@ -1164,8 +1175,8 @@ int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops, double *flopsPer
 	SA_CHECK(cudaFreeAsync(stamps, s));
 	SA_CHECK(cudaStreamSynchronize(s));
 	*tflops = best;
-	if (flopsPerClockSm) *flopsPerClockSm = bestClk;
 	if (mhz) *mhz = bestMhz;
+	if (flopsPerClockSm) *flopsPerClockSm = bestMhz > 0.0 ? best * 1e12 / ((double) sms * bestMhz * 1e6) : 0.0;
 	return SA_OK;
 }
 
@@ -1565,6 +1576,21 @@ void cg_mixed_inner(const Mesh &m, int itrMax, double innerTolSqu, CgWork &w, cu
 void cg_mixed_apply(long n, double *x, const CgWork &w, cudaStream_t s)
 {
 	k_axpy_f32<<<grid_for(n), kBlock, 0, s>>>(n, x, w.f32 + 6 * n);
+}
+
+// the scalars of many solves with one host synchronisation: one small copy per solve into pinned memory
+// (at least ws.size() CgScal-sized slots, cg_scal_bytes() each), then one wait for the stream
+size_t cg_scal_bytes() { return sizeof(CgScal); }
+
+void cg_states(const std::vector<const CgWork *> &ws, void *pinned, cudaStream_t s, std::vector<CgState> &out)
+{
+	CgScal *h = (CgScal *) pinned;
+	for (size_t k = 0; k < ws.size(); ++k)
+		SA_CHECK(cudaMemcpyAsync(h + k, ws[k]->scal, sizeof(CgScal), cudaMemcpyDeviceToHost, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	out.resize(ws.size());
+	for (size_t k = 0; k < ws.size(); ++k)
+		out[k] = CgState{h[k].code, h[k].iters, h[k].zero, h[k].done, h[k].rr, h[k].bb};
 }
 
 CgState cg_state(const CgWork &w, cudaStream_t s)

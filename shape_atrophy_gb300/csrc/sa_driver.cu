@@ -1087,6 +1087,174 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 }
 
 // ---------------------------------------------------------------------------
+// discrete adjoint (layered model): forward pass keeping the trajectory and the velocities, then one
+// backward sweep (two symmetric solves per step, sa_adjoint.cu) for the gradient of the objective with
+// respect to every parameter at once: the bump [c, h, sigma], the per-layer (lambda, mu, D), the initial
+// concentration of every node and the initial node positions
+// ---------------------------------------------------------------------------
+template <int D>
+static int adjoint_impl(sa_context *ctx, const sa_element_object *obj, const double *lmkIni, const sa_params *prm,
+                        const sa_target *tgt, const double *tauVar, int tauVarNum, double *objOut, double *gradBump,
+                        double *gradLayer, double *gradTau0, double *gradX0, sa_solve_info *info)
+{
+	cudaStream_t s = ctx->stream;
+	PhaseTrace tr(s);
+	Pool P(s);
+	Mesh m;
+	Model md;
+	fill_model(md, D, prm, tgt, P);
+	SA_REQUIRE(!md.frame && md.ldmWgt == 0.0, "adjoint: layered model (elaType isotropic, ldmWgt 0) only");
+	SA_REQUIRE(tgt && tgt->tgtElmNum > 0 && tgt->cenPosMat && tgt->uniDirMat && tgt->elmVolVec, "the adjoint needs a target");
+	SA_REQUIRE(tauVar && tauVarNum >= D + 2, "tauVarVec needs [c (dim), h, sigma]");
+	md.precision = SA_PREC_FP64;             // forward and adjoint solves in FP64
+	build_mesh(m, obj, true, true, true, md.lyrNum, P, &tr);
+	const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
+	std::vector<double> tv = to_host(tauVar, (size_t) tauVarNum, s);
+	const double *tc = P.dev(tgt->cenPosMat, (size_t) tgt->tgtElmNum * D);
+	const double *tu = P.dev(tgt->uniDirMat, (size_t) tgt->tgtElmNum * D);
+	const double *tvl = P.dev(tgt->elmVolVec, (size_t) tgt->tgtElmNum);
+	Work w;
+	alloc_work<D>(w, m, md, true, P);
+	const long n = (long) m.N * D, N = m.N;
+	const int T = md.timeNum;
+	const double dt = md.timeStp;
+	{
+		double *xa = P.alloc<double>((size_t) n);
+		launch_soa_to_aos(m.N, D, x0, xa, s);
+		k_init_sign<D><<<grid_for(m.E), kBlock, 0, s>>>(m.E, m.elmVtx, xa, m.sign0);
+	}
+	double *vAll = P.alloc<double>((size_t) n * std::max(T - 1, 1));
+	Stepper<D> st(m, md, w, s);
+	st.start(x0, tv.data());
+	tr.mark("inputs, work buffers");
+	SA_CHECK(cudaEventRecord(ctx->e0, s));
+	// forward: the one-call solve, keeping v_t
+	int status = SA_OK, adjIts = 0;
+	while (st.t < T - 1 && status == SA_OK) {
+		st.pre_velocity();
+		int its = 0;
+		int code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st.st, &its, s,
+		                        SA_PREC_FP64);
+		st.out.cgTotal += its;
+		st.out.cgMax = std::max(st.out.cgMax, its);
+		if (code != SA_OK) { status = code; break; }
+		SA_CHECK(cudaMemcpyAsync(vAll + (long) st.t * n, w.v, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+		st.post_velocity();
+		int rits = 0;
+		code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, st.tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, st.st, &rits, s,
+		                    SA_PREC_FP64);
+		st.out.rdTotal += rits;
+		if (code != SA_OK) { status = code; break; }
+		st.end_step();
+	}
+	const int steps = st.t;
+	st.finish();
+	double J = DBL_MAX;
+	std::vector<double> gb((size_t) D + 2, std::nan("")), gl((size_t) 3 * md.lyrNum, std::nan(""));
+	double *aX = P.zeros<double>(n), *aXn = P.zeros<double>(n);       // a_x^t, a_x^t+1
+	double *aT = P.zeros<double>(N), *aTn = P.zeros<double>(N);       // a_tau^t, a_tau^t+1
+	if (status == SA_OK) {
+		int err = SA_OK;
+		J = varifold<D>(m, md, w.xa, tc, tu, tvl, tgt->tgtElmNum, aXn, s, SA_PREC_FP64, &err, nullptr);
+		SA_REQUIRE(err == SA_OK, "the adjoint needs vfdIfoMat (varifold gradient)");
+		double *xt = P.alloc<double>((size_t) n), *xt1 = P.alloc<double>((size_t) n);
+		double *nu = P.zeros<double>(n), *mu = P.zeros<double>(N), *rhsV = P.alloc<double>((size_t) n);
+		double *wv = P.alloc<double>((size_t) N);
+		double *accLam = P.zeros<double>((size_t) m.E), *accMu = P.zeros<double>((size_t) m.E);
+		double *accD = P.zeros<double>((size_t) m.E);
+		Status *stt = st.st;
+		launch_soa_to_aos(m.N, D, w.trajX + (long) steps * n, xt1, s);
+		for (int t = steps - 1; t >= 0 && status == SA_OK; --t) {
+			const double *tauT = w.trajT + (long) t * N, *tauT1 = w.trajT + (long) (t + 1) * N;
+			launch_soa_to_aos(m.N, D, w.trajX + (long) t * n, xt, s);
+			launch_elem_geom<D>(m, md, xt, w.g0, stt, false, s);
+			launch_elem_geom<D>(m, md, xt1, w.g1, stt, false, s);
+			launch_assemble_rd<D>(m, md, w.g0, dt, w.Mnow, w.L, w.dinvRd, s);     // M_t (L is overwritten next)
+			launch_assemble_rd<D>(m, md, w.g1, dt, w.Mnxt, w.L, w.dinvRd, s);     // L_t+1
+			// reaction-diffusion adjoint: L_t+1 m = a_tau^t+1 (the previous step's m starts the CG)
+			int its = 0;
+			int code = cg_jacobi<1>(m, w.L, w.dinvRd, aTn, mu, md.rdItrMax, md.rdTolSqu, w.cw, stt, &its, s,
+			                        SA_PREC_FP64);
+			adjIts += its;
+			if (code != SA_OK) { status = code; break; }
+			launch_adj_rd<D>(m, md, w.g1.rec, mu, tauT1, -1.0, -1.0, aXn, s);     // -(d(L tau_t+1)/dx_t+1)^T m
+			launch_adj_diffusivity<D>(m, md, w.g1.rec, mu, tauT1, accD, s);
+			launch_activity<D>(m, md, tauT, w.fy, w.fr, s);
+			launch_adj_axpy(N, tauT, dt, w.fr, wv, s);                             // w = tau_t + dt R(tau_t)
+			SA_CHECK(cudaMemsetAsync(aX, 0, sizeof(double) * n, s));
+			launch_adj_rd<D>(m, md, w.g0.rec, mu, wv, 1.0, 0.0, aX, s);             // (d(M w)/dx_t)^T m
+			launch_adj_tau(m, md, w.Mnow, mu, tauT, aT, s);                         // (I + dt R') M_t m
+			// node update: a_x^t += a_x^t+1, a_v = dt a_x^t+1
+			launch_adj_axpy(n, aX, 1.0, aXn, aX, s);
+			launch_adj_axpy(n, aXn, dt - 1.0, aXn, rhsV, s);
+			// velocity adjoint: K(x_t) n = a_v
+			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xt, w.pd, s);
+			launch_assemble_elastic<D>(m, md, w.g0, w.pd, w.blk, w.dinv, nullptr, s);
+			code = cg_jacobi<D>(m, w.blk, w.dinv, rhsV, nu, md.cgItrMax, md.cgTolSqu, w.cw, stt, &its, s,
+			                    SA_PREC_FP64);
+			adjIts += its;
+			if (code != SA_OK) { status = code; break; }
+			const double *vt = vAll + (long) t * n;
+			launch_adj_velocity<D>(m, md, w.g0.rec, w.fy, xt, vt, nu, aX, aT, s);
+			launch_adj_moduli<D>(m, w.g0.rec, vt, nu, accLam, accMu, s);
+			w.cw.launches += 14;
+			std::swap(aX, aXn);
+			std::swap(aT, aTn);
+			std::swap(xt, xt1);
+		}
+		if (status == SA_OK) {
+			// aXn, aTn: a_x^0, a_tau^0.  The bump's parameters, and its dependence on the initial shape
+			double *x0a = xt1, *tmp = rhsV;
+			const double *tau0 = w.trajT;
+			for (int k = 0; k < D + 2; ++k) {
+				launch_tau0_tan<D>(m, x0a, tau0, tv.data(), k, tmp, s);
+				std::vector<double> hd = to_host(tmp, (size_t) N, s), ha = to_host(aTn, (size_t) N, s);
+				double acc = 0.0;
+				for (long q = 0; q < N; ++q) acc += ha[q] * hd[q];
+				gb[k] = acc;
+			}
+			launch_adj_tau0_x<D>(m, x0a, tau0, aTn, tv.data(), aXn, s);
+			if (gradLayer) {
+				std::vector<double> hl = to_host(accLam, (size_t) m.E, s), hm = to_host(accMu, (size_t) m.E, s);
+				std::vector<double> hD = to_host(accD, (size_t) m.E, s);
+				std::vector<int> ly = to_host(m.elmLyr, (size_t) m.E, s);
+				for (int l = 0; l < 3 * md.lyrNum; ++l) gl[l] = 0.0;
+				for (long e = 0; e < m.E; ++e) {
+					gl[3 * ly[e]] += hl[e];
+					gl[3 * ly[e] + 1] += hm[e];
+					gl[3 * ly[e] + 2] += hD[e];
+				}
+			}
+			if (gradTau0) SA_CHECK(cudaMemcpyAsync(gradTau0, aTn, sizeof(double) * N, cudaMemcpyDefault, s));
+			if (gradX0) {
+				launch_aos_to_soa(m.N, D, aXn, tmp, s);
+				SA_CHECK(cudaMemcpyAsync(gradX0, tmp, sizeof(double) * n, cudaMemcpyDefault, s));
+			}
+		}
+		if (status != SA_OK) J = DBL_MAX;
+	}
+	SA_CHECK(cudaEventRecord(ctx->e1, s));
+	SA_CHECK(cudaEventSynchronize(ctx->e1));
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, ctx->e0, ctx->e1);
+	tr.mark("forward, adjoint sweep, gradients");
+	if (objOut) SA_CHECK(cudaMemcpyAsync(objOut, &J, sizeof(double), cudaMemcpyDefault, s));
+	if (gradBump) SA_CHECK(cudaMemcpyAsync(gradBump, gb.data(), sizeof(double) * gb.size(), cudaMemcpyDefault, s));
+	if (gradLayer) SA_CHECK(cudaMemcpyAsync(gradLayer, gl.data(), sizeof(double) * gl.size(), cudaMemcpyDefault, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	if (info) {
+		info->status = status;
+		info->cgIterTotal = st.out.cgTotal;
+		info->rdIterTotal = st.out.rdTotal;
+		info->cgIterMax = adjIts;            // iterations of all adjoint solves
+		info->invertedElements = st.out.inverted;
+		info->elapsedMs = ms;
+		info->kernelLaunches = w.cw.launches;
+	}
+	return SA_OK;
+}
+
+// ---------------------------------------------------------------------------
 // sessions: one parameter vector, stepped on demand, state device-resident
 // ---------------------------------------------------------------------------
 struct SessionBase {
@@ -1603,6 +1771,7 @@ struct Server {
 			             batchLaunches[1], batchLaunches[2], batchLaunches[3]);
 		cudaSetDevice(ctx->device);
 		if (devJobs) cudaFree(devJobs);
+		if (statPinned) cudaFreeHost(statPinned);
 		if (s) cudaStreamDestroy(s);
 	}
 
@@ -1619,6 +1788,24 @@ struct Server {
 	// mixed precision are latency bound, so their length follows their iteration count: they are ordered
 	// longest first, so that long solves share launches.  The FP64 solves are FP64-pipe bound and keep
 	// arrival order (measured faster on the served stream).  Results do not depend on the order.
+	// CG scalars of every instance in g with one host synchronisation (pinned staging grows as needed)
+	void *statPinned = nullptr;
+	size_t statCap = 0;
+	std::vector<CgState> states(const std::vector<InstBase *> &g)
+	{
+		if (g.size() > statCap) {
+			if (statPinned) SA_CHECK(cudaFreeHost(statPinned));
+			statPinned = nullptr;
+			statCap = std::max(g.size(), (size_t) 256);
+			SA_CHECK(cudaHostAlloc(&statPinned, statCap * cg_scal_bytes(), cudaHostAllocDefault));
+		}
+		std::vector<const CgWork *> ws;
+		for (InstBase *in : g) ws.push_back(&in->cg());
+		std::vector<CgState> out;
+		cg_states(ws, statPinned, s, out);
+		return out;
+	}
+
 	// Mixed precision: FP64 iterative refinement of one solve of every instance in g (all of dimension B's
 	// kind), each refinement round one batched FP32 launch over the instances still refining.  Leaves each
 	// instance's FP32 iterations in mixedTotal; failed instances are marked.
@@ -1628,8 +1815,10 @@ struct Server {
 		for (int outer = 0; outer < 64 && !g.empty(); ++outer) {
 			for (InstBase *in : g) in->mixed_outer(kind, outer == 0);
 			std::vector<InstBase *> inner;
-			for (InstBase *in : g) {
-				CgState c = cg_state(in->cg(), s);
+			const std::vector<CgState> cs = states(g);
+			for (size_t q = 0; q < g.size(); ++q) {
+				InstBase *in = g[q];
+				const CgState &c = cs[q];
 				const Model &md = in->model();
 				const double tolSqu = kind == kMixedVelocity ? md.cgTolSqu : md.rdTolSqu;
 				const int itrMax = kind == kMixedVelocity ? md.cgItrMax : md.rdItrMax;
@@ -1651,8 +1840,10 @@ struct Server {
 			                   : B == 2 ? cg_batch_run<2, float, float, float>(bs, smCount, devJobs, kMaxJobs, s)
 			                            : cg_batch_run<3, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
 			std::vector<InstBase *> next;
-			for (InstBase *in : inner) {
-				CgState c = cg_state(in->cg(), s);
+			const std::vector<CgState> ci = states(inner);
+			for (size_t q = 0; q < inner.size(); ++q) {
+				InstBase *in = inner[q];
+				const CgState &c = ci[q];
 				in->mixedTotal += c.iters;
 				if (c.code == SA_ERR_NONFINITE) { fail(*in, SA_ERR_NONFINITE); continue; }
 				in->mixed_apply(kind);
@@ -1681,10 +1872,10 @@ struct Server {
 			batchLaunches[0] += D == 2 ? cg_batch_run<2, double, double, double>(bs, smCount, devJobs, kMaxJobs, s)
 			                           : cg_batch_run<3, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
 			for (InstBase *in : g) in->finish_velocity_fp64();
-			for (InstBase *in : g) {
-				CgState c = cg_state(in->cg(), s);
-				in->its = c.iters;
-				if (c.code != SA_OK) fail(*in, c.code);
+			const std::vector<CgState> cs = states(g);
+			for (size_t q = 0; q < g.size(); ++q) {
+				g[q]->its = cs[q].iters;
+				if (cs[q].code != SA_OK) fail(*g[q], cs[q].code);
 			}
 		}
 		mark(1);
@@ -1711,10 +1902,10 @@ struct Server {
 			for (InstBase *in : rd) { in->prepare_rd(); bs.push_back(in->rd_solve()); }
 			batchLaunches[2] += cg_batch_run<1, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
 			for (InstBase *in : rd) in->finish_rd();
-			for (InstBase *in : rd) {
-				CgState c = cg_state(in->cg(), s);
-				in->rits = c.iters;
-				if (c.code != SA_OK) fail(*in, c.code);
+			const std::vector<CgState> cs = states(rd);
+			for (size_t q = 0; q < rd.size(); ++q) {
+				rd[q]->rits = cs[q].iters;
+				if (cs[q].code != SA_OK) fail(*rd[q], cs[q].code);
 			}
 		}
 		if (!rdMixed.empty()) {
@@ -2004,6 +2195,21 @@ int sa_objective_gradient(sa_context *ctx, const sa_element_object *obj, const d
 			return sa::gradient_impl<2>(ctx, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum, objOut, gradOut, info);
 		SA_REQUIRE(obj->dim == 3, "dim must be 2 or 3");
 		return sa::gradient_impl<3>(ctx, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum, objOut, gradOut, info);
+	});
+}
+
+int sa_objective_adjoint(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat, const sa_params *prm,
+                         const sa_target *tgt, const double *tauVarVec, int tauVarNum, double *objOut,
+                         double *gradBump, double *gradLayer, double *gradTau0, double *gradX0, sa_solve_info *info)
+{
+	if (!obj || !lmkIniMat || !prm || !tgt || !tauVarVec) return SA_ERR_ARG;
+	return sa::guarded(ctx, [&]() {
+		if (obj->dim == 2)
+			return sa::adjoint_impl<2>(ctx, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum, objOut, gradBump,
+			                           gradLayer, gradTau0, gradX0, info);
+		SA_REQUIRE(obj->dim == 3, "dim must be 2 or 3");
+		return sa::adjoint_impl<3>(ctx, obj, lmkIniMat, prm, tgt, tauVarVec, tauVarNum, objOut, gradBump, gradLayer,
+		                           gradTau0, gradX0, info);
 	});
 }
 

@@ -328,6 +328,21 @@ template <int D> void launch_rd_tan_rhs(const Mesh &m, const Model &md, const do
 template <int D> void launch_tau0_tan(const Mesh &m, const double *x, const double *tau0, const double *tv, int k,
                                       double *dtau, cudaStream_t s);
 void launch_aos_to_soa(int N, int D, const double *aos, double *soa, cudaStream_t s);
+// discrete adjoint kernels of the layered model (sa_adjoint.cu)
+template <int D> void launch_adj_velocity(const Mesh &m, const Model &md, const double *rec, const double *fy,
+                                          const double *x, const double *v, const double *nu, double *ax,
+                                          double *atau, cudaStream_t s);
+template <int D> void launch_adj_rd(const Mesh &m, const Model &md, const double *rec, const double *mu,
+                                    const double *w, double sgnM, double sgnG, double *ax, cudaStream_t s);
+template <int D> void launch_adj_moduli(const Mesh &m, const double *rec, const double *v, const double *nu,
+                                        double *accLam, double *accMu, cudaStream_t s);
+template <int D> void launch_adj_diffusivity(const Mesh &m, const Model &md, const double *rec, const double *mu,
+                                             const double *tau, double *accD, cudaStream_t s);
+void launch_adj_tau(const Mesh &m, const Model &md, const double *Mval, const double *mu, const double *tau,
+                    double *atau, cudaStream_t s);
+template <int D> void launch_adj_tau0_x(const Mesh &m, const double *x, const double *tau0, const double *atau,
+                                        const double *tv, double *ax, cudaStream_t s);
+void launch_adj_axpy(long n, const double *a, double sc, const double *b, double *out, cudaStream_t s);
 
 
 // --------------------------------------------------------------------------
@@ -418,6 +433,8 @@ int cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJ
 template <int B> void cg_finish_fp64(const Mesh &m, double *x, CgWork &w, cudaStream_t s);
 // host copy of the scalars (synchronises s)
 CgState cg_state(const CgWork &w, cudaStream_t s);
+size_t cg_scal_bytes();
+void cg_states(const std::vector<const CgWork *> &ws, void *pinned, cudaStream_t s, std::vector<CgState> &out);
 // bounded grid wait self-test: CTAs that gave up, and the abort flag they left
 int barrier_selftest(cudaStream_t s, int *ctasGaveUp, int *abortFlag);
 int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops, double *flopsPerClockSm, double *mhz);
