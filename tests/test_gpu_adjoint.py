@@ -89,7 +89,8 @@ def test_layer_gradients_match_oracle_differences(run):
                 def setter(sp, val, l=l, j=j):
                     a = mv0.copy(); a[2 * l + j] = val; sp["modVec"] = a
                 v0 = mv0[2 * l + j]
-            fd.append(_central(spec, setter, v0, 1e-5 * v0))
+            fd.append(_central(spec, setter, v0, 1e-3 * v0))     # the objective moves little with a modulus:
+                                                                  # smaller steps are dominated by solve noise
             got.append(adj["grad_layer"][l, j])
     got, fd = np.array(got), np.array(fd)
     for j in range(3):                        # each kind of modulus against its own scale
@@ -108,7 +109,7 @@ def test_shape_gradient_matches_oracle_differences(run):
         for d in range(spec["dim"]):
             def setter(sp, val, i=i, d=d):
                 x = x0.copy(); x[d, i] = val; sp["lmkIniMat"] = x
-            fd.append(_central(spec, setter, x0[d, i], 1e-6))
+            fd.append(_central(spec, setter, x0[d, i], 1e-4))
             got.append(adj["grad_x0"][d, i])
     got, fd = np.array(got), np.array(fd)
     assert np.abs(got - fd).max() <= 1e-5 * np.abs(adj["grad_x0"]).max(), (got, fd)
