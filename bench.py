@@ -546,9 +546,9 @@ def main():
             "achieved_tflops": fl, "peak_tflops": peak_at_clock, "frac": fl / peak_at_clock,
             "peak_flops_per_clock_sm": pk["flops_per_clock_sm"], "peak_clock_mhz": mhz,
             "fma_loop_tflops": pk["tflops"], "fma_loop_sm_mhz": pk["sm_mhz"],
-            "peak_source": "measured in this run: sa_selftest_fma_peak (8 independent FMA chains per thread, "
-                           "8 x 256-thread CTAs per SM, best of 3 launches), flops per SM clock (clock64) x SMs x "
-                           "the SM clock sampled during the timed steps",
+            "peak_source": "measured in this run: sa_selftest_fma_peak (independent FMA chains per thread, "
+                           "256-thread CTAs, 2/4/8 CTAs per SM, best launch), its rate per SM clock x SMs x the "
+                           "SM clock sampled during the timed steps",
             "flops_model": "2 x (9 x operator slots + 8 x rows) per CG iteration (assembled 3x3 blocks)"}
 
     e2e = None
