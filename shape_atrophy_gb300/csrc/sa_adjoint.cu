@@ -115,7 +115,7 @@ __global__ void k_adj_velocity(int N, int E, const int *__restrict__ vtxElm, con
 template <int D>
 __global__ void k_adj_penalty(int Nb, int Bt, const int *__restrict__ vtxBtm, const int *__restrict__ btmVtx,
                               const double *__restrict__ x, const double *__restrict__ v,
-                              const double *__restrict__ nu, double btmWgt, double *__restrict__ ax)
+                              const double *__restrict__ nu, double btmWgt, int projected, double *__restrict__ ax)
 {
 	int c = blockIdx.x * blockDim.x + threadIdx.x;
 	if (c >= Nb) return;
@@ -136,6 +136,16 @@ __global__ void k_adj_penalty(int Nb, int Bt, const int *__restrict__ vtxBtm, co
 			Vec<D> t = vsub(load_node<D>(x, q[1]), load_node<D>(x, q[0]));
 			const double len = sqrt(vdot(t, t));
 			for (int d = 0; d < D; ++d) dA[d] = (l == 1 ? 1.0 : -1.0) * t.c[d] / len;
+		} else if (projected) {
+			// frame model: area of the face's (x, y) projection (3D_frame/applyPenaltyOperator.cu:13-14)
+			Vec<3> a0 = load_node<3>(x, q[0]), a1 = load_node<3>(x, q[1]), a2 = load_node<3>(x, q[2]);
+			Vec<3> e1 = vsub(a1, a0), e2 = vsub(a2, a0);
+			const double cz = e1.c[0] * e2.c[1] - e1.c[1] * e2.c[0];
+			const double sg = cz > 0.0 ? 0.5 : (cz < 0.0 ? -0.5 : 0.0);
+			const double d1[2] = {e2.c[1], -e2.c[0]}, d2[2] = {-e1.c[1], e1.c[0]};
+			for (int d = 0; d < 2; ++d)
+				dA[d] = sg * (l == 1 ? d1[d] : (l == 2 ? d2[d] : -(d1[d] + d2[d])));
+			dA[D - 1] = 0.0;
 		} else {
 			Vec<3> a0 = load_node<3>(x, q[0]), a1 = load_node<3>(x, q[1]), a2 = load_node<3>(x, q[2]);
 			Vec<3> e1 = vsub(a1, a0), e2 = vsub(a2, a0);
@@ -275,7 +285,8 @@ void launch_adj_velocity(const Mesh &m, const Model &md, const double *rec, cons
 	k_adj_velocity<D><<<grid_for(m.N), kBlock, 0, s>>>(m.N, m.E, m.vtxElm, m.elmVtx, rec, m.elmLyr, md.lyrMod, fy,
 	                                                    md.ynk[0], v, nu, ax, atau);
 	if (m.Bt > 0 && md.btmWgt != 0.0)
-		k_adj_penalty<D><<<grid_for(m.Nb), kBlock, 0, s>>>(m.Nb, m.Bt, m.vtxBtm, m.btmVtx, x, v, nu, md.btmWgt, ax);
+		k_adj_penalty<D><<<grid_for(m.Nb), kBlock, 0, s>>>(m.Nb, m.Bt, m.vtxBtm, m.btmVtx, x, v, nu, md.btmWgt, 0,
+		                                                    ax);
 }
 
 template <int D>

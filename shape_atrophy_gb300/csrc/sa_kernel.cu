@@ -121,6 +121,86 @@ __device__ __forceinline__ double kernel_value(int order, double w, double d2)
 	}
 }
 
+// dk/d(d2), the kernel's derivative with respect to the squared distance (discrete adjoint of the frame
+// model).  2D Matern through d(x K1)/dx = -x K0 = -p0 / x and d(x^2 K0)/dx = 2 p0 / x - x p1; every order
+// but 0 carries a factor x that cancels dx/d(d2) = 1 / (2 w^2 x).  Not called at d2 = 0.
+template <int D>
+__device__ __forceinline__ double kernel_dvalue(int order, double w, double d2)
+{
+	if (order == -1) return -exp(-(d2 / (w * w))) / (w * w);
+	const double w2 = w * w;
+	if (D == 2) {
+		double x = sqrt(d2) / w, xs = x * x;
+		double f1 = p1fcn(x), f0 = p0fcn(x);
+		switch (order) {
+		case 0: return -f0 / (2.0 * w2 * xs);
+		case 1: return -0.5 * f1 / (2.0 * w2);
+		case 2: return -(2.0 * f1 + f0) / (16.0 * w2);
+		case 3: return -(4.0 * f0 + (8.0 + xs) * f1) / (96.0 * w2);
+		default: return -((24.0 + xs) * f0 + (48.0 + 8.0 * xs) * f1) / (768.0 * w2);
+		}
+	}
+	double r = sqrt(d2) / w, ex = exp(-r);
+	switch (order) {
+	case 0: return -ex / (2.0 * w2 * r);
+	case 1: return -ex / (2.0 * w2);
+	case 2: return -(1.0 + r) * ex / (6.0 * w2);
+	case 3: return -(3.0 + r * (3.0 + r)) * ex / (30.0 * w2);
+	default: return -(15.0 + r * (15.0 + r * (6.0 + r))) * ex / (210.0 * w2);
+	}
+}
+
+// a_x_i += ldm sum_{j != i} 2 dk/d(d2)(x_i - x_j) sum_d (alpha_id beta_jd + alpha_jd beta_id): the vector-Jacobian
+// product of x -> -ldm n^T K(x)^{-1} v with alpha = K^{-1} n, beta = K^{-1} v (nodal vectors, interleaved).
+// One thread per node, the other nodes in shared-memory tiles.
+template <int D>
+__global__ void k_adj_kernel_term(int N, const double *__restrict__ x, const double *__restrict__ alpha,
+                                  const double *__restrict__ beta, int order, double w, double ldm,
+                                  double *__restrict__ ax)
+{
+	__shared__ double tx[128 * D], ta[128 * D], tb[128 * D];
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	Vec<D> xi, ai, bi;
+	for (int d = 0; d < D; ++d) {
+		xi.c[d] = i < N ? x[(long) i * D + d] : 0.0;
+		ai.c[d] = i < N ? alpha[(long) i * D + d] : 0.0;
+		bi.c[d] = i < N ? beta[(long) i * D + d] : 0.0;
+	}
+	double acc[D];
+	for (int d = 0; d < D; ++d) acc[d] = 0.0;
+	for (int j0 = 0; j0 < N; j0 += 128) {
+		const int nt = min(128, N - j0);
+		__syncthreads();
+		for (int t = threadIdx.x; t < nt * D; t += blockDim.x) {
+			tx[t] = x[(long) j0 * D + t];
+			ta[t] = alpha[(long) j0 * D + t];
+			tb[t] = beta[(long) j0 * D + t];
+		}
+		__syncthreads();
+		if (i >= N) continue;
+		for (int jj = 0; jj < nt; ++jj) {
+			if (j0 + jj == i) continue;
+			double d2 = 0.0, ab = 0.0, dx[D];
+			for (int d = 0; d < D; ++d) {
+				dx[d] = xi.c[d] - tx[jj * D + d];
+				d2 += dx[d] * dx[d];
+				ab += ai.c[d] * tb[jj * D + d] + ta[jj * D + d] * bi.c[d];
+			}
+			const double g = 2.0 * kernel_dvalue<D>(order, w, d2) * ab;
+			for (int d = 0; d < D; ++d) acc[d] += g * dx[d];
+		}
+	}
+	if (i < N)
+		for (int d = 0; d < D; ++d) ax[(long) i * D + d] += ldm * acc[d];
+}
+
+template <int D>
+void launch_adj_kernel_term(const Model &md, int N, const double *x, const double *alpha, const double *beta,
+                            double *ax, cudaStream_t s)
+{
+	k_adj_kernel_term<D><<<grid_for(N, 128), 128, 0, s>>>(N, x, alpha, beta, md.knlOrder, md.knlWidth, md.ldmWgt, ax);
+}
+
 // K[j*N + i] = k(|q_i - q_j| / w) + eps * delta_ij
 template <int D>
 __global__ void k_kernel_matrix(int N, const double *__restrict__ x, int order, double w, double eps,
@@ -440,6 +520,10 @@ int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, con
 	return h.code;
 }
 
+template void launch_adj_kernel_term<2>(const Model &, int, const double *, const double *, const double *, double *,
+                                        cudaStream_t);
+template void launch_adj_kernel_term<3>(const Model &, int, const double *, const double *, const double *, double *,
+                                        cudaStream_t);
 template void launch_kernel_matrix<2>(const Model &, int, const double *, double *, cudaStream_t);
 template void launch_kernel_matrix<3>(const Model &, int, const double *, double *, cudaStream_t);
 template int kpcg<2>(const Mesh &, const Model &, const double *, const double *, const double *, double *,

@@ -259,54 +259,6 @@ void launch_penalty_diag(const Mesh &m, const Model &md, const double *x, double
 }
 
 // ---------------------------------------------------------------------------
-// stress laws
-// ---------------------------------------------------------------------------
-struct FrameMod { double m[4]; };
-
-// computePreMat 2D (2D_frame/applyFrameElasticOperator.cu:7-39)
-__device__ __forceinline__ void pre_frame(Mat<2> &pm, const Vec<2> &t, const Vec<2> &s, const FrameMod &md,
-                                          const Mat<2> &ep)
-{
-	double muT = md.m[0], muS = md.m[1], muA = md.m[2];
-	Vec<2> evS;
-	evS.c[0] = ep.m[0][0] * s.c[0] + ep.m[0][1] * s.c[1];
-	evS.c[1] = ep.m[1][0] * s.c[0] + ep.m[1][1] * s.c[1];
-	double TvT = t.c[0] * (ep.m[0][0] * t.c[0] + ep.m[0][1] * t.c[1]) + t.c[1] * (ep.m[1][0] * t.c[0] + ep.m[1][1] * t.c[1]);
-	double SvS = vdot(s, evS), TvS = vdot(t, evS);
-	for (int i = 0; i < 2; ++i)
-		for (int j = 0; j < 2; ++j) {
-			double v = muT * (t.c[i] * t.c[j]) * TvT;
-			v += muS * (s.c[i] * s.c[j]) * SvS;
-			v += muA * (i == j ? 2.0 * t.c[i] * s.c[j] : t.c[i] * s.c[j] + s.c[i] * t.c[j]) * TvS;
-			pm.m[i][j] = v;
-		}
-}
-
-// computePreMat 3D (3D_frame/applyFrameElasticOperator.cu:7-111)
-__device__ __forceinline__ void pre_frame(Mat<3> &pm, const Vec<3> &n, const Vec<3> &s, const FrameMod &md,
-                                          const Mat<3> &ep)
-{
-	double ldT = md.m[0], muT = md.m[1], muS = md.m[2], muA = md.m[3];
-	Vec<3> evN, evS;
-	for (int i = 0; i < 3; ++i) {
-		evN.c[i] = ep.m[i][0] * n.c[0] + ep.m[i][1] * n.c[1] + ep.m[i][2] * n.c[2];
-		evS.c[i] = ep.m[i][0] * s.c[0] + ep.m[i][1] * s.c[1] + ep.m[i][2] * s.c[2];
-	}
-	double NvN = vdot(n, evN), SvS = vdot(s, evS), NvS = vdot(n, evS);
-	double ldv = (ep.m[0][0] + ep.m[1][1] + ep.m[2][2]) - NvN;
-	for (int i = 0; i < 3; ++i)
-		for (int j = 0; j < 3; ++j) {
-			double v = ldT * (i == j ? 1.0 - n.c[i] * n.c[j] : -n.c[i] * n.c[j]) * ldv;
-			if (i == j) v += muT * (ep.m[i][j] - (2.0 * evN.c[i] * n.c[j]) + NvN * n.c[i] * n.c[j]);
-			else v += muT * (ep.m[i][j] - (evN.c[i] * n.c[j] + n.c[i] * evN.c[j]) + NvN * n.c[i] * n.c[j]);
-			v += muS * SvS * s.c[i] * s.c[j];
-			if (i == j) v += muA * (2.0 * evS.c[i] * s.c[j] - NvS * 2.0 * n.c[i] * s.c[j]);
-			else v += muA * ((evS.c[i] * s.c[j] + s.c[i] * evS.c[j]) - NvS * (n.c[i] * s.c[j] + s.c[i] * n.c[j]));
-			pm.m[i][j] = v;
-		}
-}
-
-// ---------------------------------------------------------------------------
 // elasticity block assembly: one thread per femVtxMat slot (i, j) with
 // i <= j, diagonal slots first (Mesh::asmOrder); the contributions are the elements listed for the slot in
 // femIfoMat (same order), with ordered local indices (a, b) precomputed in
