@@ -182,23 +182,30 @@ int sa_objective_gradient(sa_context *ctx, const sa_element_object *obj, const d
                           double *objOut, double *gradOut, sa_solve_info *info);
 
 /* Objective and its gradient by the discrete adjoint (no reference
- * counterpart).  Layered model, one parameter vector [c (dim), h, sigma]:
- * the forward solve keeps the trajectory and the velocities on the device
- * (N x dim x timeNum doubles twice), then one backward sweep solves two
- * adjoint systems per step (the forward operators are symmetric: the same
- * Jacobi-PCG, FP64) and accumulates the gradient with respect to every
- * parameter at once, at about twice the cost of a forward solve whatever the
- * parameter count:
- *   gradBump  (dim + 2, optional): dJ/d[c, h, sigma], as sa_objective_gradient;
- *   gradLayer (3 x lyrNum, optional): dJ/d(lambda_l, mu_l, D_l) per material
- *             layer, in that order per layer;
+ * counterpart; the reference ships derivative kernels it never calls,
+ * 2D_frame/varifold.cu:359-498, tauInitial.cu:68-116, inc/activity.h).  One
+ * parameter vector: the forward solve keeps the trajectory and the
+ * velocities on the device (N x dim x timeNum doubles twice; the frame model
+ * also K^{-1} v), then one backward sweep solves two adjoint systems per step
+ * (the forward operators are symmetric: the same CG as the forward solves,
+ * FP64) and accumulates the gradient with respect to every parameter at
+ * once, at a cost independent of the parameter count:
+ *   gradBump  (optional): layered model (elaType isotropic, ldmWgt 0):
+ *             dJ/d[c (dim), h, sigma] (dim + 2 values), as
+ *             sa_objective_gradient; frame model: dJ/d tauVarVec, 4 values
+ *             (2D [cx, cy, h, R], 3D [cx, cy, cz, h]);
+ *   gradLayer (3 x lyrNum, optional, layered model): dJ/d(lambda_l, mu_l, D_l)
+ *             per material layer, in that order per layer;
  *   gradTau0  (N, optional): dJ/dtau_0 at every node (the initial
  *             concentration as free parameters);
  *   gradX0    (N x dim column-major, optional): dJ/d(initial node positions),
  *             including the bump's dependence on them.
- * prm->precision is ignored (FP64 throughout).  A failed solve gives objOut
- * = DBL_MAX, NaN gradients and its status in info; info->cgIterMax holds the
- * iterations of all adjoint solves.  Needs vfdIfoMat. */
+ * The frame model's sweep differentiates its frames (built from other
+ * nodes), frame stress, anisotropic diffusion, projected 3D penalty, activity
+ * templates and the dense RKHS term ldmWgt K^{-1}.  prm->precision is
+ * ignored (FP64 throughout).  A failed solve gives objOut = DBL_MAX, NaN
+ * gradients and its status in info; info->cgIterMax holds the iterations of
+ * all adjoint solves.  Needs vfdIfoMat. */
 int sa_objective_adjoint(sa_context *ctx, const sa_element_object *obj, const double *lmkIniMat,
                          const sa_params *prm, const sa_target *tgt, const double *tauVarVec, int tauVarNum,
                          double *objOut, double *gradBump, double *gradLayer, double *gradTau0, double *gradX0,

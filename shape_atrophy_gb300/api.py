@@ -279,9 +279,11 @@ def gradient(spec: dict, tauVarVec=None, precision: str = "fp64", device: int = 
 
 def adjoint(spec: dict, tauVarVec=None, layers: bool = True, tau0: bool = True, x0: bool = True,
             device: int = 0) -> dict:
-    """Objective and its gradient by the discrete adjoint (sa_objective_adjoint), layered model, FP64:
-    dict(obj, grad (dim + 2: d/d[c, h, sigma]), grad_layer (lyrNum, 3: d/d(lambda, mu, D)), grad_tau0 (N,),
-    grad_x0 (D, N), info).  About twice the cost of one forward solve for all of them together."""
+    """Objective and its gradient by the discrete adjoint (sa_objective_adjoint), FP64: dict(obj, grad,
+    grad_layer, grad_tau0 (N,), grad_x0 (D, N), info).  Layered model: grad = d/d[c, h, sigma] (dim + 2),
+    grad_layer (lyrNum, 3) = d/d(lambda, mu, D) per layer.  Frame model (the reference's): grad = d/d tauVar
+    (2D [cx, cy, h, R], 3D [cx, cy, cz, h]), grad_layer None.  About twice (layered) the cost of one forward
+    solve for all of them together."""
     ctx = context(device)
     D = int(spec["dim"])
     lmk = np.ascontiguousarray(np.asarray(spec["lmkIniMat"], dtype=np.float64))
@@ -294,9 +296,10 @@ def adjoint(spec: dict, tauVarVec=None, layers: bool = True, tau0: bool = True, 
         o.elmLyrVec = K.i32(spec["elmLyrVec"])
     p = _params(spec, K, "fp64")
     t = _target(spec, K)
-    L = int(np.asarray(spec["spdLyrVec"]).size)
-    obj, gb = np.zeros(1), np.zeros(D + 2)
-    gl = np.zeros((L, 3)) if layers else None
+    frame = spec["elaType"] == "frame"
+    L = 0 if frame else int(np.asarray(spec["spdLyrVec"]).size)
+    obj, gb = np.zeros(1), np.zeros(4 if frame else D + 2)
+    gl = np.zeros((L, 3)) if (layers and not frame) else None
     gt = np.zeros(N) if tau0 else None
     gx = np.zeros((D, N)) if x0 else None
     info = _lib.SolveInfo()

@@ -1087,6 +1087,176 @@ static int gradient_impl(sa_context *ctx, const sa_element_object *obj, const do
 }
 
 // ---------------------------------------------------------------------------
+// discrete adjoint of the frame model (the reference's own): the same sweep as the layered one below, with
+// the frame operators (frame stress, anisotropic diffusion, frames built from other nodes, projected 3D
+// penalty), the activity templates, the dense RKHS term ldm K^{-1} of the velocity operator and the
+// polynomial bump.  The forward solve keeps v_t and K_t^{-1} v_t (tracked by the K-preconditioned CG); the
+// velocity adjoint solve is the same K-preconditioned CG and leaves K_t^{-1} n in its tracked vector.
+// Returns dJ/d tauVar (2D [cx, cy, h, R], 3D [cx, cy, cz, h]), dJ/dtau_0 and dJ/d(initial positions).
+// ---------------------------------------------------------------------------
+template <int D>
+static int adjoint_frame_impl(sa_context *ctx, Pool &P, Mesh &m, Model &md, const double *x0,
+                              const std::vector<double> &tv, const double *tc, const double *tu, const double *tvl,
+                              int Vt, double *objOut, double *gradBump, double *gradTau0, double *gradX0,
+                              sa_solve_info *info, PhaseTrace &tr)
+{
+	cudaStream_t s = ctx->stream;
+	Work w;
+	alloc_work<D>(w, m, md, true, P);
+	const long n = (long) m.N * D, N = m.N;
+	const int T = md.timeNum;
+	const double dt = md.timeStp;
+	{
+		double *xa = P.alloc<double>((size_t) n);
+		launch_soa_to_aos(m.N, D, x0, xa, s);
+		k_init_sign<D><<<grid_for(m.E), kBlock, 0, s>>>(m.E, m.elmVtx, xa, m.sign0);
+	}
+	// inverse maps node -> (element, role) of the frame-building node lists
+	int *fRow = nullptr, *fEnt = nullptr;
+	{
+		const int cols = D == 2 ? 4 : 6;
+		std::vector<int> hf = to_host(m.frmVtx, (size_t) m.E * cols, s), ht = to_host(m.tsvVtx, (size_t) m.E * cols, s);
+		std::vector<int> cnt((size_t) N + 1, 0);
+		for (int which = 0; which < 2; ++which)
+			for (int k = 0; k < cols; ++k)
+				for (long e = 0; e < m.E; ++e) ++cnt[(size_t) (which ? ht : hf)[(size_t) k * m.E + e] + 1];
+		for (long i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
+		std::vector<int> ent((size_t) cnt[N]), pos(cnt.begin(), cnt.end() - 1);
+		for (long e = 0; e < m.E; ++e)
+			for (int which = 0; which < 2; ++which)
+				for (int k = 0; k < cols; ++k) {
+					const int node = (which ? ht : hf)[(size_t) k * m.E + e];
+					ent[(size_t) pos[node]++] = (int) (e * 16 + which * 8 + k);
+				}
+		fRow = (int *) P.dev(cnt.data(), cnt.size());
+		fEnt = (int *) P.dev(ent.data(), ent.size());
+		SA_CHECK(cudaStreamSynchronize(s));
+	}
+	double *vAll = P.alloc<double>((size_t) n * std::max(T - 1, 1));
+	double *bAll = P.alloc<double>((size_t) n * std::max(T - 1, 1));       // K_t^{-1} v_t
+	Stepper<D> st(m, md, w, s);
+	st.start(x0, tv.data());
+	tr.mark("inputs, work buffers");
+	SA_CHECK(cudaEventRecord(ctx->e0, s));
+	int status = SA_OK, adjIts = 0;
+	while (st.t < T - 1 && status == SA_OK) {
+		st.pre_velocity();
+		int its = 0;
+		int code = kpcg<D>(m, md, w.blk, w.K, w.b, w.v, w.kw, st.st, &its, s);
+		st.out.cgTotal += its;
+		st.out.cgMax = std::max(st.out.cgMax, its);
+		if (code != SA_OK) { status = code; break; }
+		SA_CHECK(cudaMemcpyAsync(vAll + (long) st.t * n, w.v, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+		SA_CHECK(cudaMemcpyAsync(bAll + (long) st.t * n, w.kw.wK, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+		st.post_velocity();
+		int rits = 0;
+		code = cg_jacobi<1>(m, w.L, w.dinvRd, w.rhs, st.tau_next(), md.rdItrMax, md.rdTolSqu, w.cw, st.st, &rits, s,
+		                    SA_PREC_FP64);
+		st.out.rdTotal += rits;
+		if (code != SA_OK) { status = code; break; }
+		st.end_step();
+	}
+	const int steps = st.t;
+	st.finish();
+	double J = DBL_MAX;
+	std::vector<double> gb((size_t) 4, std::nan(""));
+	double *aX = P.zeros<double>(n), *aXn = P.zeros<double>(n);
+	double *aT = P.zeros<double>(N), *aTn = P.zeros<double>(N);
+	if (status == SA_OK) {
+		int err = SA_OK;
+		J = varifold<D>(m, md, w.xa, tc, tu, tvl, Vt, aXn, s, SA_PREC_FP64, &err, nullptr);
+		SA_REQUIRE(err == SA_OK, "the adjoint needs vfdIfoMat (varifold gradient)");
+		double *xt = P.alloc<double>((size_t) n), *xt1 = P.alloc<double>((size_t) n);
+		double *nu = P.zeros<double>(n), *mu = P.zeros<double>(N), *rhsV = P.alloc<double>((size_t) n);
+		double *wv = P.alloc<double>((size_t) N), *fyd = P.alloc<double>((size_t) N), *frd = P.alloc<double>((size_t) N);
+		double *gF = P.alloc<double>((size_t) D * m.E), *gS = P.alloc<double>((size_t) D * m.E);
+		Status *stt = st.st;
+		SA_CHECK(cudaMemsetAsync(w.kw.wK, 0, sizeof(double) * n, s));      // the first adjoint solve starts at 0
+		launch_soa_to_aos(m.N, D, w.trajX + (long) steps * n, xt1, s);
+		for (int t = steps - 1; t >= 0 && status == SA_OK; --t) {
+			const double *tauT = w.trajT + (long) t * N, *tauT1 = w.trajT + (long) (t + 1) * N;
+			launch_soa_to_aos(m.N, D, w.trajX + (long) t * n, xt, s);
+			launch_elem_geom<D>(m, md, xt, w.g0, stt, false, s);
+			launch_elem_geom<D>(m, md, xt1, w.g1, stt, false, s);
+			launch_assemble_rd<D>(m, md, w.g0, dt, w.Mnow, w.L, w.dinvRd, s);
+			launch_assemble_rd<D>(m, md, w.g1, dt, w.Mnxt, w.L, w.dinvRd, s);
+			int its = 0;
+			int code = cg_jacobi<1>(m, w.L, w.dinvRd, aTn, mu, md.rdItrMax, md.rdTolSqu, w.cw, stt, &its, s,
+			                        SA_PREC_FP64);
+			adjIts += its;
+			if (code != SA_OK) { status = code; break; }
+			// -(d(L tau_t+1)/dx_t+1)^T m: mass and anisotropic diffusion at fixed frames, then the frames
+			SA_CHECK(cudaMemsetAsync(gF, 0, sizeof(double) * D * m.E, s));
+			SA_CHECK(cudaMemsetAsync(gS, 0, sizeof(double) * D * m.E, s));
+			launch_adj_rd_frame<D>(m, md, w.g1, mu, tauT1, -1.0, -1.0, aXn, gF, gS, s);
+			launch_adj_frame_scatter<D>(m, fRow, fEnt, xt1, gF, gS, aXn, s);
+			launch_activity<D>(m, md, tauT, w.fy, w.fr, s);
+			launch_act_deriv(m, md, tauT, fyd, frd, s);
+			launch_adj_axpy(N, tauT, dt, w.fr, wv, s);
+			SA_CHECK(cudaMemsetAsync(aX, 0, sizeof(double) * n, s));
+			launch_adj_rd_frame<D>(m, md, w.g0, mu, wv, 1.0, 0.0, aX, nullptr, nullptr, s);   // mass only
+			launch_adj_tau_d(m, md, w.Mnow, mu, frd, aT, s);
+			launch_adj_axpy(n, aX, 1.0, aXn, aX, s);
+			launch_adj_axpy(n, aXn, dt - 1.0, aXn, rhsV, s);
+			// velocity adjoint: (ldm K_t^{-1} + E_t) n = a_v, K-preconditioned CG started from K_t times the
+			// previous step's K^{-1} n
+			launch_kernel_matrix<D>(md, m.N, xt, w.K, s);
+			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xt, w.pd, s);
+			launch_assemble_elastic<D>(m, md, w.g0, w.pd, w.blk, w.dinv, nullptr, s);
+			code = kpcg<D>(m, md, w.blk, w.K, rhsV, nu, w.kw, stt, &its, s);
+			adjIts += its;
+			if (code != SA_OK) { status = code; break; }
+			const double *vt = vAll + (long) t * n, *bt = bAll + (long) t * n;
+			SA_CHECK(cudaMemsetAsync(gF, 0, sizeof(double) * D * m.E, s));
+			SA_CHECK(cudaMemsetAsync(gS, 0, sizeof(double) * D * m.E, s));
+			launch_adj_velocity_frame<D>(m, md, w.g0, w.fy, fyd, xt, vt, nu, aX, aT, gF, gS, s);
+			launch_adj_frame_scatter<D>(m, fRow, fEnt, xt, gF, gS, aX, s);
+			if (md.ldmWgt != 0.0) launch_adj_kernel_term<D>(md, m.N, xt, w.kw.wK, bt, aX, s);
+			w.cw.launches += 24;
+			std::swap(aX, aXn);
+			std::swap(aT, aTn);
+			std::swap(xt, xt1);
+		}
+		if (status == SA_OK) {
+			// aXn, aTn: a_x^0, a_tau^0; the polynomial bump's parameters and its dependence on x_0
+			double *x0a = xt1, *tmp = P.alloc<double>((size_t) 4 * N);
+			launch_adj_bump_poly<D>(m, md, x0a, aTn, tv.data(), tmp, aXn, s);
+			std::vector<double> ht = to_host(tmp, (size_t) 4 * N, s);
+			for (int k = 0; k < 4; ++k) {
+				double acc = 0.0;
+				for (long q = 0; q < N; ++q) acc += ht[(size_t) k * N + q];
+				gb[k] = acc;
+			}
+			if (gradTau0) SA_CHECK(cudaMemcpyAsync(gradTau0, aTn, sizeof(double) * N, cudaMemcpyDefault, s));
+			if (gradX0) {
+				launch_aos_to_soa(m.N, D, aXn, rhsV, s);
+				SA_CHECK(cudaMemcpyAsync(gradX0, rhsV, sizeof(double) * n, cudaMemcpyDefault, s));
+			}
+		} else {
+			J = DBL_MAX;
+		}
+	}
+	SA_CHECK(cudaEventRecord(ctx->e1, s));
+	SA_CHECK(cudaEventSynchronize(ctx->e1));
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, ctx->e0, ctx->e1);
+	tr.mark("forward, adjoint sweep, gradients");
+	if (objOut) SA_CHECK(cudaMemcpyAsync(objOut, &J, sizeof(double), cudaMemcpyDefault, s));
+	if (gradBump) SA_CHECK(cudaMemcpyAsync(gradBump, gb.data(), sizeof(double) * 4, cudaMemcpyDefault, s));
+	SA_CHECK(cudaStreamSynchronize(s));
+	if (info) {
+		info->status = status;
+		info->cgIterTotal = st.out.cgTotal;
+		info->rdIterTotal = st.out.rdTotal;
+		info->cgIterMax = adjIts;
+		info->invertedElements = st.out.inverted;
+		info->elapsedMs = ms;
+		info->kernelLaunches = w.cw.launches;
+	}
+	return SA_OK;
+}
+
+// ---------------------------------------------------------------------------
 // discrete adjoint (layered model): forward pass keeping the trajectory and the velocities, then one
 // backward sweep (two symmetric solves per step, sa_adjoint.cu) for the gradient of the objective with
 // respect to every parameter at once: the bump [c, h, sigma], the per-layer (lambda, mu, D), the initial
@@ -1103,10 +1273,22 @@ static int adjoint_impl(sa_context *ctx, const sa_element_object *obj, const dou
 	Mesh m;
 	Model md;
 	fill_model(md, D, prm, tgt, P);
-	SA_REQUIRE(!md.frame && md.ldmWgt == 0.0, "adjoint: layered model (elaType isotropic, ldmWgt 0) only");
+	SA_REQUIRE(md.frame || md.ldmWgt == 0.0, "adjoint: layered model with ldmWgt 0, or the frame model");
 	SA_REQUIRE(tgt && tgt->tgtElmNum > 0 && tgt->cenPosMat && tgt->uniDirMat && tgt->elmVolVec, "the adjoint needs a target");
-	SA_REQUIRE(tauVar && tauVarNum >= D + 2, "tauVarVec needs [c (dim), h, sigma]");
 	md.precision = SA_PREC_FP64;             // forward and adjoint solves in FP64
+	if (md.frame) {
+		SA_REQUIRE(tauVar && tauVarNum >= 4, "tauVarVec needs 4 values (2D [cx, cy, h, R], 3D [cx, cy, cz, h])");
+		build_mesh(m, obj, true, true, false, 0, P, &tr);
+		const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
+		std::vector<double> tv = to_host(tauVar, (size_t) tauVarNum, s);
+		const double *tc = P.dev(tgt->cenPosMat, (size_t) tgt->tgtElmNum * D);
+		const double *tu = P.dev(tgt->uniDirMat, (size_t) tgt->tgtElmNum * D);
+		const double *tvl = P.dev(tgt->elmVolVec, (size_t) tgt->tgtElmNum);
+		SA_REQUIRE((size_t) m.N * m.N * sizeof(double) <= kDenseLimitBytes, "frame mode: N too large for the dense RKHS matrix");
+		return adjoint_frame_impl<D>(ctx, P, m, md, x0, tv, tc, tu, tvl, tgt->tgtElmNum, objOut, gradBump, gradTau0,
+		                             gradX0, info, tr);
+	}
+	SA_REQUIRE(tauVar && tauVarNum >= D + 2, "tauVarVec needs [c (dim), h, sigma]");
 	build_mesh(m, obj, true, true, true, md.lyrNum, P, &tr);
 	const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
 	std::vector<double> tv = to_host(tauVar, (size_t) tauVarNum, s);

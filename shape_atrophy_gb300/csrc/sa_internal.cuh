@@ -419,6 +419,20 @@ void launch_adj_tau(const Mesh &m, const Model &md, const double *Mval, const do
 template <int D> void launch_adj_tau0_x(const Mesh &m, const double *x, const double *tau0, const double *atau,
                                         const double *tv, double *ax, cudaStream_t s);
 void launch_adj_axpy(long n, const double *a, double sc, const double *b, double *out, cudaStream_t s);
+template <int D> void launch_adj_velocity_frame(const Mesh &m, const Model &md, const Geom &g, const double *fy,
+                                                const double *fyd, const double *x, const double *v,
+                                                const double *nu, double *ax, double *atau, double *gF, double *gS,
+                                                cudaStream_t s);
+template <int D> void launch_adj_rd_frame(const Mesh &m, const Model &md, const Geom &g, const double *mu,
+                                          const double *w, double sgnM, double sgnG, double *ax, double *gF,
+                                          double *gS, cudaStream_t s);
+template <int D> void launch_adj_frame_scatter(const Mesh &m, const int *rowPtr, const int *ent, const double *x,
+                                               const double *gF, const double *gS, double *ax, cudaStream_t s);
+void launch_act_deriv(const Mesh &m, const Model &md, const double *tau, double *fyd, double *frd, cudaStream_t s);
+void launch_adj_tau_d(const Mesh &m, const Model &md, const double *Mval, const double *mu, const double *frd,
+                      double *atau, cudaStream_t s);
+template <int D> void launch_adj_bump_poly(const Mesh &m, const Model &md, const double *x, const double *atau,
+                                           const double *tv, double *out, double *ax, cudaStream_t s);
 
 
 // --------------------------------------------------------------------------
@@ -524,6 +538,8 @@ struct KpcgWork {
 template <int D> int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *b,
                           double *x, KpcgWork &w, Status *st, int *itersOut, cudaStream_t s);
 template <int D> void launch_kernel_matrix(const Model &md, int N, const double *x, double *K, cudaStream_t s);
+template <int D> void launch_adj_kernel_term(const Model &md, int N, const double *x, const double *alpha,
+                                             const double *beta, double *ax, cudaStream_t s);
 
 // the target-target rows of the varifold objective (they depend on the target only), kept between calls
 struct VfdTargetCache {
