@@ -353,7 +353,11 @@ int sa_elmobj_free(sa_elmobj *obj);
  * "batchSlicesPerWarp" (1..16, 32-row slices per warp when a batched solve's
  * CTAs are sized), "vfdCtasPerSm" (1..32, CTAs per SM of the varifold pair
  * sums), "mixedInnerFloor" (4..16: mixed precision's FP32 inner solves stop at
- * a squared relative residual of 10^-k at the lowest).  shape_atrophy_gb300/autotune.py measures them on the GPU and writes
+ * a squared relative residual of 10^-k at the lowest), "kernelMatrixFree" (0 or
+ * 1: the frame model's RKHS products evaluate each kernel-matrix entry from
+ * the node positions instead of reading the stored N x N matrix, the same
+ * bits at ~15x the cost; automatic when the matrix would exceed 96 GiB or
+ * three quarters of the free device memory).  shape_atrophy_gb300/autotune.py measures them on the GPU and writes
  * shape_atrophy_gb300/tuning.json, which the Python API applies; the compiled
  * defaults are the values measured best on GB300.  They change how partial
  * sums are grouped: results are reproducible for a given setting.  Set them

@@ -29,7 +29,8 @@ from . import _lib
 
 _CTX = {}
 
-TUNING_NAMES = ("persistMaxWarps", "batchBlock", "batchSlicesPerWarp", "vfdCtasPerSm", "mixedInnerFloor")
+TUNING_NAMES = ("persistMaxWarps", "batchBlock", "batchSlicesPerWarp", "vfdCtasPerSm", "mixedInnerFloor",
+                "kernelMatrixFree")
 TUNING_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
 _TUNED = {"applied": None}
 

@@ -561,7 +561,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 		k.Kr = P.alloc<double>(n); k.dv = P.alloc<double>(n); k.wK = P.zeros<double>(n);
 		k.part = P.alloc<double>((size_t) 4 * nb + 16 * n + 64); k.scal = P.zeros<double>(32);
 		k.maxBlocks = nb;
-		w.K = P.alloc<double>((size_t) N * N);
+		if (!md.kernelFree) w.K = P.alloc<double>((size_t) N * N);
 	}
 	if (wantTraj) {
 		w.trajX = P.zeros<double>((size_t) n * md.timeNum);
@@ -628,12 +628,13 @@ struct Stepper {
 		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
 		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, w.cw.binv32, s);
 		launch_yank_rhs<D>(m, *gn, w.fy, w.b, s);
-		if (useK) launch_kernel_matrix<D>(md, m.N, xn, w.K, s);
-		else if (md.precision == SA_PREC_MIXED)
+		if (useK) {
+			if (!md.kernelFree) launch_kernel_matrix<D>(md, m.N, xn, w.K, s);
+		} else if (md.precision == SA_PREC_MIXED)
 			k_to_f32<<<grid_for(m.slTotal * sell_vals<D>()), kBlock, 0, s>>>(m.slTotal * sell_vals<D>(), w.blk,
 			                                                                  w.cw.blk32);
 		// activity, (penalty), elastic assembly, yank, (kernel matrix or FP32 copy)
-		w.cw.launches += 3 + (m.Bt > 0 && md.btmWgt != 0.0) + (useK || md.precision == SA_PREC_MIXED);
+		w.cw.launches += 3 + (m.Bt > 0 && md.btmWgt != 0.0) + ((useK && !md.kernelFree) || md.precision == SA_PREC_MIXED);
 	}
 
 	// step part 2 (after the velocity solve): new shape, reaction-diffusion operator and right-hand side
@@ -697,7 +698,7 @@ struct Stepper {
 			pre_velocity();
 			int its = 0, code;
 			if (useK) {
-				code = kpcg<D>(m, md, w.blk, w.K, w.b, w.v, w.kw, st, &its, s);
+				code = kpcg<D>(m, md, w.blk, w.K, xn, w.b, w.v, w.kw, st, &its, s);
 			} else {
 				w.cw.profileOn = 1;
 				code = cg_jacobi<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, st, &its, s,
@@ -799,7 +800,23 @@ static void fill_model(Model &md, int dim, const sa_params *p, const sa_target *
 	}
 }
 
-static const size_t kDenseLimitBytes = (size_t) 16 << 30;   // dense RKHS matrix budget (frame mode)
+static const size_t kDenseCapBytes = (size_t) 96 << 30;   // stored RKHS matrix cap: N <= 113 511
+
+// The RKHS term's N x N kernel matrix (frame model, or ldmWgt != 0) is stored when it fits: up to 96 GiB of
+// the 288 GB part and three quarters of the device memory free now.  A K x product then streams 8 bytes per
+// entry.  Beyond that (or with the kernelMatrixFree tuning switch) the products evaluate each entry from the
+// node positions instead, with the same instructions in the same order, so the choice changes the speed and
+// never the bits.  The evaluation costs a square root and an exponential (2D Matern: Bessel rational
+// approximations too) per entry, ~15x the stored matrix's product time on this part.
+static void choose_kernel_storage(Model &md, int N)
+{
+	md.kernelFree = 0;
+	if (!md.frame && md.ldmWgt == 0.0) return;
+	size_t freeBytes = 0, totalBytes = 0;
+	SA_CHECK(cudaMemGetInfo(&freeBytes, &totalBytes));
+	const size_t need = (size_t) N * N * sizeof(double);
+	md.kernelFree = tuning().kernelMatrixFree != 0 || need > kDenseCapBytes || need > freeBytes / 4 * 3;
+}
 
 template <int D>
 static int forward_impl(sa_context *ctx, const sa_element_object *obj, const double *lmkIni, const sa_params *prm,
@@ -837,9 +854,7 @@ static int forward_impl(sa_context *ctx, const sa_element_object *obj, const dou
 		}
 	}
 	build_mesh(m, obj, tgt != nullptr, false, !md.frame, md.lyrNum, P, &tr);
-	if (md.frame || md.ldmWgt != 0.0)
-		SA_REQUIRE((size_t) m.N * m.N * sizeof(double) <= kDenseLimitBytes && m.N <= 65535,
-		           "dense RKHS kernel matrix exceeds the device budget for this node count");
+	choose_kernel_storage(md, m.N);
 	SA_REQUIRE(tauVarMat && tauVarNum >= (md.frame ? (D == 2 ? 4 : 4) : D + 2) && objNum >= 1,
 	           "tauVarMat too small");
 	const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
@@ -1142,7 +1157,7 @@ static int adjoint_frame_impl(sa_context *ctx, Pool &P, Mesh &m, Model &md, cons
 	while (st.t < T - 1 && status == SA_OK) {
 		st.pre_velocity();
 		int its = 0;
-		int code = kpcg<D>(m, md, w.blk, w.K, w.b, w.v, w.kw, st.st, &its, s);
+		int code = kpcg<D>(m, md, w.blk, w.K, st.xn, w.b, w.v, w.kw, st.st, &its, s);
 		st.out.cgTotal += its;
 		st.out.cgMax = std::max(st.out.cgMax, its);
 		if (code != SA_OK) { status = code; break; }
@@ -1200,10 +1215,10 @@ static int adjoint_frame_impl(sa_context *ctx, Pool &P, Mesh &m, Model &md, cons
 			launch_adj_axpy(n, aXn, dt - 1.0, aXn, rhsV, s);
 			// velocity adjoint: (ldm K_t^{-1} + E_t) n = a_v, K-preconditioned CG started from K_t times the
 			// previous step's K^{-1} n
-			launch_kernel_matrix<D>(md, m.N, xt, w.K, s);
+			if (!md.kernelFree) launch_kernel_matrix<D>(md, m.N, xt, w.K, s);
 			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xt, w.pd, s);
 			launch_assemble_elastic<D>(m, md, w.g0, w.pd, w.blk, w.dinv, nullptr, s);
-			code = kpcg<D>(m, md, w.blk, w.K, rhsV, nu, w.kw, stt, &its, s);
+			code = kpcg<D>(m, md, w.blk, w.K, xt, rhsV, nu, w.kw, stt, &its, s);
 			adjIts += its;
 			if (code != SA_OK) { status = code; break; }
 			const double *vt = vAll + (long) t * n, *bt = bAll + (long) t * n;
@@ -1284,7 +1299,7 @@ static int adjoint_impl(sa_context *ctx, const sa_element_object *obj, const dou
 		const double *tc = P.dev(tgt->cenPosMat, (size_t) tgt->tgtElmNum * D);
 		const double *tu = P.dev(tgt->uniDirMat, (size_t) tgt->tgtElmNum * D);
 		const double *tvl = P.dev(tgt->elmVolVec, (size_t) tgt->tgtElmNum);
-		SA_REQUIRE((size_t) m.N * m.N * sizeof(double) <= kDenseLimitBytes, "frame mode: N too large for the dense RKHS matrix");
+		choose_kernel_storage(md, m.N);
 		return adjoint_frame_impl<D>(ctx, P, m, md, x0, tv, tc, tu, tvl, tgt->tgtElmNum, objOut, gradBump, gradTau0,
 		                             gradX0, info, tr);
 	}
@@ -1470,9 +1485,7 @@ struct Session : SessionBase {
 		cudaStream_t s = c->stream;
 		fill_model(md, D, prm, tgt, P);
 		build_mesh(m, obj, tgt != nullptr, false, !md.frame, md.lyrNum, P);
-		if (md.frame || md.ldmWgt != 0.0)
-			SA_REQUIRE((size_t) m.N * m.N * sizeof(double) <= kDenseLimitBytes && m.N <= 65535,
-			           "dense RKHS kernel matrix exceeds the device budget for this node count");
+		choose_kernel_storage(md, m.N);
 		SA_REQUIRE(tv && tvNum >= (md.frame ? 4 : D + 2), "tauVarVec too small");
 		tauVar = to_host(tv, (size_t) tvNum, s);
 		const double *x0 = P.dev(lmkIni, (size_t) m.N * D);
@@ -2784,6 +2797,7 @@ int sa_set_tuning(const char *name, int value)
 	else if (n == "batchSlicesPerWarp" && value >= 1 && value <= 16) t.batchSlicesPerWarp = value;
 	else if (n == "vfdCtasPerSm" && value >= 1 && value <= 32) t.vfdCtasPerSm = value;
 	else if (n == "mixedInnerFloor" && value >= 4 && value <= 16) t.mixedInnerFloor = value;
+	else if (n == "kernelMatrixFree" && (value == 0 || value == 1)) t.kernelMatrixFree = value;
 	else return SA_ERR_ARG;
 	return SA_OK;
 }
@@ -2811,6 +2825,7 @@ int sa_get_tuning(const char *name, int *value)
 	else if (n == "batchSlicesPerWarp") *value = t.batchSlicesPerWarp;
 	else if (n == "vfdCtasPerSm") *value = t.vfdCtasPerSm;
 	else if (n == "mixedInnerFloor") *value = t.mixedInnerFloor;
+	else if (n == "kernelMatrixFree") *value = t.kernelMatrixFree;
 	else return SA_ERR_ARG;
 	return SA_OK;
 }

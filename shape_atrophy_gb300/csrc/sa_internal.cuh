@@ -248,6 +248,7 @@ struct Model {
 	int precision;             // SA_PREC_FP64 or SA_PREC_MIXED
 	int cgKernel = 0;          // SA_CG_AUTO / SA_CG_PERSISTENT / SA_CG_TWO_KERNEL
 	int velocityGuess = 0;     // layered model: SA_GUESS_PREVIOUS or SA_GUESS_EXTRAPOLATE
+	int kernelFree = 0;        // RKHS matrix evaluated on the fly instead of stored (too large, or requested)
 };
 
 // ---------------------------------------------------------------------------
@@ -450,6 +451,7 @@ struct Tuning {
 	int batchSlicesPerWarp = 2;    // 32-row slices per warp when a batched solve's CTAs are sized
 	int vfdCtasPerSm = 8;          // CTAs per SM of the varifold pair sums (column chunks)
 	int mixedInnerFloor = 10;      // mixed precision: inner FP32 solves stop at 10^-k squared relative residual
+	int kernelMatrixFree = 0;      // frame model: 1 = evaluate the RKHS matrix on the fly at every size
 };
 Tuning &tuning();
 
@@ -535,8 +537,9 @@ struct KpcgWork {
 	double *part, *scal;
 	int maxBlocks;
 };
-template <int D> int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *b,
-                          double *x, KpcgWork &w, Status *st, int *itersOut, cudaStream_t s);
+// K: the stored kernel matrix, or null to evaluate it on the fly from the node positions q (interleaved)
+template <int D> int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *q,
+                          const double *b, double *x, KpcgWork &w, Status *st, int *itersOut, cudaStream_t s);
 template <int D> void launch_kernel_matrix(const Model &md, int N, const double *x, double *K, cudaStream_t s);
 template <int D> void launch_adj_kernel_term(const Model &md, int N, const double *x, const double *alpha,
                                              const double *beta, double *ax, cudaStream_t s);

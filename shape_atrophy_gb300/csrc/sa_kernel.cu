@@ -201,26 +201,37 @@ void launch_adj_kernel_term(const Model &md, int N, const double *x, const doubl
 	k_adj_kernel_term<D><<<grid_for(N, 128), 128, 0, s>>>(N, x, alpha, beta, md.knlOrder, md.knlWidth, md.ldmWgt, ax);
 }
 
+// One RKHS matrix entry k(|q_i - q_j| / w) (without the eps diagonal).  Compiled once, not inlined: the
+// stored matrix and the matrix-free products evaluate it with the same instructions, so the compiler's
+// multiply-add fusion cannot differ between the two callers and both give the same bits.  Symmetric bit for
+// bit: (a - b)^2 = (b - a)^2 exactly.
+template <int D>
+__device__ __noinline__ double kernel_entry(int order, double w, Vec<D> qi, Vec<D> qj)
+{
+	double d2 = (qi.c[0] - qj.c[0]) * (qi.c[0] - qj.c[0]);
+	for (int d = 1; d < D; ++d) d2 = d2 + (qi.c[d] - qj.c[d]) * (qi.c[d] - qj.c[d]);
+	return kernel_value<D>(order, w, d2);
+}
+
 // K[j*N + i] = k(|q_i - q_j| / w) + eps * delta_ij
 template <int D>
 __global__ void k_kernel_matrix(int N, const double *__restrict__ x, int order, double w, double eps,
                                 double *__restrict__ K)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	int j = blockIdx.y;
 	if (i >= N) return;
-	Vec<D> qi = load_node<D>(x, i), qj = load_node<D>(x, j);
-	double d2 = (qi.c[0] - qj.c[0]) * (qi.c[0] - qj.c[0]);
-	for (int d = 1; d < D; ++d) d2 = d2 + (qi.c[d] - qj.c[d]) * (qi.c[d] - qj.c[d]);
-	double v = kernel_value<D>(order, w, d2);
-	if (i == j) v += eps;
-	K[(long) j * N + i] = v;
+	const Vec<D> qi = load_node<D>(x, i);
+	for (int j = blockIdx.y; j < N; j += gridDim.y) {
+		double v = kernel_entry<D>(order, w, qi, load_node<D>(x, j));
+		if (i == j) v += eps;
+		K[(long) j * N + i] = v;
+	}
 }
 
 template <int D>
 void launch_kernel_matrix(const Model &md, int N, const double *x, double *K, cudaStream_t s)
 {
-	dim3 g(grid_for(N, 128), N);
+	dim3 g(grid_for(N, 128), std::min(N, 65535));
 	k_kernel_matrix<D><<<g, 128, 0, s>>>(N, x, md.knlOrder, md.knlWidth, md.knlEps, K);
 }
 
@@ -270,6 +281,59 @@ void launch_dense_matvec(int N, const double *K, const double *x, double *y, dou
 {
 	dim3 g(grid_for(N, kDenseRows), kDenseSlices);
 	k_dense_partial<D><<<g, kDenseRows, 0, s>>>(N, K, x, part);
+	k_dense_sum<D><<<grid_for((long) N * D), kBlock, 0, s>>>(N, part, y);
+}
+
+// K X without the stored matrix (meshes whose N x N matrix does not fit): the same slices, tiles and
+// summation order as k_dense_partial, each K entry evaluated on the fly by the same kernel_entry as
+// k_kernel_matrix, so the result equals the stored-matrix product bit for bit.  Costs one kernel
+// evaluation (a square root, an exponential, and for 2D Matern the Bessel rational approximations) per
+// matrix entry instead of one 8-byte read.
+template <int D>
+__global__ void k_kernel_partial(int N, const double *__restrict__ q, int order, double w, double eps,
+                                 const double *__restrict__ X, double *__restrict__ part)
+{
+	__shared__ double xs[kDenseTile * D], qs[kDenseTile * D];
+	int i = blockIdx.x * kDenseRows + threadIdx.x;
+	int s = blockIdx.y;
+	int per = (N + kDenseSlices - 1) / kDenseSlices;
+	int j0 = s * per, j1 = min(N, j0 + per);
+	Vec<D> qi;
+	for (int d = 0; d < D; ++d) qi.c[d] = i < N ? q[(long) i * D + d] : 0.0;
+	double acc[D];
+	for (int d = 0; d < D; ++d) acc[d] = 0.0;
+	for (int jt = j0; jt < j1; jt += kDenseTile) {
+		int nt = min(kDenseTile, j1 - jt);
+		__syncthreads();
+		for (int t = threadIdx.x; t < nt * D; t += blockDim.x) {
+			xs[t] = X[(long) jt * D + t];
+			qs[t] = q[(long) jt * D + t];
+		}
+		__syncthreads();
+		if (i < N)
+			for (int jj = 0; jj < nt; ++jj) {
+				Vec<D> qj;
+				for (int d = 0; d < D; ++d) qj.c[d] = qs[jj * D + d];
+				double k = kernel_entry<D>(order, w, qi, qj);
+				if (i == jt + jj) k += eps;
+				for (int d = 0; d < D; ++d) acc[d] += k * xs[jj * D + d];
+			}
+	}
+	if (i < N)
+		for (int d = 0; d < D; ++d) part[((long) s * N + i) * D + d] = acc[d];
+}
+
+// y = K x with K stored (dense) or, when K is null, evaluated from the node positions q
+template <int D>
+static void kernel_matvec(const Model &md, int N, const double *K, const double *q, const double *x, double *y,
+                          double *part, cudaStream_t s)
+{
+	if (K) {
+		launch_dense_matvec<D>(N, K, x, y, part, s);
+		return;
+	}
+	dim3 g(grid_for(N, kDenseRows), kDenseSlices);
+	k_kernel_partial<D><<<g, kDenseRows, 0, s>>>(N, q, md.knlOrder, md.knlWidth, md.knlEps, x, part);
 	k_dense_sum<D><<<grid_for((long) N * D), kBlock, 0, s>>>(N, part, y);
 }
 
@@ -480,8 +544,8 @@ __global__ void k_kp_zero(long n, double *x, double *w, const KScal *sc)
 }
 
 template <int D>
-int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *b, double *x,
-         KpcgWork &wk, Status *st, int *itersOut, cudaStream_t s)
+int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *q, const double *b,
+         double *x, KpcgWork &wk, Status *st, int *itersOut, cudaStream_t s)
 {
 	(void) st;
 	int N = m.N;
@@ -494,9 +558,9 @@ int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, con
 	double *dpart = wk.part + 4 * (long) nb;     // dense matvec slice partials
 	k_kp_bnorm<D><<<nb, kKBlock, 0, s>>>(N, b, wk.part, sc);
 	// warm start x0 = K w (w = K^{-1} v of the previous step)
-	launch_dense_matvec<D>(N, K, wk.wK, x, dpart, s);
+	kernel_matvec<D>(md, N, K, q, wk.wK, x, dpart, s);
 	k_kp_init_r<D><<<nb, kKBlock, 0, s>>>(sell_of(m), blk, b, x, wk.wK, wk.r, wk.part, sc);
-	launch_dense_matvec<D>(N, K, wk.r, wk.Kr, dpart, s);
+	kernel_matvec<D>(md, N, K, q, wk.r, wk.Kr, dpart, s);
 	k_kp_rkr<D><<<nb, kKBlock, 0, s>>>(N, wk.r, wk.Kr, wk.part, sc, 1);
 	k_kp_dir<D><<<grid_for(n), kBlock, 0, s>>>(N, wk.r, wk.Kr, wk.Kid, wk.dv, sc, 1);
 	const int chunk = 8;
@@ -504,7 +568,7 @@ int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, con
 		for (int k = 0; k < chunk; ++k) {
 			k_kp_ad<D><<<nb, kKBlock, 0, s>>>(sell_of(m), blk, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
 			k_kp_step<D><<<nb, kKBlock, 0, s>>>(N, x, wk.wK, wk.r, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
-			launch_dense_matvec<D>(N, K, wk.r, wk.Kr, dpart, s);
+			kernel_matvec<D>(md, N, K, q, wk.r, wk.Kr, dpart, s);
 			k_kp_rkr<D><<<nb, kKBlock, 0, s>>>(N, wk.r, wk.Kr, wk.part, sc, 0);
 			k_kp_dir<D><<<grid_for(n), kBlock, 0, s>>>(N, wk.r, wk.Kr, wk.Kid, wk.dv, sc, 0);
 		}
@@ -526,9 +590,9 @@ template void launch_adj_kernel_term<3>(const Model &, int, const double *, cons
                                         cudaStream_t);
 template void launch_kernel_matrix<2>(const Model &, int, const double *, double *, cudaStream_t);
 template void launch_kernel_matrix<3>(const Model &, int, const double *, double *, cudaStream_t);
-template int kpcg<2>(const Mesh &, const Model &, const double *, const double *, const double *, double *,
-                     KpcgWork &, Status *, int *, cudaStream_t);
-template int kpcg<3>(const Mesh &, const Model &, const double *, const double *, const double *, double *,
-                     KpcgWork &, Status *, int *, cudaStream_t);
+template int kpcg<2>(const Mesh &, const Model &, const double *, const double *, const double *, const double *,
+                     double *, KpcgWork &, Status *, int *, cudaStream_t);
+template int kpcg<3>(const Mesh &, const Model &, const double *, const double *, const double *, const double *,
+                     double *, KpcgWork &, Status *, int *, cudaStream_t);
 
 }  // namespace sa

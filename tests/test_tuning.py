@@ -10,7 +10,7 @@ import pytest
 from shape_atrophy_gb300 import api
 
 DEFAULTS = {"persistMaxWarps": 20, "batchBlock": 256, "batchSlicesPerWarp": 2, "vfdCtasPerSm": 8,
-            "mixedInnerFloor": 10}
+            "mixedInnerFloor": 10, "kernelMatrixFree": 0}
 
 
 @pytest.fixture
@@ -27,14 +27,16 @@ def test_compiled_defaults(restore):
 
 
 def test_set_get_round_trip(restore):
-    api.set_tuning(persistMaxWarps=8, batchBlock=128, batchSlicesPerWarp=4, vfdCtasPerSm=2, mixedInnerFloor=12)
+    api.set_tuning(persistMaxWarps=8, batchBlock=128, batchSlicesPerWarp=4, vfdCtasPerSm=2, mixedInnerFloor=12,
+                   kernelMatrixFree=1)
     assert api.get_tuning() == {"persistMaxWarps": 8, "batchBlock": 128, "batchSlicesPerWarp": 4,
-                                "vfdCtasPerSm": 2, "mixedInnerFloor": 12}
+                                "vfdCtasPerSm": 2, "mixedInnerFloor": 12, "kernelMatrixFree": 1}
 
 
 @pytest.mark.parametrize("name,value", [("persistMaxWarps", 0), ("persistMaxWarps", 21), ("batchBlock", 192),
                                         ("batchBlock", 512), ("batchSlicesPerWarp", 0), ("vfdCtasPerSm", 33),
                                         ("mixedInnerFloor", 3), ("mixedInnerFloor", 17),
+                                        ("kernelMatrixFree", 2),
                                         ("noSuchShape", 1)])
 def test_bad_values_refused(restore, name, value):
     before = api.get_tuning()
