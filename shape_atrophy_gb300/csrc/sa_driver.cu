@@ -559,8 +559,10 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 		KpcgWork &k = w.kw;
 		k.Ad = P.alloc<double>(n); k.Kid = P.alloc<double>(n); k.r = P.alloc<double>(n);
 		k.Kr = P.alloc<double>(n); k.dv = P.alloc<double>(n); k.wK = P.zeros<double>(n);
-		k.part = P.alloc<double>((size_t) 4 * nb + 16 * n + 64); k.scal = P.zeros<double>(32);
+		k.partLen = (long) 4 * nb + 16 * n + 64;
+		k.part = P.alloc<double>((size_t) k.partLen); k.scal = P.zeros<double>(32);
 		k.maxBlocks = nb;
+		k.dv2 = P.alloc<double>(n); k.bar = P.zeros<char>(kGridBarBytes);
 		if (!md.kernelFree) w.K = P.alloc<double>((size_t) N * N);
 	}
 	if (wantTraj) {

@@ -534,8 +534,11 @@ int fma_peak_selftest(cudaStream_t s, int fp64, double *tflops, double *flopsPer
 // frame mode K-preconditioned CG (2D/ipcg.cu:11-100) with dense K
 struct KpcgWork {
 	double *Ad, *Kid, *r, *Kr, *dv, *wK;  // wK tracks K^{-1} x
+	double *dv2 = nullptr;                // second direction buffer of the persistent K-PCG
+	void *bar = nullptr;                  // its grid barrier (kGridBarBytes)
 	double *part, *scal;
 	int maxBlocks;
+	long partLen = 0;                     // doubles in part
 };
 // K: the stored kernel matrix, or null to evaluate it on the fly from the node positions q (interleaved)
 template <int D> int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *q,

@@ -16,6 +16,7 @@
 // exactly.  The converged velocity is the same solution of the same system
 // to the CG tolerance.
 #include "sa_internal.cuh"
+#include "sa_grid.cuh"
 #include <cmath>
 
 namespace sa {
@@ -543,6 +544,197 @@ __global__ void k_kp_zero(long n, double *x, double *w, const KScal *sc)
 	if (k < n) { x[k] = 0.0; w[k] = 0.0; }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent K-preconditioned CG: one cooperative launch runs all iterations of the loop below (six
+// launches per iteration there).  One CTA per SM, kKpWarps warps.  Per iteration three grid-wide exact
+// sums (sa_grid.cuh), which are also the grid's barriers:
+//   A  rows (grid-stride, one thread per row): Kid = r + beta Kid, d = Kr + beta d and
+//      Ad = ldm Kid + (E + btm P) d, with (d, Ad) -> alpha.  A row that gathers a neighbour's d forms it
+//      the same way from the neighbour's previous d and Kr (two d buffers alternate), so no barrier
+//      separates the direction update from the operator;
+//   B  rows: x += alpha d, w += alpha Kid, r -= alpha Ad, with (r, r) -> stop test;
+//   C  Kr = K r, with (r, Kr) -> beta.  Each CTA forms the whole rows of its row range: K is symmetric bit
+//      for bit (kernel_entry squares differences), so row i is read contiguously, lanes over columns,
+//      warps over (row, column segment) units, a fixed shuffle tree per unit and the segments added in a
+//      fixed order in shared memory.  The matrix-free form evaluates each entry with the same
+//      kernel_entry call the stored matrix was written with, in the same place: both give the same bits.
+// Vectors that other CTAs write during the launch are read with __ldcg (L2), never through the
+// incoherent L1.  Iterates, stopping rule and status codes are those of the loop below.
+// ---------------------------------------------------------------------------
+constexpr int kKpWarps = 16;
+constexpr int kKpUnits = 512;     // (row, segment) units per chunk of phase C
+
+struct KpVec {
+	double *x, *w, *r, *Kr, *Kid, *d0, *d1, *Ad;
+};
+
+__device__ __forceinline__ double kp_dir(double kr, double dOld, double be, bool first)
+{
+	return first ? kr : __fma_rn(be, dOld, kr);
+}
+
+template <int D, bool kFree>
+__global__ void __launch_bounds__(32 * kKpWarps, 1)
+k_kpcg_persist(SellOp A, const double *__restrict__ blk, const double *__restrict__ K, const double *__restrict__ q,
+               int order, double kw, double eps, KpVec v, double *part, KScal *sc, GridBar *bar)
+{
+	__shared__ FxScratch fs;
+	__shared__ double segPart[kKpUnits][D];
+	if (sc->done) return;                       // set before the launch: the same for every CTA
+	const int N = A.N, nctas = gridDim.x, lc = blockIdx.x;
+	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, W = blockDim.x >> 5;
+	const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+	const double bSqu = sc->bSqu, tolSqu = sc->tolSqu, ldm = sc->ldmWgt;
+	const int itrMax = sc->itrMax;
+	double rKr = sc->rKr, rr = sc->rSqu, be = 0.0;
+	int it = sc->iters, code = SA_OK;
+	bool first = true;
+	unsigned int target = 0;
+	double *partA = part, *partB = part + nctas, *partC = part + 2 * nctas;
+	// phase C's row range and (row, segment) units
+	const int r0 = (int) ((long) N * lc / nctas), r1 = (int) ((long) N * (lc + 1) / nctas), R = r1 - r0;
+	const int SEG = min(8, max(1, (2 * W + max(R, 1) - 1) / max(R, 1)));
+	const int RC = kKpUnits / SEG;
+	double *dOld = v.d0, *dNew = v.d1;
+	for (;;) {
+		// A: direction, operator, (d, Ad)
+		double loc[1] = {0.0}, res[1];
+		for (int i = gtid; i < N; i += gstride) {
+			const int sl = i >> 5, ln = i & 31;
+			const int wdt = __ldg(A.width + sl);
+			const long base = __ldg(A.off + sl) + ln;
+			double acc[D];
+			for (int c = 0; c < D; ++c) acc[c] = 0.0;
+			for (int k = 0; k < wdt; ++k) {
+				const long idx = base + ((long) k << 5);
+				const int j = __ldg(A.col + idx);
+				double dj[D];
+				for (int c = 0; c < D; ++c)
+					dj[c] = kp_dir(__ldcg(v.Kr + (long) j * D + c), first ? 0.0 : __ldcg(dOld + (long) j * D + c),
+					               be, first);
+				double a[D * D];
+				load_block<D, double>(blk, A.total, idx, a);
+				for (int r = 0; r < D; ++r)
+					for (int c = 0; c < D; ++c) acc[r] += a[r * D + c] * dj[c];
+			}
+			for (int c = 0; c < D; ++c) {
+				const long k = (long) i * D + c;
+				const double ri = __ldcg(v.r + k);
+				const double kid = first ? ri : __fma_rn(be, v.Kid[k], ri);
+				const double di = kp_dir(__ldcg(v.Kr + k), first ? 0.0 : __ldcg(dOld + k), be, first);
+				const double ad = __fma_rn(ldm, kid, acc[c]);
+				v.Kid[k] = kid;
+				dNew[k] = di;
+				v.Ad[k] = ad;
+				loc[0] += di * ad;
+			}
+		}
+		if (!grid_reduce<1, double>(loc, res, partA, lc, nctas, bar, target, fs)) { code = SA_ERR_TIMEOUT; break; }
+		const double dAd = res[0];
+		if (dAd == 0.0 || !isfinite(dAd)) { code = isfinite(dAd) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE; break; }
+		const double alpha = rKr / dAd;
+		// B: x, w, r and (r, r)
+		loc[0] = 0.0;
+		for (int i = gtid; i < N; i += gstride)
+			for (int c = 0; c < D; ++c) {
+				const long k = (long) i * D + c;
+				v.x[k] = __fma_rn(alpha, dNew[k], v.x[k]);
+				v.w[k] = __fma_rn(alpha, v.Kid[k], v.w[k]);
+				const double rk = __fma_rn(-alpha, v.Ad[k], v.r[k]);
+				v.r[k] = rk;
+				loc[0] += rk * rk;
+			}
+		if (!grid_reduce<1, double>(loc, res, partB, lc, nctas, bar, target, fs)) { code = SA_ERR_TIMEOUT; break; }
+		rr = res[0];
+		++it;
+		if (!isfinite(rr)) { code = SA_ERR_NONFINITE; break; }
+		if (rr < bSqu * tolSqu) { code = SA_OK; break; }
+		if (it >= itrMax) { code = SA_ERR_NOT_CONVERGED; break; }
+		// C: Kr = K r over the CTA's rows, (r, Kr)
+		loc[0] = 0.0;
+		for (int c0 = r0; c0 < r1; c0 += RC) {
+			const int rc = min(RC, r1 - c0), units = rc * SEG;
+			for (int u = wp; u < units; u += W) {
+				const int i = c0 + u / SEG, sg = u % SEG;
+				const int j0 = (int) ((long) N * sg / SEG), j1 = (int) ((long) N * (sg + 1) / SEG);
+				double acc[D];
+				for (int c = 0; c < D; ++c) acc[c] = 0.0;
+				Vec<D> qi;
+				if constexpr (kFree) qi = load_node<D>(q, i);
+#pragma unroll 4
+				for (int j = j0 + lane; j < j1; j += 32) {
+					double kij;
+					if constexpr (kFree) {
+						kij = kernel_entry<D>(order, kw, load_node<D>(q, j), qi);   // as K[i N + j] was written
+						if (i == j) kij += eps;
+					} else {
+						kij = __ldg(K + (long) i * N + j);
+					}
+					for (int c = 0; c < D; ++c) acc[c] += kij * __ldcg(v.r + (long) j * D + c);
+				}
+				for (int c = 0; c < D; ++c)
+					for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], off);
+				if (lane == 0)
+					for (int c = 0; c < D; ++c) segPart[u][c] = acc[c];
+			}
+			__syncthreads();
+			for (int t = threadIdx.x; t < rc * D; t += blockDim.x) {
+				const int il = t / D, c = t - il * D;
+				double sum = 0.0;
+				for (int sg = 0; sg < SEG; ++sg) sum += segPart[il * SEG + sg][c];
+				const long k = (long) (c0 + il) * D + c;
+				v.Kr[k] = sum;
+				loc[0] += v.r[k] * sum;
+			}
+			__syncthreads();
+		}
+		if (!grid_reduce<1, double>(loc, res, partC, lc, nctas, bar, target, fs)) { code = SA_ERR_TIMEOUT; break; }
+		const double o = res[0];
+		if (o == 0.0 || !isfinite(o)) { code = isfinite(o) ? SA_ERR_BREAKDOWN : SA_ERR_NONFINITE; break; }
+		be = o / rKr;
+		rKr = o;
+		first = false;
+		double *t = dOld; dOld = dNew; dNew = t;
+	}
+	if (lc == 0 && threadIdx.x == 0) {
+		sc->iters = it; sc->code = code; sc->rSqu = rr; sc->rKr = rKr; sc->done = 1;
+	}
+}
+
+static int device_sm_count()
+{
+	int dev = 0, n = 0;
+	SA_CHECK(cudaGetDevice(&dev));
+	SA_CHECK(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+	return n;
+}
+
+// one cooperative launch of the persistent K-PCG when every SM can hold one of its CTAs; false: use the loop
+template <int D, bool kFree>
+static bool kpcg_persist_launch(const Mesh &m, const Model &md, const double *blk, const double *K, const double *q,
+                                double *x, KpcgWork &wk, KScal *sc, cudaStream_t s)
+{
+	int occ = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_kpcg_persist<D, kFree>, 32 * kKpWarps, 0) !=
+	    cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	const int nctas = device_sm_count();
+	if (occ < 1 || 3L * nctas > wk.partLen) return false;
+	GridBar *bar = (GridBar *) wk.bar;
+	SA_CHECK(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
+	SellOp A = sell_of(m);
+	KpVec v{x, wk.wK, wk.r, wk.Kr, wk.Kid, wk.dv, wk.dv2, wk.Ad};
+	int order = md.knlOrder;
+	double kw = md.knlWidth, eps = md.knlEps;
+	double *part = wk.part;
+	void *args[] = {&A, (void *) &blk, (void *) &K, (void *) &q, &order, &kw, &eps, &v, &part, &sc, &bar};
+	SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_kpcg_persist<D, kFree>, dim3(nctas), dim3(32 * kKpWarps),
+	                                     args, 0, s));
+	return true;
+}
+
 template <int D>
 int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, const double *q, const double *b,
          double *x, KpcgWork &wk, Status *st, int *itersOut, cudaStream_t s)
@@ -563,8 +755,11 @@ int kpcg(const Mesh &m, const Model &md, const double *blk, const double *K, con
 	kernel_matvec<D>(md, N, K, q, wk.r, wk.Kr, dpart, s);
 	k_kp_rkr<D><<<nb, kKBlock, 0, s>>>(N, wk.r, wk.Kr, wk.part, sc, 1);
 	k_kp_dir<D><<<grid_for(n), kBlock, 0, s>>>(N, wk.r, wk.Kr, wk.Kid, wk.dv, sc, 1);
+	const bool persist = md.cgKernel != SA_CG_TWO_KERNEL && wk.bar && wk.dv2 &&
+	                     (K ? kpcg_persist_launch<D, false>(m, md, blk, K, q, x, wk, sc, s)
+	                        : kpcg_persist_launch<D, true>(m, md, blk, K, q, x, wk, sc, s));
 	const int chunk = 8;
-	for (int it = 0; it < md.cgItrMax + chunk; it += chunk) {
+	for (int it = 0; !persist && it < md.cgItrMax + chunk; it += chunk) {
 		for (int k = 0; k < chunk; ++k) {
 			k_kp_ad<D><<<nb, kKBlock, 0, s>>>(sell_of(m), blk, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
 			k_kp_step<D><<<nb, kKBlock, 0, s>>>(N, x, wk.wK, wk.r, wk.dv, wk.Kid, wk.Ad, wk.part, sc);
