@@ -13,6 +13,8 @@ instructions in the same order.  Checked:
 - every reference golden case (2D and 3D, Matern orders 0-4 and Gaussian, CG failure): the matrix-free
   forward equals the stored-matrix forward bit for bit (positions, concentration, objective);
 - the frame adjoint (2D demo strip): bit for bit;
+- the layered model with the LDDMM term switched on (annulus and shell): the CPU oracle at 1e-10, the launch
+  loop at 1e-10, matrix-free bit for bit;
 - a 30 744-node shell (7.6 GB matrix, one step): bit for bit at that size;
 - a 71 694-node shell, whose 41 GB matrix has more than 65 535 columns: the solve runs, and its
   displacement is invariant to a translation of the mesh and the bump centre, to 1e-6 of its largest
@@ -134,3 +136,32 @@ def test_large_stored_matrix_translation_invariant():
           "translation difference", np.abs(da - db).max() / np.abs(da).max())
     assert np.abs(da - db).max() <= 1e-6 * np.abs(da).max()
     assert np.abs(a["tauMat"] - b["tauMat"]).max() <= 1e-6 * np.abs(a["tauMat"]).max()
+
+
+def _layered_rkhs(case):
+    from shape_atrophy_gb300 import problems
+    if case == "annulus":
+        spec = problems.annulus_layered(angNum=48, radNum=7, steps=4, cgTolVal=1e-12)
+    else:
+        spec = problems.shell_layered(level=2, lyrCntNum=4, steps=3, cgTolVal=1e-12)
+    return dict(spec, ldmWgt=1e-2, knlOrder=1, knlWidth=0.2, knlEps=1e-10)
+
+
+@pytest.mark.parametrize("case", ["annulus", "shell"])
+def test_layered_model_with_rkhs_term(matrix_free, case):
+    """The layered model with the LDDMM term switched on (ldmWgt != 0) runs the same K-preconditioned CG on
+    the layered operator: oracle parity at 1e-10, the launch loop at 1e-10, matrix-free bit for bit."""
+    from oracle.oracle import Problem
+    from shape_atrophy_gb300 import api
+    spec = _layered_rkhs(case)
+    want = Problem(spec).forward(spec["tauVarVec"], with_obj=True)
+    assert want["status"] == 0
+    a, b = _both(lambda: api.forward(spec, trajectory=True, objective=True), matrix_free)
+    loop = api.forward(dict(spec, cgKernel="two-kernel"), trajectory=True, objective=True)
+    for got in (a, b, loop):
+        assert got["info"]["status"] == 0
+        assert rel(got["lmkStk"], want["lmkStk"]) < 1e-10
+        assert rel(got["tauMat"], want["tauMat"]) < 1e-10
+        assert abs(got["obj"][0] - want["obj"]) <= 1e-10 * abs(want["obj"])
+    np.testing.assert_array_equal(a["lmkStk"], b["lmkStk"])
+    np.testing.assert_array_equal(a["obj"], b["obj"])
