@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <queue>
 
 namespace sa {
 
@@ -450,7 +451,7 @@ constexpr int kColSmemMax = 160 * 1024;    // shared memory for a CTA's column i
 template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
 k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, const TV *__restrict__ binv, TX *x,
-             const TV *r0, TV *u, double *part, CgScal *sc, GridBar *bar)
+             const TV *r0, TV *u, double *part, CgScal *sc, GridBar *bar, const int *__restrict__ ctaTab)
 {
 	__shared__ FxScratch fs;                     // block sums; fs.tot = gamma, rr of the last update
 	__shared__ double nx[4];                     // next gamma, rr, beta, beta * gamma / alphaPrev
@@ -462,19 +463,20 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
 	const int H = (blockDim.x >> 5) - 1;         // the reducer warp; warps 0 .. H-1 own one slice each
 	const bool reducer = wp == H;
-	const int sl = lc * H + wp;
-	const int nsl = (A.N + 31) >> 5;
+	// the slice of each row warp (-1: none) and its place in the CTA's column cache: slices are dealt to
+	// CTAs by slot count, so every CTA's matvec takes about as long (ctaTab, built on the host)
+	const int sl = reducer ? -1 : __ldg(ctaTab + lc * H + wp);
 	const int i = sl * 32 + lane;
-	const bool rowWarp = !reducer && sl < nsl;
+	const bool rowWarp = sl >= 0;
 	const bool own = rowWarp && i < A.N;
 	const int wdt = rowWarp ? __ldg(A.width + sl) : 0;
 	const long base = rowWarp ? __ldg(A.off + sl) + lane : 0;
-	// the CTA's slices are consecutive, so their slots are one range [c0, c1) of the sliced layout; its
-	// columns do not change during the solve: one coalesced copy, then no dependent column load per slot
-	const long c0 = __ldg(A.off + lc * H);
-	const long c1 = (lc + 1) * H < nsl ? (long) __ldg(A.off + (lc + 1) * H) : A.total;
-	for (long t = threadIdx.x; t < c1 - c0; t += blockDim.x) scol[t] = __ldg(A.col + c0 + t);
-	const int lbase = (int) (base - c0);         // local slot of lane's slot 0 (row warps)
+	// the columns do not change during the solve: each row warp copies its slice's into the CTA's cache
+	// once, then no slot waits for a column load
+	const int coff = rowWarp ? __ldg(ctaTab + (long) gridDim.x * H + lc * H + wp) : 0;
+	if (rowWarp)
+		for (int t = lane; t < 32 * wdt; t += 32) scol[coff + t] = __ldg(A.col + (base - lane) + t);
+	const int lbase = coff + lane;               // local slot of lane's slot 0 (row warps)
 	__syncthreads();                             // scol and gaveUp before their first use
 	const double bb = sc->bb, tolSqu = sc->tolSqu;
 	const int itrMax = sc->itrMax;
@@ -546,8 +548,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 				partD[lc] = cta1[0];
 				__threadfence();
 				atomicAdd(&bar->count, 1u);
-				ok = wait_grid(bar, target) ? 1 : 0;
-				__threadfence();
+				ok = wait_grid(bar, target) ? 1 : 0;      // its acquire load orders the reads below
 			}
 			ok = __shfl_sync(0xffffffffu, ok, 0);
 			__syncwarp();                        // orders lane 0's acquire before the other lanes' loads
@@ -593,8 +594,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			partG[nctas + lc] = cta2[1];
 			__threadfence();
 			atomicAdd(&bar->count, 1u);
-			if (!wait_grid(bar, target)) gaveUp = 1;
-			__threadfence();
+			if (!wait_grid(bar, target)) gaveUp = 1;   // its acquire load orders the reads below
 		} else if (own) {
 			for (int c = 0; c < B; ++c) xv[c] = xv[c] + (TX) al_ * (TX) pv[c];   // while the reducer waits
 		}
@@ -709,8 +709,7 @@ k_cg_persist_g(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv
 				partD[lc] = cta1[0];
 				__threadfence();
 				atomicAdd(&bar->count, 1u);
-				ok = wait_grid(bar, target) ? 1 : 0;
-				__threadfence();
+				ok = wait_grid(bar, target) ? 1 : 0;      // its acquire load orders the reads below
 			}
 			ok = __shfl_sync(0xffffffffu, ok, 0);
 			__syncwarp();
@@ -771,8 +770,7 @@ k_cg_persist_g(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv
 				partG[nctas + lc] = cta2[1];
 				__threadfence();
 				atomicAdd(&bar->count, 1u);
-				if (!wait_grid(bar, target)) gaveUp = 1;
-				__threadfence();
+				if (!wait_grid(bar, target)) gaveUp = 1;   // its acquire load orders the reads below
 			}
 		} else {
 			for (int sl = s0 + wp; sl < s1; sl += H) {
@@ -1133,15 +1131,49 @@ static size_t col_span_bytes_even(const Mesh &m, int nctas)
 	return (size_t) span * sizeof(int);
 }
 
-// largest slot range of one CTA (pw consecutive slices), in column-index bytes
-static size_t col_span_bytes(const Mesh &m, int pw)
+// Slices of the persistent CG's CTAs: nctas CTAs x pw row warps, one slice per warp; warp w runs on SM
+// sub-partition w % 4, whose FP64 pipe serves only its own warps.  Slices are dealt by slot count, largest
+// first, each to the (CTA, sub-partition) with the least work that still has a free warp, so every
+// sub-partition's matvec takes about as long (on the layered shell the inner and outer node layers have
+// about half the neighbours of the others: consecutive slices per CTA left the busiest sub-partition 11 %
+// above the mean, this 7 %).  The per-row arithmetic and the exact grid sums do not depend on where a row
+// runs, so the assignment changes no result.  Layout: nctas * pw slice ids (-1: none), then nctas * pw
+// offsets into the CTA's column cache.  Returns the largest column cache in bytes, or (size_t) -1 without
+// the host copy of the slice offsets.
+static size_t balanced_cta_table(const Mesh &m, int pw, int nctas, std::vector<int> &tab)
 {
-	long span = 0;
 	const std::vector<int> &off = m.slOffHost;
-	if ((int) off.size() != m.nslice + 1) return (size_t) -1;
-	for (int s0 = 0; s0 < m.nslice; s0 += pw) {
-		const int s1 = std::min(m.nslice, s0 + pw);
-		span = std::max(span, (long) off[s1] - off[s0]);
+	const int ns = m.nslice;
+	if ((int) off.size() != ns + 1 || pw < 1 || (long) nctas * pw < ns) return (size_t) -1;
+	auto slots = [&](int sl) { return (long) off[sl + 1] - off[sl]; };
+	std::vector<int> order(ns);
+	for (int k = 0; k < ns; ++k) order[k] = k;
+	std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return slots(a) > slots(b); });
+	int cap[4] = {0, 0, 0, 0};                          // row warps per sub-partition
+	for (int w = 0; w < pw; ++w) ++cap[w % 4];
+	typedef std::pair<long, int> Load;                  // (slots so far, bin = 4 CTA + sub-partition)
+	std::priority_queue<Load, std::vector<Load>, std::greater<Load>> open;
+	for (int c = 0; c < nctas; ++c)
+		for (int q = 0; q < 4; ++q)
+			if (cap[q] > 0) open.push(Load(0, 4 * c + q));
+	std::vector<int> used((size_t) 4 * nctas, 0);
+	tab.assign((size_t) 2 * nctas * pw, -1);
+	for (int sl : order) {
+		const Load l = open.top();
+		open.pop();
+		const int c = l.second >> 2, q = l.second & 3;
+		tab[(size_t) c * pw + q + 4 * used[l.second]] = sl;
+		if (++used[l.second] < cap[q]) open.push(Load(l.first + slots(sl), l.second));
+	}
+	long span = 0;
+	for (int c = 0; c < nctas; ++c) {
+		long cache = 0;
+		for (int w = 0; w < pw; ++w) {
+			tab[(size_t) nctas * pw + (size_t) c * pw + w] = (int) cache;
+			const int sl = tab[(size_t) c * pw + w];
+			if (sl >= 0) cache += slots(sl);
+		}
+		span = std::max(span, cache);
 	}
 	return (size_t) span * sizeof(int);
 }
@@ -1172,9 +1204,19 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	const int pwCap = std::max(1, std::min(kPersistMaxWarps, tuning().persistMaxWarps) - 1);
 	const int pw = std::max(1, std::min(pwCap, (m.nslice + prof->smCount - 1) / prof->smCount));
 	const int nctas = (m.nslice + pw - 1) / pw;
-	const size_t colSmem = col_span_bytes(m, pw);
+	if (prof->ctaTab && (prof->ctaTabWarps != pw || prof->ctaTabCtas != nctas) && 2L * nctas * pw <= prof->ctaTabCap) {
+		prof->ctaTabSmem = balanced_cta_table(m, pw, nctas, prof->ctaTabHost);
+		if (prof->ctaTabSmem != (size_t) -1) {
+			SA_CHECK(cudaMemcpyAsync(prof->ctaTab, prof->ctaTabHost.data(), sizeof(int) * prof->ctaTabHost.size(),
+			                         cudaMemcpyHostToDevice, s));
+			prof->ctaTabWarps = pw;
+			prof->ctaTabCtas = nctas;
+		}
+	}
+	const bool tabOk = prof->ctaTab && prof->ctaTabWarps == pw && prof->ctaTabCtas == nctas;
+	const size_t colSmem = tabOk ? prof->ctaTabSmem : (size_t) -1;
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->cgKernel != SA_CG_PERSISTENT_GLOBAL && prof->bar &&
-	                     (!block_prec<TV>() || prof->binv32) &&
+	                     (!block_prec<TV>() || prof->binv32) && tabOk &&
 	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw + 1, colSmem);
 	if (persist) {
 		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first).  FP32
@@ -1190,8 +1232,9 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		SA_CHECK(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
 		SellOp A = sell_of(m);
 		const TV *r0 = r;
+		const int *tab = prof->ctaTab;
 		void *args[] = {&A, (void *) &blk, (void *) &dinv, (void *) &binv, (void *) &x, (void *) &r0, (void *) &u,
-		                (void *) &part, (void *) &sc, (void *) &bar};
+		                (void *) &part, (void *) &sc, (void *) &bar, (void *) &tab};
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
 		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
 		                                     dim3(32 * (pw + 1)), args, colSmem, s));

@@ -2,7 +2,10 @@
 //
 // A reduction is also a barrier: every CTA publishes its partial sums, counts itself in, waits for the
 // count of the whole grid and then adds all partials exactly in 128-bit fixed point (sa_fixsum.cuh:
-// order-independent, rounded once), so every CTA obtains the same value.  Waits are bounded: a CTA that
+// order-independent, rounded once), so every CTA obtains the same value.  Ordering: the arriving thread
+// fences its CTA's writes (after a CTA barrier) before its relaxed atomic arrival, the waiting thread reads
+// the count with acquire loads, and a CTA (or warp) barrier then passes the order on to the other threads:
+// a release-acquire chain at GPU scope, without a second fence after the wait.  Waits are bounded: a CTA that
 // waits longer than kBarWaitNs (or sees another CTA give up) returns false and the kernel stops with a
 // timeout status.
 #pragma once
@@ -118,8 +121,7 @@ __device__ __forceinline__ bool grid_reduce(const T (&v)[K], double (&res)[K], d
 			if (load_acquire(&bar->abort)) { ok = 0; break; }
 			if (global_ns() - t0 > kBarWaitNs) { atomicExch(&bar->abort, 1u); ok = 0; break; }
 		}
-		__threadfence();
-		fs.ok = ok;
+		fs.ok = ok;            // the acquire load that saw the count orders the partial reads after the barrier
 	}
 	__syncthreads();
 	if (!fs.ok) return false;

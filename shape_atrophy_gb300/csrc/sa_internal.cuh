@@ -476,6 +476,13 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	long long launches = 0;       // kernel launches issued (CG loops and the time stepper)
 	void *pinned = nullptr;       // two host copies of the CG status (chunk pipelining)
 	cudaEvent_t chunkEv[2] = {};
+	// persistent CG: slices of each CTA's row warps, balanced by slot count (device: slice ids, then column
+	// cache offsets, nctas x warps each; host copy kept until its upload has completed)
+	int *ctaTab = nullptr;
+	long ctaTabCap = 0;           // ints allocated at ctaTab
+	int ctaTabWarps = 0, ctaTabCtas = 0;
+	size_t ctaTabSmem = 0;        // largest column cache of one CTA, bytes
+	std::vector<int> ctaTabHost;
 
 	CgWork() = default;
 	CgWork(const CgWork &) = delete;
