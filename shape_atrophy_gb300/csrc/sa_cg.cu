@@ -433,17 +433,79 @@ __device__ __forceinline__ void spmv_slot_cg(const SellOp &A, const TM *__restri
 // after the next matvec (that matvec is discarded), so iterates and iteration counts are those of the
 // plain Chronopoulos-Gear loop.
 
-// a slot whose column is already known (the persistent CG keeps its CTA's columns in shared memory)
-template <int B, typename TM, typename TV>
+// Stride of the persistent CG's gather copy of u: 3-component node blocks padded to 4, so a gathered node
+// is one 16-byte load (FP32) or two (FP64) instead of three scalar loads, each of which is its own L2
+// request for a random node; 2-component blocks load as one vector.
+template <int B> constexpr int gather_stride() { return B == 3 ? 4 : B; }
+
+// node j of u (stride S; read through L2: written during the launch)
+template <int B, int S, typename TV>
+__device__ __forceinline__ void load_node_u(const TV *u, int j, TV (&x)[B])
+{
+	if constexpr (B == 3 && S == 4 && sizeof(TV) == 4) {
+		const float4 v = __ldcg(reinterpret_cast<const float4 *>(u) + j);
+		x[0] = v.x; x[1] = v.y; x[2] = v.z;
+	} else if constexpr (B == 3 && S == 4 && sizeof(TV) == 8) {
+		const double2 a = __ldcg(reinterpret_cast<const double2 *>(u) + 2 * (long) j);
+		const double2 b = __ldcg(reinterpret_cast<const double2 *>(u) + 2 * (long) j + 1);
+		x[0] = a.x; x[1] = a.y; x[2] = b.x;
+	} else if constexpr (B == 2 && S == 2 && sizeof(TV) == 4) {
+		const float2 v = __ldcg(reinterpret_cast<const float2 *>(u) + j);
+		x[0] = v.x; x[1] = v.y;
+	} else if constexpr (B == 2 && S == 2 && sizeof(TV) == 8) {
+		const double2 v = __ldcg(reinterpret_cast<const double2 *>(u) + j);
+		x[0] = v.x; x[1] = v.y;
+	} else {
+		for (int c = 0; c < B; ++c) x[c] = __ldcg(u + (long) j * S + c);
+	}
+}
+
+template <int B, int S, typename TV>
+__device__ __forceinline__ void store_node_u(TV *u, int i, const TV (&x)[B])
+{
+	if constexpr (B == 3 && S == 4 && sizeof(TV) == 4) {
+		reinterpret_cast<float4 *>(u)[i] = make_float4(x[0], x[1], x[2], 0.f);
+	} else if constexpr (B == 3 && S == 4 && sizeof(TV) == 8) {
+		reinterpret_cast<double2 *>(u)[2 * (long) i] = make_double2(x[0], x[1]);
+		reinterpret_cast<double2 *>(u)[2 * (long) i + 1] = make_double2(x[2], 0.0);
+	} else {
+		for (int c = 0; c < B; ++c) u[(long) i * S + c] = x[c];
+	}
+}
+
+// u (stride B) -> its gather copy (stride gather_stride<B>())
+template <int B, typename TV>
+__global__ void k_pad_u(int N, const TV *__restrict__ u, TV *__restrict__ ug)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	TV x[B];
+	for (int c = 0; c < B; ++c) x[c] = u[(long) i * B + c];
+	store_node_u<B, gather_stride<B>(), TV>(ug, i, x);
+}
+
+// a slot whose column is already known (the persistent CG keeps its CTA's columns in shared memory); u has
+// stride S
+template <int B, typename TM, typename TV, int S = B>
 __device__ __forceinline__ void spmv_slot_col(const SellOp &A, const TM *__restrict__ blk, const TV *u, long idx, int j,
                                               TV (&acc)[B])
 {
 	TV xj[B];
-	for (int c = 0; c < B; ++c) xj[c] = __ldcg(u + (long) j * B + c);   // written during the launch
+	load_node_u<B, S, TV>(u, j, xj);
 	TM a[B * B];
 	load_block<B, TM>(blk, A.total, idx, a);
 	for (int r = 0; r < B; ++r)
 		for (int c = 0; c < B; ++c) acc[r] += (TV) a[r * B + c] * xj[c];
+}
+
+// a slot whose operator block sits in shared memory ([entry][lane] with stride 32; cs points at lane's entry 0)
+template <int B, typename TM, typename TV, int S>
+__device__ __forceinline__ void spmv_slot_smem(const TM *cs, const TV *u, int j, TV (&acc)[B])
+{
+	TV xj[B];
+	load_node_u<B, S, TV>(u, j, xj);
+	for (int r = 0; r < B; ++r)
+		for (int c = 0; c < B; ++c) acc[r] += (TV) cs[32 * (r * B + c)] * xj[c];
 }
 
 constexpr int kColSmemMax = 160 * 1024;    // shared memory for a CTA's column indices (else two-kernel CG)
@@ -451,7 +513,8 @@ constexpr int kColSmemMax = 160 * 1024;    // shared memory for a CTA's column i
 template <int B, typename TM, typename TV, typename TX>
 __global__ void __launch_bounds__(32 * kPersistMaxWarps, 1)
 k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, const TV *__restrict__ binv, TX *x,
-             const TV *r0, TV *u, double *part, CgScal *sc, GridBar *bar, const int *__restrict__ ctaTab)
+             const TV *r0, const TV *u, TV *ug, double *part, CgScal *sc, GridBar *bar, const int *__restrict__ ctaTab,
+             int colInts, int kc)
 {
 	__shared__ FxScratch fs;                     // block sums; fs.tot = gamma, rr of the last update
 	__shared__ double nx[4];                     // next gamma, rr, beta, beta * gamma / alphaPrev
@@ -477,7 +540,17 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	if (rowWarp)
 		for (int t = lane; t < 32 * wdt; t += 32) scol[coff + t] = __ldg(A.col + (base - lane) + t);
 	const int lbase = coff + lane;               // local slot of lane's slot 0 (row warps)
-	__syncthreads();                             // scol and gaveUp before their first use
+	// FP32 operators (mixed precision): the first kc slots of each row warp's slice also stay in shared
+	// memory, [warp][slot][entry][lane], so the matvec reads only the rest of the operator from L2
+	constexpr int BB = B * B;
+	constexpr int S = gather_stride<B>();                   // ug: u in the gather layout (the matvec's reads)
+	constexpr bool kCache = sizeof(TM) == sizeof(float);    // FP64 operators never use it (kc = 0)
+	TM *scache = reinterpret_cast<TM *>(scol + colInts);
+	if (kCache && kc > 0 && rowWarp)
+		for (int k = 0; k < min(kc, wdt); ++k)
+			for (int e = 0; e < BB; ++e)
+				scache[((wp * kc + k) * BB + e) * 32 + lane] = __ldg(blk + (base - lane + ((long) k << 5)) * BB + 32 * e + lane);
+	__syncthreads();                             // scol, the block cache and gaveUp before their first use
 	const double bb = sc->bb, tolSqu = sc->tolSqu;
 	const int itrMax = sc->itrMax;
 	double gam = sc->gam, rr = sc->rr, alpha = 1.0, beta = 0.0;
@@ -509,12 +582,21 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			TV acc0[B], acc1[B];
 			for (int c = 0; c < B; ++c) { acc0[c] = (TV) 0; acc1[c] = (TV) 0; }
 			int k = 0;
+			// cached slots first, in pairs (kc is even), then the rest: slot k always goes to acc[k & 1]
+			const int kcw = kCache ? min(kc, wdt) & ~1 : 0;
+			const TM *cs = scache + (wp * kc * BB) * 32 + lane;
+			for (; kCache && k + 2 <= kcw; k += 2) {
+				const int j0 = scol[lbase + (k << 5)], j1 = scol[lbase + ((k + 1) << 5)];
+				spmv_slot_smem<B, TM, TV, S>(cs + k * BB * 32, ug, j0, acc0);
+				spmv_slot_smem<B, TM, TV, S>(cs + (k + 1) * BB * 32, ug, j1, acc1);
+			}
 			for (; k + 2 <= wdt; k += 2) {
 				const int j0 = scol[lbase + (k << 5)], j1 = scol[lbase + ((k + 1) << 5)];
-				spmv_slot_col<B, TM, TV>(A, blk, u, base + ((long) k << 5), j0, acc0);
-				spmv_slot_col<B, TM, TV>(A, blk, u, base + ((long) (k + 1) << 5), j1, acc1);
+				spmv_slot_col<B, TM, TV, S>(A, blk, ug, base + ((long) k << 5), j0, acc0);
+				spmv_slot_col<B, TM, TV, S>(A, blk, ug, base + ((long) (k + 1) << 5), j1, acc1);
 			}
-			if (k < wdt) spmv_slot_col<B, TM, TV>(A, blk, u, base + ((long) k << 5), scol[lbase + (k << 5)], acc0);
+			if (k < wdt)
+				spmv_slot_col<B, TM, TV, S>(A, blk, ug, base + ((long) k << 5), scol[lbase + (k << 5)], acc0);
 			for (int c = 0; c < B; ++c) wv[c] = acc0[c] + acc1[c];
 			if (own) d1[0] = row_dot<B, TV>(wv, uv);
 		} else if (pending) {
@@ -582,7 +664,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 			for (int c = 0; c < B; ++c) rv[c] = rv[c] - al_ * sv[c];
 			if constexpr (kBlk) prec_block<B, TV>(bv, rv, uv);
 			else for (int c = 0; c < B; ++c) uv[c] = dv[c] * rv[c];
-			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uv[c];
+			store_node_u<B, S, TV>(ug, i, uv);
 			d2[0] = row_dot<B, TV>(rv, uv);
 			d2[1] = row_dot<B, TV>(rv, rv);
 		}
@@ -1069,21 +1151,35 @@ static void set_scal(CgScal *d, double tolSqu, int itrMax, double bb, cudaStream
 }
 
 // CTAs of k_cg_persist with `warps` warps each that can be resident at once (0: it cannot run)
+// largest dynamic shared memory of one k_cg_persist CTA (the device's opt-in limit less the kernel's static
+// shared memory), set as the kernel's limit on first use; 0 if that fails
+template <int B, typename TM, typename TV, typename TX>
+static size_t persist_smem_max()
+{
+	static std::mutex mu;                    // sessions and servers may size launches from several threads
+	static size_t lim = (size_t) -1;
+	std::lock_guard<std::mutex> lock(mu);
+	if (lim == (size_t) -1) {
+		lim = 0;
+		int dev = 0, optin = 0;
+		cudaFuncAttributes fa;
+		if (cudaGetDevice(&dev) == cudaSuccess &&
+		    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
+		    cudaFuncGetAttributes(&fa, k_cg_persist<B, TM, TV, TX>) == cudaSuccess && (size_t) optin > fa.sharedSizeBytes) {
+			const size_t want = (size_t) optin - fa.sharedSizeBytes;
+			if (cudaFuncSetAttribute(k_cg_persist<B, TM, TV, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                         (int) want) == cudaSuccess)
+				lim = want;
+		}
+		cudaGetLastError();
+	}
+	return lim;
+}
+
 template <int B, typename TM, typename TV, typename TX>
 static int persist_capacity(int smCount, int warps, size_t smemBytes)
 {
-	static std::mutex mu;                    // sessions and servers may size launches from several threads
-	static bool attr = false;
-	if (warps < 1 || warps > kPersistMaxWarps || smemBytes > (size_t) kColSmemMax) return 0;
-	std::lock_guard<std::mutex> lock(mu);
-	if (!attr) {               // allow the column cache beyond the default 48 KB of dynamic shared memory
-		if (cudaFuncSetAttribute(k_cg_persist<B, TM, TV, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                         kColSmemMax) != cudaSuccess) {
-			cudaGetLastError();
-			return 0;
-		}
-		attr = true;
-	}
+	if (warps < 1 || warps > kPersistMaxWarps || smemBytes > persist_smem_max<B, TM, TV, TX>()) return 0;
 	int v = 0;
 	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cg_persist<B, TM, TV, TX>, 32 * warps, smemBytes) !=
 	    cudaSuccess) {
@@ -1213,11 +1309,24 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 			prof->ctaTabCtas = nctas;
 		}
 	}
-	const bool tabOk = prof->ctaTab && prof->ctaTabWarps == pw && prof->ctaTabCtas == nctas;
+	const bool tabOk = prof->ctaTab && prof->ctaTabWarps == pw && prof->ctaTabCtas == nctas &&
+	                   prof->ctaTabSmem <= (size_t) kColSmemMax;
 	const size_t colSmem = tabOk ? prof->ctaTabSmem : (size_t) -1;
+	// FP32 operators: cache the leading slots of every slice in the shared memory left over (an even count)
+	int kc = 0;
+	size_t dynSmem = colSmem;
+	if (sizeof(TM) == sizeof(float) && tabOk) {
+		const size_t lim = persist_smem_max<B, TM, TV, TX>(), perSlot = (size_t) pw * 32 * B * B * sizeof(TM);
+		int widest = 0;
+		for (int sl = 0; sl < m.nslice; ++sl)
+			widest = std::max(widest, (m.slOffHost[sl + 1] - m.slOffHost[sl]) / 32);
+		if (lim > colSmem) kc = (int) std::min<size_t>((size_t) widest + 1, (lim - colSmem) / perSlot) & ~1;
+		dynSmem = colSmem + (size_t) kc * perSlot;
+	}
+	const int colInts = tabOk ? (int) (colSmem / sizeof(int)) : 0;
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->cgKernel != SA_CG_PERSISTENT_GLOBAL && prof->bar &&
-	                     (!block_prec<TV>() || prof->binv32) && tabOk &&
-	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw + 1, colSmem);
+	                     (!block_prec<TV>() || prof->binv32) && tabOk && (B != 3 || prof->u4) &&
+	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw + 1, dynSmem);
 	if (persist) {
 		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first).  FP32
 		// inner solves of mixed precision are block-Jacobi preconditioned (3x3 node blocks)
@@ -1228,16 +1337,25 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		} else {
 			k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
 		}
+		// the matvec gathers u from a copy in its own layout (3-component nodes padded to 4)
+		TV *ug = u;
+		if (B == 3) {
+			ug = reinterpret_cast<TV *>(prof->u4);
+			k_pad_u<B, TV><<<grid_for(N), kBlock, 0, s>>>(N, u, ug);
+			++prof->launches;
+		}
 		GridBar *bar = (GridBar *) prof->bar;
 		SA_CHECK(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
 		SellOp A = sell_of(m);
 		const TV *r0 = r;
+		const TV *uc = u;
 		const int *tab = prof->ctaTab;
-		void *args[] = {&A, (void *) &blk, (void *) &dinv, (void *) &binv, (void *) &x, (void *) &r0, (void *) &u,
-		                (void *) &part, (void *) &sc, (void *) &bar, (void *) &tab};
+		void *args[] = {&A, (void *) &blk, (void *) &dinv, (void *) &binv, (void *) &x, (void *) &r0, (void *) &uc,
+		                (void *) &ug, (void *) &part, (void *) &sc, (void *) &bar, (void *) &tab, (void *) &colInts,
+		                (void *) &kc};
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[0], s));
 		SA_CHECK(cudaLaunchCooperativeKernel((const void *) k_cg_persist<B, TM, TV, TX>, dim3(nctas),
-		                                     dim3(32 * (pw + 1)), args, colSmem, s));
+		                                     dim3(32 * (pw + 1)), args, dynSmem, s));
 		if (timing) SA_CHECK(cudaEventRecord(prof->ev[1], s));
 		k_cg_zero<TX><<<grid_for(n), kBlock, 0, s>>>(n, x, sc);
 		prof->launches += 3;

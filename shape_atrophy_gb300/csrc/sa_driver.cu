@@ -541,6 +541,7 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 	int nbCg = std::max(grid_for(n, 256), std::max(m.nslice, nb));
 	c.part = P.alloc<double>((size_t) 3 * nbCg + 64); c.scal = P.zeros<double>(32); c.maxBlocks = nbCg;
 	c.bar = P.zeros<char>(kGridBarBytes);
+	c.u4 = P.alloc<double>((size_t) 4 * N);
 	c.ctaTabCap = 2L * (m.nslice + 64);
 	c.ctaTab = P.alloc<int>((size_t) c.ctaTabCap);
 	c.cgKernel = md.cgKernel;

@@ -468,6 +468,7 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	float *binv32 = nullptr;      // FP32 inverses of its diagonal blocks (block-Jacobi, mixed precision)
 	float *f32 = nullptr;         // 7 n FP32 vectors of the inner solve (mixed precision)
 	double *xr = nullptr;         // 3 n FP64 refinement scratch
+	double *u4 = nullptr;         // 4 N: the persistent CG's gather copy of u (3-component nodes padded to 4)
 	// optional CUDA-event timing of the velocity matvec kernel (k_cg_spmv)
 	int profileEnabled = 0, profileOn = 0;
 	cudaEvent_t ev[64] = {};
