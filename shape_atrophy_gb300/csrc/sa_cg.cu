@@ -1232,8 +1232,9 @@ static size_t col_span_bytes_even(const Mesh &m, int nctas)
 // first, each to the (CTA, sub-partition) with the least work that still has a free warp, so every
 // sub-partition's matvec takes about as long (on the layered shell the inner and outer node layers have
 // about half the neighbours of the others: consecutive slices per CTA left the busiest sub-partition 11 %
-// above the mean, this 7 %).  The per-row arithmetic and the exact grid sums do not depend on where a row
-// runs, so the assignment changes no result.  Layout: nctas * pw slice ids (-1: none), then nctas * pw
+// above the mean, this 7 %).  Rows are computed alike wherever they run, but each CTA's partial sums are
+// rounded once to FP64 before the grid sum, so the grouping can move results in the last bits; it is fixed
+// for a mesh and an SM count, so results are reproducible.  Layout: nctas * pw slice ids (-1: none), then nctas * pw
 // offsets into the CTA's column cache.  Returns the largest column cache in bytes, or (size_t) -1 without
 // the host copy of the slice offsets.
 static size_t balanced_cta_table(const Mesh &m, int pw, int nctas, std::vector<int> &tab)
