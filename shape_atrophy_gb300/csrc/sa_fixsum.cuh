@@ -171,18 +171,34 @@ SA_FX_HD double fx_to_double(Fx s, int emax)
 }
 
 #if defined(__CUDACC__)
-__device__ __forceinline__ Fx fx_shfl_down(Fx a, int off)
+// b << sh in 128 bits, b < 2^32
+__device__ __forceinline__ Fx fx_shl_small(unsigned long long b, int sh)
 {
 	Fx r;
-	r.lo = __shfl_down_sync(0xffffffffu, a.lo, off);
-	r.hi = __shfl_down_sync(0xffffffffu, a.hi, off);
+	if (sh == 0) { r.lo = b; r.hi = 0ull; }
+	else if (sh < 64) { r.lo = b << sh; r.hi = b >> (64 - sh); }
+	else { r.lo = 0ull; r.hi = b << (sh - 64); }
 	return r;
 }
 
-__device__ __forceinline__ Fx fx_warp_sum(Fx a)      // lane 0 gets the sum
+// Sum over the warp; every lane gets it.  The 128-bit two's-complement values are cut into six 24-bit
+// limbs, each limb summed over the 32 lanes with one warp-reduce instruction (a sum of 32 limbs stays
+// below 2^29), and the limb sums recombined modulo 2^128: the same exact sum as a shuffle tree of
+// 128-bit adds (5 levels of 4 shuffles each), in 6 reduce instructions.
+__device__ __forceinline__ Fx fx_warp_sum(Fx a)
 {
-	for (int off = 16; off > 0; off >>= 1) a = fx_add(a, fx_shfl_down(a, off));
-	return a;
+	const unsigned long long m24 = 0xFFFFFFull;
+	unsigned l[6];
+	l[0] = (unsigned) (a.lo & m24);
+	l[1] = (unsigned) ((a.lo >> 24) & m24);
+	l[2] = (unsigned) (((a.lo >> 48) | (a.hi << 16)) & m24);
+	l[3] = (unsigned) ((a.hi >> 8) & m24);
+	l[4] = (unsigned) ((a.hi >> 32) & m24);
+	l[5] = (unsigned) (a.hi >> 56);
+	Fx r = fx_zero();
+#pragma unroll
+	for (int k = 0; k < 6; ++k) r = fx_add(r, fx_shl_small(__reduce_add_sync(0xffffffffu, l[k]), 24 * k));
+	return r;
 }
 
 __device__ __forceinline__ int fx_warp_max(int e) { return (int) __reduce_max_sync(0xffffffffu, (unsigned) e); }
