@@ -583,7 +583,9 @@ k_kpcg_persist(SellOp A, const double *__restrict__ blk, const double *__restric
 	if (sc->done) return;                       // set before the launch: the same for every CTA
 	const int N = A.N, nctas = gridDim.x, lc = blockIdx.x;
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, W = blockDim.x >> 5;
-	const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+	// rows of phases A and B: 32-row slices dealt round-robin over the CTAs first, so that a small mesh
+	// spreads its row work (gathers) over all SMs instead of the first few CTAs
+	const int nsl = (N + 31) >> 5, sl0 = blockIdx.x + gridDim.x * wp, slStride = gridDim.x * W;
 	const double bSqu = sc->bSqu, tolSqu = sc->tolSqu, ldm = sc->ldmWgt;
 	const int itrMax = sc->itrMax;
 	double rKr = sc->rKr, rr = sc->rSqu, be = 0.0;
@@ -599,8 +601,9 @@ k_kpcg_persist(SellOp A, const double *__restrict__ blk, const double *__restric
 	for (;;) {
 		// A: direction, operator, (d, Ad)
 		double loc[1] = {0.0}, res[1];
-		for (int i = gtid; i < N; i += gstride) {
-			const int sl = i >> 5, ln = i & 31;
+		for (int sl = sl0; sl < nsl; sl += slStride) {
+			const int i = sl * 32 + lane, ln = lane;
+			if (i >= N) continue;
 			const int wdt = __ldg(A.width + sl);
 			const long base = __ldg(A.off + sl) + ln;
 			double acc[D];
@@ -635,7 +638,9 @@ k_kpcg_persist(SellOp A, const double *__restrict__ blk, const double *__restric
 		const double alpha = rKr / dAd;
 		// B: x, w, r and (r, r)
 		loc[0] = 0.0;
-		for (int i = gtid; i < N; i += gstride)
+		for (int sl = sl0; sl < nsl; sl += slStride) {
+			const int i = sl * 32 + lane;
+			if (i >= N) continue;
 			for (int c = 0; c < D; ++c) {
 				const long k = (long) i * D + c;
 				v.x[k] = __fma_rn(alpha, dNew[k], v.x[k]);
@@ -644,6 +649,7 @@ k_kpcg_persist(SellOp A, const double *__restrict__ blk, const double *__restric
 				v.r[k] = rk;
 				loc[0] += rk * rk;
 			}
+		}
 		if (!grid_reduce<1, double>(loc, res, partB, lc, nctas, bar, target, fs)) { code = SA_ERR_TIMEOUT; break; }
 		rr = res[0];
 		++it;
