@@ -1934,9 +1934,32 @@ struct Server {
 	double phaseMs[5] = {0, 0, 0, 0, 0};
 	long long batchLaunches[4] = {0, 0, 0, 0};   // FP64 velocity, FP32 velocity, FP64 RD, FP32 RD
 	std::chrono::steady_clock::time_point tMark;
+	// The instances' own work (element kernels, per-instance solve set-up and updates) runs on
+	// kInstStreams streams, instance k on stream k mod kInstStreams, so that the many small kernels of
+	// different instances overlap on the GPU; the batched solves run on s.  join() makes s wait for all
+	// instance streams (before a batched launch or a read of the instances' CG scalars), fork() makes the
+	// instance streams wait for s (after a batched launch).  Each instance's work stays in order on its own
+	// stream, so results do not depend on the streams.
+	static constexpr int kInstStreams = 8;
+	cudaStream_t pool[kInstStreams] = {};
+	cudaEvent_t poolEv[kInstStreams] = {}, mainEv = nullptr;
+	int nextStream = 0;
+	void join()
+	{
+		for (int k = 0; k < kInstStreams; ++k) {
+			SA_CHECK(cudaEventRecord(poolEv[k], pool[k]));
+			SA_CHECK(cudaStreamWaitEvent(s, poolEv[k], 0));
+		}
+	}
+	void fork()
+	{
+		SA_CHECK(cudaEventRecord(mainEv, s));
+		for (int k = 0; k < kInstStreams; ++k) SA_CHECK(cudaStreamWaitEvent(pool[k], mainEv, 0));
+	}
 	void mark(int phase)
 	{
 		if (!trace) return;
+		join();
 		cudaStreamSynchronize(s);
 		const auto t = std::chrono::steady_clock::now();
 		if (phase >= 0) phaseMs[phase] += std::chrono::duration<double, std::milli>(t - tMark).count();
@@ -1949,6 +1972,11 @@ struct Server {
 	{
 		SA_CHECK(cudaSetDevice(ctx->device));
 		SA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+		for (int k = 0; k < kInstStreams; ++k) {
+			SA_CHECK(cudaStreamCreateWithFlags(&pool[k], cudaStreamNonBlocking));
+			SA_CHECK(cudaEventCreateWithFlags(&poolEv[k], cudaEventDisableTiming));
+		}
+		SA_CHECK(cudaEventCreateWithFlags(&mainEv, cudaEventDisableTiming));
 		SA_CHECK(cudaMalloc(&devJobs, sizeof(CgJob) * kMaxJobs));
 		SA_CHECK(cudaDeviceGetAttribute(&smCount, cudaDevAttrMultiProcessorCount, ctx->device));
 		th = std::thread([this] { loop(); });
@@ -1970,6 +1998,11 @@ struct Server {
 			             ticks, phaseMs[0], phaseMs[1], phaseMs[2], phaseMs[3], phaseMs[4], batchLaunches[0],
 			             batchLaunches[1], batchLaunches[2], batchLaunches[3]);
 		cudaSetDevice(ctx->device);
+		for (int k = 0; k < kInstStreams; ++k) {
+			if (pool[k]) { cudaStreamSynchronize(pool[k]); cudaStreamDestroy(pool[k]); }
+			if (poolEv[k]) cudaEventDestroy(poolEv[k]);
+		}
+		if (mainEv) cudaEventDestroy(mainEv);
 		if (devJobs) cudaFree(devJobs);
 		if (statPinned) cudaFreeHost(statPinned);
 		if (s) cudaStreamDestroy(s);
@@ -2002,6 +2035,7 @@ struct Server {
 		std::vector<const CgWork *> ws;
 		for (InstBase *in : g) ws.push_back(&in->cg());
 		std::vector<CgState> out;
+		join();                              // the scalars may come from the instances' own streams
 		cg_states(ws, statPinned, s, out);
 		return out;
 	}
@@ -2036,9 +2070,11 @@ struct Server {
 			std::vector<BatchSolve> bs;
 			for (InstBase *in : inner) { in->mixed_inner(kind); bs.push_back(in->mixed_solve(kind)); }
 			const int li = kind == kMixedVelocity ? 1 : 3;
+			join();
 			batchLaunches[li] += B == 1 ? cg_batch_run<1, float, float, float>(bs, smCount, devJobs, kMaxJobs, s)
 			                   : B == 2 ? cg_batch_run<2, float, float, float>(bs, smCount, devJobs, kMaxJobs, s)
 			                            : cg_batch_run<3, float, float, float>(bs, smCount, devJobs, kMaxJobs, s);
+			fork();
 			std::vector<InstBase *> next;
 			const std::vector<CgState> ci = states(inner);
 			for (size_t q = 0; q < inner.size(); ++q) {
@@ -2069,8 +2105,10 @@ struct Server {
 			if (g.empty()) continue;
 			std::vector<BatchSolve> bs;
 			for (InstBase *in : g) { in->prepare_velocity_fp64(); bs.push_back(in->velocity_fp64()); }
+			join();
 			batchLaunches[0] += D == 2 ? cg_batch_run<2, double, double, double>(bs, smCount, devJobs, kMaxJobs, s)
 			                           : cg_batch_run<3, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
+			fork();
 			for (InstBase *in : g) in->finish_velocity_fp64();
 			const std::vector<CgState> cs = states(g);
 			for (size_t q = 0; q < g.size(); ++q) {
@@ -2100,7 +2138,9 @@ struct Server {
 		if (!rd.empty()) {
 			std::vector<BatchSolve> bs;
 			for (InstBase *in : rd) { in->prepare_rd(); bs.push_back(in->rd_solve()); }
+			join();
 			batchLaunches[2] += cg_batch_run<1, double, double, double>(bs, smCount, devJobs, kMaxJobs, s);
+			fork();
 			for (InstBase *in : rd) in->finish_rd();
 			const std::vector<CgState> cs = states(rd);
 			for (size_t q = 0; q < rd.size(); ++q) {
@@ -2134,8 +2174,10 @@ struct Server {
 			std::string err;
 			int code = SA_OK;
 			try {
-				if (r->dim == 2) in.reset(new Inst<2>(r, s));
-				else in.reset(new Inst<3>(r, s));
+				cudaStream_t is = pool[nextStream];
+				nextStream = (nextStream + 1) % kInstStreams;
+				if (r->dim == 2) in.reset(new Inst<2>(r, is));
+				else in.reset(new Inst<3>(r, is));
 			} catch (const ArgError &e) { code = SA_ERR_ARG; err = e.msg; }
 			catch (const CudaError &e) { code = SA_ERR_CUDA; err = std::string(e.where) + ": " + cudaGetErrorString(e.e); cudaGetLastError(); }
 			catch (const std::bad_alloc &) { code = SA_ERR_CUDA; err = "host allocation failed"; }
