@@ -10,6 +10,9 @@
 - a solve that does not converge fails only its own request (objective
   DBL_MAX, status SA_ERR_NOT_CONVERGED), the others are unaffected;
 - mixed precision served results stay within 1e-6 of FP64;
+- with more requests than the server's instance streams (eight), so that
+  instances share streams with others, a request is still bitwise the same
+  alone and in the mix, in FP64 and in mixed precision;
 - requests the server does not run (frame model) are rejected at submit.
 """
 import numpy as np
@@ -126,6 +129,26 @@ def test_mixed_precision_served_within_1e6():
         assert rel(a["lmk"], b["lmk"]) < 1e-6
         assert rel(a["tau"], b["tau"]) < 1e-6
         assert abs(a["obj"] - b["obj"]) <= 1e-6 * abs(b["obj"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_alone_equals_mix_with_shared_instance_streams(precision):
+    from shape_atrophy_gb300 import api, problems
+    specs = [problems.annulus_layered(angNum=32 + 8 * k, radNum=6, steps=3, target_seed=k) for k in range(6)]
+    specs += [problems.shell_layered(level=2, lyrCntNum=3 + k % 2, steps=3, target_seed=k) for k in range(5)]
+    probe = 9                                     # the tenth instance shares a stream with the second
+    alone = api.Server(hbm_budget=8e9, max_instances=4)
+    a = alone.result(alone.submit(specs[probe], precision=precision))
+    alone.close()
+    mix = api.Server(hbm_budget=8e9, max_instances=32)
+    ids = [mix.submit(sp, precision=precision) for sp in specs]
+    res = [mix.result(i) for i in ids]
+    mix.close()
+    b = res[probe]
+    assert all(r["info"]["status"] == 0 for r in res)
+    np.testing.assert_array_equal(a["lmk"], b["lmk"])
+    np.testing.assert_array_equal(a["tau"], b["tau"])
+    assert a["obj"] == b["obj"]
 
 
 def test_frame_request_is_rejected():
