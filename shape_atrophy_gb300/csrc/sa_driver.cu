@@ -2347,6 +2347,16 @@ int sa_create(sa_context **out, int device)
 		delete c;
 		return SA_ERR_CUDA;
 	}
+	// the one-call entry points allocate their work buffers stream-ordered from the device's default
+	// memory pool; by default the pool hands freed memory back to the driver at every synchronisation, so
+	// each call mapped its ~0.5 GB again (tens of ms, varying from call to call).  Keep up to 4 GiB of
+	// freed memory in the pool between calls.
+	cudaMemPool_t mp;
+	if (cudaDeviceGetDefaultMemPool(&mp, device) == cudaSuccess) {
+		unsigned long long keep = 4ull << 30;
+		cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+	}
+	cudaGetLastError();
 	*out = c;
 	return SA_OK;
 }
