@@ -974,7 +974,7 @@ typedef struct {
 	double *lmk;                /* current node positions */
 	double *elYElm, *elY, *pnl;
 	double *knlMat, *knLMat;    /* frame K-PCG */
-	double *diag;               /* isotropic Jacobi */
+	double *diag;               /* isotropic: inverse node blocks (block-Jacobi) */
 } vstate;
 
 /* y = E x + btmWgt P x */
@@ -1051,11 +1051,26 @@ done:
 }
 
 /* Jacobi-PCG (layered model): same stopping rule as the reference's ipcg
- * (|r|^2 < tol^2 |b|^2, b = 0 gives x = 0). */
+ * (|r|^2 < tol^2 |b|^2, b = 0 gives x = 0).  The preconditioner is block-Jacobi
+ * over node blocks of bdim components: pinv holds the inverse of every node's
+ * bdim x bdim diagonal block of the operator, entry (a, c) of node i at
+ * pinv[(a * bdim + c) * N + i] (bdim = 1: the inverse diagonal, point Jacobi). */
 typedef void (*apply_fn)(void *ctx, const double *x, double *y);
-static int jpcg(apply_fn A, void *ctx, const double *dinv, long n, double *x, const double *b,
+static void prec_apply(const double *pinv, int N, int bdim, const double *r, double *z)
+{
+	#pragma omp parallel for schedule(static)
+	for (int i = 0; i < N; ++i)
+		for (int a = 0; a < bdim; ++a) {
+			double t = pinv[(size_t) (a * bdim) * N + i] * r[i];
+			for (int c = 1; c < bdim; ++c) t += pinv[(size_t) (a * bdim + c) * N + i] * r[(size_t) c * N + i];
+			z[(size_t) a * N + i] = t;
+		}
+}
+
+static int jpcg(apply_fn A, void *ctx, const double *pinv, int N, int bdim, double *x, const double *b,
                 int itrMax, double tolSqu, int *itrOut)
 {
+	long n = (long) N * bdim;
 	double *r = malloc(sizeof(double) * n), *z = malloc(sizeof(double) * n);
 	double *p = malloc(sizeof(double) * n), *q = malloc(sizeof(double) * n);
 	int status = 1, itr = 0;
@@ -1066,7 +1081,8 @@ static int jpcg(apply_fn A, void *ctx, const double *dinv, long n, double *x, co
 	for (long i = 0; i < n; ++i) r[i] = b[i] - q[i];
 	double rr = ddot(r, r, n);
 	if (rr < relTolSqu) { status = 0; goto done; }
-	for (long i = 0; i < n; ++i) { z[i] = dinv[i] * r[i]; p[i] = z[i]; }
+	prec_apply(pinv, N, bdim, r, z);
+	for (long i = 0; i < n; ++i) p[i] = z[i];
 	double rz = ddot(r, z, n);
 	for (itr = 0; itr < itrMax; ++itr) {
 		A(ctx, p, q);
@@ -1076,7 +1092,7 @@ static int jpcg(apply_fn A, void *ctx, const double *dinv, long n, double *x, co
 		for (long i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
 		rr = ddot(r, r, n);
 		if (rr < relTolSqu) { status = 0; ++itr; goto done; }
-		for (long i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
+		prec_apply(pinv, N, bdim, r, z);
 		double rzn = ddot(r, z, n);
 		double beta = rzn / rz;
 		for (long i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
@@ -1090,11 +1106,16 @@ done:
 
 static void velocity_apply(void *ctx, const double *x, double *y) { second_mult((vstate *) ctx, x, y); }
 
-/* diagonal of E + btmWgt P for the layered model */
-static void elastic_diag_state(const orc_problem *P, const double *lmk, const double *edg, double *diag)
+/* node blocks of E + btmWgt P for the layered model: entry (r, c) of node i's
+ * DIM x DIM diagonal block at blk[(r * DIM + c) * N + i].  Element e adds
+ * vol ((lam + mu) g_k g_k^T + mu |g_k|^2 I) to its vertex k (g_k the P1 shape
+ * gradient, the a = b term of the element stiffness); the bottom penalty is a
+ * scalar per node (P applied to the all-ones field) on the block's diagonal. */
+static void elastic_blocks_state(const orc_problem *P, const double *lmk, const double *edg, double *blk)
 {
 	int N = P->lmkNum, E = P->elmNum;
-	double *dElm = malloc(sizeof(double) * (size_t) E * VTX * DIM);
+	const int DD = DIM * DIM;
+	double *bElm = malloc(sizeof(double) * (size_t) E * VTX * DD);
 	#pragma omp parallel for schedule(static)
 	for (int e = 0; e < E; ++e) {
 		vec q[DIM]; get_edges(edg, e, E, q);
@@ -1112,39 +1133,89 @@ static void elastic_diag_state(const orc_problem *P, const double *lmk, const do
 		for (int k = 0; k < VTX; ++k) {
 			double g2 = G[k][0] * G[k][0];
 			for (int d = 1; d < DIM; ++d) g2 = g2 + G[k][d] * G[k][d];
-			for (int d = 0; d < DIM; ++d)
-				dElm[(k * DIM + d) * E + e] = volVal * ((lam + mu) * G[k][d] * G[k][d] + mu * g2);
+			for (int r = 0; r < DIM; ++r)
+				for (int c = 0; c < DIM; ++c)
+					bElm[(size_t) (k * DD + r * DIM + c) * E + e] =
+						volVal * ((lam + mu) * G[k][r] * G[k][c] + (r == c ? mu * g2 : 0.0));
 		}
 	}
 	const int *ve = P->vtxElmMat;
 	#pragma omp parallel for schedule(static)
 	for (int i = 0; i < N; ++i) {
-		double s[DIM]; for (int d = 0; d < DIM; ++d) s[d] = 0.0;
+		double s[DIM * DIM]; for (int d = 0; d < DD; ++d) s[d] = 0.0;
 		int adjNum = ve[i];
 		for (int a = 0; a < adjNum; ++a) {
 			int e = ve[(1 + 2 * a) * N + i], l = ve[(2 + 2 * a) * N + i];
-			for (int d = 0; d < DIM; ++d) s[d] += dElm[l * E * DIM + d * E + e];
+			for (int d = 0; d < DD; ++d) s[d] += bElm[(size_t) (l * DD + d) * E + e];
 		}
-		for (int d = 0; d < DIM; ++d) diag[d * N + i] = s[d];
+		for (int d = 0; d < DD; ++d) blk[(size_t) d * N + i] = s[d];
 	}
-	free(dElm);
+	free(bElm);
 	if (P->btmWgt != 0.0) {
-		/* penalty diagonal: P applied to the all-ones field */
 		double *one = malloc(sizeof(double) * (size_t) N * DIM), *pd = malloc(sizeof(double) * (size_t) N * DIM);
 		for (long i = 0; i < (long) N * DIM; ++i) one[i] = 1.0;
 		penalty_apply(P, lmk, one, pd);
-		for (long i = 0; i < (long) N * DIM; ++i) diag[i] += P->btmWgt * pd[i];
+		for (int i = 0; i < N; ++i)
+			for (int d = 0; d < DIM; ++d) blk[(size_t) (d * DIM + d) * N + i] += P->btmWgt * pd[(size_t) d * N + i];
 		free(one); free(pd);
 	}
+}
+
+/* in place: every node block replaced by its inverse (cofactors over the determinant) */
+static void invert_node_blocks(double *blk, int N)
+{
+	#pragma omp parallel for schedule(static)
+	for (int i = 0; i < N; ++i) {
+		double a[DIM][DIM], v[DIM][DIM];
+		for (int r = 0; r < DIM; ++r)
+			for (int c = 0; c < DIM; ++c) a[r][c] = blk[(size_t) (r * DIM + c) * N + i];
+#if DIM == 2
+		double det = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+		v[0][0] = a[1][1] / det; v[0][1] = -a[0][1] / det;
+		v[1][0] = -a[1][0] / det; v[1][1] = a[0][0] / det;
+#else
+		for (int r = 0; r < 3; ++r)
+			for (int c = 0; c < 3; ++c) {
+				/* cofactor of a[c][r] (the adjugate is the transposed cofactor matrix) */
+				int r0 = (c + 1) % 3, r1 = (c + 2) % 3, c0 = (r + 1) % 3, c1 = (r + 2) % 3;
+				v[r][c] = a[r0][c0] * a[r1][c1] - a[r0][c1] * a[r1][c0];
+			}
+		double det = a[0][0] * v[0][0] + a[0][1] * v[1][0] + a[0][2] * v[2][0];
+		for (int r = 0; r < 3; ++r)
+			for (int c = 0; c < 3; ++c) v[r][c] = v[r][c] / det;
+#endif
+		for (int r = 0; r < DIM; ++r)
+			for (int c = 0; c < DIM; ++c) blk[(size_t) (r * DIM + c) * N + i] = v[r][c];
+	}
+}
+
+/* node blocks (blk[(r * DIM + c) * N + i]) and, with inverse != 0, their inverses: the
+ * block-Jacobi preconditioner of the layered velocity solve */
+void orc_elastic_blocks(const orc_problem *P, const double *lmk, int inverse, double *blk)
+{
+	int E = P->elmNum;
+	if (P->elaType == ORC_FRAME || !P->elmLyrVec) {     /* layered model only: zeros otherwise */
+		memset(blk, 0, sizeof(double) * (size_t) P->lmkNum * DIM * DIM);
+		return;
+	}
+	double *edg = malloc(sizeof(double) * (size_t) E * DIM * DIM);
+	orc_edges(P, lmk, edg);
+	elastic_blocks_state(P, lmk, edg, blk);
+	if (inverse) invert_node_blocks(blk, P->lmkNum);
+	free(edg);
 }
 
 void orc_elastic_diag(const orc_problem *P, const double *lmk, double *diag)
 {
 	int E = P->elmNum;
+	int N = P->lmkNum;
 	double *edg = malloc(sizeof(double) * (size_t) E * DIM * DIM);
+	double *blk = malloc(sizeof(double) * (size_t) N * DIM * DIM);
 	orc_edges(P, lmk, edg);
-	elastic_diag_state(P, lmk, edg, diag);
-	free(edg);
+	elastic_blocks_state(P, lmk, edg, blk);
+	for (int d = 0; d < DIM; ++d)
+		memcpy(diag + (size_t) d * N, blk + (size_t) (d * DIM + d) * N, sizeof(double) * N);
+	free(edg); free(blk);
 }
 
 /* CSR matrix apply for the reaction-diffusion system */
@@ -1399,7 +1470,7 @@ int orc_forward_timed(const orc_problem *P, const double *tauVarVec, double *lmk
 	} else {
 		ppdValNow = malloc(sizeof(double) * Z); ppdValNxt = malloc(sizeof(double) * Z);
 		ggdValNxt = malloc(sizeof(double) * Z); lftVal = malloc(sizeof(double) * Z);
-		S.diag = malloc(sizeof(double) * nd);
+		S.diag = malloc(sizeof(double) * nd * DIM);
 	}
 	if (useK) {
 		S.knlMat = malloc(sizeof(double) * (size_t) N * N);
@@ -1462,9 +1533,10 @@ int orc_forward_timed(const orc_problem *P, const double *tauVarVec, double *lmk
 		}
 		if (useK) st = ipcg(&S, vlc, exY, &itr);
 		else {
-			elastic_diag_state(P, lmkNow, edgNow, S.diag);
-			for (long i = 0; i < nd; ++i) S.diag[i] = 1.0 / S.diag[i];
-			st = jpcg(velocity_apply, &S, S.diag, nd, vlc, exY, P->cgItrMax, P->cgTolSqu, &itr);
+			/* block-Jacobi over the DIM x DIM node blocks */
+			elastic_blocks_state(P, lmkNow, edgNow, S.diag);
+			invert_node_blocks(S.diag, N);
+			st = jpcg(velocity_apply, &S, S.diag, N, DIM, vlc, exY, P->cgItrMax, P->cgTolSqu, &itr);
 		}
 		if (cgItr) cgItr[t] = itr;
 		if (st != 0) { status = 1; break; }
@@ -1510,7 +1582,7 @@ int orc_forward_timed(const orc_problem *P, const double *tauVarVec, double *lmk
 				memcpy(tauNxt, tauNow, sizeof(double) * N);   /* warm start */
 			csrctx C1 = { P, lftVal };
 			int rdItr = 0;
-			if (jpcg(csr_apply, &C1, dinv, N, tauNxt, rpd, P->rdItrMax, P->rdTolSqu, &rdItr) != 0) {
+			if (jpcg(csr_apply, &C1, dinv, N, 1, tauNxt, rpd, P->rdItrMax, P->rdTolSqu, &rdItr) != 0) {
 				free(dinv); free(pv); free(gv); status = 1; break;
 			}
 			free(dinv);

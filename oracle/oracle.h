@@ -104,6 +104,7 @@ void orc_elastic_apply(const orc_problem *P, const double *lmk, const double *v,
 void orc_penalty_apply(const orc_problem *P, const double *lmk, const double *v, double *y);
 /* diagonal of E + btmWgt P (isotropic mode Jacobi preconditioner) */
 void orc_elastic_diag(const orc_problem *P, const double *lmk, double *diag);
+void orc_elastic_blocks(const orc_problem *P, const double *lmk, int inverse, double *blk);
 /* yank right-hand side b from nodal tau */
 void orc_yank(const orc_problem *P, const double *lmk, const double *tau, double *b);
 /* reaction load vector from nodal tau (consistent mass) */

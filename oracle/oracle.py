@@ -177,6 +177,13 @@ class Problem:
         self.lib.orc_elastic_diag(C.byref(self.p), _d(np.ascontiguousarray(lmk, dtype=np.float64)), _d(y))
         return y
 
+    def elastic_blocks(self, lmk, inverse: bool = False):
+        """(N, D, D): every node's diagonal block of E + btmWgt P, or its inverse."""
+        y = np.zeros((self.dim, self.dim, self.N))
+        self.lib.orc_elastic_blocks(C.byref(self.p), _d(np.ascontiguousarray(lmk, dtype=np.float64)),
+                                    C.c_int(1 if inverse else 0), _d(y))
+        return np.moveaxis(y, -1, 0)
+
     def fem_csr(self, lmk):
         Z = self.p.nzrNum
         a, b = np.zeros(Z), np.zeros(Z)

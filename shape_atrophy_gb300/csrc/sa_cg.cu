@@ -78,8 +78,7 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *sm)
 		}
 }
 
-// u = M^-1 r for one row with the row's B x B block-Jacobi inverse bv (row-major); the FP32 inner
-// solves of mixed precision use it, the FP64 solves point Jacobi
+// u = M^-1 r for one row with the row's B x B block-Jacobi inverse bv (row-major)
 template <int B, typename TV>
 __device__ __forceinline__ void prec_block(const TV *bv, const TV (&r)[B], TV (&u)[B])
 {
@@ -90,8 +89,20 @@ __device__ __forceinline__ void prec_block(const TV *bv, const TV (&r)[B], TV (&
 	}
 }
 
-// block-Jacobi is chosen at compile time: FP32 vectors (mixed-precision inner solves) only
-template <typename TV> constexpr bool block_prec() { return sizeof(TV) == sizeof(float); }
+// the same with the inverse read from global memory through the read-only path
+template <int B, typename TV>
+__device__ __forceinline__ void prec_block_ldg(const TV *__restrict__ bv, const TV (&r)[B], TV (&u)[B])
+{
+	TV m[B * B];
+	for (int t = 0; t < B * B; ++t) m[t] = __ldg(bv + t);
+	prec_block<B, TV>(m, r, u);
+}
+
+// The preconditioner is chosen at compile time.  Velocity solves (B = D node blocks) are block-Jacobi
+// preconditioned in both precisions, with the inverses of the operator's diagonal D x D blocks; FP32
+// reaction-diffusion inner solves (B = 1) take their 1 x 1 "blocks" from the same inverse pointer; FP64
+// reaction-diffusion solves use the inverse diagonal (point Jacobi, the same preconditioner for B = 1).
+template <int B, typename TV> constexpr bool block_prec() { return B > 1 || sizeof(TV) == sizeof(float); }
 
 // block partials part[k * nb + blockIdx.x]; returns true in the block that
 // arrives last (the one that finishes the reduction)
@@ -213,6 +224,23 @@ __global__ void __launch_bounds__(kSpmvBlock) k_cg_spmv(SellOp A, const TM *__re
 // p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^{-1} r
 // and the dots (r, u), (r, r)
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void cg_update_finish(double (&v)[2], double *part, CgScal *sc)
+{
+	if (!reduce_partials<2, kCgBlock>(v, part, &sc->counter)) return;
+	double d[2];
+	finish_partials<2, kCgBlock>(d, part);
+	if (threadIdx.x == 0) {
+		sc->gamPrev = sc->gam;
+		sc->gam = d[0];
+		sc->rr = d[1];
+		sc->iters += 1;
+		if (!isfinite(d[0]) || !isfinite(d[1])) { sc->code = SA_ERR_NONFINITE; sc->done = 1; }
+		else if (d[1] < sc->tolSqu * sc->bb) { sc->code = SA_OK; sc->done = 1; }
+		else if (sc->iters >= sc->itrMax) { sc->code = SA_ERR_NOT_CONVERGED; sc->done = 1; }
+		sc->counter = 0;
+	}
+}
+
 template <typename TV, typename TX>
 __global__ void __launch_bounds__(kCgBlock) k_cg_update(long n, TX *__restrict__ x, TV *__restrict__ r,
                                                         TV *__restrict__ u, const TV *__restrict__ w,
@@ -236,19 +264,39 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_update(long n, TX *__restrict__
 		v[0] += (double) rk * (double) uk;
 		v[1] += (double) rk * (double) rk;
 	}
-	if (!reduce_partials<2, kCgBlock>(v, part, &sc->counter)) return;
-	double d[2];
-	finish_partials<2, kCgBlock>(d, part);
-	if (threadIdx.x == 0) {
-		sc->gamPrev = sc->gam;
-		sc->gam = d[0];
-		sc->rr = d[1];
-		sc->iters += 1;
-		if (!isfinite(d[0]) || !isfinite(d[1])) { sc->code = SA_ERR_NONFINITE; sc->done = 1; }
-		else if (d[1] < sc->tolSqu * sc->bb) { sc->code = SA_OK; sc->done = 1; }
-		else if (sc->iters >= sc->itrMax) { sc->code = SA_ERR_NOT_CONVERGED; sc->done = 1; }
-		sc->counter = 0;
+	cg_update_finish(v, part, sc);
+}
+
+// the same with the block-Jacobi preconditioner: grid-stride over rows (B entries each), u = Binv r
+template <int B, typename TV, typename TX>
+__global__ void __launch_bounds__(kCgBlock) k_cg_update_blk(int N, TX *__restrict__ x, TV *__restrict__ r,
+                                                            TV *__restrict__ u, const TV *__restrict__ w,
+                                                            TV *__restrict__ p, TV *__restrict__ s,
+                                                            const TV *__restrict__ binv, double *part, CgScal *sc)
+{
+	if (sc->done) return;
+	const int stride = gridDim.x * blockDim.x;
+	double v[2] = {0.0, 0.0};
+	const TV al = (TV) sc->alpha, be = (TV) sc->beta;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+		TV rk[B], uk[B];
+		for (int c = 0; c < B; ++c) {
+			const long k = (long) i * B + c;
+			TV pk = u[k] + be * p[k];
+			TV sk = w[k] + be * s[k];
+			p[k] = pk; s[k] = sk;
+			x[k] = x[k] + (TX) al * (TX) pk;
+			rk[c] = r[k] - al * sk;
+			r[k] = rk[c];
+		}
+		prec_block_ldg<B, TV>(binv + (long) i * B * B, rk, uk);
+		for (int c = 0; c < B; ++c) {
+			u[(long) i * B + c] = uk[c];
+			v[0] += (double) rk[c] * (double) uk[c];
+			v[1] += (double) rk[c] * (double) rk[c];
+		}
 	}
+	cg_update_finish(v, part, sc);
 }
 
 // r = b - q, u = D^{-1} r, partials (b, b), (r, r), (r, u)
@@ -283,27 +331,27 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_init(long n, const double *__re
 	}
 }
 
-// k_cg_init for the FP32 inner solves with the block-Jacobi preconditioner: one row (B entries) per
-// thread, r = b - q, u = Binv r, partials (b, b), (r, r), (r, u)
-template <int B>
+// k_cg_init for the block-Jacobi preconditioner: one row (B entries) per thread, r = b - q, u = Binv r,
+// partials (b, b), (r, r), (r, u)
+template <int B, typename TV>
 __global__ void __launch_bounds__(kCgBlock) k_cg_init_blk(int N, const double *__restrict__ b,
                                                           const double *__restrict__ q,
-                                                          const float *__restrict__ binv, float *__restrict__ r,
-                                                          float *__restrict__ u, double *part, CgScal *sc)
+                                                          const TV *__restrict__ binv, TV *__restrict__ r,
+                                                          TV *__restrict__ u, double *part, CgScal *sc)
 {
 	const int stride = gridDim.x * blockDim.x;
 	double v[3] = {0.0, 0.0, 0.0};
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
-		float rt[B], ut[B];
+		TV rt[B], ut[B];
 		for (int c = 0; c < B; ++c) {
 			const long k = (long) i * B + c;
 			double rk = b[k] - q[k];
-			rt[c] = (float) rk;
+			rt[c] = (TV) rk;
 			r[k] = rt[c];
 			v[0] += b[k] * b[k];
 			v[1] += rk * rk;
 		}
-		prec_block<B, float>(binv + (long) i * B * B, rt, ut);
+		prec_block_ldg<B, TV>(binv + (long) i * B * B, rt, ut);
 		for (int c = 0; c < B; ++c) {
 			u[(long) i * B + c] = ut[c];
 			v[2] += (double) rt[c] * (double) ut[c];
@@ -520,7 +568,7 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	__shared__ double nx[4];                     // next gamma, rr, beta, beta * gamma / alphaPrev
 	__shared__ double al[2];                     // alpha, delta of the iteration
 	__shared__ int gaveUp;
-	extern __shared__ int scol[];                // the column of every slot of the CTA's slices
+	extern __shared__ __align__(16) int scol[];  // the column of every slot of the CTA's slices
 	if (sc->done) return;                        // set by k_cg_init: the same for every CTA
 	const int nctas = gridDim.x, lc = blockIdx.x;
 	const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
@@ -558,19 +606,28 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	unsigned int target = 0;                     // bar->count is zeroed before the launch
 	if (threadIdx.x == 0) gaveUp = 0;
 	TX xv[B];
-	// block-Jacobi for FP32 vectors (the mixed inner solves, binv given); FP64 point Jacobi
-	constexpr bool kBlk = block_prec<TV>();
-	constexpr int kBV = kBlk ? B * B : 1;
+	// block-Jacobi (binv): FP32 inverses stay in registers, FP64 ones (twice the registers) are read from
+	// L2 in each update; FP64 B = 1 solves: point Jacobi, the inverse diagonal in registers
+	constexpr bool kBlk = block_prec<B, TV>();
+	constexpr bool kBlkReg = kBlk && sizeof(TV) == sizeof(float);
+	constexpr int kBV = kBlkReg ? B * B : 1;
 	TV rv[B], uv[B], pv[B], sv[B], dv[B], bv[kBV];
 	for (int c = 0; c < B; ++c) {
 		xv[c] = (TX) 0; rv[c] = uv[c] = pv[c] = sv[c] = dv[c] = (TV) 0;
 		if (own) {
 			long k = (long) i * B + c;
-			xv[c] = x[k]; rv[c] = r0[k]; uv[c] = u[k]; dv[c] = dinv[k];
+			xv[c] = x[k]; rv[c] = r0[k]; uv[c] = u[k];
+			if constexpr (!kBlk) dv[c] = dinv[k];
 		}
 	}
-	if constexpr (kBlk)
+	if constexpr (kBlkReg)
 		for (int t = 0; t < kBV; ++t) bv[t] = own ? binv[(long) i * B * B + t] : (TV) 0;
+	// FP64 block inverses: in shared memory after the column cache (8-byte aligned), [warp][entry][lane],
+	// copied once per solve like the columns; sbinv points at this thread's entry 0
+	TV *sbinv = reinterpret_cast<TV *>(scol + ((colInts + 1) & ~1)) + wp * B * B * 32 + lane;
+	if constexpr (kBlk && !kBlkReg)
+		if (rowWarp)
+			for (int t = 0; t < B * B; ++t) sbinv[t * 32] = own ? __ldg(binv + (long) i * B * B + t) : (TV) 0;
 	int it = 0, code = SA_OK;
 	bool first = true, pending = false;
 	for (;;) {
@@ -662,7 +719,12 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 		const TV al_ = (TV) alpha;
 		if (own) {
 			for (int c = 0; c < B; ++c) rv[c] = rv[c] - al_ * sv[c];
-			if constexpr (kBlk) prec_block<B, TV>(bv, rv, uv);
+			if constexpr (kBlkReg) prec_block<B, TV>(bv, rv, uv);
+			else if constexpr (kBlk) {
+				TV m[B * B];
+				for (int t = 0; t < B * B; ++t) m[t] = sbinv[t * 32];
+				prec_block<B, TV>(m, rv, uv);
+			}
 			else for (int c = 0; c < B; ++c) uv[c] = dv[c] * rv[c];
 			store_node_u<B, S, TV>(ug, i, uv);
 			d2[0] = row_dot<B, TV>(rv, uv);
@@ -727,7 +789,7 @@ k_cg_persist_g(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv
 	double gam = sc->gam, rr = sc->rr, alpha = 1.0, beta = 0.0;
 	double *partD = part, *partG = part + nctas;
 	unsigned int target = 0;
-	constexpr bool kBlk = block_prec<TV>();
+	constexpr bool kBlk = block_prec<B, TV>();
 	int it = 0, code = SA_OK;
 	bool first = true, pending = false;
 	for (;;) {
@@ -910,7 +972,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 	const SellOp A = J.A;
 	const TM *blk = (const TM *) J.blk;
 	const TV *dinv = (const TV *) J.dinv;
-	const TV *binv = (const TV *) J.binv;          // FP32 solves only (block-Jacobi), never read in FP64
+	const TV *binv = (const TV *) J.binv;          // block-Jacobi inverses (read only when block_prec)
 	TX *x = (TX *) J.x;
 	TV *r = (TV *) J.r, *u = (TV *) J.u, *w = (TV *) J.w, *p = (TV *) J.p, *sv = (TV *) J.s;
 	GridBar *bar = (GridBar *) J.bar;
@@ -965,7 +1027,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 		for (int sl = wj; sl < nsl; sl += WJ) {
 			const int i = sl * 32 + lane;
 			if (i >= A.N) continue;
-			TV rk[B], uk[B], dk[B];
+			TV rk[B], uk[B];
 			for (int c = 0; c < B; ++c) {
 				const long k = (long) i * B + c;
 				TV pk = __ldcg(u + k) + be * p[k];
@@ -974,10 +1036,9 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 				x[k] = x[k] + (TX) al * (TX) pk;
 				rk[c] = r[k] - al * sk;
 				r[k] = rk[c];
-				dk[c] = dinv[k];
 			}
-			if constexpr (block_prec<TV>()) prec_block<B, TV>(binv + (long) i * B * B, rk, uk);
-			else for (int c = 0; c < B; ++c) uk[c] = dk[c] * rk[c];
+			if constexpr (block_prec<B, TV>()) prec_block<B, TV>(binv + (long) i * B * B, rk, uk);
+			else for (int c = 0; c < B; ++c) uk[c] = dinv[(long) i * B + c] * rk[c];
 			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uk[c];
 			dot_row<B, TV>(d2[0], rk, uk);
 			dot_row<B, TV>(d2[1], rk, rk);
@@ -1297,6 +1358,13 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	if (timing && !prof->ev[0])
 		for (int k = 0; k < 4 * chunk; ++k) SA_CHECK(cudaEventCreate(&prof->ev[k]));
 	set_scal(sc, tolSqu, itrMax, bb, s);
+	// block-Jacobi inverses of this solve (FP32 copies for FP32 vectors); every CG path uses them
+	const TV *binv = nullptr;
+	if constexpr (block_prec<B, TV>()) {
+		binv = sizeof(TV) == sizeof(float) ? (const TV *) (const void *) prof->binv32
+		                                   : (const TV *) (const void *) prof->binv64;
+		if (!binv) throw CudaError{cudaErrorInvalidValue, "block-Jacobi CG without block inverses"};
+	}
 	// persistent launch: one CTA per SM, one slice per row warp plus the reducer warp
 	const int pwCap = std::max(1, std::min(kPersistMaxWarps, tuning().persistMaxWarps) - 1);
 	const int pw = std::max(1, std::min(pwCap, (m.nslice + prof->smCount - 1) / prof->smCount));
@@ -1324,20 +1392,19 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		if (lim > colSmem) kc = (int) std::min<size_t>((size_t) widest + 1, (lim - colSmem) / perSlot) & ~1;
 		dynSmem = colSmem + (size_t) kc * perSlot;
 	}
+	// FP64 block-Jacobi: every row warp's block inverses after the columns, 8-byte aligned
+	if (block_prec<B, TV>() && sizeof(TV) == sizeof(double) && tabOk)
+		dynSmem = ((colSmem + 7) & ~(size_t) 7) + (size_t) pw * 32 * B * B * sizeof(TV);
 	const int colInts = tabOk ? (int) (colSmem / sizeof(int)) : 0;
 	const bool persist = prof->cgKernel != SA_CG_TWO_KERNEL && prof->cgKernel != SA_CG_PERSISTENT_GLOBAL && prof->bar &&
-	                     (!block_prec<TV>() || prof->binv32) && tabOk && (B != 3 || prof->u4) &&
+	                     tabOk && (B != 3 || prof->u4) &&
 	                     nctas <= persist_capacity<B, TM, TV, TX>(prof->smCount, pw + 1, dynSmem);
 	if (persist) {
-		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first).  FP32
-		// inner solves of mixed precision are block-Jacobi preconditioned (3x3 node blocks)
-		const TV *binv = nullptr;
-		if constexpr (block_prec<TV>()) {
-			binv = prof->binv32;
-			k_cg_init_blk<B><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
-		} else {
+		// one cooperative launch for the whole solve (k_cg_init sets r, u and the scalars first)
+		if constexpr (block_prec<B, TV>())
+			k_cg_init_blk<B, TV><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
+		else
 			k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
-		}
 		// the matvec gathers u from a copy in its own layout (3-component nodes padded to 4)
 		TV *ug = u;
 		if (B == 3) {
@@ -1380,20 +1447,17 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 		return h;
 	}
 	// too large for row state in registers: the global-state persistent kernel, one CTA per SM
-	if (prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar && (!block_prec<TV>() || prof->binv32)) {
+	if (prof->cgKernel != SA_CG_TWO_KERNEL && prof->bar) {
 		const int warpsG = pwCap + 1;
 		const int nctasG = std::min(prof->smCount, m.nslice);
 		const size_t span = col_span_bytes_even(m, nctasG);
 		const int cached = span <= (size_t) kColSmemMax ? 1 : 0;
 		const size_t smemG = cached ? span : 0;
 		if (nctasG >= 1 && nctasG <= persist_g_capacity<B, TM, TV, TX>(prof->smCount, warpsG, smemG)) {
-			const TV *binv = nullptr;
-			if constexpr (block_prec<TV>()) {
-				binv = prof->binv32;
-				k_cg_init_blk<B><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
-			} else {
+			if constexpr (block_prec<B, TV>())
+				k_cg_init_blk<B, TV><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
+			else
 				k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
-			}
 			SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
 			SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
 			GridBar *bar = (GridBar *) prof->bar;
@@ -1428,7 +1492,11 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 	}
 	SA_CHECK(cudaMemsetAsync(p, 0, sizeof(TV) * n, s));
 	SA_CHECK(cudaMemsetAsync(sv, 0, sizeof(TV) * n, s));
-	k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
+	if constexpr (block_prec<B, TV>())
+		k_cg_init_blk<B, TV><<<vec_grid(N, prof->smCount), kCgBlock, 0, s>>>(N, b, q, binv, r, u, part, sc);
+	else
+		k_cg_init<TV><<<nb, kCgBlock, 0, s>>>(n, b, q, dinv, r, u, part, sc);
+	const int nbRows = vec_grid(N, prof->smCount);
 	if (!prof->pinned) {
 		SA_CHECK(cudaHostAlloc(&prof->pinned, 2 * sizeof(CgScal), cudaHostAllocDefault));
 		for (int k = 0; k < 2; ++k) SA_CHECK(cudaEventCreateWithFlags(&prof->chunkEv[k], cudaEventDisableTiming));
@@ -1443,7 +1511,10 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 			k_cg_spmv<B, TM, TV><<<(m.nslice + kSlicesPerCta - 1) / kSlicesPerCta, kSpmvBlock, 0, s>>>(
 				sell_of(m), blk, u, w, part, sc);
 			if (timing) SA_CHECK(cudaEventRecord(prof->ev[set * 2 * chunk + 2 * k + 1], s));
-			k_cg_update<TV, TX><<<nb, kCgBlock, 0, s>>>(n, x, r, u, w, p, sv, dinv, part, sc);
+			if constexpr (block_prec<B, TV>())
+				k_cg_update_blk<B, TV, TX><<<nbRows, kCgBlock, 0, s>>>(N, x, r, u, w, p, sv, binv, part, sc);
+			else
+				k_cg_update<TV, TX><<<nb, kCgBlock, 0, s>>>(n, x, r, u, w, p, sv, dinv, part, sc);
 		}
 		SA_CHECK(cudaMemcpyAsync(hs + set, sc, sizeof(CgScal), cudaMemcpyDeviceToHost, s));
 		SA_CHECK(cudaEventRecord(prof->chunkEv[set], s));
@@ -1557,8 +1628,14 @@ void cg_prepare_fp64(const Mesh &m, const double *blk, const double *dinv, const
 	set_scal((CgScal *) w.scal, tolSqu, itrMax, -1.0, s);
 	SA_CHECK(cudaMemsetAsync(w.p, 0, sizeof(double) * n, s));
 	SA_CHECK(cudaMemsetAsync(w.sv, 0, sizeof(double) * n, s));
-	k_cg_init<double><<<vec_grid(n, w.smCount), kCgBlock, 0, s>>>(n, b, q, dinv, w.r, w.u, w.part,
-	                                                                (CgScal *) w.scal);
+	if constexpr (block_prec<B, double>()) {
+		if (!w.binv64) throw CudaError{cudaErrorInvalidValue, "block-Jacobi CG without block inverses"};
+		k_cg_init_blk<B, double><<<vec_grid(m.N, w.smCount), kCgBlock, 0, s>>>(m.N, b, q, w.binv64, w.r, w.u,
+		                                                                        w.part, (CgScal *) w.scal);
+	} else {
+		k_cg_init<double><<<vec_grid(n, w.smCount), kCgBlock, 0, s>>>(n, b, q, dinv, w.r, w.u, w.part,
+		                                                                (CgScal *) w.scal);
+	}
 	w.launches += 2;
 }
 
@@ -1600,7 +1677,7 @@ void cg_mixed_inner(const Mesh &m, int itrMax, double innerTolSqu, CgWork &w, cu
 	set_scal((CgScal *) w.scal, innerTolSqu, itrMax, -1.0, s);
 	if (!w.binv32) throw CudaError{cudaErrorInvalidValue, "mixed precision without block inverses"};
 	(void) dinv32;
-	k_cg_init_blk<B><<<vec_grid(m.N, w.smCount), kCgBlock, 0, s>>>(m.N, rin, zero, w.binv32, r32, u32, w.part,
+	k_cg_init_blk<B, float><<<vec_grid(m.N, w.smCount), kCgBlock, 0, s>>>(m.N, rin, zero, w.binv32, r32, u32, w.part,
 	                                                                (CgScal *) w.scal);
 	w.launches += 1;
 }
@@ -1681,7 +1758,7 @@ int cg_batch_run(const std::vector<BatchSolve> &solves, int smCount, CgJob *devJ
 			CgWork &w = *b.cw;
 			CgJob j;
 			j.A = sell_of(m);
-			if (block_prec<TV>() && !b.binv) throw CudaError{cudaErrorInvalidValue, "batched FP32 CG without block inverses"};
+			if (block_prec<B, TV>() && !b.binv) throw CudaError{cudaErrorInvalidValue, "batched CG without block inverses"};
 			j.blk = b.blk; j.dinv = b.dinv; j.binv = b.binv; j.x = b.x;
 			if (sizeof(TV) == sizeof(double)) {
 				j.r = w.r; j.u = w.u; j.w = w.w; j.p = w.p; j.s = w.sv;

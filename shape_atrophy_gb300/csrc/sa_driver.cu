@@ -551,13 +551,15 @@ static void alloc_work(Work &w, const Mesh &m, const Model &md, bool wantTraj, P
 		SA_CHECK(cudaDeviceGetAttribute(&c.smCount, cudaDevAttrMultiProcessorCount, dev));
 	}
 	c.xr = P.alloc<double>((size_t) 3 * n);
+	bool useK = md.frame || md.ldmWgt != 0.0;
+	// the velocity solves' block-Jacobi inverses: FP64 for FP64 Jacobi-PCG, FP32 for the mixed inner solves
+	if (md.precision == SA_PREC_FP64 && !useK) c.binv64 = P.alloc<double>((size_t) N * D * D);
 	if (md.precision == SA_PREC_MIXED) {
 		c.blk32 = P.alloc<float>((size_t) T * sell_vals<D>());
 		c.binv32 = P.alloc<float>((size_t) N * D * D);
 		c.f32 = P.alloc<float>((size_t) 7 * n);
 		if (!md.frame) { w.L32 = P.zeros<float>(T); w.rdInv32 = P.alloc<float>(N); }
 	}
-	bool useK = md.frame || md.ldmWgt != 0.0;
 	if (useK) {
 		KpcgWork &k = w.kw;
 		k.Ad = P.alloc<double>(n); k.Kid = P.alloc<double>(n); k.r = P.alloc<double>(n);
@@ -631,7 +633,7 @@ struct Stepper {
 		if (md.velocityGuess > 0 && !useK) launch_extrap_poly(m.N * (long) D, md.velocityGuess, t, w.v, w.vHist, s);
 		launch_activity<D>(m, md, tau_now(), w.fy, w.fr, s);
 		if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xn, w.pd, s);
-		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, w.cw.binv32, s);
+		launch_assemble_elastic<D>(m, md, *gn, w.pd, w.blk, w.dinv, w.cw.binv64, w.cw.binv32, s);
 		launch_yank_rhs<D>(m, *gn, w.fy, w.b, s);
 		if (useK) {
 			if (!md.kernelFree) launch_kernel_matrix<D>(md, m.N, xn, w.K, s);
@@ -1222,7 +1224,7 @@ static int adjoint_frame_impl(sa_context *ctx, Pool &P, Mesh &m, Model &md, cons
 			// previous step's K^{-1} n
 			if (!md.kernelFree) launch_kernel_matrix<D>(md, m.N, xt, w.K, s);
 			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xt, w.pd, s);
-			launch_assemble_elastic<D>(m, md, w.g0, w.pd, w.blk, w.dinv, nullptr, s);
+			launch_assemble_elastic<D>(m, md, w.g0, w.pd, w.blk, w.dinv, w.cw.binv64, nullptr, s);
 			code = kpcg<D>(m, md, w.blk, w.K, xt, rhsV, nu, w.kw, stt, &its, s);
 			adjIts += its;
 			if (code != SA_OK) { status = code; break; }
@@ -1391,7 +1393,7 @@ static int adjoint_impl(sa_context *ctx, const sa_element_object *obj, const dou
 			launch_adj_axpy(n, aXn, dt - 1.0, aXn, rhsV, s);
 			// velocity adjoint: K(x_t) n = a_v
 			if (m.Bt > 0 && md.btmWgt != 0.0) launch_penalty_diag<D>(m, md, xt, w.pd, s);
-			launch_assemble_elastic<D>(m, md, w.g0, w.pd, w.blk, w.dinv, nullptr, s);
+			launch_assemble_elastic<D>(m, md, w.g0, w.pd, w.blk, w.dinv, w.cw.binv64, nullptr, s);
 			code = cg_jacobi<D>(m, w.blk, w.dinv, rhsV, nu, md.cgItrMax, md.cgTolSqu, w.cw, stt, &its, s,
 			                    SA_PREC_FP64);
 			adjIts += its;
@@ -1725,7 +1727,8 @@ static size_t estimate_bytes(const Request &r)
 	size_t ints = E * (D + 1) + N * o.vtxElmCols + Z * (2 + o.femIfoCols) + Z * 4 + slots + 2 * E +
 	              (size_t) o.btmElmNum * D + (size_t) o.btmLmkNum * o.vtxBtmCols + (size_t) o.vfdElmNum * D;
 	size_t dbl = slots * (D * D + 1) + 2 * Z + 2 * E * (D == 3 ? 16 : 8) + 20 * N * D + 8 * N + T * N;
-	if (r.prm.precision == SA_PREC_MIXED) dbl += (slots * D * D + 7 * N * D) / 2;
+	if (r.prm.precision == SA_PREC_MIXED) dbl += (slots * D * D + 7 * N * D + N * D * D) / 2;
+	else dbl += N * D * D;                                         // FP64 block-Jacobi inverses
 	if (r.hasTgt) dbl += (size_t) r.tgt.tgtElmNum * (2 * D + 1) + (size_t) o.vfdElmNum * (3 * D + 2);
 	return 4 * ints + 8 * dbl + (1 << 20);
 }
@@ -1813,7 +1816,7 @@ struct Inst : InstBase {
 		cg_prepare_fp64<D>(m, w.blk, w.dinv, w.b, w.v, md.cgItrMax, md.cgTolSqu, w.cw, s);
 	}
 	void finish_velocity_fp64() override { cg_finish_fp64<D>(m, w.v, w.cw, s); }
-	BatchSolve velocity_fp64() override { return BatchSolve{&m, &w.cw, w.blk, w.dinv, w.v, nullptr}; }
+	BatchSolve velocity_fp64() override { return BatchSolve{&m, &w.cw, w.blk, w.dinv, w.v, w.cw.binv64}; }
 	void mixed_outer(int kind, int first) override
 	{
 		if (kind == kMixedVelocity) {

@@ -375,10 +375,11 @@ template <int D> void launch_yank_rhs(const Mesh &m, const Geom &g, const double
                                       cudaStream_t s);
 template <int D> void launch_penalty_diag(const Mesh &m, const Model &md, const double *x, double *pd,
                                           cudaStream_t s);
-// binv32 (optional, N x D x D): FP32 inverses of the diagonal blocks (block-Jacobi of the FP32 inner solves)
+// binv64 / binv32 (each optional, N x D x D): FP64 / FP32 inverses of the diagonal blocks (the block-Jacobi
+// preconditioner of the FP64 velocity solves / of the FP32 inner solves of mixed precision)
 template <int D> void launch_assemble_elastic(const Mesh &m, const Model &md, const Geom &g,
-                                              const double *pd, double *blk, double *dinv, float *binv32,
-                                              cudaStream_t s);
+                                              const double *pd, double *blk, double *dinv, double *binv64,
+                                              float *binv32, cudaStream_t s);
 template <int D> void launch_assemble_rd(const Mesh &m, const Model &md, const Geom &g, double dt,
                                          double *Mval, double *Lval, double *dinv, cudaStream_t s);
 template <int D> void launch_rd_rhs(const Mesh &m, const Geom &gNow, const double *Mnow, const double *tau,
@@ -466,6 +467,7 @@ struct CgWork {            // scratch of the Jacobi CG (Chronopoulos-Gear form)
 	double profBytes = 0.0, profFlops = 0.0;   // algorithmic bytes / flops of the timed launches
 	float *blk32 = nullptr;       // FP32 copy of the operator (mixed precision)
 	float *binv32 = nullptr;      // FP32 inverses of its diagonal blocks (block-Jacobi, mixed precision)
+	double *binv64 = nullptr;     // FP64 inverses of its diagonal blocks (block-Jacobi of the FP64 solves)
 	float *f32 = nullptr;         // 7 n FP32 vectors of the inner solve (mixed precision)
 	double *xr = nullptr;         // 3 n FP64 refinement scratch
 	double *u4 = nullptr;         // 4 N: the persistent CG's gather copy of u (3-component nodes padded to 4)

@@ -277,7 +277,8 @@ __global__ void k_asm_elastic(int Z, int E, int asmCols, const int *__restrict__
                               double btmWgt, const double *__restrict__ pd, int Nb,
                               const int *__restrict__ slDest, const int *__restrict__ transZ, long total,
                               const int *__restrict__ order, int nOrd,
-                              double *__restrict__ blk, double *__restrict__ dinv, float *__restrict__ binv32)
+                              double *__restrict__ blk, double *__restrict__ dinv, double *__restrict__ binv64,
+                              float *__restrict__ binv32)
 {
 	int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= nOrd) return;
@@ -328,12 +329,16 @@ __global__ void k_asm_elastic(int Z, int E, int asmCols, const int *__restrict__
 			dinv[(long) i * D + d] = 1.0 / acc[d][d];
 		}
 		store_block<D>(blk, total, slDest[z], acc);
-		if (binv32) {                      // block-Jacobi preconditioner of the FP32 inner solves
+		if (binv64 || binv32) {            // block-Jacobi preconditioner (FP64 solves, FP32 inner solves)
 			Mat<D> a, inv;
 			for (int r = 0; r < D; ++r) for (int c = 0; c < D; ++c) a.m[r][c] = acc[r][c];
 			inv = mat_inverse<D>(a);
 			for (int r = 0; r < D; ++r)
-				for (int c = 0; c < D; ++c) binv32[(long) i * D * D + r * D + c] = (float) inv.m[r][c];
+				for (int c = 0; c < D; ++c) {
+					const long k = (long) i * D * D + r * D + c;
+					if (binv64) binv64[k] = inv.m[r][c];
+					if (binv32) binv32[k] = (float) inv.m[r][c];
+				}
 		}
 		return;
 	}
@@ -345,14 +350,14 @@ __global__ void k_asm_elastic(int Z, int E, int asmCols, const int *__restrict__
 
 template <int D>
 void launch_assemble_elastic(const Mesh &m, const Model &md, const Geom &g, const double *pd, double *blk,
-                             double *dinv, float *binv32, cudaStream_t s)
+                             double *dinv, double *binv64, float *binv32, cudaStream_t s)
 {
 	FrameMod fm;
 	for (int k = 0; k < 4; ++k) fm.m[k] = md.mod[k];
 	k_asm_elastic<D><<<grid_for(m.nAsm, 128), 128, 0, s>>>(m.Z, m.E, m.asmCols, m.femVtx, m.femIfo, m.asmTab, g.rec,
 	                                                        md.frame, fm, g.frm, g.tsv, m.elmLyr, md.lyrMod, md.btmWgt,
 	                                                        pd, m.Nb, m.slDest, m.transZ, m.slTotal, m.asmOrder,
-	                                                        m.nAsm, blk, dinv, binv32);
+	                                                        m.nAsm, blk, dinv, binv64, binv32);
 }
 
 // ---------------------------------------------------------------------------
@@ -524,7 +529,7 @@ void launch_aos_to_soa(int N, int D, const double *aos, double *soa, cudaStream_
 	template void launch_yank_rhs<D>(const Mesh &, const Geom &, const double *, double *, cudaStream_t);      \
 	template void launch_penalty_diag<D>(const Mesh &, const Model &, const double *, double *, cudaStream_t); \
 	template void launch_assemble_elastic<D>(const Mesh &, const Model &, const Geom &, const double *,        \
-	                                         double *, double *, float *, cudaStream_t);                       \
+	                                         double *, double *, double *, float *, cudaStream_t);             \
 	template void launch_assemble_rd<D>(const Mesh &, const Model &, const Geom &, double, double *, double *, \
 	                                    double *, cudaStream_t);                                               \
 	template void launch_rd_rhs<D>(const Mesh &, const Geom &, const double *, const double *, const double *, \

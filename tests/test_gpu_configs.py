@@ -3,12 +3,17 @@
 * 2D layered annulus: 16 radial x 256 angular nodes (4096 nodes, 7680
   triangles), 4 material layers, 50 steps of dt 0.02 -- the whole workload,
   every step compared: 1e-10 relative at CG tolerance 1e-12, and at the
-  workload's own tolerance 1e-8 1e-9 in positions and concentration, 1e-8
-  in the objective.
+  workload's own tolerance 1e-8 1e-9 in positions, 1e-8 in concentration
+  and objective.  At 1e-8 the concentration is known only to its solve's
+  tolerance: the oracle itself moves by ~1e-9 in concentration when the
+  initial nodes are perturbed by 1e-15 relative (the velocity and
+  reaction-diffusion solves stop an iteration earlier or later), so the
+  bound there is the solves' relative residual; the test prints that
+  spread beside the GPU's difference.
 * 3D layered shell: icosphere 5 x 8 prism layers (92 178 nodes, 491 520
   tets), 3 material layers, dt 0.01: the first 20 steps at the workload's
-  tolerance 1e-8 (1e-9 / 1e-8 as above), the first 5 steps at 1e-12
-  (1e-10).
+  tolerance 1e-8 (1e-9 in positions and concentration, 1e-8 in the
+  objective), the first 5 steps at 1e-12 (1e-10).
 * Mixed precision on the same shell (FP32 operator and inner CG, FP64 dots
   and refinement, FP32 pair sums): against the FP64 oracle at steps 10 and
   20, at most 1e-6 relative in positions, concentration and objective.
@@ -43,8 +48,8 @@ def report(name, **errs):
 # ---------------------------------------------------------------------------
 # 2D annulus, the whole workload
 # ---------------------------------------------------------------------------
-@pytest.mark.parametrize("tol,bound,obj_bound", [(1e-12, 1e-10, 1e-10), (1e-8, 1e-9, 1e-8)])
-def test_annulus_workload_matches_oracle(tol, bound, obj_bound):
+@pytest.mark.parametrize("tol,bound,tau_bound,obj_bound", [(1e-12, 1e-10, 1e-10, 1e-10), (1e-8, 1e-9, 1e-8, 1e-8)])
+def test_annulus_workload_matches_oracle(tol, bound, tau_bound, obj_bound):
     from shape_atrophy_gb300 import api, problems
     spec = problems.annulus_layered(cgTolVal=tol)
     assert spec["lmkIniMat"].shape[1] == 4096 and spec["elmObj"]["elmVtxMat"].shape[1] == 7680
@@ -56,7 +61,15 @@ def test_annulus_workload_matches_oracle(tol, bound, obj_bound):
              displacement=rel(got["lmkStk"] - got["lmkStk"][0], want["lmkStk"] - want["lmkStk"][0]),
              objective=abs(got["obj"][0] - want["obj"]) / abs(want["obj"]))
     report(f"annulus 4096 nodes, 50 steps, cg tol {tol:g}", **e)
-    assert e["positions"] < bound and e["concentration"] < bound
+    if tol > 1e-10:
+        # the oracle against itself, initial nodes perturbed by 1e-15 relative
+        pert = dict(spec)
+        pert["lmkIniMat"] = spec["lmkIniMat"] * (1.0 + 1e-15 * np.random.default_rng(1).standard_normal(
+            spec["lmkIniMat"].shape))
+        again = oracle(pert)
+        report("oracle, initial nodes perturbed by 1e-15", positions=rel(again["lmkStk"], want["lmkStk"]),
+               concentration=rel(again["tauMat"], want["tauMat"]))
+    assert e["positions"] < bound and e["concentration"] < tau_bound
     assert e["objective"] < obj_bound
 
 

@@ -10,6 +10,8 @@ the golden vectors:
   rotations and is symmetric
   (x . E y = y . E x), frame and layered models, 2D and 3D; the bottom
   penalty is symmetric;
+* the layered velocity solve's block-Jacobi blocks are the diagonal blocks of
+  E + btmWgt P (probed with unit fields), symmetric, and inverted exactly;
 * the RKHS kernel matrix equals the closed forms of the half-integer Matern
   kernels (nu = p + 1/2: e^-r times a degree-p polynomial, generated here
   from the general formula) and the Gaussian in 3D; in 2D (rational Bessel
@@ -87,6 +89,35 @@ def test_elasticity_annihilates_rigid_motions_and_is_symmetric(name):
     if spec["btmWgt"] != 0.0 or spec["elmObj"]["btmVtxMat"].shape[1] > 0:
         Px, Py = P.penalty(lmk, x), P.penalty(lmk, y)
         assert np.vdot(x, Py) == pytest.approx(np.vdot(y, Px), rel=1e-12, abs=1e-14)
+
+
+@pytest.mark.parametrize("name", [k for k in CASES if k.endswith("layered")])
+def test_block_jacobi_blocks_are_the_operator_diagonal_blocks(name):
+    """The velocity solve's block-Jacobi preconditioner: node i's D x D block equals rows i of
+    (E + btmWgt P) applied to the unit fields e_(i,c), every block is symmetric, and the inverse
+    returned times the block is the identity."""
+    spec = CASES[name]()
+    P = Problem(spec)
+    lmk = spec["lmkIniMat"]
+    D, N = lmk.shape
+    blk = P.elastic_blocks(lmk)
+    inv = P.elastic_blocks(lmk, inverse=True)
+    rng = np.random.default_rng(5)
+    nodes = rng.choice(N, size=min(N, 12), replace=False)
+    btm = spec["elmObj"]["btmVtxMat"]
+    if btm.shape[1] > 0:
+        nodes = np.concatenate([nodes, btm[0, :3]])    # some with the bottom penalty
+    scale = np.abs(blk).max()
+    for i in nodes:
+        for c in range(D):
+            e = np.zeros((D, N))
+            e[c, i] = 1.0
+            col = P.elastic(lmk, e)[:, i] + spec["btmWgt"] * P.penalty(lmk, e)[:, i]
+            np.testing.assert_allclose(blk[i][:, c], col, rtol=0, atol=1e-13 * scale)
+    np.testing.assert_allclose(blk, np.swapaxes(blk, 1, 2), rtol=0, atol=1e-14 * scale)
+    eye = np.einsum("nab,nbc->nac", inv, blk)
+    np.testing.assert_allclose(eye, np.broadcast_to(np.eye(D), eye.shape), rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(np.stack([blk[:, d, d] for d in range(D)]), P.elastic_diag(lmk))
 
 
 def _matern_half_integer(p, r):
