@@ -549,7 +549,9 @@ def main():
             "peak_source": "measured in this run: sa_selftest_fma_peak (independent FMA chains per thread, "
                            "256-thread CTAs, 2/4/8 CTAs per SM, best launch), its rate per SM clock x SMs x the "
                            "SM clock sampled during the timed steps",
-            "flops_model": "2 x (9 x operator slots + 8 x rows) per CG iteration (assembled 3x3 blocks)"}
+            "flops_model": "2 x (9 x operator slots + 10 x vector entries) per CG iteration (assembled 3x3 blocks; "
+                           "per entry the x, r, p, s updates, three dot terms and a row of the 3x3 block-Jacobi "
+                           "inverse)"}
 
     e2e = None
     if not args.no_e2e and rank == 0:

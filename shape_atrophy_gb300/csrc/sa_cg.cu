@@ -1440,7 +1440,9 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 			prof->profBytes += (double) h.iters * ((double) m.slTotal * (B * B * sizeof(TM) + 4.0) +
 			                                       8.0 * m.nslice + 2.0 * sizeof(TV) * n) +
 			                   4.0 * sizeof(TV) * n + sizeof(TX) * n;
-			prof->profFlops += (double) h.iters * 2.0 * ((double) B * B * m.slTotal + 8.0 * n);
+			// FMAs per vector entry: x, r, p, s updates, three dot terms, and u = D^-1 r (1) or the
+			// entry's row of the block inverse (B)
+			prof->profFlops += (double) h.iters * 2.0 * ((double) B * B * m.slTotal + (block_prec<B, TV>() ? 7.0 + B : 8.0) * n);
 		}
 		// any CTA that gave up leaves the abort flag set, whatever CTA 0 reported
 		if (gaveUp || h.code == SA_ERR_TIMEOUT) throw DeviceWaitError{"persistent CG grid barrier"};
@@ -1484,7 +1486,7 @@ static CgScal run_cg(const Mesh &m, const TM *blk, const TV *dinv, const double 
 				// vectors w, p, s, r, x read and written, u read twice and written
 				prof->profBytes += (double) h.iters * ((double) m.slTotal * (B * B * sizeof(TM) + (cached ? 0.0 : 4.0)) +
 				                                       8.0 * m.nslice + 14.0 * sizeof(TV) * n);
-				prof->profFlops += (double) h.iters * 2.0 * ((double) B * B * m.slTotal + 8.0 * n);
+				prof->profFlops += (double) h.iters * 2.0 * ((double) B * B * m.slTotal + (block_prec<B, TV>() ? 7.0 + B : 8.0) * n);
 			}
 			if (gaveUp || h.code == SA_ERR_TIMEOUT) throw DeviceWaitError{"persistent CG grid barrier"};
 			return h;
