@@ -3,7 +3,7 @@
 Workload (default): the 3D layered spherical shell -- icosphere level 5
 (10242 surface vertices) x 9 node layers (8 prism layers, 3 tets each) =
 92178 nodes, 491520 P1 tets, 3 material layers, Fisher-KPP + isotropic
-elasticity, Jacobi-PCG tolerance 1e-8, dt 0.01, plain FP64.  A "step" is
+elasticity, block-Jacobi PCG tolerance 1e-8, dt 0.01, plain FP64.  A "step" is
 one time step of the forward model (velocity solve, node update,
 reaction-diffusion solve).  Inputs are synthetic (seeded mesh + bump), the
 per-step working set (operator blocks, geometry, CG vectors, ~0.3 GB) is
@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "3D shell steps/s"
 WORKLOAD = ("3D layered spherical shell: icosphere level 5 x 8 prism layers, 92178 nodes, 491520 P1 tets, "
-            "3 material layers, Fisher-KPP + layered isotropic elasticity, Jacobi-PCG 1e-8, dt 0.01")
+            "3 material layers, Fisher-KPP + layered isotropic elasticity, block-Jacobi PCG 1e-8, dt 0.01")
 
 
 def dist_init():

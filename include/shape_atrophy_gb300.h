@@ -47,7 +47,7 @@ extern "C" {
 #define SA_ERR_TIMEOUT        7   /* a bounded device-side wait (grid barrier) gave up */
 
 #define SA_ELA_FRAME          0   /* reference frame elasticity, K-preconditioned CG */
-#define SA_ELA_ISOTROPIC      1   /* layered isotropic elasticity, Jacobi-PCG */
+#define SA_ELA_ISOTROPIC      1   /* layered isotropic elasticity, block-Jacobi PCG */
 
 #define SA_PREC_FP64          0   /* all arithmetic in FP64 */
 #define SA_PREC_MIXED         1   /* FP32 operators, FP64 dots/residuals + refinement */

@@ -11,11 +11,11 @@ dirKnlType, dirKnlWidth).
   lyrNdeNum x lyrCntNum strip of [-3,3] x [-1,1] (frame elasticity, 2D).
 * ``frame_shell``  -- frame elasticity on a small icosphere shell (3D).
 * ``annulus_layered`` -- layered 2D annulus: 16 radial x 256 angular nodes,
-  7680 triangles, 4 layers, Fisher-KPP, Gaussian bump, Jacobi-PCG 1e-8,
+  7680 triangles, 4 layers, Fisher-KPP, Gaussian bump, block-Jacobi PCG 1e-8,
   Gaussian varifold (width 0.1) on inner+outer boundary (512 segments).
 * ``shell_layered`` -- layered 3D shell: icosphere level 5 x 9 node layers
   (92178 nodes, 491520 tets), 3 material layers, 100 steps dt 0.01,
-  Jacobi-PCG 1e-8, Matern-3/2 varifold (width 0.08) on the 20480 outer
+  block-Jacobi PCG 1e-8, Matern-3/2 varifold (width 0.08) on the 20480 outer
   triangles.
 
 Choices the layered workloads leave open are fixed here: bottom penalty weight ``btmWgt`` (anchors the inner boundary;
