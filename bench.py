@@ -126,6 +126,36 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# element-object arrays the layered forward call reads (the frame model's tan/nml and tsv arrays and the
+# boundary-segment arrays are not uploaded for it)
+LAYERED_OBJ_KEYS = ("elmVtxMat", "vtxElmMat", "btmVtxMat", "vtxBtmMat", "femVtxMat", "femIfoMat", "vfdVtxMat",
+                    "elmLyrVec")
+
+
+def pinned_inputs(spec):
+    """The spec with every array the call uploads copied into page-locked host memory (the inputs of the
+    end-to-end leg), and the bytes the call copies to the device."""
+    import torch
+
+    def pin(a, dtype):
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dtype))).pin_memory().numpy()
+
+    s = dict(spec)
+    obj = dict(spec["elmObj"])
+    for k in LAYERED_OBJ_KEYS:
+        if k in obj:
+            obj[k] = pin(obj[k], np.int32)
+    s["elmObj"] = obj
+    if "elmLyrVec" in spec:
+        s["elmLyrVec"] = pin(spec["elmLyrVec"], np.int32)
+    s["lmkIniMat"] = pin(spec["lmkIniMat"], np.float64)
+    s["tgt"] = tuple(pin(a, np.float64) for a in spec["tgt"])
+    s["tauVarVec"] = pin(spec["tauVarVec"], np.float64)
+    h2d = s["lmkIniMat"].nbytes + sum(obj[k].nbytes for k in LAYERED_OBJ_KEYS if k in obj) + \
+        sum(a.nbytes for a in s["tgt"]) + s["tauVarVec"].nbytes
+    return s, h2d
+
+
 def spec_for(args, steps: int):
     from shape_atrophy_gb300 import problems
     if args.workload == "annulus":
@@ -555,23 +585,21 @@ def main():
 
     e2e = None
     if not args.no_e2e and rank == 0:
-        spec_e = spec_for(args, K)
+        spec_e, h2d = pinned_inputs(spec_for(args, K))
         # one untimed call of the same entry point first (a single step): loads the objective's kernels, which
         # the timed step leg above does not launch, so the timed call measures a user's repeated calls
         api.forward(dict(spec_e, timeNum=2), trajectory=True, objective=True, precision=args.precision, device=local)
         walls = []
-        for _ in range(3):                      # a single call varies by ~10 % (host set-up on the CPU)
+        for _ in range(3):                      # a single call varies by a few % (host set-up on the CPU)
             t0 = time.perf_counter()
             r = api.forward(spec_e, trajectory=True, objective=True, precision=args.precision, device=local)
             walls.append(time.perf_counter() - t0)
         wall = sorted(walls)[1]
-        obj = spec_e["elmObj"]
-        h2d = spec_e["lmkIniMat"].nbytes + sum(v.nbytes for k, v in obj.items() if hasattr(v, "nbytes")) + \
-            sum(a.nbytes for a in spec_e["tgt"]) + 8 * len(spec_e["tauVarVec"])
         d2h = r["lmkStk"].nbytes + r["tauMat"].nbytes + r["obj"].nbytes
         e2e = {"value": K / wall, "unit": "steps/s", "h2d_bytes_per_step": h2d // K, "d2h_bytes_per_step": d2h // K,
-               "what": f"one sa_forward call ({K} steps + objective) with host buffers: mesh upload and set-up, "
-                       "solve, trajectory download; median of 3 calls after one untimed one-step call",
+               "what": f"one sa_forward call ({K} steps + objective) with its inputs in pinned host memory: mesh "
+                       "upload and set-up, solve, trajectory download; median of 3 calls after one untimed "
+                       "one-step call",
                "calls_s": [round(w, 4) for w in walls]}
 
     served = None

@@ -210,6 +210,23 @@ template <typename F> static void parallel_chunks(long n, F &&f)
 		if (!e.empty()) throw ArgError{e};
 }
 
+// the same with the chunk's index t (chunks 0 .. chunk_count(n) - 1, in order over [0, n))
+static int chunk_count(long n)
+{
+	const int T = HostPool::get().size();
+	return n < 32768 || T <= 1 ? 1 : T;
+}
+
+template <typename F> static void parallel_chunks_t(long n, F &&f)
+{
+	const int T = chunk_count(n);
+	if (T == 1) {
+		f(0, 0L, n);
+		return;
+	}
+	HostPool::get().run([&](int t) { f(t, n * t / T, n * (t + 1) / T); });
+}
+
 template <typename T> static std::vector<T> to_host(const T *p, size_t n, cudaStream_t s)
 {
 	std::vector<T> h(n);
@@ -265,9 +282,9 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 	m.Bt = o->btmElmNum; m.Nb = o->btmLmkNum; m.Vd = needVfd ? o->vfdElmNum : 0;
 	SA_REQUIRE(m.N > 0 && m.E > 0 && m.Z >= m.N, "empty mesh or femVtxMat smaller than the node count");
 	SA_REQUIRE(o->elmVtxMat && o->vtxElmMat && o->femVtxMat && o->femIfoMat, "missing element-object array");
-	// the frame arrays are read by the frame model only
+	// the frame arrays are read by the frame model only (the layered model neither uploads nor checks them)
 	SA_REQUIRE(layered || (o->frmVtxMat && o->tsvVtxMat), "frame model needs tanVtxMat/nmlVtxMat and tsvVtxMat");
-	const bool haveFrame = o->frmVtxMat && o->tsvVtxMat;
+	const bool haveFrame = !layered && o->frmVtxMat && o->tsvVtxMat;
 	SA_REQUIRE(o->vtxElmCols >= 1 && o->femIfoCols >= 2, "adjacency matrices need a count column");
 	SA_REQUIRE((long) m.E * 16 < (1L << 31), "too many elements for the 32-bit assembly table");
 	m.vtxElmCols = o->vtxElmCols; m.femIfoCols = o->femIfoCols;
@@ -434,7 +451,9 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 			total += 32L * wid[sl];
 		}
 		SA_REQUIRE(total < (1L << 31) / 8, "operator too large for 32-bit slot offsets");
-		std::vector<int> col(total), dest(m.Z);
+		if (tr) tr->mark("mesh: slice widths");
+		// every entry of col and dest is written below: no zero fill (the pages are touched by the threads)
+		std::unique_ptr<int[]> col(new int[total > 0 ? total : 1]), dest(new int[m.Z]);
 		parallel_chunks(nsl, [&](long lo, long up) {
 			for (long sl = lo; sl < up; ++sl)
 				for (int lane = 0; lane < 32; ++lane) {
@@ -449,6 +468,7 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 					}
 				}
 		});
+		if (tr) tr->mark("mesh: slot columns");
 		m.nslice = nsl;
 		m.slTotal = total;
 		m.slWidth = P.alloc<int>(nsl);
@@ -457,7 +477,7 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		m.slDest = P.alloc<int>(m.Z);
 		// slot of the transposed entry: row j of femVtxMat is sorted by column
 		// (checked above), so (j, i) is found by bisection
-		std::vector<int> tz(m.Z);
+		std::unique_ptr<int[]> tz(new int[m.Z]);
 		parallel_chunks(m.Z, [&](long lo, long up) {
 			for (long z = lo; z < up; ++z) {
 				int i = fv[z], j = fv[m.Z + z];
@@ -468,15 +488,33 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 				SA_REQUIRE(fi[z] == fi[tz[z]], "femIfoMat lists differ between (i, j) and (j, i)");
 			}
 		});
+		if (tr) tr->mark("mesh: transposes");
 		m.transZ = P.alloc<int>(m.Z);
-		SA_CHECK(cudaMemcpyAsync(m.transZ, tz.data(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
+		SA_CHECK(cudaMemcpyAsync(m.transZ, tz.get(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
 		// assembly order: the N diagonal slots (many elements each) first, then
 		// the strictly upper slots (few elements each), so a warp's threads
-		// loop over similar element counts
-		std::vector<int> ord;
-		ord.reserve((m.Z + m.N) / 2 + 1);
-		for (int z = 0; z < m.Z; ++z) if (fv[z] == fv[m.Z + z]) ord.push_back(z);
-		for (int z = 0; z < m.Z; ++z) if (fv[z] < fv[m.Z + z]) ord.push_back(z);
+		// loop over similar element counts; per host chunk counts, then each chunk writes at its offsets
+		const int nch = chunk_count(m.Z);
+		std::vector<long> nDiag(nch + 1, 0), nUp(nch + 1, 0);
+		parallel_chunks_t(m.Z, [&](int t, long lo, long up) {
+			long a = 0, b = 0;
+			for (long z = lo; z < up; ++z) {
+				a += fv[z] == fv[m.Z + z];
+				b += fv[z] < fv[m.Z + z];
+			}
+			nDiag[t + 1] = a;
+			nUp[t + 1] = b;
+		});
+		for (int t = 0; t < nch; ++t) { nDiag[t + 1] += nDiag[t]; nUp[t + 1] += nUp[t]; }
+		std::vector<int> ord((size_t) (nDiag[nch] + nUp[nch]));
+		parallel_chunks_t(m.Z, [&](int t, long lo, long up) {
+			long a = nDiag[t], b = nDiag[nch] + nUp[t];
+			for (long z = lo; z < up; ++z) {
+				if (fv[z] == fv[m.Z + z]) ord[a++] = (int) z;
+				else if (fv[z] < fv[m.Z + z]) ord[b++] = (int) z;
+			}
+		});
+		if (tr) tr->mark("mesh: assembly order");
 		m.nAsm = (int) ord.size();
 		m.asmOrder = P.alloc<int>(ord.size());
 		SA_CHECK(cudaMemcpyAsync(m.asmOrder, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, s));
@@ -484,14 +522,15 @@ static void build_mesh(Mesh &m, const sa_element_object *o, bool needVfd, bool n
 		SA_CHECK(cudaMemcpyAsync(m.slOff, off.data(), sizeof(int) * nsl, cudaMemcpyHostToDevice, s));
 		m.slOffHost = off;
 		m.slOffHost.push_back((int) total);
-		SA_CHECK(cudaMemcpyAsync(m.slCol, col.data(), sizeof(int) * total, cudaMemcpyHostToDevice, s));
-		SA_CHECK(cudaMemcpyAsync(m.slDest, dest.data(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
+		SA_CHECK(cudaMemcpyAsync(m.slCol, col.get(), sizeof(int) * total, cudaMemcpyHostToDevice, s));
+		SA_CHECK(cudaMemcpyAsync(m.slDest, dest.get(), sizeof(int) * m.Z, cudaMemcpyHostToDevice, s));
 		SA_CHECK(cudaStreamSynchronize(s));      // host vectors go out of scope
 	}
-	if (tr) tr->mark("mesh: sliced layout, transposes");
+	if (tr) tr->mark("mesh: layout upload");
 	m.asmCols = maxAdj;
 	m.asmTab = P.alloc<int>((size_t) std::max(1, maxAdj) * m.Z);
 	int *bad = P.zeros<int>(1);
+	if (tr) tr->mark("mesh: assembly table memory");
 	k_asm_table<<<grid_for(m.Z), kBlock, 0, s>>>(m.Z, m.E, m.V, m.femVtx, m.femIfo, m.elmVtx, m.asmTab, bad);
 	int hbad = 0;
 	SA_CHECK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
