@@ -606,8 +606,8 @@ k_cg_persist(SellOp A, const TM *__restrict__ blk, const TV *__restrict__ dinv, 
 	unsigned int target = 0;                     // bar->count is zeroed before the launch
 	if (threadIdx.x == 0) gaveUp = 0;
 	TX xv[B];
-	// block-Jacobi (binv): FP32 inverses stay in registers, FP64 ones (twice the registers) are read from
-	// L2 in each update; FP64 B = 1 solves: point Jacobi, the inverse diagonal in registers
+	// block-Jacobi (binv): FP32 inverses stay in registers, FP64 ones (twice the registers: they would
+	// spill) in shared memory; FP64 B = 1 solves: point Jacobi, the inverse diagonal in registers
 	constexpr bool kBlk = block_prec<B, TV>();
 	constexpr bool kBlkReg = kBlk && sizeof(TV) == sizeof(float);
 	constexpr int kBV = kBlkReg ? B * B : 1;
