@@ -87,3 +87,24 @@ def test_unused_direction_width_accepted(spec):
     from shape_atrophy_gb300 import api
     sp = dict(spec, vfd=("M", 0.08, "B", 0.0))
     assert np.isfinite(api.varifold(sp, sp["lmkIniMat"]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("where", ["node", "bump"])
+def test_nonfinite_input_ends_the_solve_with_dbl_max(spec, where, precision):
+    """A NaN in the initial nodes or in the bump parameters reaches the first velocity solve's right-hand
+    side: the solve stops with SA_ERR_NONFINITE and the column's objective is DBL_MAX, as for a failed CG
+    (2D_frame/deform.cu:68-73); the call itself returns normally."""
+    from shape_atrophy_gb300 import _lib, api
+    sp = dict(spec)
+    if where == "node":
+        x = np.array(sp["lmkIniMat"], copy=True)
+        x[0, 7] = float("nan")
+        sp["lmkIniMat"] = x
+    else:
+        tv = np.array(sp["tauVarVec"], dtype=float, copy=True)
+        tv[-1] = float("nan")                                  # the bump's width
+        sp["tauVarVec"] = tv
+    got = api.forward(sp, trajectory=False, objective=True, precision=precision)
+    assert got["info"]["status"] == _lib.SA_ERR_NONFINITE
+    assert got["obj"][0] == np.finfo(np.float64).max
