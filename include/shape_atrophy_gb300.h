@@ -81,8 +81,9 @@ typedef struct sa_element_object {
 	int lmkNum, elmNum;            /* N, E */
 	const int *elmVtxMat;          /* E x (dim+1) */
 	const int *vtxElmMat;  int vtxElmCols;   /* N x cols */
-	const int *frmVtxMat;          /* E x 4 (2D) / E x 6 (3D) */
-	const int *tsvVtxMat;          /* E x 4 (2D) / E x 6 (3D) */
+	const int *frmVtxMat;          /* E x 4 (2D) / E x 6 (3D); frame model only (the isotropic model
+	                                  neither reads nor checks it; may be NULL there) */
+	const int *tsvVtxMat;          /* E x 4 (2D) / E x 6 (3D); frame model only, as frmVtxMat */
 	const int *bdrVtxMat;  int bdrElmNum;    /* unused by the model; may be NULL */
 	const int *vtxBdrMat;  int vtxBdrCols;   /* unused by the model; may be NULL */
 	const int *btmVtxMat;  int btmElmNum;    /* Bt x dim */
