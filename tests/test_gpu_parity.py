@@ -108,3 +108,44 @@ def test_bad_index_is_rejected(api):
     spec["elmObj"]["elmVtxMat"] = bad
     with pytest.raises(RuntimeError, match="out of range"):
         api.forward(spec)
+
+
+@pytest.mark.parametrize("case", ["annulus", "shell", "frame"])
+def test_zero_time_steps_return_the_initial_state(api, case):
+    """timeNum = 1 (no step, as deform's loop over timeNum - 1 steps allows): the trajectory is the initial
+    shape and the initial concentration, and the objective is the varifold distance of the initial shape
+    to the target, as the oracle gives it."""
+    from oracle.oracle import Problem
+    from shape_atrophy_gb300 import problems
+    if case == "frame":
+        spec = problems.demo_strip(13, 5, timeEnd=0.02)
+    else:
+        spec = dict(_layered_cases())[case]
+    spec = dict(spec, timeNum=1)
+    got = api.forward(spec, trajectory=True, objective=True)
+    want = Problem(spec).forward(spec["tauVarVec"], with_obj=True)
+    assert got["info"]["status"] == 0 and want["status"] == 0
+    assert got["info"]["cgIterTotal"] == 0
+    assert got["lmkStk"].shape[0] == 1
+    np.testing.assert_array_equal(got["lmkStk"][0], spec["lmkIniMat"])
+    assert rel(got["tauMat"], want["tauMat"]) < TOL
+    assert abs(got["obj"][0] - want["obj"]) <= TOL * abs(want["obj"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_layered_columns_are_independent(api, precision):
+    """Several rows of tauVarMat (the optimiser's batch, 2D_frame/computeObjfcn.cu:61-62,162-166) in one
+    call: each row's objective equals the oracle's for that row alone (mixed: within 1e-6), and the trajectory
+    returned is the last row's."""
+    from oracle.oracle import Problem
+    spec = dict(_layered_cases())["annulus"]
+    tv = np.asarray(spec["tauVarVec"], dtype=float)                # [cx, cy, height, width]
+    rows = np.stack([tv, tv * np.array([1.0, 1.0, 0.7, 1.3]), tv])
+    got = api.forward(spec, rows, trajectory=True, objective=True, precision=precision)
+    tol = TOL if precision == "fp64" else 1e-6
+    P = Problem(spec)
+    for k in range(rows.shape[0]):
+        want = P.forward(rows[k], with_obj=True)
+        assert abs(got["obj"][k] - want["obj"]) <= tol * abs(want["obj"]), k
+    assert got["obj"][0] == got["obj"][2]          # the same row gives the same bits
+    assert rel(got["lmkStk"], want["lmkStk"]) < tol
