@@ -1037,7 +1037,7 @@ __global__ void __launch_bounds__(kBatchBlock, kBatchMinCtas) k_cg_batch(const C
 				rk[c] = r[k] - al * sk;
 				r[k] = rk[c];
 			}
-			if constexpr (block_prec<B, TV>()) prec_block<B, TV>(binv + (long) i * B * B, rk, uk);
+			if constexpr (block_prec<B, TV>()) prec_block_ldg<B, TV>(binv + (long) i * B * B, rk, uk);
 			else for (int c = 0; c < B; ++c) uk[c] = dinv[(long) i * B + c] * rk[c];
 			for (int c = 0; c < B; ++c) u[(long) i * B + c] = uk[c];
 			dot_row<B, TV>(d2[0], rk, uk);
